@@ -1,0 +1,359 @@
+/*
+ * lace_gb300 - GB300 (sm_103a) implementation of LACE's preconditioned-solve
+ * path: ParILU(0) -> sparse triangular solves -> FGMRES-Householder.
+ *
+ * Two layers, both plain C ABI (no C++ or torch types in any signature):
+ *
+ *  1. Drop-in entry points with LACE's own names and signatures
+ *     (include/sparse.h of LACE).  A program built against LACE links this
+ *     library in place of LACE's src/parilu_v0_3*.cpp, src/trisolve.cpp's
+ *     data_parcsrtrsv, blas/zspmv.cpp and src/fgmres_householder*.cpp; the
+ *     rest of LACE (IO, conversions, free) stays as it is.  Containers are
+ *     LACE's data_d_matrix (host memory); every call uploads, runs on the
+ *     GPU and downloads.  Unlike LACE, nothing here calls exit(): failures
+ *     return DEV_ERR_* codes (ParILU, which LACE declares void, reports
+ *     through log->sweeps = -1 and sets lace_gpu_last_error()).
+ *
+ *  2. GPU-resident entry points (lace_gpu_*) that keep a matrix, its factors
+ *     and the Krylov workspace in HBM across calls.  All return DEV_SUCCESS
+ *     (0) or a DEV_ERR_* code.
+ *
+ * The container and log structs below are byte-compatible with LACE's
+ * include/sparse_types.h:14-176 (same members, same 64-byte alignment);
+ * when LACE's own headers are included first they are used instead.
+ */
+#ifndef LACE_GB300_H
+#define LACE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* everything declared here is exported from liblace_gb300.so (the library
+ * is built with hidden visibility by default) */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ------------------------------------------------------------------------
+ * LACE types (include/dense_types.h, include/sparse_types.h)
+ * ---------------------------------------------------------------------- */
+#ifndef DEV_TYPES_H
+#define LACE_GB300_DEFINES_DEV_TYPES 1
+#define DEV_ALIGN 64
+typedef int data_int_t;
+typedef double dataType;
+/* error codes, include/dense_types.h:134-160 */
+#define DEV_SUCCESS 0
+#define DEV_ERR -100
+#define DEV_ERR_NOT_INITIALIZED -101
+#define DEV_ERR_NOT_SUPPORTED -103
+#define DEV_ERR_ILLEGAL_VALUE -104
+#define DEV_ERR_NOT_FOUND -105
+#define DEV_ERR_ALLOCATION -106
+#define DEV_ERR_INTERNAL_LIMIT -107
+#define DEV_ERR_HOST_ALLOC -112
+#define DEV_ERR_DEVICE_ALLOC -113
+#define DEV_ERR_INVALID_PTR -115
+#define DEV_ERR_UNKNOWN -116
+#define DEV_ERR_NOT_IMPLEMENTED -117
+#define DEV_ERR_NAN -118
+#define DEV_ERR_BADPRECOND -204
+#define DEV_NOTCONVERGED -205
+typedef enum { MagmaRowMajor = 101, MagmaColMajor = 102 } data_order_t;
+typedef enum { MagmaUpper = 121, MagmaLower = 122, MagmaFull = 123, MagmaHessenberg = 124 } data_uplo_t;
+typedef enum {
+  Magma_CSR = 611, Magma_ELLPACKT = 612, Magma_ELL = 613, Magma_DENSE = 614,
+  Magma_BCSR = 615, Magma_CSC = 616, Magma_HYB = 617, Magma_COO = 618,
+  Magma_ELLRT = 619, Magma_SPMVFUNCTION = 620, Magma_SELLP = 621,
+  Magma_ELLD = 622, Magma_CSRLIST = 623, Magma_CSRD = 624, Magma_CSRL = 627,
+  Magma_CSRU = 628, Magma_CSRCOO = 629, Magma_CUCSR = 630, Magma_COOLIST = 631,
+  Magma_CSR5 = 632, Magma_CSCD = 633, Magma_CSCL = 634, Magma_CSCU = 635,
+  Magma_CSCCOO = 636, Magma_DENSEL = 637, Magma_DENSEU = 638,
+  Magma_DENSED = 639, Magma_BCSRD = 640, Magma_BCSRL = 641, Magma_BCSRU = 642,
+  Magma_BCSC = 643, Magma_BCSCD = 644, Magma_BCSCL = 645, Magma_BCSCU = 646
+} data_storage_t;
+typedef enum { Magma_GENERAL = 581, Magma_SYMMETRIC = 582 } data_symmetry_t;
+typedef enum {
+  Magma_ORDERED = 591, Magma_DIAGFIRST = 592, Magma_UNITY = 593,
+  Magma_VALUE = 594, Magma_ZERO = 595, Magma_NODIAG = 596
+} data_diagorder_t;
+#endif /* DEV_TYPES_H */
+
+#ifndef SPARSE_TYPES_H
+#define LACE_GB300_DEFINES_SPARSE_TYPES 1
+/* include/sparse_types.h:14-41 */
+typedef struct data_d_matrix {
+  data_storage_t storage_type;
+  data_symmetry_t sym;
+  data_diagorder_t diagorder_type;
+  data_uplo_t fill_mode;
+  data_int_t num_rows;
+  data_int_t num_cols;
+  data_int_t nnz;
+  data_int_t max_nnz_row;
+  data_int_t diameter;
+  data_int_t true_nnz;
+  dataType *val __attribute__((aligned(DEV_ALIGN)));
+  dataType *diag __attribute__((aligned(DEV_ALIGN)));
+  data_int_t *row __attribute__((aligned(DEV_ALIGN)));
+  data_int_t *rowidx __attribute__((aligned(DEV_ALIGN)));
+  data_int_t *col __attribute__((aligned(DEV_ALIGN)));
+  data_int_t *list;
+  data_int_t *blockinfo;
+  data_int_t blocksize;
+  data_int_t ldblock;
+  data_int_t numblocks;
+  data_int_t alignment;
+  data_order_t major;
+  data_int_t ld;
+  data_int_t pad_rows;
+  data_int_t pad_cols;
+} __attribute__((aligned(DEV_ALIGN))) data_d_matrix;
+
+/* include/sparse_types.h:131-144 */
+typedef struct data_z_preconditioner_log {
+  data_int_t sweeps;
+  data_int_t maxSweeps;
+  dataType tol;
+  dataType finalStep;
+  dataType A_Frobenius;
+  dataType precond_generation_time;
+  dataType initial_residual;
+  dataType initial_nonlinear_residual;
+  dataType residual;
+  dataType nonlinear_residual;
+  data_int_t omp_num_threads;
+} __attribute__((aligned(DEV_ALIGN))) data_d_preconditioner_log;
+
+/* include/sparse_types.h:147-156 */
+typedef struct data_z_gmres_log {
+  data_int_t restarts;
+  data_int_t search_directions;
+  dataType solve_time;
+  dataType initial_residual;
+  dataType final_residual;
+  dataType scaled_residual;
+  dataType original_residual;
+} __attribute__((aligned(DEV_ALIGN))) data_d_gmres_log;
+
+/* include/sparse_types.h:158-176 */
+typedef struct data_z_gmres_param {
+  data_int_t search_max;
+  data_int_t tol_type;
+  dataType rtol;
+  data_int_t reorth;
+  data_int_t user_csrtrsv_choice;
+  data_int_t monitorOrthog;
+  data_int_t restart_max;
+  data_int_t precondition;
+  dataType parilu_reduction;
+  data_int_t reorder;
+} __attribute__((aligned(DEV_ALIGN))) data_d_gmres_param;
+#endif /* SPARSE_TYPES_H */
+
+/* ------------------------------------------------------------------------
+ * 1. Drop-in entry points (LACE names and signatures)
+ * ---------------------------------------------------------------------- */
+
+/* Replaces src/parilu_v0_3.cpp:16 (CSR, and src/parilu_v0_3_bcsr.cpp:16 when
+ * A->storage_type == Magma_BCSR).  Synchronous ParILU(0) sweeps on the GPU
+ * until step <= reduction * initial residual or 20 sweeps.  Outputs L as
+ * Magma_CSRL (unit diagonal last in each row) and U as Magma_CSCU
+ * (diagonal last in each column), host arrays allocated with
+ * posix_memalign(64) so data_zmfree() releases them. */
+void data_PariLU_v0_3(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U,
+                      dataType reduction, data_d_preconditioner_log *log);
+
+/* Replaces src/parilu_v0_3_prescribedSweeps.cpp:17: stops after
+ * log->maxSweeps sweeps or step <= 4*eps. */
+void data_PariLU_v0_3_prescribedSweeps(data_d_matrix *A, data_d_matrix *L,
+                                       data_d_matrix *U, dataType reduction,
+                                       data_d_preconditioner_log *log);
+
+/* Replaces src/parilu_v0_3_gpu.cpp:110 (nthreads is accepted and ignored:
+ * the launch shape is chosen for the GPU). */
+void data_PariLU_v0_3_gpu(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U,
+                          dataType reduction, data_d_preconditioner_log *log,
+                          int nthreads);
+
+/* Replaces src/parilu_v0_3_gpu_prescribedSweeps.cpp:111 */
+void data_PariLU_v0_3_gpu_prescribedSweeps(data_d_matrix *A, data_d_matrix *L,
+                                           data_d_matrix *U, dataType reduction,
+                                           data_d_preconditioner_log *log);
+
+/* Replaces src/trisolve.cpp:256.  Triangular sweeps until
+ * sum (y_new - y_old)^2 <= tol or a non-finite step (GPU: synchronous
+ * Jacobi sweeps).  uplo MagmaLower needs storage Magma_CSRL (diagonal last),
+ * MagmaUpper needs Magma_CSRU (diagonal first); otherwise returns -1 as
+ * LACE does.  Host arrays. */
+int data_parcsrtrsv(const data_uplo_t uplo, const data_storage_t storage,
+                    const data_diagorder_t diag, const int num_rows,
+                    const dataType *Aval, const int *row, const int *col,
+                    const dataType *rhsval, dataType *yval, const dataType tol,
+                    int *iter);
+
+/* Replaces blas/zspmv.cpp:48: y = alpha*A*x + beta*y for CSR/CSRL/CSRU,
+ * and (beyond LACE) Magma_BCSR; DEV_ERR_NOT_SUPPORTED otherwise. */
+int data_z_spmv(dataType alpha, data_d_matrix *A, data_d_matrix *x,
+                dataType beta, data_d_matrix *y);
+
+/* Replaces src/fgmres_householder_restart.cpp:63.  Right-preconditioned
+ * restarted FGMRES with Householder Arnoldi; preconditioner M = L*U given as
+ * L (Magma_CSRL) and U (Magma_CSRU, or Magma_CSCU as ParILU returns it).
+ * gmres_par->user_csrtrsv_choice: 0 exact triangular solves (sync-free
+ * SpTRSV), 1 Jacobi ParCSRTRSV sweeps with tol 1.0, 2 no preconditioner.
+ * x0 is overwritten with the solution (LACE frees and re-allocates
+ * x0->val; this replacement writes into the existing array).  Returns
+ * DEV_SUCCESS when the residual target was reached, DEV_NOTCONVERGED
+ * otherwise (LACE's own return value is inverted, see
+ * src/fgmres_householder_restart.cpp:768-770). */
+int data_fgmres_householder_restart(data_d_matrix *A, data_d_matrix *b,
+                                    data_d_matrix *x0, data_d_matrix *L,
+                                    data_d_matrix *U,
+                                    data_d_gmres_param *gmres_par,
+                                    data_d_gmres_log *gmres_log);
+
+/* Replaces src/fgmres_householder_opt4.cpp:63 (one cycle, no restarts). */
+int data_fgmres_householder(data_d_matrix *A, data_d_matrix *b,
+                            data_d_matrix *x0, data_d_matrix *L,
+                            data_d_matrix *U, data_d_gmres_param *gmres_par,
+                            data_d_gmres_log *gmres_log);
+
+/* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
+ * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives
+ * the same value (the fill-in part of LACE's res is not formed) and LU is
+ * left untouched.  L: Magma_CSRL, U: Magma_CSCU or Magma_CSRU. */
+int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U,
+                 data_d_matrix *LU, dataType *res, dataType *nonlinres);
+
+/* ------------------------------------------------------------------------
+ * 2. GPU-resident API
+ * ---------------------------------------------------------------------- */
+
+typedef struct lace_gpu_ctx lace_gpu_ctx;
+
+/* precision of the ParILU factors and of both triangular solves; the outer
+ * FGMRES, its SpMV and the reflectors are always FP64 */
+enum { LACE_PREC_FP64 = 0, LACE_PREC_FP32 = 1, LACE_PREC_BF16_STORE = 2 };
+/* how M^{-1} is applied */
+enum {
+  LACE_TRSV_SYNCFREE = 0, /* exact, sync-free (ready flags per row chunk) */
+  LACE_TRSV_LEVELS = 1,   /* exact, level-scheduled                       */
+  LACE_TRSV_JACOBI = 2,   /* ParCSRTRSV: synchronous Jacobi sweeps        */
+  LACE_TRSV_NONE = 3      /* identity                                     */
+};
+
+typedef struct lace_gpu_options {
+  int precision;        /* LACE_PREC_*                                   */
+  int trsv_mode;        /* LACE_TRSV_*                                   */
+  int jacobi_sweeps;    /* sweeps per triangle for LACE_TRSV_JACOBI      */
+  double jacobi_tol;    /* ... or stop when sum (dy)^2 <= tol            */
+  int use_graph;        /* capture each Arnoldi cycle in a CUDA graph    */
+  int spmv_lanes;       /* lanes per CSR row; 0 = autotune               */
+  int trsv_rows_per_lane; /* sync-free chunk = 32 * this rows; 0 = auto  */
+  int monitor_orthog;   /* ||I - Q^T Q||_inf after every step (slow)     */
+} lace_gpu_options;
+
+void lace_gpu_default_options(lace_gpu_options *opt);
+
+/* stream: a cudaStream_t (NULL = a stream owned by the context) */
+int lace_gpu_ctx_create(lace_gpu_ctx **ctx, int device, void *stream);
+int lace_gpu_ctx_destroy(lace_gpu_ctx *ctx);
+int lace_gpu_set_options(lace_gpu_ctx *ctx, const lace_gpu_options *opt);
+void *lace_gpu_stream(lace_gpu_ctx *ctx);
+
+/* Upload A (zero-based CSR, sorted columns, every diagonal present) and run
+ * the structural analysis: L/U split, CSC image of U, A->factor position
+ * maps, SpTRSV chunk classification and level sets, SpMV autotuning.
+ * _host: arrays in host memory; _device: arrays already in device memory. */
+int lace_gpu_upload_csr_host(lace_gpu_ctx *ctx, int n, int nnz, const int *row,
+                             const int *col, const double *val);
+int lace_gpu_upload_csr_device(lace_gpu_ctx *ctx, int n, int nnz,
+                               const int *row, const int *col,
+                               const double *val);
+/* BCSR with row-major bs x bs blocks (host arrays); nblk blocks */
+int lace_gpu_upload_bcsr_host(lace_gpu_ctx *ctx, int nbrows, int bs, int nblk,
+                              const int *row, const int *col, const double *val);
+/* refresh only the values of A (same pattern), device array */
+int lace_gpu_update_values_device(lace_gpu_ctx *ctx, const double *val);
+
+/* ParILU(0): `sweeps` synchronous sweeps from the A-initial guess.
+ * step_out (may be NULL): step of the last sweep, normalised by ||A||_F.
+ * nonlinres_out (may be NULL): ||(A-LU)|_S||_F / ||A||_F after the sweeps. */
+int lace_gpu_parilu0(lace_gpu_ctx *ctx, int sweeps, double *step_out,
+                     double *nonlinres_out);
+
+/* y = alpha*A*x + beta*y, device vectors (FP64) */
+int lace_gpu_spmv(lace_gpu_ctx *ctx, double alpha, const double *x,
+                  double beta, double *y);
+
+/* z = M^{-1} q with the current factors and options (device FP64) */
+int lace_gpu_apply_precond(lace_gpu_ctx *ctx, const double *q, double *z);
+
+/* one triangle: which 0 = L (unit lower), 1 = U (upper), 2 = U^T (lower),
+ * 3 = L^T (unit upper); device FP64 in/out (converted internally) */
+int lace_gpu_sptrsv(lace_gpu_ctx *ctx, int which, const double *b, double *x);
+
+/* FGMRES-Householder on device vectors b, x (x: initial guess in, solution
+ * out).  par: LACE's parameter struct (search_max, restart_max, tol_type,
+ * rtol, user_csrtrsv_choice is ignored here: the context options decide);
+ * log: LACE's log struct (search_directions = directions of the final
+ * cycle, restarts = index of the final cycle, as LACE fills it).
+ * total_iters (may be NULL): search directions over all cycles. */
+int lace_gpu_fgmres_householder(lace_gpu_ctx *ctx, const double *b, double *x,
+                                const data_d_gmres_param *par,
+                                data_d_gmres_log *log, int *total_iters);
+
+/* Adjoint of the solve x = A^{-1} b for a loss L(x): given dL/dx (device),
+ * solves A^T lambda = dL/dx with FGMRES-Householder preconditioned by the
+ * transposed factors (U^T then L^T), and returns dL/db = lambda and
+ * dL/dA_ij = -lambda_i x_j on A's pattern (nnz values, CSR order).
+ * x is the forward solution (device).  Either output may be NULL. */
+int lace_gpu_solve_backward(lace_gpu_ctx *ctx, const double *x,
+                            const double *dLdx, const data_d_gmres_param *par,
+                            double *dLdb, double *dLdA_val, int *total_iters);
+
+/* Last error recorded on this thread (for the void drop-in calls). */
+int lace_gpu_last_error(void);
+const char *lace_gpu_error_string(int code);
+
+/* ------------------------------------------------------------------------
+ * Batched solves: many independent CSR systems, several right-hand sides
+ * each, all ParILU sweeps and all FGMRES cycles advanced together in a few
+ * persistent launches per Arnoldi step (captured in a CUDA graph).
+ * ---------------------------------------------------------------------- */
+typedef struct lace_gpu_batch lace_gpu_batch;
+
+/* Host arrays: system s has n[s] rows, its CSR arrays start at
+ * row_off[s] / nnz_off[s] in the concatenated row/col/val arrays (row
+ * pointers local to the system).  nrhs right-hand sides per system. */
+int lace_gpu_batch_create(lace_gpu_batch **batch, lace_gpu_ctx *ctx, int nsys,
+                          const int *n, const int *row_off, const int *nnz_off,
+                          const int *row, const int *col, const double *val,
+                          int nrhs);
+int lace_gpu_batch_destroy(lace_gpu_batch *batch);
+/* ParILU sweeps for every system, then FGMRES-Householder(search_max) on
+ * every (system, rhs) pair to rtol (relative).  b, x: device arrays holding,
+ * per system, nrhs consecutive vectors of length n[s] (system-major, in the
+ * order of row_off).  iters_out (host, nsys*nrhs, may be NULL). */
+int lace_gpu_batch_solve(lace_gpu_batch *batch, int sweeps, int search_max,
+                         int restart_max, double rtol, const double *b,
+                         double *x, int *iters_out);
+
+/* ABI self-description for bindings: sizeof and member offsets of the
+ * LACE structs as compiled into this library. */
+int lace_gpu_abi_layout(int *out, int cap);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LACE_GB300_H */

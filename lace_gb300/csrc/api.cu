@@ -1,0 +1,471 @@
+// Drop-in entry points with LACE's names and signatures (the first half of
+// include/lace_gb300.h).  Each call uploads the caller's host containers,
+// runs on the GPU through a process-wide context and writes the results back
+// into the same containers, allocating output arrays the way LACE does
+// (64-byte aligned, released with free() by data_zmfree).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <vector>
+
+#include "context.h"
+
+using namespace lace;
+
+namespace {
+
+std::mutex g_mu;
+lace_gpu_ctx *g_ctx = nullptr;
+
+int default_ctx(lace_gpu_ctx **out) {
+  if (!g_ctx) {
+    int dev = 0;
+    if (const char *e = getenv("LACE_GB300_DEVICE")) dev = atoi(e);
+    int rc = lace_gpu_ctx_create(&g_ctx, dev, nullptr);
+    if (rc) return rc;
+    g_ctx->verbose = getenv("LACE_GB300_VERBOSE") != nullptr;
+  }
+  cudaSetDevice(g_ctx->device);
+  *out = g_ctx;
+  return 0;
+}
+
+template <typename T>
+T *lace_alloc(size_t count) {
+  // LACE_CALLOC (include/dense_types.h:430-449): posix_memalign(64), zeroed
+  void *p = nullptr;
+  size_t bytes = count * sizeof(T);
+  size_t padded = (bytes / 64 + 1) * 64;
+  if (posix_memalign(&p, 64, padded) != 0) return nullptr;
+  memset(p, 0, padded);
+  return (T *)p;
+}
+
+// data_zmconvert frees these members of the output container first
+// (control/magma_zmconverter.cpp:221-248)
+void release_members(data_d_matrix *B) {
+  free(B->val);
+  free(B->col);
+  free(B->row);
+  free(B->rowidx);
+  free(B->list);
+  free(B->blockinfo);
+  free(B->diag);
+  B->val = nullptr;
+  B->col = nullptr;
+  B->row = nullptr;
+  B->rowidx = nullptr;
+  B->list = nullptr;
+  B->blockinfo = nullptr;
+  B->diag = nullptr;
+}
+
+bool is_csr(data_storage_t s) {
+  return s == Magma_CSR || s == Magma_CUCSR || s == Magma_CSRL || s == Magma_CSRU;
+}
+
+// ||L0 U0 - A|| over pattern(L0 U0) for the A-initial guess (the initial
+// residual LACE's ParILU records via data_zilures, src/parilu_v0_3.cpp:30-34)
+double initial_full_residual(const data_d_matrix *A) {
+  const int n = A->num_rows;
+  std::vector<double> acc(n, 0.0);
+  std::vector<int> mark(n, -1), list;
+  list.reserve(64);
+  double res = 0.0;
+  for (int i = 0; i < n; ++i) {
+    list.clear();
+    for (int p = A->row[i]; p < A->row[i + 1]; ++p) {
+      const int k = A->col[p];
+      if (k > i) break;
+      const double lik = (k == i) ? 1.0 : A->val[p];
+      for (int q = A->row[k]; q < A->row[k + 1]; ++q) {
+        const int j = A->col[q];
+        if (j < k) continue;
+        if (mark[j] != i) {
+          mark[j] = i;
+          acc[j] = 0.0;
+          list.push_back(j);
+        }
+        acc[j] += lik * A->val[q];
+      }
+    }
+    for (int p = A->row[i]; p < A->row[i + 1]; ++p)
+      if (mark[A->col[p]] == i) acc[A->col[p]] -= A->val[p];
+    for (int j : list) res += acc[j] * acc[j];
+  }
+  return std::sqrt(res);
+}
+
+int fill_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
+                 const std::vector<int> &idx, const std::vector<double> &val, int blocksize) {
+  release_members(B);
+  const int ld = blocksize > 0 ? blocksize * blocksize : 1;
+  B->storage_type = st;
+  B->major = MagmaRowMajor;
+  B->fill_mode = fill;
+  B->num_rows = n;
+  B->num_cols = n;
+  B->row = lace_alloc<int>(n + 1);
+  B->col = lace_alloc<int>(idx.size() + 1);
+  B->val = lace_alloc<double>(idx.size() * ld + 1);
+  if (!B->row || !B->col || !B->val) return DEV_ERR_HOST_ALLOC;
+  memcpy(B->row, ptr.data(), 4 * ptr.size());
+  memcpy(B->col, idx.data(), 4 * idx.size());
+  memcpy(B->val, val.data(), 8 * val.size());
+  if (blocksize > 0) {
+    B->blocksize = blocksize;
+    B->ldblock = ld;
+    B->numblocks = (int)idx.size();
+    B->nnz = (int)idx.size() * ld;
+  } else {
+    B->nnz = (int)idx.size();
+  }
+  B->true_nnz = B->nnz;
+  return 0;
+}
+
+// mode 0: data_PariLU_v0_3 stop rule (step <= reduction*Ares, <= 20 sweeps,
+// src/parilu_v0_3.cpp:43-62); mode 1: prescribed sweeps (log->maxSweeps, step
+// > 4 eps, src/parilu_v0_3_prescribedSweeps.cpp:62)
+void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataType reduction,
+                   data_d_preconditioner_log *log, int mode) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto fail = [&](int code) {
+    set_err(code);
+    if (log) log->sweeps = -1;
+  };
+  if (!A || !L || !U || !log) return fail(DEV_ERR_INVALID_PTR);
+  lace_gpu_ctx *c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return fail(rc);
+  lace_gpu_options o;
+  lace_gpu_default_options(&o);
+  lace_gpu_set_options(c, &o);
+  const bool bcsr = A->storage_type == Magma_BCSR;
+  const int n = A->num_rows;
+  if (bcsr) {
+    const int bs = A->blocksize;
+    const int nblk = A->numblocks > 0 ? A->numblocks : A->row[n];
+    rc = lace_gpu_upload_bcsr_host(c, n, bs, nblk, A->row, A->col, A->val);
+  } else if (is_csr(A->storage_type)) {
+    rc = lace_gpu_upload_csr_host(c, n, A->row[n], A->row, A->col, A->val);
+  } else {
+    rc = DEV_ERR_NOT_SUPPORTED;
+  }
+  if (rc) return fail(rc);
+  const double ares = bcsr ? 0.0 : initial_full_residual(A);
+  double tol;
+  int maxs;
+  if (bcsr) {  // src/parilu_v0_3_bcsr.cpp:61,118: un-normalised step <= reduction
+    tol = reduction / c->anorm;
+    maxs = 100;
+  } else if (mode == 0) {
+    tol = reduction * ares;
+    maxs = 20;
+  } else {
+    tol = std::numeric_limits<double>::epsilon() * 4.0;
+    maxs = log->maxSweeps;
+  }
+  double nonlin0 = NAN;
+  if (!bcsr) {
+    // nonlinear residual of the initial guess (0 sweeps)
+    rc = c->parilu(0, nullptr, &nonlin0, true, nullptr);
+    if (rc) return fail(rc);
+    nonlin0 *= c->anorm;
+  }
+  std::vector<double> steps;
+  double step = 0.0, nonlin = 0.0;
+  auto t0 = std::chrono::steady_clock::now();
+  rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol);
+  const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rc) return fail(rc);
+  // download: L values (CSRL order), U values (CSCU order), FP64
+  const int ld = bcsr ? A->blocksize * A->blocksize : 1;
+  std::vector<double> lv((size_t)c->nnzL * ld), uv((size_t)c->nnzU * ld);
+  if (c->vtype() != VType::F64) return fail(DEV_ERR_NOT_SUPPORTED);
+  cudaMemcpy(lv.data(), c->Lv[c->cur].p, 8 * lv.size(), cudaMemcpyDeviceToHost);
+  cudaMemcpy(uv.data(), c->Ucv[c->cur].p, 8 * uv.size(), cudaMemcpyDeviceToHost);
+  if (cudaGetLastError() != cudaSuccess) return fail(DEV_ERR_UNKNOWN);
+  L->diagorder_type = Magma_UNITY;
+  U->diagorder_type = Magma_VALUE;
+  rc = fill_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, lv,
+                    bcsr ? A->blocksize : 0);
+  if (!rc)
+    rc = fill_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, uv,
+                      bcsr ? A->blocksize : 0);
+  if (rc) return fail(rc);
+  U->major = MagmaColMajor;
+  log->sweeps = (int)steps.size();
+  log->tol = tol;
+  log->finalStep = steps.empty() ? 0.0 : steps.back();
+  log->A_Frobenius = c->anorm;
+  log->precond_generation_time = gen;
+  log->initial_residual = ares;
+  log->initial_nonlinear_residual = nonlin0;
+  log->nonlinear_residual = bcsr ? 0.0 : nonlin * c->anorm;
+  log->omp_num_threads = num_sms();
+  set_err(0);
+}
+
+int upload_vec(DBuf &d, const double *h, int n, cudaStream_t s) { return d.upload(h, 8 * (size_t)n, s); }
+
+}  // namespace
+
+extern "C" void data_PariLU_v0_3(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataType reduction,
+                                 data_d_preconditioner_log *log) {
+  parilu_dropin(A, L, U, reduction, log, 0);
+}
+
+extern "C" void data_PariLU_v0_3_prescribedSweeps(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U,
+                                                  dataType reduction, data_d_preconditioner_log *log) {
+  parilu_dropin(A, L, U, reduction, log, 1);
+}
+
+extern "C" void data_PariLU_v0_3_gpu(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U,
+                                     dataType reduction, data_d_preconditioner_log *log, int nthreads) {
+  (void)nthreads;
+  parilu_dropin(A, L, U, reduction, log, 0);
+}
+
+extern "C" void data_PariLU_v0_3_gpu_prescribedSweeps(data_d_matrix *A, data_d_matrix *L,
+                                                      data_d_matrix *U, dataType reduction,
+                                                      data_d_preconditioner_log *log) {
+  parilu_dropin(A, L, U, reduction, log, 1);
+}
+
+extern "C" int data_parcsrtrsv(const data_uplo_t uplo, const data_storage_t storage,
+                               const data_diagorder_t diag, const int num_rows, const dataType *Aval,
+                               const int *row, const int *col, const dataType *rhsval, dataType *yval,
+                               const dataType tol, int *iter) {
+  // storage / fill checks of src/trisolve.cpp:262-345
+  bool lower;
+  if (storage == Magma_CSRL && uplo == MagmaLower && diag != Magma_NODIAG) lower = true;
+  else if (storage == Magma_CSRL || uplo == MagmaLower) return -1;
+  else if (storage == Magma_CSRU && uplo == MagmaUpper && diag != Magma_NODIAG) lower = false;
+  else if (storage == Magma_CSRU || uplo == MagmaUpper) return -1;
+  else return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  lace_gpu_ctx *c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return set_err(rc);
+  const int n = num_rows;
+  const int nnz = row[n];
+  DBuf drow, dcol, dval, drhs, y0, y1;
+  if (drow.upload(row, 4 * (size_t)(n + 1), c->stream) || dcol.upload(col, 4 * (size_t)nnz, c->stream) ||
+      dval.upload(Aval, 8 * (size_t)nnz, c->stream) || upload_vec(drhs, rhsval, n, c->stream) ||
+      upload_vec(y0, yval, n, c->stream) || y1.ensure(8 * (size_t)n))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  TriDev t;
+  t.n = n;
+  t.nnz = nnz;
+  t.row = (const int *)drow.p;
+  t.col = (const int *)dcol.p;
+  t.val = dval.p;
+  t.lower = lower ? 1 : 0;
+  t.unit = 0;  // LACE divides by the stored diagonal (last / first in the row)
+  double *partials = (double *)c->part_ensure();
+  if (!partials) return set_err(DEV_ERR_DEVICE_ALLOC);
+  void *cur = y0.p, *nxt = y1.p;
+  double step = 1.e8;
+  *iter = 0;
+  // Jacobi sweeps converge in at most (number of levels) sweeps; bound the loop
+  const int cap = n + 2;
+  while (step > tol && std::isfinite(step) && *iter < cap) {
+    launch_jacobi_sweep(c->stream, t, VType::F64, drhs.p, 0, cur, nxt, 0, nullptr, false);
+    launch_sqdiff(c->stream, n, nxt, cur, 0, partials, (int *)c->cnt_buf.p + 9, (double *)c->scal_buf.p + 9);
+    cudaMemcpyAsync(c->h_scal + 9, (double *)c->scal_buf.p + 9, 8, cudaMemcpyDeviceToHost, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
+    step = c->h_scal[9];
+    std::swap(cur, nxt);
+    *iter = *iter + 1;
+  }
+  if (cudaMemcpy(yval, cur, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
+  return 0;
+}
+
+extern "C" int data_z_spmv(dataType alpha, data_d_matrix *A, data_d_matrix *x, dataType beta,
+                           data_d_matrix *y) {
+  if (!A || !x || !y) return set_err(DEV_ERR_INVALID_PTR);
+  const bool bcsr = A->storage_type == Magma_BCSR;
+  const int bs = bcsr ? A->blocksize : 1;
+  const int ncols = bcsr ? A->num_cols * bs : A->num_cols;
+  if (!(ncols == x->num_rows && x->num_cols == 1)) return DEV_ERR_NOT_SUPPORTED;  // blas/zspmv.cpp:71-75
+  if (!bcsr && !is_csr(A->storage_type)) return DEV_ERR_NOT_SUPPORTED;         // :65-68
+  std::lock_guard<std::mutex> lk(g_mu);
+  lace_gpu_ctx *c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return set_err(rc);
+  const int nr = A->num_rows;
+  const int nnz = A->row[nr];
+  const int ld = bcsr ? bs * bs : 1;
+  const int nout = bcsr ? nr * bs : nr;
+  DBuf drow, dcol, dval, dx, dy;
+  if (drow.upload(A->row, 4 * (size_t)(nr + 1), c->stream) || dcol.upload(A->col, 4 * (size_t)nnz, c->stream) ||
+      dval.upload(A->val, 8 * (size_t)nnz * ld, c->stream) || upload_vec(dx, x->val, ncols, c->stream) ||
+      (beta != 0.0 ? upload_vec(dy, y->val, nout, c->stream) : dy.ensure(8 * (size_t)nout)))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  if (bcsr)
+    launch_bcsr_spmv(c->stream, nr, bs, (const int *)drow.p, (const int *)dcol.p, (const double *)dval.p,
+                     (const double *)dx.p, alpha, beta, (double *)dy.p);
+  else {
+    const double avg = nr ? (double)nnz / nr : 1.0;
+    const int lanes = avg > 24 ? 32 : (avg > 12 ? 16 : (avg > 6 ? 8 : 4));
+    launch_spmv_f64x(c->stream, lanes, nr, (const int *)drow.p, (const int *)dcol.p, (const double *)dval.p,
+                     (const double *)dx.p, alpha, beta, (double *)dy.p);
+  }
+  if (cudaMemcpyAsync(y->val, dy.p, 8 * (size_t)nout, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return set_err(DEV_ERR_UNKNOWN);
+  return DEV_SUCCESS;
+}
+
+namespace {
+
+// U as CSR with the diagonal first: CSRU as given, or the transpose of CSCU
+void u_as_csr(const data_d_matrix *U, std::vector<int> &ptr, std::vector<int> &idx,
+              std::vector<double> &val) {
+  const int n = U->num_rows;
+  const int nnz = U->row[n];
+  if (U->storage_type == Magma_CSCU || U->storage_type == Magma_CSC) {
+    Pattern P, T;
+    P.n = n;
+    P.ptr.assign(U->row, U->row + n + 1);
+    P.idx.assign(U->col, U->col + nnz);
+    std::vector<int> t2p;
+    transpose_pattern(P, T, t2p);
+    ptr = T.ptr;
+    idx = T.idx;
+    val.resize(nnz);
+    for (int q = 0; q < nnz; ++q) val[q] = U->val[t2p[q]];
+  } else {
+    ptr.assign(U->row, U->row + n + 1);
+    idx.assign(U->col, U->col + nnz);
+    val.assign(U->val, U->val + nnz);
+  }
+}
+
+int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_matrix *L,
+                  data_d_matrix *U, data_d_gmres_param *par, data_d_gmres_log *log, int restart_max) {
+  if (!A || !b || !x0 || !par || !log) return set_err(DEV_ERR_INVALID_PTR);
+  if (!is_csr(A->storage_type)) return set_err(DEV_ERR_NOT_SUPPORTED);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto t0 = std::chrono::steady_clock::now();
+  lace_gpu_ctx *c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return set_err(rc);
+  lace_gpu_options o;
+  lace_gpu_default_options(&o);
+  o.monitor_orthog = par->monitorOrthog == 1;
+  const int choice = par->user_csrtrsv_choice;
+  o.trsv_mode = choice == 1 ? LACE_TRSV_JACOBI : (choice == 2 ? LACE_TRSV_NONE : LACE_TRSV_SYNCFREE);
+  lace_gpu_set_options(c, &o);
+  const int n = A->num_rows;
+  rc = lace_gpu_upload_csr_host(c, n, A->row[n], A->row, A->col, A->val);
+  if (rc) return set_err(rc);
+  if (choice != 2) {
+    if (!L || !U) return set_err(DEV_ERR_INVALID_PTR);
+    std::vector<int> up, ui;
+    std::vector<double> uv;
+    u_as_csr(U, up, ui, uv);
+    rc = c->set_factors_host(n, L->row, L->col, L->val, up.data(), ui.data(), uv.data());
+    if (rc) return set_err(rc);
+  }
+  DBuf db, dx;
+  if (upload_vec(db, b->val, n, c->stream) || upload_vec(dx, x0->val, n, c->stream))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  int total = 0;
+  rc = c->fgmres((const double *)db.p, (double *)dx.p, par->search_max, restart_max, par->tol_type,
+                 par->rtol, false, log, &total, nullptr);
+  if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
+  if (cudaMemcpy(x0->val, dx.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return set_err(DEV_ERR_UNKNOWN);
+  log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (c->verbose)
+    printf("gmres_search_directions = %d;\ngmres_total_search_directions = %d;\n", log->search_directions,
+           total);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int data_fgmres_householder_restart(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
+                                               data_d_matrix *L, data_d_matrix *U,
+                                               data_d_gmres_param *gmres_par, data_d_gmres_log *gmres_log) {
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, gmres_par ? gmres_par->restart_max : 0);
+}
+
+extern "C" int data_fgmres_householder(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
+                                       data_d_matrix *L, data_d_matrix *U, data_d_gmres_param *gmres_par,
+                                       data_d_gmres_log *gmres_log) {
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, 1);
+}
+
+extern "C" int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U, data_d_matrix *LU,
+                            dataType *res, dataType *nonlinres) {
+  (void)LU;
+  if (!res || !nonlinres) return set_err(DEV_ERR_INVALID_PTR);
+  if (!is_csr(A.storage_type)) return set_err(DEV_ERR_NOT_SUPPORTED);
+  std::lock_guard<std::mutex> lk(g_mu);
+  lace_gpu_ctx *c = nullptr;
+  int rc = default_ctx(&c);
+  if (rc) return set_err(rc);
+  lace_gpu_options o;
+  lace_gpu_default_options(&o);
+  lace_gpu_set_options(c, &o);
+  const int n = A.num_rows;
+  rc = lace_gpu_upload_csr_host(c, n, A.row[n], A.row, A.col, A.val);
+  if (rc) return set_err(rc);
+  std::vector<int> up, ui;
+  std::vector<double> uv;
+  u_as_csr(&U, up, ui, uv);
+  rc = c->set_factors_host(n, L.row, L.col, L.val, up.data(), ui.data(), uv.data());
+  if (rc) return set_err(rc);
+  // the residual kernel walks A's rows with L (CSRL) and U (CSCU) current values
+  IluArgs a = c->ilu_args();
+  launch_ilu_residual(c->stream, a, c->vtype(), c->Lv[c->cur].p, c->Ucv[c->cur].p, (double *)c->scal_buf.p + 41);
+  cudaMemcpyAsync(c->h_scal + 41, (double *)c->scal_buf.p + 41, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
+  *nonlinres = std::sqrt(c->h_scal[41]);
+  *res = *nonlinres;
+  return DEV_SUCCESS;
+}
+
+// ABI self-description: sizes and member offsets of LACE's structs
+extern "C" int lace_gpu_abi_layout(int *out, int cap) {
+  const int v[] = {
+      (int)sizeof(data_d_matrix),
+      (int)offsetof(data_d_matrix, num_rows),
+      (int)offsetof(data_d_matrix, nnz),
+      (int)offsetof(data_d_matrix, val),
+      (int)offsetof(data_d_matrix, diag),
+      (int)offsetof(data_d_matrix, row),
+      (int)offsetof(data_d_matrix, rowidx),
+      (int)offsetof(data_d_matrix, col),
+      (int)offsetof(data_d_matrix, list),
+      (int)offsetof(data_d_matrix, blockinfo),
+      (int)offsetof(data_d_matrix, blocksize),
+      (int)offsetof(data_d_matrix, ldblock),
+      (int)offsetof(data_d_matrix, numblocks),
+      (int)offsetof(data_d_matrix, major),
+      (int)offsetof(data_d_matrix, ld),
+      (int)offsetof(data_d_matrix, pad_cols),
+      (int)sizeof(data_d_preconditioner_log),
+      (int)offsetof(data_d_preconditioner_log, tol),
+      (int)offsetof(data_d_preconditioner_log, omp_num_threads),
+      (int)sizeof(data_d_gmres_log),
+      (int)offsetof(data_d_gmres_log, solve_time),
+      (int)offsetof(data_d_gmres_log, original_residual),
+      (int)sizeof(data_d_gmres_param),
+      (int)offsetof(data_d_gmres_param, rtol),
+      (int)offsetof(data_d_gmres_param, restart_max),
+      (int)offsetof(data_d_gmres_param, parilu_reduction),
+      (int)offsetof(data_d_gmres_param, reorder),
+  };
+  const int nv = (int)(sizeof(v) / sizeof(v[0]));
+  for (int i = 0; i < nv && i < cap; ++i) out[i] = v[i];
+  return nv;
+}

@@ -1,0 +1,93 @@
+// Device-side helpers shared by the lace_gb300 kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace lace {
+
+constexpr int kWarp = 32;
+
+// Bit set in Control::status when a bounded wait gave up.
+constexpr int kStatusSpinTimeout = 1;
+// Bit set when a kernel met a non-finite value it must not divide by.
+constexpr int kStatusBreakdown = 2;
+// Upper bound on polls of one ready flag before a wait gives up.  A poll is
+// one L2 round trip (~0.5 us), so this is ~1 s - far above any correct wait.
+constexpr int kMaxSpins = 1 << 21;
+
+// Per-solve device control block (lives in device memory; every kernel of an
+// Arnoldi cycle reads `done` first and returns at once when it is set).
+struct Control {
+  int done;           // cycle finished (converged or search_max reached)
+  int converged;      // |g_{j+1}| < rtol reached
+  int nsteps;         // search directions in the finished cycle
+  int status;         // kStatus* bits
+  int trsv_epoch[4];  // last epoch published per triangle (L, U, U^T, L^T)
+  int tickets[4][2];  // per-triangle {next chunk ticket, warps exited}
+  int block_count[8]; // last-block counters, one per reducing kernel
+  double rtol_abs;    // absolute tolerance of the current solve
+  double rnorm0;      // initial residual of the solve
+  double resid;       // |g_{j+1}| of the latest step
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// value conversions for the factor storage types
+template <typename T> __device__ __forceinline__ float to_f(T v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<double>(double v) { return (float)v; }
+template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename C, typename T> __device__ __forceinline__ C cvt(T v) { return (C)v; }
+template <> __device__ __forceinline__ float cvt<float, __nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <> __device__ __forceinline__ double cvt<double, __nv_bfloat16>(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16, float>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16, double>(double v) { return __float2bfloat16_rn((float)v); }
+
+// Deterministic grid reduction helper: every block writes its partials to
+// partials[blockIdx.x * stride + k]; the block that arrives last (counter
+// protocol with a fence) returns true and may then read all partials.  The
+// counter is reset by that block.
+__device__ __forceinline__ bool arrive_last(int *counter) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int prev = atomicAdd(counter, 1);
+    s_last = (prev == (int)gridDim.x - 1);
+    if (s_last) *counter = 0;
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last != 0;
+}
+
+// mysgn of LACE (include/sparse.h:1129-1133): +1 for v >= 0, -1 otherwise
+__device__ __forceinline__ double mysgn(double v) { return v >= 0.0 ? 1.0 : -1.0; }
+
+}  // namespace lace

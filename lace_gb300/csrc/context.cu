@@ -1,0 +1,1173 @@
+// GPU-resident context: device layout of the matrix, its factors and the
+// Krylov workspace; the host drivers of ParILU, SpTRSV and FGMRES-Householder
+// (the lace_gpu_* half of include/lace_gb300.h).
+//
+// HBM layout for one CSR system (n rows, nnz entries):
+//   A      row[n+1] col[nnz] i32, val[nnz] f64
+//   L      CSRL  (strict lower + unit diagonal last)  ptr/idx i32, 2 value buffers
+//   U      CSCU  (column form, diagonal last) for the sweeps, 2 value buffers,
+//          plus its CSR form (diagonal first) for the solves, with a position
+//          map csr->csc (the CSR values are gathered after the sweeps)
+//   L^T    CSR of L's transpose (adjoint solves), with a position map
+//   per triangle: chunk kinds (u8), ready flags (i32), level lists (i32)
+//   Krylov V[ldv x (m+1)] f64 column-major (ldv = n rounded up to 32),
+//          Z[ldv x m] f32 (mixed precision) or f64, w/q/t vectors
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "context.h"
+
+namespace lace {
+
+thread_local int g_last_error = 0;
+
+int set_err(int code) {
+  g_last_error = code;
+  return code;
+}
+
+int cuda_code(cudaError_t e) {
+  if (e == cudaSuccess) return DEV_SUCCESS;
+  if (e == cudaErrorMemoryAllocation) return DEV_ERR_DEVICE_ALLOC;
+  return DEV_ERR_UNKNOWN;
+}
+
+#define LCHK(expr)                                             \
+  do {                                                         \
+    cudaError_t e_ = (expr);                                   \
+    if (e_ != cudaSuccess) return set_err(cuda_code(e_));      \
+  } while (0)
+
+// ------------------------------------------------------------ device buffers
+void DBuf::free() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+int DBuf::ensure(size_t b) {
+  if (b <= bytes && p) return 0;
+  free();
+  if (b == 0) b = 16;
+  cudaError_t e = cudaMalloc(&p, b);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    cudaGetLastError();
+    return DEV_ERR_DEVICE_ALLOC;
+  }
+  bytes = b;
+  return 0;
+}
+int DBuf::upload(const void *h, size_t b, cudaStream_t s) {
+  int rc = ensure(b);
+  if (rc) return rc;
+  if (b) {
+    if (cudaMemcpyAsync(p, h, b, cudaMemcpyHostToDevice, s) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  }
+  return 0;
+}
+
+static size_t vsize(VType t) { return t == VType::F64 ? 8 : (t == VType::F32 ? 4 : 2); }
+
+// ---------------------------------------------------------- small kernels
+
+// Lv[p] = 1 on the diagonal (map -1), A value otherwise, in value type T
+template <typename T>
+__global__ void k_init_from_A(int count, const int *__restrict__ map, const double *__restrict__ Aval,
+                              int ld, T *__restrict__ out) {
+  // ld > 1: block values (map indexes blocks), diagonal blocks = identity
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)count * ld;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int p = (int)(q / ld), e = (int)(q % ld);
+    const int src = map[p];
+    double v;
+    if (src >= 0) v = Aval[(size_t)src * ld + e];
+    else {
+      int bs = 1;
+      while (bs * bs < ld) ++bs;
+      v = (e / bs == e % bs) ? 1.0 : 0.0;
+    }
+    out[q] = cvt<T>(v);
+  }
+}
+
+static void init_from_A(cudaStream_t s, int count, const int *map, const double *Aval, int ld,
+                        VType t, void *out) {
+  long long tot = (long long)count * ld;
+  int grid = (int)std::min<long long>((tot + 255) / 256, (long long)num_sms() * 16);
+  if (grid < 1) return;
+  switch (t) {
+    case VType::F64: k_init_from_A<double><<<grid, 256, 0, s>>>(count, map, Aval, ld, (double *)out); break;
+    case VType::F32: k_init_from_A<float><<<grid, 256, 0, s>>>(count, map, Aval, ld, (float *)out); break;
+    case VType::BF16: k_init_from_A<__nv_bfloat16><<<grid, 256, 0, s>>>(count, map, Aval, ld, (__nv_bfloat16 *)out); break;
+  }
+}
+
+// dLdA_ij = -lambda_i x_j on A's pattern (CSR order)
+__global__ void k_grad_A(int n, const int *__restrict__ row, const int *__restrict__ col,
+                         const double *__restrict__ lam, const double *__restrict__ x,
+                         double *__restrict__ g) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double li = lam[i];
+    for (int p = row[i]; p < row[i + 1]; ++p) g[p] = -li * x[col[p]];
+  }
+}
+
+// ------------------------------------------------------------- analysis
+
+int validate_csr(int n, int nnz, const int *row, const int *col) {
+  if (n < 0 || nnz < 0) return DEV_ERR_ILLEGAL_VALUE;
+  if (row[0] != 0 || row[n] != nnz) return DEV_ERR_ILLEGAL_VALUE;
+  for (int i = 0; i < n; ++i) {
+    if (row[i + 1] < row[i]) return DEV_ERR_ILLEGAL_VALUE;
+    bool diag = false;
+    for (int p = row[i]; p < row[i + 1]; ++p) {
+      if (col[p] < 0 || col[p] >= n) return DEV_ERR_ILLEGAL_VALUE;
+      if (p > row[i] && col[p] <= col[p - 1]) return DEV_ERR_NOT_SUPPORTED;  // unsorted / duplicate
+      if (col[p] == i) diag = true;
+    }
+    if (!diag) return DEV_ERR_NOT_SUPPORTED;  // ParILU needs every diagonal entry
+  }
+  return 0;
+}
+
+void transpose_pattern(const Pattern &P, Pattern &T, std::vector<int> &t2p) {
+  const int n = P.n;
+  T.n = n;
+  T.ptr.assign(n + 1, 0);
+  for (int i : P.idx) T.ptr[i + 1]++;
+  for (int i = 0; i < n; ++i) T.ptr[i + 1] += T.ptr[i];
+  T.idx.resize(P.idx.size());
+  t2p.resize(P.idx.size());
+  std::vector<int> fill(T.ptr.begin(), T.ptr.end() - 1);
+  for (int i = 0; i < n; ++i)
+    for (int p = P.ptr[i]; p < P.ptr[i + 1]; ++p) {
+      const int q = fill[P.idx[p]]++;
+      T.idx[q] = i;
+      t2p[q] = p;
+    }
+}
+
+// chunk kinds for the sync-free solve: 0 = every in-chunk dependency is the
+// previous row in solve order (affine scan), 1 = serial
+void chunk_kinds(const Pattern &T, bool lower, int R, std::vector<uint8_t> &kind) {
+  const int CS = 32 * R;
+  const int n = T.n;
+  const int nch = (n + CS - 1) / CS;
+  kind.assign(nch, 0);
+  for (int i = 0; i < n; ++i) {
+    const int c = i / CS;
+    const int prev = lower ? i - 1 : i + 1;
+    for (int p = T.ptr[i]; p < T.ptr[i + 1]; ++p) {
+      const int j = T.idx[p];
+      if (j == i) continue;
+      if (lower ? j > i : j < i) continue;
+      if (j / CS == c && j != prev) kind[c] = 1;
+    }
+  }
+}
+
+int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int> &lrows) {
+  const int n = T.n;
+  std::vector<int> lev(n, 0);
+  int nl = 0;
+  for (int k = 0; k < n; ++k) {
+    const int i = lower ? k : n - 1 - k;
+    int l = 0;
+    for (int p = T.ptr[i]; p < T.ptr[i + 1]; ++p) {
+      const int j = T.idx[p];
+      if (lower ? j < i : j > i) l = std::max(l, lev[j] + 1);
+    }
+    lev[i] = l;
+    nl = std::max(nl, l + 1);
+  }
+  lptr.assign(nl + 1, 0);
+  for (int i = 0; i < n; ++i) lptr[lev[i] + 1]++;
+  for (int l = 0; l < nl; ++l) lptr[l + 1] += lptr[l];
+  lrows.resize(n);
+  std::vector<int> fill(lptr.begin(), lptr.end() - 1);
+  for (int k = 0; k < n; ++k) {
+    const int i = lower ? k : n - 1 - k;
+    lrows[fill[lev[i]]++] = i;
+  }
+  return nl;
+}
+
+}  // namespace lace
+
+using namespace lace;
+
+// ======================================================================
+// context lifetime
+// ======================================================================
+
+extern "C" void lace_gpu_default_options(lace_gpu_options *o) {
+  o->precision = LACE_PREC_FP64;
+  o->trsv_mode = LACE_TRSV_SYNCFREE;
+  o->jacobi_sweeps = 8;
+  o->jacobi_tol = 0.0;
+  o->use_graph = 1;
+  o->spmv_lanes = 0;
+  o->trsv_rows_per_lane = 0;
+  o->monitor_orthog = 0;
+}
+
+extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream) {
+  if (!out) return set_err(DEV_ERR_INVALID_PTR);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(DEV_ERR_NOT_INITIALIZED);
+  }
+  if (device < 0 || device >= ndev) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  LCHK(cudaSetDevice(device));
+  lace_gpu_ctx *c = new lace_gpu_ctx();
+  c->device = device;
+  lace_gpu_default_options(&c->opt);
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return set_err(DEV_ERR_UNKNOWN);
+    }
+    c->own_stream = true;
+  }
+  if (c->ctrl_buf.ensure(sizeof(Control) * 2) || c->cycle_buf.ensure(sizeof(Cycle)) ||
+      c->scal_buf.ensure(64 * sizeof(double)) || c->cnt_buf.ensure(64 * sizeof(int))) {
+    delete c;
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  }
+  cudaMemsetAsync(c->ctrl_buf.p, 0, sizeof(Control) * 2, c->stream);
+  cudaMemsetAsync(c->cycle_buf.p, 0, sizeof(Cycle), c->stream);
+  cudaMemsetAsync(c->cnt_buf.p, 0, 64 * sizeof(int), c->stream);
+  if (cudaMallocHost(&c->h_ctrl, sizeof(Control)) != cudaSuccess ||
+      cudaMallocHost(&c->h_scal, 64 * sizeof(double)) != cudaSuccess) {
+    delete c;
+    return set_err(DEV_ERR_HOST_ALLOC);
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    delete c;
+    return set_err(DEV_ERR_UNKNOWN);
+  }
+  *out = c;
+  return DEV_SUCCESS;
+}
+
+lace_gpu_ctx::~lace_gpu_ctx() {
+  for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+  if (h_ctrl) cudaFreeHost(h_ctrl);
+  if (h_scal) cudaFreeHost(h_scal);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+extern "C" int lace_gpu_ctx_destroy(lace_gpu_ctx *c) {
+  if (!c) return DEV_SUCCESS;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  delete c;
+  return DEV_SUCCESS;
+}
+
+extern "C" void *lace_gpu_stream(lace_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+void lace_gpu_ctx::drop_graphs() {
+  for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+}
+
+extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) {
+  if (!c || !o) return set_err(DEV_ERR_INVALID_PTR);
+  if (o->precision < 0 || o->precision > 2 || o->trsv_mode < 0 || o->trsv_mode > 3)
+    return set_err(DEV_ERR_ILLEGAL_VALUE);
+  const bool prec_changed = o->precision != c->opt.precision;
+  c->opt = *o;
+  c->drop_graphs();
+  if (prec_changed) c->factors_ready = false;
+  if (o->trsv_rows_per_lane > 0) c->set_rows_per_lane(o->trsv_rows_per_lane);
+  if (o->spmv_lanes > 0) c->lanes = o->spmv_lanes;
+  return DEV_SUCCESS;
+}
+
+// ======================================================================
+// upload + analysis
+// ======================================================================
+
+int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
+  n_blk = n_;
+  bs = bs_;
+  Pattern A;
+  A.n = n_;
+  A.ptr.assign(row, row + n_ + 1);
+  A.idx.assign(col, col + row[n_]);
+  // L = strict lower + diagonal last (CSRL), U = diagonal + upper (CSRU)
+  Pattern L, Ur;
+  L.n = Ur.n = n_;
+  L.ptr.assign(n_ + 1, 0);
+  Ur.ptr.assign(n_ + 1, 0);
+  std::vector<int> l2a, ur2a;
+  for (int i = 0; i < n_; ++i) {
+    int dpos = -1;
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
+      const int j = A.idx[p];
+      if (j < i) {
+        L.idx.push_back(j);
+        l2a.push_back(p);
+      } else if (j == i) {
+        dpos = p;
+      }
+    }
+    L.idx.push_back(i);
+    l2a.push_back(-1);  // unit diagonal
+    L.ptr[i + 1] = (int)L.idx.size();
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
+      const int j = A.idx[p];
+      if (j > i || p == dpos) {
+        Ur.idx.push_back(j);
+        ur2a.push_back(p);
+      }
+    }
+    Ur.ptr[i + 1] = (int)Ur.idx.size();
+  }
+  int rc = analyse_factors(L, Ur);
+  if (rc) return rc;
+  std::vector<int> uc2a(hUc.idx.size());
+  for (size_t q = 0; q < uc2a.size(); ++q) uc2a[q] = ur2a[uc2ur_h[q]];
+  rc |= map_l2a.upload(l2a.data(), 4 * l2a.size(), stream);
+  rc |= map_uc2a.upload(uc2a.data(), 4 * uc2a.size(), stream);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  AT_ready = false;
+  return 0;
+}
+
+// factor patterns L (CSRL) and U (CSRU) -> CSC of U, L^T, maps, chunk kinds,
+// level sets, ready flags
+int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
+  Pattern Uc, Lt;
+  std::vector<int> lt2l;
+  transpose_pattern(Ur, Uc, uc2ur_h);
+  transpose_pattern(L, Lt, lt2l);
+  std::vector<int> ur2uc(uc2ur_h.size());
+  for (size_t q = 0; q < uc2ur_h.size(); ++q) ur2uc[uc2ur_h[q]] = (int)q;
+  nnzL = (int)L.idx.size();
+  nnzU = (int)Ur.idx.size();
+  hL = L;
+  hU = Ur;
+  hUc = Uc;
+  hLt = Lt;
+  map_ur2uc_el.free();
+  int rc = 0;
+  rc |= Lrow.upload(L.ptr.data(), 4 * L.ptr.size(), stream);
+  rc |= Lcol.upload(L.idx.data(), 4 * L.idx.size(), stream);
+  rc |= Ucp.upload(Uc.ptr.data(), 4 * Uc.ptr.size(), stream);
+  rc |= Uri.upload(Uc.idx.data(), 4 * Uc.idx.size(), stream);
+  rc |= Urow.upload(Ur.ptr.data(), 4 * Ur.ptr.size(), stream);
+  rc |= Ucol.upload(Ur.idx.data(), 4 * Ur.idx.size(), stream);
+  rc |= Ltp.upload(Lt.ptr.data(), 4 * Lt.ptr.size(), stream);
+  rc |= Lti.upload(Lt.idx.data(), 4 * Lt.idx.size(), stream);
+  rc |= map_ur2uc.upload(ur2uc.data(), 4 * ur2uc.size(), stream);
+  rc |= map_lt2l.upload(lt2l.data(), 4 * lt2l.size(), stream);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  // level sets of the four triangles (level-scheduled option + reporting)
+  const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
+  const bool low[4] = {true, false, true, false};
+  for (int t = 0; t < 4; ++t) {
+    std::vector<int> lp, lr;
+    nlevels[t] = levels(*pats[t], low[t], lp, lr);
+    rc |= lvl_ptr[t].upload(lp.data(), 4 * lp.size(), stream);
+    rc |= lvl_rows[t].upload(lr.data(), 4 * lr.size(), stream);
+    // ready flags: one per chunk at the smallest chunk size; zero = never set
+    const int maxch = (L.n + 31) / 32 + 1;
+    rc |= ready[t].ensure(4 * (size_t)maxch);
+    if (!rc) cudaMemsetAsync(ready[t].p, 0, 4 * (size_t)maxch, stream);
+    for (int ri = 0; ri < 4; ++ri) {
+      const int R = 1 << ri;
+      std::vector<uint8_t> k;
+      chunk_kinds(*pats[t], low[t], R, k);
+      rc |= kinds[t][ri].upload(k.data(), k.size(), stream);
+    }
+  }
+  // the epochs of the new ready arrays restart with the zeroed flags
+  Control zero;
+  memset(&zero, 0, sizeof(zero));
+  cudaMemsetAsync(ctrl_buf.p, 0, sizeof(Control) * 2, stream);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  factors_ready = false;
+  trsv_tuned = false;
+  ws_m = 0;
+  drop_graphs();
+  return 0;
+}
+
+// caller-supplied factors (host, FP64): L CSRL, U CSR (diagonal first).  The
+// factor analysis is redone only when the patterns differ from the current
+// ones.  Values are stored in the context's precision.
+int lace_gpu_ctx::set_factors_host(int nrows, const int *lrow, const int *lcol, const double *lval,
+                                   const int *urow, const int *ucol, const double *uval) {
+  if (bs) return DEV_ERR_NOT_SUPPORTED;
+  Pattern L, Ur;
+  L.n = Ur.n = nrows;
+  L.ptr.assign(lrow, lrow + nrows + 1);
+  L.idx.assign(lcol, lcol + lrow[nrows]);
+  Ur.ptr.assign(urow, urow + nrows + 1);
+  Ur.idx.assign(ucol, ucol + urow[nrows]);
+  // structural requirements of the solves: L diagonal last, U diagonal first
+  for (int i = 0; i < nrows; ++i) {
+    if (L.ptr[i + 1] <= L.ptr[i] || L.idx[L.ptr[i + 1] - 1] != i) return DEV_ERR_NOT_SUPPORTED;
+    if (Ur.ptr[i + 1] <= Ur.ptr[i] || Ur.idx[Ur.ptr[i]] != i) return DEV_ERR_NOT_SUPPORTED;
+    for (int p = L.ptr[i]; p < L.ptr[i + 1] - 1; ++p)
+      if (L.idx[p] >= i || (p > L.ptr[i] && L.idx[p] <= L.idx[p - 1])) return DEV_ERR_NOT_SUPPORTED;
+    for (int p = Ur.ptr[i] + 1; p < Ur.ptr[i + 1]; ++p)
+      if (Ur.idx[p] <= Ur.idx[p - 1] || Ur.idx[p] >= nrows) return DEV_ERR_NOT_SUPPORTED;
+  }
+  const bool same = (L.ptr == hL.ptr && L.idx == hL.idx && Ur.ptr == hU.ptr && Ur.idx == hU.idx);
+  if (!same) {
+    int rc = analyse_factors(L, Ur);
+    if (rc) return rc;
+  }
+  int rc = alloc_factor_values();
+  if (rc) return rc;
+  const VType t = vtype();
+  DBuf tl, tu;
+  if (tl.upload(lval, 8 * (size_t)nnzL, stream) || tu.upload(uval, 8 * (size_t)nnzU, stream))
+    return DEV_ERR_DEVICE_ALLOC;
+  cur = 0;
+  launch_convert(stream, nnzL, VType::F64, tl.p, t, Lv[0].p);
+  launch_convert(stream, nnzU, VType::F64, tu.p, t, Urv.p);
+  // CSC image of U and L^T from the CSR values
+  std::vector<int> uc2ur = uc2ur_h;
+  DBuf m;
+  if (m.upload(uc2ur.data(), 4 * uc2ur.size(), stream)) return DEV_ERR_DEVICE_ALLOC;
+  launch_gather(stream, nnzU, (const int *)m.p, VType::F64, tu.p, t, Ucv[0].p);
+  launch_gather(stream, nnzL, (const int *)map_lt2l.p, VType::F64, tl.p, t, Ltv.p);
+  factors_ready = true;
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  return 0;
+}
+
+void lace_gpu_ctx::set_rows_per_lane(int R) {
+  if (R != 1 && R != 2 && R != 4 && R != 8) R = 4;
+  rows_per_lane = R;
+  drop_graphs();
+}
+
+TriDev lace_gpu_ctx::tri(int which) const {
+  // which: 0 L, 1 U, 2 U^T, 3 L^T
+  TriDev t;
+  t.n = bs ? n_blk * bs : n_blk;
+  t.slot = which;
+  t.ready = (int *)ready[which].p;
+  int ri = 0;
+  while ((1 << ri) < rows_per_lane) ++ri;
+  t.kind = (const uint8_t *)kinds[which][ri].p;
+  t.rows_per_lane = rows_per_lane;
+  t.nchunks = (n_blk + 32 * rows_per_lane - 1) / (32 * rows_per_lane);
+  t.lvl_ptr = (const int *)lvl_ptr[which].p;
+  t.lvl_rows = (const int *)lvl_rows[which].p;
+  t.nlevels = nlevels[which];
+  switch (which) {
+    case 0: t.row = (const int *)Lrow.p; t.col = (const int *)Lcol.p; t.val = Lv[cur].p; t.lower = 1; t.unit = 1; t.nnz = nnzL; break;
+    case 1: t.row = (const int *)Urow.p; t.col = (const int *)Ucol.p; t.val = Urv.p; t.lower = 0; t.unit = 0; t.nnz = nnzU; break;
+    case 2: t.row = (const int *)Ucp.p; t.col = (const int *)Uri.p; t.val = Ucv[cur].p; t.lower = 1; t.unit = 0; t.nnz = nnzU; break;
+    default: t.row = (const int *)Ltp.p; t.col = (const int *)Lti.p; t.val = Ltv.p; t.lower = 0; t.unit = 1; t.nnz = nnzL; break;
+  }
+  return t;
+}
+
+int lace_gpu_ctx::upload_common(int n_, int nnz_, const int *hrow, const int *hcol, int bs_) {
+  int rc = analyse(n_, hrow, hcol, bs_);
+  if (rc) return rc;
+  n = bs_ ? n_ * bs_ : n_;
+  nnzA = nnz_;
+  // Frobenius norm of A (data_zfrobenius) - computed on upload from device values
+  return 0;
+}
+
+extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const int *row,
+                                        const int *col, const double *val) {
+  if (!c || !row || (nnz > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
+  cudaSetDevice(c->device);
+  int rc = validate_csr(n, nnz, row, col);
+  if (rc) return set_err(rc);
+  if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) || c->Acol.upload(col, 4 * (size_t)nnz, c->stream) ||
+      c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  rc = c->upload_common(n, nnz, row, col, 0);
+  if (rc) return set_err(rc);
+  double s = 0.0;
+  for (int p = 0; p < nnz; ++p) s += val[p] * val[p];
+  c->anorm = std::sqrt(s);
+  c->AT_ready = false;
+  LCHK(cudaStreamSynchronize(c->stream));
+  return c->autotune_spmv();
+}
+
+extern "C" int lace_gpu_upload_csr_device(lace_gpu_ctx *c, int n, int nnz, const int *row,
+                                          const int *col, const double *val) {
+  if (!c || !row || (nnz > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
+  cudaSetDevice(c->device);
+  std::vector<int> hrow(n + 1), hcol(nnz);
+  std::vector<double> hval(nnz);
+  LCHK(cudaMemcpy(hrow.data(), row, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost));
+  LCHK(cudaMemcpy(hcol.data(), col, 4 * (size_t)nnz, cudaMemcpyDeviceToHost));
+  LCHK(cudaMemcpy(hval.data(), val, 8 * (size_t)nnz, cudaMemcpyDeviceToHost));
+  return lace_gpu_upload_csr_host(c, n, nnz, hrow.data(), hcol.data(), hval.data());
+}
+
+extern "C" int lace_gpu_upload_bcsr_host(lace_gpu_ctx *c, int nb, int bs, int nblk, const int *row,
+                                         const int *col, const double *val) {
+  if (!c || !row || (nblk > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
+  if (bs < 1 || bs > 8) return set_err(DEV_ERR_NOT_SUPPORTED);
+  cudaSetDevice(c->device);
+  int rc = validate_csr(nb, nblk, row, col);
+  if (rc) return set_err(rc);
+  const size_t ld = (size_t)bs * bs;
+  if (c->Arow.upload(row, 4 * (size_t)(nb + 1), c->stream) || c->Acol.upload(col, 4 * (size_t)nblk, c->stream) ||
+      c->Aval.upload(val, 8 * (size_t)nblk * ld, c->stream))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
+  rc = c->upload_common(nb, nblk, row, col, bs);
+  if (rc) return set_err(rc);
+  double s = 0.0;
+  for (size_t p = 0; p < (size_t)nblk * ld; ++p) s += val[p] * val[p];
+  c->anorm = std::sqrt(s);
+  c->AT_ready = false;
+  if (c->opt.trsv_rows_per_lane <= 0) c->rows_per_lane = 1;  // BCSR chunks: block rows
+  LCHK(cudaStreamSynchronize(c->stream));
+  return DEV_SUCCESS;
+}
+
+extern "C" int lace_gpu_update_values_device(lace_gpu_ctx *c, const double *val) {
+  if (!c || !val) return set_err(DEV_ERR_INVALID_PTR);
+  const size_t ld = c->bs ? (size_t)c->bs * c->bs : 1;
+  LCHK(cudaMemcpyAsync(c->Aval.p, val, 8 * (size_t)c->nnzA * ld, cudaMemcpyDeviceToDevice, c->stream));
+  // ||A||_F on the device
+  double *partials = (double *)c->part_ensure();
+  if (!partials) return set_err(DEV_ERR_DEVICE_ALLOC);
+  launch_sqdiff(c->stream, (int)(c->nnzA * ld), c->Aval.p, c->zeros(c->nnzA * ld), 0, partials,
+                (int *)c->cnt_buf.p + 8, (double *)c->scal_buf.p + 8);
+  LCHK(cudaMemcpyAsync(c->h_scal + 8, (double *)c->scal_buf.p + 8, 8, cudaMemcpyDeviceToHost, c->stream));
+  LCHK(cudaStreamSynchronize(c->stream));
+  c->anorm = std::sqrt(c->h_scal[8]);
+  c->factors_ready = false;
+  c->AT_ready = false;
+  return DEV_SUCCESS;
+}
+
+void *lace_gpu_ctx::part_ensure() {
+  const size_t need = sizeof(double) * (size_t)(num_sms() * 16 + 8) * kLdT;
+  if (part_buf.ensure(need)) return nullptr;
+  return part_buf.p;
+}
+
+const void *lace_gpu_ctx::zeros(size_t count) {
+  if (zero_buf.bytes < count * 8) {
+    if (zero_buf.ensure(count * 8)) return nullptr;
+    cudaMemsetAsync(zero_buf.p, 0, count * 8, stream);
+  }
+  return zero_buf.p;
+}
+
+int lace_gpu_ctx::autotune_spmv() {
+  if (opt.spmv_lanes > 0) {
+    lanes = opt.spmv_lanes;
+    return DEV_SUCCESS;
+  }
+  if (bs) return DEV_SUCCESS;
+  const double avg = n_blk ? (double)nnzA / n_blk : 1.0;
+  // signature cache: rows, nnz, rounded average row length
+  auto key = std::make_tuple(n_blk, nnzA);
+  static std::map<std::tuple<int, int>, int> cache;
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    lanes = it->second;
+    return DEV_SUCCESS;
+  }
+  int cand[5] = {2, 4, 8, 16, 32};
+  DBuf xb, yb;
+  if (xb.ensure(8 * (size_t)n_blk) || yb.ensure(8 * (size_t)n_blk)) return set_err(DEV_ERR_DEVICE_ALLOC);
+  cudaMemsetAsync(xb.p, 0, 8 * (size_t)n_blk, stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bestl = avg > 12 ? 16 : 8;
+  for (int ci = 0; ci < 5; ++ci) {
+    const int L = cand[ci];
+    if (L > 4 * std::max(1.0, avg) && L > 4) continue;
+    launch_spmv_f64x(stream, L, n_blk, (const int *)Arow.p, (const int *)Acol.p, (const double *)Aval.p,
+                     (const double *)xb.p, 1.0, 0.0, (double *)yb.p);
+    cudaEventRecord(e0, stream);
+    for (int r = 0; r < 3; ++r)
+      launch_spmv_f64x(stream, L, n_blk, (const int *)Arow.p, (const int *)Acol.p,
+                       (const double *)Aval.p, (const double *)xb.p, 1.0, 0.0, (double *)yb.p);
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      bestl = L;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  lanes = bestl;
+  cache[key] = bestl;
+  return cudaGetLastError() == cudaSuccess ? DEV_SUCCESS : set_err(DEV_ERR_UNKNOWN);
+}
+
+// ======================================================================
+// ParILU
+// ======================================================================
+
+VType lace_gpu_ctx::vtype() const {
+  return opt.precision == LACE_PREC_FP64 ? VType::F64 : (opt.precision == LACE_PREC_FP32 ? VType::F32 : VType::BF16);
+}
+
+int lace_gpu_ctx::alloc_factor_values() {
+  const VType t = vtype();
+  const size_t ld = bs ? (size_t)bs * bs : 1;
+  const size_t s = vsize(t);
+  int rc = 0;
+  for (int k = 0; k < 2; ++k) {
+    rc |= Lv[k].ensure(s * nnzL * ld);
+    rc |= Ucv[k].ensure(s * nnzU * ld);
+  }
+  rc |= Urv.ensure(s * nnzU * ld);
+  rc |= Ltv.ensure(s * nnzL * ld);
+  if (bs) rc |= dinv.ensure(s * (size_t)n_blk * ld);
+  return rc ? DEV_ERR_DEVICE_ALLOC : 0;
+}
+
+IluArgs lace_gpu_ctx::ilu_args() {
+  IluArgs a;
+  a.n = n_blk;
+  a.nnzA = nnzA;
+  a.Arow = (const int *)Arow.p;
+  a.Acol = (const int *)Acol.p;
+  a.Aval = (const double *)Aval.p;
+  a.Lrow = (const int *)Lrow.p;
+  a.Lcol = (const int *)Lcol.p;
+  a.Ucp = (const int *)Ucp.p;
+  a.Uri = (const int *)Uri.p;
+  a.bs = bs;
+  a.partials = (double *)part_ensure();
+  a.counter = (int *)cnt_buf.p;
+  return a;
+}
+
+// values for the solves from the sweep buffers: U CSR (gather), L^T (gather),
+// BCSR diagonal inverses
+int lace_gpu_ctx::finish_factors() {
+  const VType t = vtype();
+  const int ld = bs ? bs * bs : 1;
+  if (bs == 0) {
+    launch_gather(stream, nnzU, (const int *)map_ur2uc.p, t, Ucv[cur].p, t, Urv.p);
+    launch_gather(stream, nnzL, (const int *)map_lt2l.p, t, Lv[cur].p, t, Ltv.p);
+  } else {
+    // block values move as ld-element records: gather each component
+    std::vector<int> dummy;
+    // expand block maps into element maps once
+    if (!map_ur2uc_el.p) {
+      std::vector<int> m(hU.idx.size() * ld);
+      std::vector<int> ur2uc(hU.idx.size());
+      cudaMemcpy(ur2uc.data(), map_ur2uc.p, 4 * ur2uc.size(), cudaMemcpyDeviceToHost);
+      for (size_t p = 0; p < ur2uc.size(); ++p)
+        for (int e = 0; e < ld; ++e) m[p * ld + e] = ur2uc[p] * ld + e;
+      if (map_ur2uc_el.upload(m.data(), 4 * m.size(), stream)) return DEV_ERR_DEVICE_ALLOC;
+    }
+    launch_gather(stream, nnzU * ld, (const int *)map_ur2uc_el.p, t, Ucv[cur].p, t, Urv.p);
+    launch_block_diag_inverse(stream, n_blk, bs, (const int *)Urow.p, t, Urv.p, dinv.p,
+                              &ctrl()->status);
+  }
+  factors_ready = true;
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+int lace_gpu_ctx::init_factors() {
+  int rc = alloc_factor_values();
+  if (rc) return rc;
+  const VType t = vtype();
+  const int ld = bs ? bs * bs : 1;
+  for (int k = 0; k < 2; ++k) {
+    init_from_A(stream, nnzL, (const int *)map_l2a.p, (const double *)Aval.p, ld, t, Lv[k].p);
+    init_from_A(stream, nnzU, (const int *)map_uc2a.p, (const double *)Aval.p, ld, t, Ucv[k].p);
+  }
+  cur = 0;
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
+                         std::vector<double> *steps, double stop_below) {
+  if (!n_blk) return DEV_ERR_NOT_INITIALIZED;
+  int rc = init_factors();
+  if (rc) return rc;
+  IluArgs a = ilu_args();
+  if (!a.partials) return DEV_ERR_DEVICE_ALLOC;
+  const VType t = vtype();
+  double *dstep = (double *)scal_buf.p;  // [0..] per sweep
+  for (int s = 0; s < sweeps; ++s) {
+    launch_parilu_sweep(stream, a, t, Lv[cur].p, Lv[1 - cur].p, Ucv[cur].p, Ucv[1 - cur].p,
+                        dstep + (s % 32));
+    cur = 1 - cur;
+    if (sync_each || s % 32 == 31 || s == sweeps - 1) {
+      const int cnt = s % 32 + 1;
+      LCHK(cudaMemcpyAsync(h_scal, dstep, 8 * cnt, cudaMemcpyDeviceToHost, stream));
+      LCHK(cudaStreamSynchronize(stream));
+      if (steps)
+        for (int k = 0; k < cnt; ++k) steps->push_back(h_scal[k] / anorm);
+      if (step_out) *step_out = h_scal[cnt - 1] / anorm;
+      if (sync_each && !(h_scal[cnt - 1] / anorm > stop_below)) break;
+    }
+  }
+  rc = finish_factors();
+  if (rc) return rc;
+  if (nonlin_out) {
+    if (bs) {
+      *nonlin_out = NAN;  // block residual is not formed on the GPU
+    } else {
+      launch_ilu_residual(stream, a, t, Lv[cur].p, Ucv[cur].p, (double *)scal_buf.p + 40);
+      LCHK(cudaMemcpyAsync(h_scal + 40, (double *)scal_buf.p + 40, 8, cudaMemcpyDeviceToHost, stream));
+      LCHK(cudaStreamSynchronize(stream));
+      *nonlin_out = std::sqrt(h_scal[40]) / anorm;
+    }
+  }
+  LCHK(cudaStreamSynchronize(stream));
+  if (h_status() & kStatusBreakdown) return DEV_ERR_BADPRECOND;
+  return DEV_SUCCESS;
+}
+
+int lace_gpu_ctx::h_status() {
+  int st = 0;
+  cudaMemcpy(&st, &ctrl()->status, 4, cudaMemcpyDeviceToHost);
+  return st;
+}
+
+extern "C" int lace_gpu_parilu0(lace_gpu_ctx *c, int sweeps, double *step_out, double *nonlin_out) {
+  if (!c) return set_err(DEV_ERR_INVALID_PTR);
+  if (sweeps < 0) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  cudaSetDevice(c->device);
+  int rc = c->parilu(sweeps, step_out, nonlin_out, false, nullptr);
+  return rc ? set_err(rc) : DEV_SUCCESS;
+}
+
+// ======================================================================
+// SpMV / SpTRSV
+// ======================================================================
+
+extern "C" int lace_gpu_spmv(lace_gpu_ctx *c, double alpha, const double *x, double beta, double *y) {
+  if (!c || !x || !y) return set_err(DEV_ERR_INVALID_PTR);
+  if (!c->n_blk) return set_err(DEV_ERR_NOT_INITIALIZED);
+  if (c->bs)
+    launch_bcsr_spmv(c->stream, c->n_blk, c->bs, (const int *)c->Arow.p, (const int *)c->Acol.p,
+                     (const double *)c->Aval.p, x, alpha, beta, y);
+  else
+    launch_spmv_f64x(c->stream, c->lanes, c->n_blk, (const int *)c->Arow.p, (const int *)c->Acol.p,
+                     (const double *)c->Aval.p, x, alpha, beta, y);
+  LCHK(cudaGetLastError());
+  return DEV_SUCCESS;
+}
+
+// one triangle solve with the configured mode; in/out typed
+int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int out_f32,
+                            bool honor_done, void *tmp) {
+  TriDev t = tri(which);
+  const VType vt = vtype();
+  Control *cb = ctrl();
+  switch (opt.trsv_mode) {
+    case LACE_TRSV_LEVELS:
+      if (bs) return DEV_ERR_NOT_SUPPORTED;
+      launch_sptrsv_levels(stream, t, vt, b, in_f32, x, out_f32, cb, honor_done);
+      break;
+    case LACE_TRSV_JACOBI: {
+      if (bs) return DEV_ERR_NOT_SUPPORTED;
+      // sweeps from y = 0 (LACE starts from a zeroed vector); ping-pong so
+      // that the last sweep lands in x
+      const int k = std::max(1, opt.jacobi_sweeps);
+      void *bufs[2] = {tmp, x};
+      int w = (k % 2 == 1) ? 1 : 0;  // first write target so that sweep k-1 writes x
+      const void *yold = nullptr;
+      for (int s = 0; s < k; ++s) {
+        launch_jacobi_sweep(stream, t, vt, b, in_f32, yold, bufs[w], out_f32, cb, honor_done);
+        yold = bufs[w];
+        w = 1 - w;
+      }
+      break;
+    }
+    case LACE_TRSV_NONE:
+      launch_convert(stream, n, in_f32 ? VType::F32 : VType::F64, b, out_f32 ? VType::F32 : VType::F64, x);
+      break;
+    default:
+      if (bs)
+        launch_bcsr_sptrsv(stream, t, bs, vt, which == 1 ? dinv.p : nullptr, b, in_f32, x, out_f32, cb,
+                           0, honor_done);
+      else
+        launch_sptrsv_syncfree(stream, t, vt, b, in_f32, x, out_f32, cb, 0, honor_done);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+int lace_gpu_ctx::ensure_vectors() {
+  const size_t ldv_ = ((size_t)n + 31) / 32 * 32;
+  int rc = 0;
+  rc |= vec_w.ensure(8 * ldv_);
+  rc |= vec_q.ensure(8 * ldv_);
+  rc |= vec_t.ensure(8 * ldv_);
+  rc |= vec_t2.ensure(8 * ldv_);
+  rc |= vec_r.ensure(8 * ldv_);
+  return rc ? DEV_ERR_DEVICE_ALLOC : 0;
+}
+
+int lace_gpu_ctx::autotune_trsv() {
+  if (bs || opt.trsv_mode != LACE_TRSV_SYNCFREE) return 0;
+  if (opt.trsv_rows_per_lane > 0) {
+    rows_per_lane = opt.trsv_rows_per_lane;
+    return 0;
+  }
+  if (trsv_tuned) return 0;
+  int rc = ensure_vectors();
+  if (rc) return rc;
+  const bool f32 = vtype() != VType::F64;
+  cudaMemsetAsync(vec_q.p, 0, 8 * (size_t)n, stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bestR = 4;
+  for (int R : {1, 2, 4, 8}) {
+    rows_per_lane = R;
+    solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+    cudaEventRecord(e0, stream);
+    for (int r = 0; r < 2; ++r) {
+      solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+      solve_tri(1, vec_t.p, f32, vec_t2.p, f32, false, vec_r.p);
+    }
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      bestR = R;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  rows_per_lane = bestR;
+  trsv_tuned = true;
+  drop_graphs();
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+extern "C" int lace_gpu_sptrsv(lace_gpu_ctx *c, int which, const double *b, double *x) {
+  if (!c || !b || !x) return set_err(DEV_ERR_INVALID_PTR);
+  if (which < 0 || which > 3) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  if (!c->factors_ready) return set_err(DEV_ERR_NOT_INITIALIZED);
+  if (c->bs && which > 1) return set_err(DEV_ERR_NOT_SUPPORTED);
+  cudaSetDevice(c->device);
+  int rc = c->ensure_vectors();
+  if (!rc) rc = c->autotune_trsv();
+  if (rc) return set_err(rc);
+  const bool f32 = c->vtype() != VType::F64;
+  if (f32) {
+    rc = c->solve_tri(which, b, 0, c->vec_t.p, 1, false, c->vec_t2.p);
+    if (!rc) launch_convert(c->stream, c->n, VType::F32, c->vec_t.p, VType::F64, x);
+  } else {
+    rc = c->solve_tri(which, b, 0, x, 0, false, c->vec_t2.p);
+  }
+  if (rc) return set_err(rc);
+  LCHK(cudaStreamSynchronize(c->stream));
+  int st = c->h_status();
+  if (st & kStatusSpinTimeout) return set_err(DEV_ERR_INTERNAL_LIMIT);
+  return DEV_SUCCESS;
+}
+
+extern "C" int lace_gpu_apply_precond(lace_gpu_ctx *c, const double *q, double *z) {
+  if (!c || !q || !z) return set_err(DEV_ERR_INVALID_PTR);
+  if (!c->factors_ready) return set_err(DEV_ERR_NOT_INITIALIZED);
+  cudaSetDevice(c->device);
+  int rc = c->ensure_vectors();
+  if (!rc) rc = c->autotune_trsv();
+  if (rc) return set_err(rc);
+  const int f32 = c->vtype() != VType::F64;
+  rc = c->solve_tri(0, q, 0, c->vec_t.p, f32, false, c->vec_t2.p);
+  if (!rc) {
+    if (f32) {
+      rc = c->solve_tri(1, c->vec_t.p, 1, c->vec_r.p, 1, false, c->vec_t2.p);
+      launch_convert(c->stream, c->n, VType::F32, c->vec_r.p, VType::F64, z);
+    } else {
+      rc = c->solve_tri(1, c->vec_t.p, 0, z, 0, false, c->vec_t2.p);
+    }
+  }
+  if (rc) return set_err(rc);
+  LCHK(cudaStreamSynchronize(c->stream));
+  if (c->h_status() & kStatusSpinTimeout) return set_err(DEV_ERR_INTERNAL_LIMIT);
+  return DEV_SUCCESS;
+}
+
+// ======================================================================
+// FGMRES-Householder
+// ======================================================================
+
+int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
+  int rc = ensure_vectors();
+  if (rc) return rc;
+  const bool zf32 = vtype() != VType::F64;
+  ldv = ((size_t)n + 31) / 32 * 32;
+  if (m > ws_m || zf32 != ws_zf32) {
+    drop_graphs();
+    rc |= Vb.ensure(8 * ldv * (size_t)(m + 1));
+    rc |= Zb.ensure((zf32 ? 4 : 8) * ldv * (size_t)m);
+    if (rc) return DEV_ERR_DEVICE_ALLOC;
+    ws_m = m;
+    ws_zf32 = zf32;
+  }
+  if (monitor && Qmon.bytes < 8 * ldv * (size_t)(m + 1)) {
+    drop_graphs();
+    if (Qmon.ensure(8 * ldv * (size_t)(m + 1))) return DEV_ERR_DEVICE_ALLOC;
+  }
+  if (!part_ensure()) return DEV_ERR_DEVICE_ALLOC;
+  return 0;
+}
+
+int lace_gpu_ctx::ensure_AT() {
+  if (AT_ready) return 0;
+  if (bs) return DEV_ERR_NOT_SUPPORTED;
+  Pattern A, T;
+  A.n = n_blk;
+  A.ptr.resize(n_blk + 1);
+  A.idx.resize(nnzA);
+  cudaMemcpy(A.ptr.data(), Arow.p, 4 * (size_t)(n_blk + 1), cudaMemcpyDeviceToHost);
+  cudaMemcpy(A.idx.data(), Acol.p, 4 * (size_t)nnzA, cudaMemcpyDeviceToHost);
+  std::vector<int> t2a;
+  transpose_pattern(A, T, t2a);
+  int rc = 0;
+  rc |= ATrow.upload(T.ptr.data(), 4 * T.ptr.size(), stream);
+  rc |= ATcol.upload(T.idx.data(), 4 * T.idx.size(), stream);
+  rc |= map_at2a.upload(t2a.data(), 4 * t2a.size(), stream);
+  rc |= ATval.ensure(8 * (size_t)nnzA);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  launch_gather(stream, nnzA, (const int *)map_at2a.p, VType::F64, Aval.p, VType::F64, ATval.p);
+  AT_ready = true;
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
+  ArnoldiArgs a;
+  a.n = n;
+  a.bs = bs;
+  if (adjoint) {
+    a.row = (const int *)ATrow.p;
+    a.col = (const int *)ATcol.p;
+    a.val = (const double *)ATval.p;
+  } else {
+    a.row = (const int *)Arow.p;
+    a.col = (const int *)Acol.p;
+    a.val = (const double *)Aval.p;
+  }
+  a.lanes = lanes;
+  a.V = (double *)Vb.p;
+  a.ldv = ldv;
+  a.Z = Zb.p;
+  a.ldz = ldv;
+  a.z_f32 = ws_zf32 ? 1 : 0;
+  a.w = (double *)vec_w.p;
+  a.q = (double *)vec_q.p;
+  a.partials = (double *)part_buf.p;
+  a.grid = num_sms() * 4;
+  a.cy = (Cycle *)cycle_buf.p;
+  a.ctrl = ctrl();
+  a.m = m;
+  return a;
+}
+
+// the search-direction loop of one cycle (LACE :311-759), all on the device
+int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) {
+  const int t1 = adjoint ? 2 : 0, t2 = adjoint ? 3 : 1;
+  const int f32 = a.z_f32;
+  for (int j = 0; j < m; ++j) {
+    void *zj = (char *)a.Z + (size_t)j * a.ldz * (f32 ? 4 : 8);
+    int rc = solve_tri(t1, a.q, 0, vec_t.p, f32, true, vec_t2.p);
+    if (!rc) rc = solve_tri(t2, vec_t.p, f32, zj, f32, true, vec_t2.p);
+    if (rc) return rc;
+    launch_passA(stream, a, j);
+    launch_passB(stream, a, j);
+    launch_passC(stream, a, j);
+    if (opt.monitor_orthog && Qmon.p) {
+      // q_{j+1} into the monitor basis, then ||I - Q^T Q|| over q_0..q_j
+      cudaMemcpyAsync((double *)Qmon.p + (size_t)(j + 1) * ldv, a.q, 8 * (size_t)n,
+                      cudaMemcpyDeviceToDevice, stream);
+      launch_orthog_monitor(stream, a, j, (double *)Qmon.p, ldv);
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
+int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int tol_type,
+                         double rtol, bool adjoint, data_d_gmres_log *log, int *total_iters,
+                         std::vector<double> *hist) {
+  if (m < 1 || m > kMaxM) return DEV_ERR_NOT_SUPPORTED;
+  if (!factors_ready && opt.trsv_mode != LACE_TRSV_NONE) return DEV_ERR_NOT_INITIALIZED;
+  int rc = ensure_krylov(m, opt.monitor_orthog != 0);
+  if (!rc) rc = autotune_trsv();
+  if (!rc && adjoint) rc = ensure_AT();
+  if (rc) return rc;
+  ArnoldiArgs a = arnoldi_args(m, adjoint);
+  Cycle *cy = a.cy;
+  // tolerance set-up scalars
+  {
+    struct {
+      int tol_type, first;
+      double rtol;
+    } hs = {tol_type, 1, rtol};
+    LCHK(cudaMemcpyAsync(&cy->tol_type, &hs.tol_type, 4, cudaMemcpyHostToDevice, stream));
+    LCHK(cudaMemcpyAsync(&cy->first_cycle, &hs.first, 4, cudaMemcpyHostToDevice, stream));
+    LCHK(cudaMemcpyAsync(&cy->rtol, &hs.rtol, 8, cudaMemcpyHostToDevice, stream));
+    int zero = 0;
+    LCHK(cudaMemcpyAsync(&a.ctrl->status, &zero, 4, cudaMemcpyHostToDevice, stream));
+  }
+  const auto key = std::make_tuple(m, adjoint ? 1 : 0, opt.trsv_mode, rows_per_lane,
+                                   opt.jacobi_sweeps, (int)vtype(), opt.monitor_orthog, lanes);
+  int total = 0;
+  bool converged = false;
+  int last_cycle = 0, last_steps = 0;
+  double rnorm0 = 0.0, final_res = 0.0;
+  for (int restart = 0; restart < restart_max; ++restart) {
+    launch_cycle_residual(stream, a, b, x);
+    launch_cycle_init(stream, a);
+    if (opt.monitor_orthog && Qmon.p)
+      cudaMemcpyAsync(Qmon.p, a.q, 8 * (size_t)n, cudaMemcpyDeviceToDevice, stream);
+    if (opt.use_graph) {
+      auto it = graphs.find(key);
+      if (it == graphs.end()) {
+        cudaGraph_t g;
+        LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_cycle_body(a, m, adjoint);
+        cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        if (rc) {
+          if (ce == cudaSuccess) cudaGraphDestroy(g);
+          return rc;
+        }
+        LCHK(ce);
+        cudaGraphExec_t ge;
+        ce = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        LCHK(ce);
+        it = graphs.emplace(key, ge).first;
+      }
+      LCHK(cudaGraphLaunch(it->second, stream));
+    } else {
+      rc = enqueue_cycle_body(a, m, adjoint);
+      if (rc) return rc;
+    }
+    launch_xupdate(stream, a, x);
+    LCHK(cudaMemcpyAsync(h_ctrl, a.ctrl, sizeof(Control), cudaMemcpyDeviceToHost, stream));
+    LCHK(cudaMemcpyAsync(h_scal, cy->hist, 8 * (size_t)m, cudaMemcpyDeviceToHost, stream));
+    LCHK(cudaStreamSynchronize(stream));
+    const Control &hc = *h_ctrl;
+    if (restart == 0) rnorm0 = hc.rnorm0;
+    if (hc.status & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
+    const int ns = hc.nsteps;
+    if (hist)
+      for (int k = 0; k < ns; ++k) hist->push_back(h_scal[k]);
+    if (opt.monitor_orthog && verbose) {
+      std::vector<double> oh(ns);
+      cudaMemcpy(oh.data(), cy->orth, 8 * (size_t)ns, cudaMemcpyDeviceToHost);
+      for (int k = 0; k < ns; ++k)
+        printf("FGMRES_Householders_gpu_ortherr(%d) = %.16e;\n", total + k + 1, oh[k]);
+    }
+    total += ns;
+    if (ns > 0) {
+      last_cycle = restart;
+      last_steps = ns;
+      final_res = h_scal[ns - 1];
+    }
+    if (hc.converged) {
+      converged = true;
+      if (ns == 0) final_res = 0.0;
+      break;
+    }
+    if (hc.status & kStatusBreakdown) break;
+    if (ns == 0) break;
+    int zero = 0;
+    LCHK(cudaMemcpyAsync(&cy->first_cycle, &zero, 4, cudaMemcpyHostToDevice, stream));
+  }
+  if (log) {
+    log->restarts = last_cycle;
+    log->search_directions = last_steps;
+    log->initial_residual = rnorm0;
+    log->final_residual = final_res;
+  }
+  if (total_iters) *total_iters = total;
+  return converged ? DEV_SUCCESS : DEV_NOTCONVERGED;
+}
+
+extern "C" int lace_gpu_fgmres_householder(lace_gpu_ctx *c, const double *b, double *x,
+                                           const data_d_gmres_param *par, data_d_gmres_log *log,
+                                           int *total_iters) {
+  if (!c || !b || !x || !par) return set_err(DEV_ERR_INVALID_PTR);
+  cudaSetDevice(c->device);
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = c->fgmres(b, x, par->search_max, par->restart_max, par->tol_type, par->rtol, false, log,
+                     total_iters, &c->last_hist);
+  if (log)
+    log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
+  return rc;
+}
+
+extern "C" int lace_gpu_solve_backward(lace_gpu_ctx *c, const double *x, const double *dLdx,
+                                       const data_d_gmres_param *par, double *dLdb, double *dLdA,
+                                       int *total_iters) {
+  if (!c || !x || !dLdx || !par) return set_err(DEV_ERR_INVALID_PTR);
+  if (c->bs) return set_err(DEV_ERR_NOT_SUPPORTED);
+  cudaSetDevice(c->device);
+  int rc = c->ensure_vectors();
+  if (rc) return set_err(rc);
+  // lambda = A^{-T} dL/dx, initial guess 0
+  double *lam = dLdb;
+  DBuf tmp;
+  if (!lam) {
+    if (tmp.ensure(8 * (size_t)c->n)) return set_err(DEV_ERR_DEVICE_ALLOC);
+    lam = (double *)tmp.p;
+  }
+  cudaMemsetAsync(lam, 0, 8 * (size_t)c->n, c->stream);
+  // transposed factor values L^T follow the current L
+  rc = c->fgmres(dLdx, lam, par->search_max, par->restart_max, par->tol_type, par->rtol, true,
+                 nullptr, total_iters, nullptr);
+  if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
+  if (dLdA) {
+    int grid = std::min((c->n + 255) / 256, num_sms() * 8);
+    k_grad_A<<<grid, 256, 0, c->stream>>>(c->n, (const int *)c->Arow.p, (const int *)c->Acol.p, lam, x,
+                                          dLdA);
+  }
+  LCHK(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+extern "C" int lace_gpu_last_error(void) { return g_last_error; }
+
+extern "C" const char *lace_gpu_error_string(int code) {
+  switch (code) {
+    case DEV_SUCCESS: return "success";
+    case DEV_ERR_NOT_INITIALIZED: return "not initialized (no GPU, no matrix, or no factors)";
+    case DEV_ERR_NOT_SUPPORTED: return "not supported (format, unsorted/missing diagonal, size limit)";
+    case DEV_ERR_ILLEGAL_VALUE: return "illegal value";
+    case DEV_ERR_INTERNAL_LIMIT: return "a bounded device wait gave up (dependency never satisfied)";
+    case DEV_ERR_DEVICE_ALLOC: return "device allocation failed";
+    case DEV_ERR_HOST_ALLOC: return "host allocation failed";
+    case DEV_ERR_INVALID_PTR: return "invalid pointer";
+    case DEV_ERR_BADPRECOND: return "breakdown in the preconditioner (zero or non-finite pivot)";
+    case DEV_NOTCONVERGED: return "not converged";
+    default: return "CUDA or unknown error";
+  }
+}

@@ -1,0 +1,122 @@
+// Host-side state of a lace_gpu_ctx (see context.cu for the HBM layout).
+#pragma once
+
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "../../include/lace_gb300.h"
+#include "internal.h"
+
+namespace lace {
+
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { free(); }
+  void free();
+  int ensure(size_t b);
+  int upload(const void *h, size_t b, cudaStream_t s);
+};
+
+struct Pattern {
+  int n = 0;
+  std::vector<int> ptr, idx;
+};
+
+extern thread_local int g_last_error;
+int set_err(int code);
+int cuda_code(cudaError_t e);
+int validate_csr(int n, int nnz, const int *row, const int *col);
+void transpose_pattern(const Pattern &P, Pattern &T, std::vector<int> &t2p);
+
+}  // namespace lace
+
+struct lace_gpu_ctx {
+  using DBuf = lace::DBuf;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  lace_gpu_options opt{};
+  bool verbose = false;
+
+  // matrix (CSR: bs == 0; BCSR: n_blk block rows of bs x bs blocks)
+  int n = 0;       // scalar rows
+  int n_blk = 0;   // rows of the (block) pattern
+  int bs = 0;
+  int nnzA = 0;    // entries (blocks) of A
+  double anorm = 0.0;
+  DBuf Arow, Acol, Aval;
+  // A^T for the adjoint
+  bool AT_ready = false;
+  DBuf ATrow, ATcol, ATval, map_at2a;
+
+  // factor patterns and maps
+  int nnzL = 0, nnzU = 0;
+  lace::Pattern hL, hU, hUc, hLt;
+  DBuf Lrow, Lcol, Ucp, Uri, Urow, Ucol, Ltp, Lti;
+  DBuf map_l2a, map_uc2a, map_ur2uc, map_lt2l, map_ur2uc_el;
+  // factor values (value type from opt.precision)
+  DBuf Lv[2], Ucv[2], Urv, Ltv, dinv;
+  int cur = 0;
+  bool factors_ready = false;
+
+  // SpTRSV per triangle (0 L, 1 U, 2 U^T, 3 L^T)
+  DBuf kinds[4][4];  // [triangle][log2 rows-per-lane]
+  DBuf ready[4];
+  DBuf lvl_ptr[4], lvl_rows[4];
+  int nlevels[4] = {0, 0, 0, 0};
+  int rows_per_lane = 4;
+  bool trsv_tuned = false;
+  int lanes = 8;
+
+  // Krylov workspace
+  int ws_m = 0;
+  bool ws_zf32 = false;
+  size_t ldv = 0;
+  DBuf Vb, Zb, Qmon, vec_w, vec_q, vec_t, vec_t2, vec_r;
+  DBuf part_buf, zero_buf;
+  DBuf ctrl_buf, cycle_buf, scal_buf, cnt_buf;
+  lace::Control *h_ctrl = nullptr;
+  double *h_scal = nullptr;
+  std::map<std::tuple<int, int, int, int, int, int, int, int>, cudaGraphExec_t> graphs;
+  std::vector<double> last_hist;
+
+  ~lace_gpu_ctx();
+  lace::Control *ctrl() const { return (lace::Control *)ctrl_buf.p; }
+  void drop_graphs();
+  int analyse(int n_, const int *row, const int *col, int bs_);
+  int analyse_factors(const lace::Pattern &L, const lace::Pattern &Ur);
+  int set_factors_host(int nrows, const int *lrow, const int *lcol, const double *lval,
+                       const int *urow, const int *ucol, const double *uval);
+  std::vector<int> uc2ur_h;  // CSC position of U -> CSR position
+  int upload_common(int n_, int nnz_, const int *row, const int *col, int bs_);
+  void set_rows_per_lane(int R);
+  lace::TriDev tri(int which) const;
+  lace::VType vtype() const;
+  void *part_ensure();
+  const void *zeros(size_t count);
+  int autotune_spmv();
+  int autotune_trsv();
+  int alloc_factor_values();
+  lace::IluArgs ilu_args();
+  int init_factors();
+  int finish_factors();
+  // up to `sweeps` sweeps; with sync_each, stops once the normalised step is
+  // <= stop_below (LACE's stopping tests); steps receives every sweep's step
+  int parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
+             std::vector<double> *steps, double stop_below = -1.0);
+  int h_status();
+  int solve_tri(int which, const void *b, int in_f32, void *x, int out_f32, bool honor_done,
+                void *tmp);
+  int ensure_vectors();
+  int ensure_krylov(int m, bool monitor);
+  int ensure_AT();
+  lace::ArnoldiArgs arnoldi_args(int m, bool adjoint);
+  int enqueue_cycle_body(const lace::ArnoldiArgs &a, int m, bool adjoint);
+  int fgmres(const double *b, double *x, int m, int restart_max, int tol_type, double rtol,
+             bool adjoint, data_d_gmres_log *log, int *total_iters, std::vector<double> *hist);
+};

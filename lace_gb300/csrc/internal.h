@@ -1,0 +1,152 @@
+// Internal interfaces between the lace_gb300 translation units: device data
+// structures shared by kernels and the host-side launchers that
+// context.cu calls.  Not part of the public C ABI (include/lace_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace lace {
+
+// Largest restart length (search_max) the device FGMRES supports.
+constexpr int kMaxM = 128;
+constexpr int kLdT = kMaxM + 2;  // leading dimension of the small matrices
+
+// Device-resident scalar state of one FGMRES cycle.  The small matrices
+// are column-major with leading dimension kLdT.
+struct Cycle {
+  double T[kLdT * kLdT];  // compact-WY factor: P_0...P_j = I - V T V^T
+  double R[kLdT * kLdT];  // Givens-rotated Hessenberg (upper triangular)
+  double g[kLdT];         // rotated right-hand side of the LS problem
+  double cs[kLdT], sn[kLdT];
+  double y[kLdT];         // T^T (V^T w) of pass A
+  double c[kLdT];         // T_{j+1} rho of pass B, consumed by pass C
+  double yls[kLdT];       // least-squares solution at the end of a cycle
+  double hist[kLdT];      // |g_{j+1}| per search direction of the cycle
+  double orth[kLdT];      // ||I - Q^T Q||_inf per direction (when monitored)
+  double dd;              // sign(w_{j+1}) ||w_{j+1:}||   (H(j+1,j) = -dd)
+  double inv_alpha;       // 1 / ||w_{j+1:} + dd e_{j+1}||
+  double dd0, inv_alpha0; // first reflector of the cycle
+  double rnorm;           // ||b - A x|| at the start of the cycle
+  int tol_type;
+  int first_cycle;
+  double rtol;
+};
+
+// Handles for the two triangles of one solve direction.
+struct TriDev {
+  int n = 0;
+  int nnz = 0;
+  const int *row = nullptr;
+  const int *col = nullptr;
+  const void *val = nullptr;  // double / float / bf16 per precision
+  int lower = 1;
+  int unit = 0;
+  const uint8_t *kind = nullptr;  // per chunk: 0 scan, 1 serial
+  int rows_per_lane = 4;
+  int nchunks = 0;
+  int *ready = nullptr;
+  int slot = 0;  // index into Control::trsv_epoch / tickets
+  // level-scheduled option
+  const int *lvl_ptr = nullptr;
+  const int *lvl_rows = nullptr;
+  int nlevels = 0;
+};
+
+enum class VType { F64 = 0, F32 = 1, BF16 = 2 };
+
+// ---------------------------------------------------------------- SpMV
+// y = alpha*A*x + beta*y (x double or float), lanes per row in {1,2,4,8,16,32}
+void launch_spmv_f64x(cudaStream_t s, int lanes, int n, const int *row, const int *col,
+                      const double *val, const double *x, double alpha, double beta, double *y);
+void launch_spmv_f32x(cudaStream_t s, int lanes, int n, const int *row, const int *col,
+                      const double *val, const float *x, double alpha, double beta, double *y);
+void launch_bcsr_spmv(cudaStream_t s, int nb, int bs, const int *row, const int *col,
+                      const double *val, const double *x, double alpha, double beta, double *y);
+
+// ---------------------------------------------------- FGMRES-Householder
+struct ArnoldiArgs {
+  int n = 0;
+  // operator: CSR (bs == 0) or BCSR (bs > 0)
+  int bs = 0;
+  const int *row = nullptr, *col = nullptr;
+  const double *val = nullptr;
+  int lanes = 8;
+  double *V = nullptr;   // reflectors, n x (m+1) column-major
+  size_t ldv = 0;
+  void *Z = nullptr;     // preconditioned vectors, n x m (float or double)
+  size_t ldz = 0;
+  int z_f32 = 0;
+  double *w = nullptr;   // work vector (A z, later the transformed column)
+  double *q = nullptr;   // next Krylov vector
+  double *partials = nullptr;  // grid-reduction scratch
+  int grid = 0;          // blocks of the reducing kernels
+  Cycle *cy = nullptr;
+  Control *ctrl = nullptr;
+  int m = 0;
+};
+
+void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x);
+void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a);
+void launch_passA(cudaStream_t s, const ArnoldiArgs &a, int j);
+void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j);
+void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j);
+void launch_orthog_monitor(cudaStream_t s, const ArnoldiArgs &a, int j, double *Q, size_t ldq);
+void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
+
+// ------------------------------------------------------------ ParILU
+struct IluArgs {
+  int n = 0, nnzA = 0;
+  const int *Arow = nullptr, *Acol = nullptr;
+  const double *Aval = nullptr;
+  const int *Lrow = nullptr, *Lcol = nullptr;   // CSRL
+  const int *Ucp = nullptr, *Uri = nullptr;     // CSCU
+  int bs = 0;                                   // BCSR block size (0: CSR)
+  double *partials = nullptr;
+  int *counter = nullptr;
+  int grid = 0;
+};
+// one synchronous sweep old -> new; writes sum (new-old)^2 to *step (device)
+void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *Lold, void *Lnew,
+                         const void *Uold, void *Unew, double *step);
+// ||(A - LU)|_S||_F^2 to *out (device)
+void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
+                         double *out);
+// gather: dst[p] = src[perm[p]] with type conversion
+void launch_gather(cudaStream_t s, int count, const int *perm, VType ts, const void *src, VType td,
+                   void *dst);
+// convert / copy an array between value types
+void launch_convert(cudaStream_t s, int count, VType ts, const void *src, VType td, void *dst);
+// BCSR: inverse of each diagonal block of U (row form: diagonal block first
+// in each block row) into dinv (nb * bs*bs), value type t
+void launch_block_diag_inverse(cudaStream_t s, int nb, int bs, const int *Urow, VType t,
+                               const void *Uval, void *dinv, int *status);
+
+// ------------------------------------------------------------ SpTRSV
+// x = T^{-1} b for one triangle; b/x typed by in_f32/out_f32 (else double).
+// compute precision follows the factor value type (double for F64, float
+// otherwise).  ctrl may be null (stand-alone call).
+// honor_done: return at once when ctrl->done is set (inside an Arnoldi cycle)
+void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
+                            void *x, int out_f32, Control *ctrl, int grid_hint, bool honor_done);
+void launch_sptrsv_levels(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
+                          void *x, int out_f32, Control *ctrl, bool honor_done);
+// one synchronous Jacobi sweep y_new = D^{-1}(b - (T - D) y_old); step partial sums
+void launch_jacobi_sweep(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
+                         const void *yold, void *ynew, int y_f32, Control *ctrl, bool honor_done);
+// block (BCSR) triangular solves: lower with identity diagonal blocks, or
+// upper applying the inverted diagonal blocks dinv
+void launch_bcsr_sptrsv(cudaStream_t s, const TriDev &t, int bs, VType vt, const void *dinv,
+                        const void *b, int in_f32, void *x, int out_f32, Control *ctrl,
+                        int grid_hint, bool honor_done);
+
+// *out = sum (a_i - b_i)^2 (typed by f32), deterministic grid reduction
+void launch_sqdiff(cudaStream_t s, int n, const void *a, const void *b, int f32, double *partials,
+                   int *counter, double *out);
+
+int num_sms();
+
+}  // namespace lace

@@ -1,0 +1,588 @@
+// SpMV and the FGMRES-Householder Arnoldi kernels.
+//
+// The Arnoldi step follows LACE's FGMRES-Householder
+// (src/fgmres_householder_restart.cpp:311-757) but applies the reflectors in
+// compact-WY form: P_0 P_1 ... P_j = I - V T V^T with T upper triangular.
+//   pass A : w = A z_j fused with s = V^T w (one read of V)
+//   pass B : w <- w - V (T^T s)  (LACE :376-469, all reflectors at once),
+//            fused with d' = V^T w over rows > j and ||w_{j+1:}||^2; the last
+//            block forms the new reflector scalars (LACE :476-511), extends T,
+//            applies the Givens rotations and updates g (LACE :658-701), and
+//            on convergence solves the small least-squares system (:714-729)
+//   pass C : v_{j+1} and q = P_0...P_{j+1} e_{j+1} (LACE :519-617) in one read
+// Every kernel returns at once when Control::done is set, so a whole cycle can
+// be launched (or replayed from a CUDA graph) without host round trips.
+#include <math.h>
+#include <stdio.h>
+
+#include "internal.h"
+
+namespace lace {
+
+constexpr int kTPB = 256;   // threads per block of the row-tile kernels
+constexpr int kSlots = (kMaxM + 2 + 7) / 8;  // k-slots per warp (8 warps)
+
+// ------------------------------------------------------------------ SpMV
+
+// LPR lanes per row, 32/LPR rows per warp; the loop bound is warp-uniform so
+// every lane takes part in the segmented shuffle reduction.
+template <int LPR, typename XT>
+__global__ void __launch_bounds__(kTPB) k_spmv(int n, const int *__restrict__ row,
+                                               const int *__restrict__ col,
+                                               const double *__restrict__ val,
+                                               const XT *__restrict__ x, double alpha,
+                                               double beta, double *__restrict__ y) {
+  constexpr int GPW = 32 / LPR;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & (LPR - 1);
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int wb = gw * GPW; wb < n; wb += nw * GPW) {
+    const int i = wb + lane / LPR;
+    double s = 0.0;
+    if (i < n) {
+      const int e = row[i + 1];
+      for (int p = row[i] + sub; p < e; p += LPR) s = fma(val[p], (double)x[col[p]], s);
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+    if (sub == 0 && i < n) y[i] = (beta == 0.0) ? alpha * s : fma(beta, y[i], alpha * s);
+  }
+}
+
+template <typename XT>
+static void spmv_dispatch(cudaStream_t s, int lanes, int n, const int *row, const int *col,
+                          const double *val, const XT *x, double alpha, double beta, double *y) {
+  if (n <= 0) return;
+  long long threads = (long long)n * lanes;
+  long long g = (threads + kTPB - 1) / kTPB;
+  if (g > (long long)num_sms() * 16) g = (long long)num_sms() * 16;
+  int grid = (int)g;
+  grid = grid < 1 ? 1 : grid;
+  switch (lanes) {
+    case 1: k_spmv<1, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+    case 2: k_spmv<2, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+    case 4: k_spmv<4, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+    case 16: k_spmv<16, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+    case 32: k_spmv<32, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+    default: k_spmv<8, XT><<<grid, kTPB, 0, s>>>(n, row, col, val, x, alpha, beta, y); break;
+  }
+}
+
+void launch_spmv_f64x(cudaStream_t s, int lanes, int n, const int *row, const int *col,
+                      const double *val, const double *x, double alpha, double beta, double *y) {
+  spmv_dispatch<double>(s, lanes, n, row, col, val, x, alpha, beta, y);
+}
+void launch_spmv_f32x(cudaStream_t s, int lanes, int n, const int *row, const int *col,
+                      const double *val, const float *x, double alpha, double beta, double *y) {
+  spmv_dispatch<float>(s, lanes, n, row, col, val, x, alpha, beta, y);
+}
+
+// BCSR: one thread per scalar row, the bs threads of a block row read the
+// same blocks (row-major bs x bs)
+__global__ void __launch_bounds__(kTPB) k_bcsr_spmv(int nb, int bs, const int *__restrict__ row,
+                                                    const int *__restrict__ col,
+                                                    const double *__restrict__ val,
+                                                    const double *__restrict__ x, double alpha,
+                                                    double beta, double *__restrict__ y) {
+  const int n = nb * bs;
+  const int ld = bs * bs;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int I = i / bs, r = i - I * bs;
+    double s = 0.0;
+    for (int p = row[I]; p < row[I + 1]; ++p) {
+      const double *blk = val + (size_t)p * ld + r * bs;
+      const double *xj = x + (size_t)col[p] * bs;
+      for (int c = 0; c < bs; ++c) s = fma(blk[c], xj[c], s);
+    }
+    y[i] = (beta == 0.0) ? alpha * s : fma(beta, y[i], alpha * s);
+  }
+}
+
+void launch_bcsr_spmv(cudaStream_t s, int nb, int bs, const int *row, const int *col,
+                      const double *val, const double *x, double alpha, double beta, double *y) {
+  int n = nb * bs;
+  if (n <= 0) return;
+  int grid = min((n + kTPB - 1) / kTPB, num_sms() * 16);
+  k_bcsr_spmv<<<grid, kTPB, 0, s>>>(nb, bs, row, col, val, x, alpha, beta, y);
+}
+
+// --------------------------------------------------- row-tile machinery
+
+// operator row i of the tile: CSR (LPR lanes per row) or BCSR (thread/row)
+struct OpView {
+  int bs;
+  const int *row, *col;
+  const double *val;
+};
+
+template <int LPR, typename ZT>
+__device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, int tr,
+                                           const ZT *__restrict__ z, double *sw) {
+  if (op.bs == 0) {
+    const int sub = threadIdx.x & (LPR - 1);
+    const int grp = threadIdx.x / LPR;
+    constexpr int G = kTPB / LPR;
+    for (int t = grp; t < tr; t += G) {
+      const int i = base + t;
+      double s = 0.0;
+      if (i < n) {
+        const int e = op.row[i + 1];
+        for (int p = op.row[i] + sub; p < e; p += LPR) s = fma(op.val[p], (double)z[op.col[p]], s);
+      }
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+      if (sub == 0) sw[t] = s;
+    }
+  } else {
+    const int bs = op.bs, ld = bs * bs;
+    for (int t = threadIdx.x; t < tr; t += kTPB) {
+      const int i = base + t;
+      double s = 0.0;
+      if (i < n) {
+        const int I = i / bs, r = i - I * bs;
+        for (int p = op.row[I]; p < op.row[I + 1]; ++p) {
+          const double *blk = op.val + (size_t)p * ld + r * bs;
+          const ZT *zj = z + (size_t)op.col[p] * bs;
+          for (int c = 0; c < bs; ++c) s = fma(blk[c], (double)zj[c], s);
+        }
+      }
+      sw[t] = s;
+    }
+  }
+}
+
+// acc[slot] += sum over tile rows (masked by lo) of V[k][i] * sw[t]  with
+// k = slot*8 + warp.  Lanes walk rows, warps walk columns: every V load is a
+// coalesced 256-byte row segment of one column.
+__device__ __forceinline__ void tile_dots(const double *__restrict__ V, size_t ldv, int ncols,
+                                          int n, int base, int tr, int lo, const double *sw,
+                                          double (&acc)[kSlots]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int t = lane; t < tr; t += 32) {
+    const int i = base + t;
+    if (i >= n || i < lo) continue;
+    const double wi = sw[t];
+#pragma unroll
+    for (int sl = 0; sl < kSlots; ++sl) {
+      const int k = sl * 8 + wid;
+      if (k < ncols) acc[sl] = fma(V[(size_t)k * ldv + i], wi, acc[sl]);
+    }
+  }
+}
+
+// block-reduce acc into sred[k] (k < ncols); plus optional extra scalar
+__device__ __forceinline__ void block_reduce_slots(double (&acc)[kSlots], int ncols, double *sred) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int sl = 0; sl < kSlots; ++sl) {
+    const int k = sl * 8 + wid;
+    if (sl * 8 < ncols) {  // warp-uniform
+      double v = warp_sum(acc[sl]);
+      if (lane == 0 && k < ncols) sred[k] = v;
+    }
+  }
+}
+
+__device__ __forceinline__ double block_sum(double v, double *scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kTPB / 32; ++w) t += scratch[w];
+  return t;  // valid in thread 0
+}
+
+// ------------------------------------------------------- cycle start
+
+// r = b - A x (into a.w) and ||r||; last block sets up the first reflector
+// scalars (LACE :209-236, :239-308) and the convergence test at cycle start.
+template <int LPR>
+__global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const double *__restrict__ b,
+                                                         const double *__restrict__ x,
+                                                         double *__restrict__ r, double *partials,
+                                                         Cycle *cy, Control *ctrl) {
+  __shared__ double sw[kTPB];
+  __shared__ double scratch[kTPB / 32];
+  const int tr = (op.bs == 0) ? kTPB : (kTPB / op.bs) * op.bs;
+  double nrm = 0.0;
+  for (int base = blockIdx.x * tr; base < n; base += gridDim.x * tr) {
+    tile_apply<LPR, double>(op, n, base, tr, x, sw);
+    __syncthreads();
+    for (int t = threadIdx.x; t < tr; t += kTPB) {
+      const int i = base + t;
+      if (i < n) {
+        double ri = b[i] - sw[t];
+        r[i] = ri;
+        nrm = fma(ri, ri, nrm);
+      }
+    }
+    __syncthreads();
+  }
+  double tot = block_sum(nrm, scratch);
+  if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+  if (!arrive_last(&ctrl->block_count[0])) return;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)gridDim.x; ++k) s += partials[k];
+    const double rnorm = sqrt(s);
+    cy->rnorm = rnorm;
+    if (cy->first_cycle) {
+      ctrl->rnorm0 = rnorm;
+      ctrl->rtol_abs = cy->tol_type == 1 ? cy->rtol * rnorm : cy->rtol;
+    }
+    ctrl->nsteps = 0;
+    ctrl->status = ctrl->status;  // keep earlier bits
+    if (!(rnorm >= ctrl->rtol_abs)) {  // LACE :233 (also catches NaN: stop)
+      ctrl->done = 1;
+      ctrl->converged = (rnorm < ctrl->rtol_abs) ? 1 : 0;
+      if (!(rnorm == rnorm)) ctrl->status |= kStatusBreakdown;
+    } else {
+      const double r0 = r[0];
+      const double dd = mysgn(r0) * rnorm;
+      const double alpha = sqrt(2.0 * (s + fabs(r0) * rnorm));
+      cy->dd0 = dd;
+      cy->inv_alpha0 = alpha > 0.0 ? 1.0 / alpha : 0.0;
+      cy->g[0] = -dd;
+      cy->T[0] = 2.0;
+      ctrl->done = 0;
+      ctrl->converged = 0;
+    }
+  }
+}
+
+// V[:,0] = (r + dd e_0)/alpha,  q = -r/dd
+__global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
+                                                     double *__restrict__ V, double *__restrict__ q,
+                                                     const Cycle *cy, const Control *ctrl) {
+  if (ctrl->done) return;
+  const double dd = cy->dd0, ia = cy->inv_alpha0;
+  const double rdd = 1.0 / dd;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    V[i] = (i == 0 ? ri + dd : ri) * ia;
+    q[i] = -ri * rdd;
+  }
+}
+
+// ------------------------------------------------------------- pass A
+
+template <int LPR, typename ZT>
+__global__ void __launch_bounds__(kTPB) k_passA(int n, OpView op, const ZT *__restrict__ z,
+                                                double *__restrict__ w, const double *__restrict__ V,
+                                                size_t ldv, int jp1, double *partials, Cycle *cy,
+                                                Control *ctrl) {
+  if (ctrl->done) return;
+  __shared__ double sw[kTPB];
+  __shared__ double sred[kLdT];
+  const int tr = (op.bs == 0) ? kTPB : (kTPB / op.bs) * op.bs;
+  double acc[kSlots];
+#pragma unroll
+  for (int sl = 0; sl < kSlots; ++sl) acc[sl] = 0.0;
+  for (int base = blockIdx.x * tr; base < n; base += gridDim.x * tr) {
+    tile_apply<LPR, ZT>(op, n, base, tr, z, sw);
+    __syncthreads();
+    for (int t = threadIdx.x; t < tr; t += kTPB)
+      if (base + t < n) w[base + t] = sw[t];
+    tile_dots(V, ldv, jp1, n, base, tr, 0, sw, acc);
+    __syncthreads();
+  }
+  block_reduce_slots(acc, jp1, sred);
+  __syncthreads();
+  for (int k = threadIdx.x; k < jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
+  if (!arrive_last(&ctrl->block_count[1])) return;
+  // s = V^T w  -> y = T^T s
+  for (int k = threadIdx.x; k < jp1; k += kTPB) {
+    double s = 0.0;
+    for (int bb = 0; bb < (int)gridDim.x; ++bb) s += partials[(size_t)bb * kLdT + k];
+    sred[k] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < jp1; k += kTPB) {
+    double y = 0.0;
+    for (int l = 0; l <= k; ++l) y = fma(cy->T[l + k * kLdT], sred[l], y);
+    cy->y[k] = y;
+  }
+}
+
+// ------------------------------------------------------------- pass B
+
+__device__ void givens_rot(double a, double b, double tol, double *c, double *s) {
+  // src/givens.cpp:46-67
+  if (fabs(b) <= tol) {
+    *c = 1.0;
+    *s = 0.0;
+  } else if (fabs(b) > fabs(a)) {
+    double temp = a / b;
+    *s = 1.0 / sqrt(1.0 + temp * temp);
+    *c = temp * (*s);
+  } else {
+    double temp = b / a;
+    *c = 1.0 / sqrt(1.0 + temp * temp);
+    *s = temp * (*c);
+  }
+}
+
+__global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict__ V, size_t ldv,
+                                                int j, int m, double *__restrict__ w,
+                                                double *partials, Cycle *cy, Control *ctrl) {
+  if (ctrl->done) return;
+  __shared__ double sw[kTPB];
+  __shared__ double sy[kLdT];
+  __shared__ double sred[kLdT + 1];
+  __shared__ double scratch[kTPB / 32];
+  const int jp1 = j + 1;
+  for (int k = threadIdx.x; k < jp1; k += kTPB) sy[k] = cy->y[k];
+  __syncthreads();
+  double acc[kSlots];
+#pragma unroll
+  for (int sl = 0; sl < kSlots; ++sl) acc[sl] = 0.0;
+  double nrm = 0.0;
+  for (int base = blockIdx.x * kTPB; base < n; base += gridDim.x * kTPB) {
+    const int i = base + threadIdx.x;
+    if (i < n) {
+      double s = w[i];
+      for (int k = 0; k < jp1; ++k) s = fma(-V[(size_t)k * ldv + i], sy[k], s);
+      w[i] = s;
+      sw[threadIdx.x] = s;
+      if (i > j) nrm = fma(s, s, nrm);
+    }
+    __syncthreads();
+    tile_dots(V, ldv, jp1, n, base, kTPB, jp1, sw, acc);
+    __syncthreads();
+  }
+  block_reduce_slots(acc, jp1, sred);
+  double tot = block_sum(nrm, scratch);
+  if (threadIdx.x == 0) sred[jp1] = tot;
+  __syncthreads();
+  for (int k = threadIdx.x; k <= jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
+  if (!arrive_last(&ctrl->block_count[2])) return;
+
+  // ---- last block: new reflector, T extension, Givens, LS solve
+  __shared__ double sd[kLdT];
+  __shared__ double srho[kLdT];
+  __shared__ double s_dd, s_ia, s_vjj;
+  for (int k = threadIdx.x; k <= jp1; k += kTPB) {
+    double s = 0.0;
+    for (int bb = 0; bb < (int)gridDim.x; ++bb) s += partials[(size_t)bb * kLdT + k];
+    sred[k] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double nrm2 = sred[jp1];
+    const double wn = sqrt(nrm2);
+    const double wj1 = w[jp1];
+    const double dd = mysgn(wj1) * wn;  // LACE :477-478
+    const double alpha = sqrt(2.0 * (nrm2 + fabs(wj1) * wn));
+    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    s_dd = dd;
+    s_ia = ia;
+    s_vjj = (wj1 + dd) * ia;
+    cy->dd = dd;
+    cy->inv_alpha = ia;
+  }
+  __syncthreads();
+  // d = V_j^T v_{j+1}; rho = row j+1 of V_{j+1}
+  for (int k = threadIdx.x; k < jp1; k += kTPB) {
+    const double vk = V[(size_t)k * ldv + jp1];
+    sd[k] = (sred[k] + s_dd * vk) * s_ia;
+    srho[k] = vk;
+  }
+  if (threadIdx.x == 0) srho[jp1] = s_vjj;
+  __syncthreads();
+  // T(:, j+1) = [-2 T_j d ; 2]
+  double *T = cy->T;
+  for (int k = threadIdx.x; k < jp1; k += kTPB) {
+    double t = 0.0;
+    for (int l = k; l < jp1; ++l) t = fma(T[k + l * kLdT], sd[l], t);
+    T[k + jp1 * kLdT] = -2.0 * t;
+  }
+  if (threadIdx.x == 0) {
+    T[jp1 + jp1 * kLdT] = 2.0;
+    for (int k = jp1 + 1; k < kLdT; ++k) T[k + jp1 * kLdT] = 0.0;
+  }
+  __syncthreads();
+  // c = T_{j+1} rho  (consumed by pass C)
+  for (int k = threadIdx.x; k <= jp1; k += kTPB) {
+    double t = 0.0;
+    for (int l = k; l <= jp1; ++l) t = fma(T[k + l * kLdT], srho[l], t);
+    cy->c[k] = t;
+  }
+  if (threadIdx.x == 0) {
+    // Hessenberg column j: h_k = w_k (k <= j), h_{j+1} = -dd  (LACE :658-701)
+    double *R = cy->R + (size_t)j * kLdT;
+    for (int k = 0; k <= j; ++k) R[k] = w[k];
+    for (int k = 0; k < j; ++k) {
+      const double t0 = R[k], t1 = R[k + 1];
+      R[k + 1] = -cy->sn[k] * t0 + cy->cs[k] * t1;
+      R[k] = cy->cs[k] * t0 + cy->sn[k] * t1;
+    }
+    const double dd = s_dd;
+    double c, s;
+    givens_rot(R[j], -dd, 4.9406564584124654e-324, &c, &s);
+    cy->cs[j] = c;
+    cy->sn[j] = s;
+    R[j] = c * R[j] - s * dd;
+    cy->g[jp1] = -s * cy->g[j];
+    cy->g[j] = c * cy->g[j];
+    const double resid = fabs(cy->g[jp1]);
+    cy->hist[j] = resid;
+    ctrl->resid = resid;
+    const bool conv = resid < ctrl->rtol_abs;
+    if (conv || j == m - 1 || !(resid == resid)) {  // LACE :714 (+ opt4's non-finite stop)
+      // back-substitution, LACE :721-729
+      double *y = cy->yls;
+      for (int i = 0; i <= j; ++i) y[i] = cy->g[i] / cy->R[i + i * kLdT];
+      for (int jj = j; jj > 0; --jj)
+        for (int i = jj - 1; i >= 0; --i)
+          y[i] = y[i] - cy->R[i + jj * kLdT] * y[jj] / cy->R[i + i * kLdT];
+      ctrl->nsteps = jp1;
+      ctrl->converged = conv ? 1 : 0;
+      if (!(resid == resid)) ctrl->status |= kStatusBreakdown;
+      ctrl->done = 1;
+    }
+  }
+}
+
+// ------------------------------------------------------------- pass C
+
+__global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, size_t ldv, int j,
+                                                const double *__restrict__ w, double *__restrict__ q,
+                                                const Cycle *cy, const Control *ctrl) {
+  if (ctrl->done) return;
+  __shared__ double sc[kLdT];
+  const int jp1 = j + 1;
+  for (int k = threadIdx.x; k <= jp1; k += kTPB) sc[k] = cy->c[k];
+  __syncthreads();
+  const double dd = cy->dd, ia = cy->inv_alpha;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
+    V[(size_t)jp1 * ldv + i] = v;
+    double acc = (i == jp1 ? 1.0 : 0.0) - v * sc[jp1];
+    for (int k = 0; k < jp1; ++k) acc = fma(-V[(size_t)k * ldv + i], sc[k], acc);
+    q[i] = acc;
+  }
+}
+
+// ----------------------------------------------- orthogonality monitor
+// orth[j+1] = ||I - Q^T Q||_inf over q_0..q_{j} (LACE :628-656 evaluates it on
+// the first search+1 stored vectors); Q columns stored by the host driver.
+__global__ void k_orthog(int n, const double *__restrict__ Q, size_t ldq, int ncols, double *G) {
+  // G[a*ncols+b] = q_a . q_b, one block per (a,b) pair with a <= b
+  const int a = blockIdx.x, bcol = blockIdx.y;
+  if (a > bcol || bcol >= ncols) return;
+  __shared__ double scratch[kTPB / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kTPB) s = fma(Q[(size_t)a * ldq + i], Q[(size_t)bcol * ldq + i], s);
+  double t = block_sum(s, scratch);
+  if (threadIdx.x == 0) {
+    G[a * ncols + bcol] = t;
+    G[bcol * ncols + a] = t;
+  }
+}
+__global__ void k_orthog_norm(const double *G, int ncols, double *out) {
+  if (threadIdx.x != 0) return;
+  double mx = 0.0;
+  for (int i = 0; i < ncols; ++i) {
+    double t = 0.0;
+    for (int jj = 0; jj < ncols; ++jj) t += fabs((i == jj ? 1.0 : 0.0) - G[i * ncols + jj]);
+    if (mx < t) mx = t;
+  }
+  *out = mx;
+}
+
+void launch_orthog_monitor(cudaStream_t s, const ArnoldiArgs &a, int j, double *Q, size_t ldq) {
+  const int ncols = j + 1;
+  dim3 grid(ncols, ncols);
+  k_orthog<<<grid, kTPB, 0, s>>>(a.n, Q, ldq, ncols, a.partials);
+  k_orthog_norm<<<1, 32, 0, s>>>(a.partials, ncols, &a.cy->orth[j]);
+}
+
+// ------------------------------------------------------------- x update
+
+template <typename ZT>
+__global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ Z, size_t ldz,
+                                                  double *__restrict__ x, const Cycle *cy,
+                                                  const Control *ctrl) {
+  const int ns = ctrl->nsteps;
+  if (!ctrl->done || ns == 0) return;
+  __shared__ double sy[kLdT];
+  for (int k = threadIdx.x; k < ns; k += kTPB) sy[k] = cy->yls[k];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = x[i];
+    for (int k = 0; k < ns; ++k) s = fma((double)Z[(size_t)k * ldz + i], sy[k], s);  // LACE :735-744
+    x[i] = s;
+  }
+}
+
+// ------------------------------------------------------------ launchers
+
+static OpView opview(const ArnoldiArgs &a) { return OpView{a.bs, a.row, a.col, a.val}; }
+
+static int rowgrid(int n) {
+  int g = (n + kTPB - 1) / kTPB;
+  return min(g, num_sms() * 8);
+}
+
+void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x) {
+  OpView op = opview(a);
+  switch (a.bs ? 8 : a.lanes) {
+    case 4: k_cycle_residual<4><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
+    case 16: k_cycle_residual<16><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
+    case 32: k_cycle_residual<32><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
+    default: k_cycle_residual<8><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
+  }
+}
+
+void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
+  k_cycle_init<<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.q, a.cy, a.ctrl);
+}
+
+template <typename ZT>
+static void passA_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  OpView op = opview(a);
+  const ZT *z = (const ZT *)a.Z + (size_t)j * a.ldz;
+  switch (a.bs ? 8 : a.lanes) {
+    case 4: k_passA<4, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    case 16: k_passA<16, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    case 32: k_passA<32, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    default: k_passA<8, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+  }
+}
+
+void launch_passA(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  if (a.z_f32) passA_t<float>(s, a, j);
+  else passA_t<double>(s, a, j);
+}
+
+void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  k_passB<<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl);
+}
+
+void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  k_passC<<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, a.q, a.cy, a.ctrl);
+}
+
+void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x) {
+  if (a.z_f32)
+    k_xupdate<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, (const float *)a.Z, a.ldz, x, a.cy, a.ctrl);
+  else
+    k_xupdate<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, (const double *)a.Z, a.ldz, x, a.cy, a.ctrl);
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 132;
+  }
+  return sms;
+}
+
+}  // namespace lace

@@ -1,0 +1,354 @@
+// ParILU(0) sweeps on the GPU.
+//
+// LACE's sweep (src/parilu_v0_3.cpp:67-103, and the one-block GPU copy in
+// src/parilu_v0_3_gpu.cpp:17-105) updates L and U in place from every thread,
+// an asynchronous iteration.  Here every sweep is synchronous (Jacobi): it
+// reads the previous iterate (Lold/Uold) and writes the next (Lnew/Unew), so a
+// sweep is deterministic and the step sum is a reduction without races.
+// Per nonzero (i,j) of A:
+//     s = a_ij - sum_{k < min(i,j)} l_ik u_kj      (merge of L row i, U col j)
+//     l_ij = s / u_jj  (i > j)      u_ij = s  (i <= j)
+// L is CSRL (unit diagonal last in each row), U is CSCU (diagonal last in
+// each column).  One thread per row of A: the row's L entries are reused for
+// all of its nonzeros, and the target position of an entry is found by the
+// same merge walk (no position map is stored).
+#include "internal.h"
+
+namespace lace {
+
+constexpr int kPTPB = 256;
+
+__device__ __forceinline__ double block_sum_p(double v) {
+  __shared__ double scratch[kPTPB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kPTPB / 32; ++w) t += scratch[w];
+  return t;
+}
+
+// last block folds the per-block partials (deterministic order) into *out
+__device__ __forceinline__ void finish_sum(double local, double *partials, int *counter,
+                                           double *out) {
+  double t = block_sum_p(local);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+  if (!arrive_last(counter)) return;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) s += partials[b];
+    *out = s;
+  }
+}
+
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_parilu_sweep(
+    int n, const int *__restrict__ Arow, const int *__restrict__ Acol,
+    const double *__restrict__ Aval, const int *__restrict__ Lrow, const int *__restrict__ Lcol,
+    const FT *__restrict__ Lold, FT *__restrict__ Lnew, const int *__restrict__ Ucp,
+    const int *__restrict__ Uri, const FT *__restrict__ Uold, FT *__restrict__ Unew,
+    double *partials, int *counter, double *step) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lb = Lrow[i], le = Lrow[i + 1];
+    int lpos = lb;  // L entries of row i appear in the order of A's strict-lower entries
+    for (int p = Arow[i]; p < Arow[i + 1]; ++p) {
+      const int j = Acol[p];
+      const int kmax = i < j ? i : j;
+      CT s = (CT)Aval[p];
+      int il = lb, iu = Ucp[j];
+      const int ue = Ucp[j + 1];
+      while (il < le && iu < ue) {
+        const int jl = Lcol[il], ju = Uri[iu];
+        if (jl >= kmax || ju >= kmax) break;
+        if (jl == ju) {
+          s = fma(-cvt<CT>(Lold[il]), cvt<CT>(Uold[iu]), s);
+          ++il;
+          ++iu;
+        } else if (jl < ju) {
+          ++il;
+        } else {
+          ++iu;
+        }
+      }
+      if (i > j) {
+        const CT nv = s / cvt<CT>(Uold[ue - 1]);
+        while (Lcol[lpos] != j) ++lpos;
+        const double d = (double)nv - (double)cvt<CT>(Lold[lpos]);
+        acc = fma(d, d, acc);
+        Lnew[lpos] = cvt<FT>(nv);
+        ++lpos;
+      } else {
+        while (Uri[iu] != i) ++iu;
+        const double d = (double)s - (double)cvt<CT>(Uold[iu]);
+        acc = fma(d, d, acc);
+        Unew[iu] = cvt<FT>(s);
+      }
+    }
+  }
+  finish_sum(acc, partials, counter, step);
+}
+
+// sum over S(A) of (sum_{k<=min(i,j)} l_ik u_kj - a_ij)^2
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_ilu_residual(
+    int n, const int *__restrict__ Arow, const int *__restrict__ Acol,
+    const double *__restrict__ Aval, const int *__restrict__ Lrow, const int *__restrict__ Lcol,
+    const FT *__restrict__ L, const int *__restrict__ Ucp, const int *__restrict__ Uri,
+    const FT *__restrict__ U, double *partials, int *counter, double *out) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lb = Lrow[i], le = Lrow[i + 1];
+    for (int p = Arow[i]; p < Arow[i + 1]; ++p) {
+      const int j = Acol[p];
+      double t = 0.0;
+      int il = lb, iu = Ucp[j];
+      const int ue = Ucp[j + 1];
+      while (il < le && iu < ue) {
+        const int jl = Lcol[il], ju = Uri[iu];
+        if (jl == ju) {
+          t = fma((double)cvt<CT>(L[il]), (double)cvt<CT>(U[iu]), t);
+          ++il;
+          ++iu;
+        } else if (jl < ju) {
+          ++il;
+        } else {
+          ++iu;
+        }
+      }
+      const double d = t - Aval[p];
+      acc = fma(d, d, acc);
+    }
+  }
+  finish_sum(acc, partials, counter, out);
+}
+
+// ---------------------------------------------------------------- BCSR
+// Block sweep (src/parilu_v0_3_bcsr.cpp:129-249 in synchronous form):
+//   S = A_ij - sum_{k<min} L_ik U_kj ;  L_ij = S inv(U_jj) (i > j), U_ij = S.
+// One thread per (block, row-of-block): the bs threads of a block cooperate
+// through shared memory for the S inv(U_jj) product.  U blocks (BCSC) are
+// stored untransposed, as LACE keeps them (control/magma_zmtranspose.cpp:358-363).
+template <typename FT, typename CT>
+__device__ void blk_inverse(int bs, const CT *a, CT *inv) {
+  // Gauss-Jordan without pivoting (LACE's data_inverse is LU without
+  // pivoting, src/inverse.cpp:46); bs <= 8
+  CT w[8][16];
+  for (int r = 0; r < bs; ++r)
+    for (int c = 0; c < 2 * bs; ++c) w[r][c] = (c < bs) ? a[r * bs + c] : (CT)(c - bs == r ? 1 : 0);
+  for (int p = 0; p < bs; ++p) {
+    CT rp = (CT)1 / w[p][p];
+    for (int c = 0; c < 2 * bs; ++c) w[p][c] *= rp;
+    for (int r = 0; r < bs; ++r) {
+      if (r == p) continue;
+      CT f = w[r][p];
+      for (int c = 0; c < 2 * bs; ++c) w[r][c] -= f * w[p][c];
+    }
+  }
+  for (int r = 0; r < bs; ++r)
+    for (int c = 0; c < bs; ++c) inv[r * bs + c] = w[r][bs + c];
+}
+
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_bcsr_parilu_sweep(
+    int nb, int bs, const int *__restrict__ Arow, const int *__restrict__ Acol,
+    const double *__restrict__ Aval, const int *__restrict__ Lrow, const int *__restrict__ Lcol,
+    const FT *__restrict__ Lold, FT *__restrict__ Lnew, const int *__restrict__ Ucp,
+    const int *__restrict__ Uri, const FT *__restrict__ Uold, FT *__restrict__ Unew,
+    double *partials, int *counter, double *step) {
+  const int ld = bs * bs;
+  double acc = 0.0;
+  // one thread per block row of A
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += gridDim.x * blockDim.x) {
+    const int lb = Lrow[I], le = Lrow[I + 1];
+    int lpos = lb;
+    for (int p = Arow[I]; p < Arow[I + 1]; ++p) {
+      const int J = Acol[p];
+      const int kmax = I < J ? I : J;
+      CT S[64];
+      for (int e = 0; e < ld; ++e) S[e] = (CT)Aval[(size_t)p * ld + e];
+      int il = lb, iu = Ucp[J];
+      const int ue = Ucp[J + 1];
+      while (il < le && iu < ue) {
+        const int jl = Lcol[il], ju = Uri[iu];
+        if (jl >= kmax || ju >= kmax) break;
+        if (jl == ju) {
+          const FT *Lb = Lold + (size_t)il * ld;
+          const FT *Ub = Uold + (size_t)iu * ld;
+          for (int r = 0; r < bs; ++r)
+            for (int c = 0; c < bs; ++c) {
+              CT t = 0;
+              for (int q = 0; q < bs; ++q) t = fma(cvt<CT>(Lb[r * bs + q]), cvt<CT>(Ub[q * bs + c]), t);
+              S[r * bs + c] -= t;
+            }
+          ++il;
+          ++iu;
+        } else if (jl < ju) {
+          ++il;
+        } else {
+          ++iu;
+        }
+      }
+      if (I > J) {
+        CT D[64], Di[64];
+        const FT *Ud = Uold + (size_t)(ue - 1) * ld;
+        for (int e = 0; e < ld; ++e) D[e] = cvt<CT>(Ud[e]);
+        blk_inverse<FT, CT>(bs, D, Di);
+        while (Lcol[lpos] != J) ++lpos;
+        FT *Ln = Lnew + (size_t)lpos * ld;
+        const FT *Lo = Lold + (size_t)lpos * ld;
+        for (int r = 0; r < bs; ++r)
+          for (int c = 0; c < bs; ++c) {
+            CT t = 0;
+            for (int q = 0; q < bs; ++q) t = fma(S[r * bs + q], Di[q * bs + c], t);
+            const double d = (double)t - (double)cvt<CT>(Lo[r * bs + c]);
+            acc = fma(d, d, acc);
+            Ln[r * bs + c] = cvt<FT>(t);
+          }
+        ++lpos;
+      } else {
+        while (Uri[iu] != I) ++iu;
+        FT *Un = Unew + (size_t)iu * ld;
+        const FT *Uo = Uold + (size_t)iu * ld;
+        for (int e = 0; e < ld; ++e) {
+          const double d = (double)S[e] - (double)cvt<CT>(Uo[e]);
+          acc = fma(d, d, acc);
+          Un[e] = cvt<FT>(S[e]);
+        }
+      }
+    }
+  }
+  finish_sum(acc, partials, counter, step);
+}
+
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_block_diag_inverse(int nb, int bs,
+                                                              const int *__restrict__ Urow,
+                                                              const FT *__restrict__ U,
+                                                              FT *__restrict__ dinv, int *status) {
+  const int ld = bs * bs;
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += gridDim.x * blockDim.x) {
+    CT D[64], Di[64];
+    const FT *Ud = U + (size_t)Urow[I] * ld;  // diagonal block first in its block row
+    for (int e = 0; e < ld; ++e) D[e] = cvt<CT>(Ud[e]);
+    blk_inverse<FT, CT>(bs, D, Di);
+    bool bad = false;
+    for (int e = 0; e < ld; ++e) {
+      if (!(Di[e] == Di[e]) || isinf((double)Di[e])) bad = true;
+      dinv[(size_t)I * ld + e] = cvt<FT>(Di[e]);
+    }
+    if (bad) atomicOr(status, kStatusBreakdown);
+  }
+}
+
+// ------------------------------------------------------------ helpers
+
+template <typename S, typename D>
+__global__ void k_gather(int count, const int *__restrict__ perm, const S *__restrict__ src,
+                         D *__restrict__ dst) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
+    const int q = perm ? perm[p] : p;
+    dst[p] = cvt<D>(src[q]);
+  }
+}
+
+template <typename S>
+static void gather_dst(cudaStream_t s, int count, const int *perm, const S *src, VType td, void *dst) {
+  int grid = min((count + 255) / 256, num_sms() * 16);
+  if (grid < 1) return;
+  switch (td) {
+    case VType::F64: k_gather<S, double><<<grid, 256, 0, s>>>(count, perm, src, (double *)dst); break;
+    case VType::F32: k_gather<S, float><<<grid, 256, 0, s>>>(count, perm, src, (float *)dst); break;
+    case VType::BF16: k_gather<S, __nv_bfloat16><<<grid, 256, 0, s>>>(count, perm, src, (__nv_bfloat16 *)dst); break;
+  }
+}
+
+void launch_gather(cudaStream_t s, int count, const int *perm, VType ts, const void *src, VType td,
+                   void *dst) {
+  switch (ts) {
+    case VType::F64: gather_dst<double>(s, count, perm, (const double *)src, td, dst); break;
+    case VType::F32: gather_dst<float>(s, count, perm, (const float *)src, td, dst); break;
+    case VType::BF16: gather_dst<__nv_bfloat16>(s, count, perm, (const __nv_bfloat16 *)src, td, dst); break;
+  }
+}
+
+void launch_convert(cudaStream_t s, int count, VType ts, const void *src, VType td, void *dst) {
+  launch_gather(s, count, nullptr, ts, src, td, dst);
+}
+
+static int sweep_grid(int rows) {
+  int g = (rows + kPTPB - 1) / kPTPB;
+  int cap = num_sms() * 8;
+  return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
+void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *Lold, void *Lnew,
+                         const void *Uold, void *Unew, double *step) {
+  if (a.bs > 0) {
+    const int grid = sweep_grid(a.n);
+    if (t == VType::F64)
+      k_bcsr_parilu_sweep<double, double><<<grid, kPTPB, 0, s>>>(
+          a.n, a.bs, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const double *)Lold, (double *)Lnew,
+          a.Ucp, a.Uri, (const double *)Uold, (double *)Unew, a.partials, a.counter, step);
+    else if (t == VType::F32)
+      k_bcsr_parilu_sweep<float, float><<<grid, kPTPB, 0, s>>>(
+          a.n, a.bs, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const float *)Lold, (float *)Lnew,
+          a.Ucp, a.Uri, (const float *)Uold, (float *)Unew, a.partials, a.counter, step);
+    else
+      k_bcsr_parilu_sweep<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+          a.n, a.bs, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const __nv_bfloat16 *)Lold,
+          (__nv_bfloat16 *)Lnew, a.Ucp, a.Uri, (const __nv_bfloat16 *)Uold, (__nv_bfloat16 *)Unew,
+          a.partials, a.counter, step);
+    return;
+  }
+  const int grid = sweep_grid(a.n);
+  if (t == VType::F64)
+    k_parilu_sweep<double, double><<<grid, kPTPB, 0, s>>>(
+        a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const double *)Lold, (double *)Lnew, a.Ucp,
+        a.Uri, (const double *)Uold, (double *)Unew, a.partials, a.counter, step);
+  else if (t == VType::F32)
+    k_parilu_sweep<float, float><<<grid, kPTPB, 0, s>>>(
+        a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const float *)Lold, (float *)Lnew, a.Ucp,
+        a.Uri, (const float *)Uold, (float *)Unew, a.partials, a.counter, step);
+  else
+    k_parilu_sweep<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+        a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const __nv_bfloat16 *)Lold,
+        (__nv_bfloat16 *)Lnew, a.Ucp, a.Uri, (const __nv_bfloat16 *)Uold, (__nv_bfloat16 *)Unew,
+        a.partials, a.counter, step);
+}
+
+void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
+                         double *out) {
+  const int grid = sweep_grid(a.n);
+  if (t == VType::F64)
+    k_ilu_residual<double, double><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol,
+                                                          (const double *)L, a.Ucp, a.Uri,
+                                                          (const double *)U, a.partials, a.counter, out);
+  else if (t == VType::F32)
+    k_ilu_residual<float, float><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol,
+                                                        (const float *)L, a.Ucp, a.Uri,
+                                                        (const float *)U, a.partials, a.counter, out);
+  else
+    k_ilu_residual<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+        a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const __nv_bfloat16 *)L, a.Ucp, a.Uri,
+        (const __nv_bfloat16 *)U, a.partials, a.counter, out);
+}
+
+void launch_block_diag_inverse(cudaStream_t s, int nb, int bs, const int *Urow, VType t,
+                               const void *Uval, void *dinv, int *status) {
+  const int grid = sweep_grid(nb);
+  if (t == VType::F64)
+    k_block_diag_inverse<double, double><<<grid, kPTPB, 0, s>>>(nb, bs, Urow, (const double *)Uval,
+                                                               (double *)dinv, status);
+  else if (t == VType::F32)
+    k_block_diag_inverse<float, float><<<grid, kPTPB, 0, s>>>(nb, bs, Urow, (const float *)Uval,
+                                                             (float *)dinv, status);
+  else
+    k_block_diag_inverse<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+        nb, bs, Urow, (const __nv_bfloat16 *)Uval, (__nv_bfloat16 *)dinv, status);
+}
+
+}  // namespace lace

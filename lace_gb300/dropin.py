@@ -1,0 +1,196 @@
+"""LACE-named entry points called through LACE's data_d_matrix container.
+
+These mirror how LACE's own tests drive the path (testing/test_iLU.cpp,
+testing/test_linearSolver.cpp): build host containers, call
+data_PariLU_v0_3*, convert, call data_fgmres_householder_restart, check the
+residual.  The library allocates the output factor arrays with
+posix_memalign (as LACE_CALLOC does); `free_matrix` releases them with free().
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import DataMatrix, GmresLog, GmresParam, PrecondLog, lib
+
+# data_storage_t / data_diagorder_t / data_uplo_t (include/dense_types.h)
+Magma_CSR, Magma_DENSE, Magma_BCSR, Magma_CSC = 611, 614, 615, 616
+Magma_CSRL, Magma_CSRU, Magma_CSCU, Magma_BCSCU = 627, 628, 635, 646
+Magma_UNITY, Magma_VALUE = 593, 594
+MagmaUpper, MagmaLower, MagmaFull = 121, 122, 123
+MagmaRowMajor, MagmaColMajor = 101, 102
+
+_libc = C.CDLL(None)
+_libc.free.argtypes = [C.c_void_p]
+
+
+class Mat:
+    """A DataMatrix plus the numpy arrays it points into."""
+
+    def __init__(self):
+        self.m = DataMatrix()
+        self.keep = []
+
+    @property
+    def ref(self):
+        return C.byref(self.m)
+
+    def _own(self, a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        self.keep.append(a)
+        return a.ctypes.data
+
+
+def csr(row, col, val, n, storage=Magma_CSR) -> Mat:
+    M = Mat()
+    M.m.storage_type = storage
+    M.m.num_rows = n
+    M.m.num_cols = n
+    M.m.nnz = len(col)
+    M.m.true_nnz = len(col)
+    M.m.major = MagmaRowMajor
+    M.m.fill_mode = MagmaFull
+    M.m.row = M._own(row, np.int32)
+    M.m.col = M._own(col, np.int32)
+    M.m.val = M._own(val, np.float64)
+    return M
+
+
+def bcsr(A) -> Mat:
+    """problems.BCSR -> Magma_BCSR container (row-major blocks)."""
+    M = Mat()
+    M.m.storage_type = Magma_BCSR
+    M.m.num_rows = A.nb
+    M.m.num_cols = A.nb
+    M.m.blocksize = A.bs
+    M.m.ldblock = A.bs * A.bs
+    M.m.numblocks = A.nblk
+    M.m.nnz = A.nblk * A.bs * A.bs
+    M.m.row = M._own(A.row, np.int32)
+    M.m.col = M._own(A.col, np.int32)
+    M.m.val = M._own(np.asarray(A.val).reshape(-1), np.float64)
+    return M
+
+
+def dense(v) -> Mat:
+    v = np.asarray(v, dtype=np.float64)
+    M = Mat()
+    M.m.storage_type = Magma_DENSE
+    M.m.num_rows = len(v)
+    M.m.num_cols = 1
+    M.m.nnz = len(v)
+    M.m.ld = len(v)
+    M.m.major = MagmaColMajor
+    M.m.val = M._own(v.copy(), np.float64)
+    return M
+
+
+def vector_values(M: Mat) -> np.ndarray:
+    return np.ctypeslib.as_array(C.cast(M.m.val, C.POINTER(C.c_double)), shape=(M.m.num_rows,)).copy()
+
+
+def matrix_arrays(m: DataMatrix):
+    """(ptr, idx, val) copies of a library-filled container."""
+    n = m.num_rows
+    nidx = m.numblocks if m.blocksize > 0 and m.numblocks > 0 else m.nnz
+    nval = m.nnz
+    ptr = np.ctypeslib.as_array(C.cast(m.row, C.POINTER(C.c_int)), shape=(n + 1,)).copy()
+    idx = np.ctypeslib.as_array(C.cast(m.col, C.POINTER(C.c_int)), shape=(nidx,)).copy()
+    val = np.ctypeslib.as_array(C.cast(m.val, C.POINTER(C.c_double)), shape=(nval,)).copy()
+    return ptr, idx, val
+
+
+def free_matrix(m: DataMatrix) -> None:
+    """data_zmfree for library-allocated members."""
+    for name in ("val", "col", "row", "rowidx", "diag", "list", "blockinfo"):
+        p = getattr(m, name)
+        if p:
+            _libc.free(p)
+            setattr(m, name, None)
+
+
+def parilu(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None, gpu_name: bool = False):
+    """data_PariLU_v0_3[_gpu] (max_sweeps None) or the prescribed-sweeps
+    variants.  Returns (L arrays, U arrays (CSC), log dict)."""
+    L = DataMatrix()
+    U = DataMatrix()
+    L.storage_type = Magma_CSRL
+    U.storage_type = Magma_CSCU
+    log = PrecondLog()
+    f = lib()
+    if max_sweeps is None:
+        if gpu_name:
+            f.data_PariLU_v0_3_gpu(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log), 0)
+        else:
+            f.data_PariLU_v0_3(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log))
+    else:
+        log.maxSweeps = max_sweeps
+        if gpu_name:
+            f.data_PariLU_v0_3_gpu_prescribedSweeps(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log))
+        else:
+            f.data_PariLU_v0_3_prescribedSweeps(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log))
+    if log.sweeps < 0:
+        from . import LaceError
+        raise LaceError(f.lace_gpu_last_error(), "data_PariLU_v0_3")
+    la = matrix_arrays(L)
+    ua = matrix_arrays(U)
+    info = {k: getattr(log, k) for k in ("sweeps", "tol", "finalStep", "A_Frobenius", "precond_generation_time",
+                                         "initial_residual", "initial_nonlinear_residual",
+                                         "nonlinear_residual", "omp_num_threads")}
+    info["L_storage"] = L.storage_type
+    info["U_storage"] = U.storage_type
+    free_matrix(L)
+    free_matrix(U)
+    return la, ua, info
+
+
+def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
+                               rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, single_cycle=False):
+    bv = dense(b)
+    xv = dense(x0)
+    par = GmresParam()
+    par.search_max = search_max
+    par.restart_max = restart_max
+    par.rtol = rtol
+    par.tol_type = tol_type
+    par.user_csrtrsv_choice = choice
+    par.monitorOrthog = monitor_orthog
+    par.precondition = 1
+    log = GmresLog()
+    f = lib()
+    Lr = L.ref if L is not None else None
+    Ur = U.ref if U is not None else None
+    fn = f.data_fgmres_householder if single_cycle else f.data_fgmres_householder_restart
+    rc = fn(A.ref, bv.ref, xv.ref, Lr, Ur, C.byref(par), C.byref(log))
+    return vector_values(xv), rc, {k: getattr(log, k) for k in ("restarts", "search_directions", "solve_time",
+                                                                "initial_residual", "final_residual")}
+
+
+def spmv(alpha: float, A: Mat, x, beta: float = 0.0, y=None):
+    nout = A.m.num_rows * (A.m.blocksize if A.m.storage_type == Magma_BCSR else 1)
+    xv = dense(x)
+    yv = dense(np.zeros(nout) if y is None else y)
+    rc = lib().data_z_spmv(alpha, A.ref, xv.ref, beta, yv.ref)
+    return vector_values(yv), rc
+
+
+def parcsrtrsv(uplo, storage, diag, ptr, idx, val, rhs, y0=None, tol=1.0):
+    n = len(ptr) - 1
+    ptr = np.ascontiguousarray(ptr, dtype=np.int32)
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+    y = np.zeros(n) if y0 is None else np.ascontiguousarray(y0, dtype=np.float64).copy()
+    it = C.c_int()
+    rc = lib().data_parcsrtrsv(uplo, storage, diag, n, val.ctypes.data, ptr.ctypes.data, idx.ctypes.data,
+                               rhs.ctypes.data, y.ctypes.data, tol, C.byref(it))
+    return y, it.value, rc
+
+
+def zilures(A: Mat, L: Mat, U: Mat):
+    res = C.c_double()
+    nl = C.c_double()
+    LU = DataMatrix()
+    rc = lib().data_zilures(A.m, L.m, U.m, C.byref(LU), C.byref(res), C.byref(nl))
+    return res.value, nl.value, rc

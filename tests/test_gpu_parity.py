@@ -1,0 +1,262 @@
+"""GPU parity: every CUDA kernel of the path against the CPU oracle.
+
+Tolerances (floating point, stated per test): FP64 kernels agree with the
+oracle to rounding (1e-12 relative or tighter), FP32/BF16 factor paths are
+checked on the solve they serve (same 1e-10 relative residual, iteration
+counts within the stated band).
+"""
+import numpy as np
+import pytest
+
+from lace_gb300 import problems as P
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lg(torch_cuda):
+    import lace_gb300
+    lace_gb300.lib()
+    return lace_gb300
+
+
+def dev(torch, a):
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+MATS = {
+    "lap64": lambda: P.laplace2d(64),
+    "cd16": lambda: P.convdiff3d(16),
+    "cd_20x9x7": lambda: P.convdiff3d(20, 9, 7),
+    "tref19": lambda: P.trefethen(19),
+    "aniso77": lambda: P.aniso2d(77, 0.01),
+}
+
+
+@pytest.mark.parametrize("name", list(MATS))
+@pytest.mark.parametrize("lanes", [0, 2, 4, 8, 16, 32])
+def test_spmv(lg, torch_cuda, name, lanes):
+    A = MATS[name]()
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(A.n)
+    y0 = rng.standard_normal(A.n)
+    with lg.Context(0) as ctx:
+        ctx.set_options(spmv_lanes=lanes)
+        ctx.upload(A)
+        xd, yd = dev(torch_cuda, x), dev(torch_cuda, y0)
+        ctx.spmv(xd, yd, alpha=1.5, beta=-0.5)
+        y = yd.cpu().numpy()
+    ref = orc.spmv(A.row, A.col, A.val, x, 1.5, -0.5, y0)
+    scale = np.abs(A.val) @ np.ones(1) if False else None
+    # FMA vs separate multiply-add: bound by |alpha||A||x| + |beta||y| per row
+    bound = 1e-14 * (1.5 * np.add.reduceat(np.abs(A.val * x[A.col]), A.row[:-1]) + 0.5 * np.abs(y0)) + 1e-300
+    assert np.all(np.abs(y - ref) <= bound)
+
+
+@pytest.mark.parametrize("name", ["lap64", "cd16", "cd_20x9x7", "tref19"])
+@pytest.mark.parametrize("sweeps", [0, 1, 3, 5])
+def test_parilu_sync_sweeps(lg, name, sweeps):
+    """data_PariLU_v0_3_prescribedSweeps on the GPU == synchronous oracle
+    sweeps: factor values within 1e-12 relative, nonlinear residual within
+    1e-12 relative, identical patterns."""
+    from lace_gb300 import dropin
+    A = MATS[name]()
+    if sweeps == 0:
+        pytest.skip("prescribed sweeps need >= 1")
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(dropin.csr(A.row, A.col, A.val, A.n), max_sweeps=sweeps)
+    F = orc.parilu(A.row, A.col, A.val, sweeps, mode="sync", stop_eps=True)
+    assert np.array_equal(lp, F.L.ptr) and np.array_equal(li, F.L.idx)
+    assert np.array_equal(up, F.U.ptr) and np.array_equal(ui, F.U.idx)
+    assert relmax(lv, F.L.val) <= 1e-12
+    assert relmax(uv, F.U.val) <= 1e-12
+    assert info["sweeps"] == len(F.steps)
+    nl = orc.ilu_nonlinres(A.row, A.col, A.val, F)
+    assert abs(info["nonlinear_residual"] - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14 * info["A_Frobenius"]
+
+
+@pytest.mark.parametrize("name", ["lap64", "cd16"])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
+def test_parilu0_nonlinres(lg, name, prec, tol):
+    A = MATS[name]()
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec)
+        ctx.upload(A)
+        step, nl = ctx.parilu0(3)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync", f32=(prec == "fp32"))
+    F64 = orc.Factors(orc.Tri(F.L.ptr, F.L.idx, F.L.val.astype(np.float64)),
+                      orc.Tri(F.U.ptr, F.U.idx, F.U.val.astype(np.float64)), F.steps)
+    ref = orc.ilu_nonlinres(A.row, A.col, A.val, F64) / np.linalg.norm(A.val)
+    assert abs(nl - ref) <= tol * ref
+    assert abs(step - F.steps[-1]) <= 1e-6 * F.steps[-1] + 1e-300
+
+
+def _oracle_tri(F, which):
+    n = len(F.L.ptr) - 1
+    if which == 0:
+        return F.L, True, True
+    if which == 1:
+        return F.U_csr(), False, False
+    if which == 2:
+        return F.U, True, False
+    lp, li, lv, _ = orc.transpose(F.L.ptr, F.L.idx, F.L.val, n)
+    return orc.Tri(lp, li, lv), False, True
+
+
+@pytest.mark.parametrize("name", ["lap64", "cd16", "cd_20x9x7", "aniso77", "tref19"])
+@pytest.mark.parametrize("mode,rpl", [("syncfree", 1), ("syncfree", 2), ("syncfree", 4), ("syncfree", 8),
+                                      ("levels", 0)])
+def test_sptrsv_fp64(lg, torch_cuda, name, mode, rpl):
+    """Exact solves with all four triangles (L, U, U^T, L^T): within 1e-12
+    relative of the oracle's sequential solve."""
+    A = MATS[name]()
+    F = orc.parilu(A.row, A.col, A.val, 2, mode="sync")
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(A.n)
+    with lg.Context(0) as ctx:
+        ctx.set_options(trsv=mode, rows_per_lane=rpl)
+        ctx.upload(A)
+        ctx.parilu0(2)
+        for which in range(4):
+            xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+            ctx.sptrsv(which, dev(torch_cuda, b), xd)
+            T, lower, unit = _oracle_tri(F, which)
+            ref = orc.trsv(T.ptr, T.idx, T.val, b, lower, unit)
+            assert relmax(xd.cpu().numpy(), ref) <= 1e-12, (which, relmax(xd.cpu().numpy(), ref))
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", 1e-4), ("bf16", 5e-2)])
+def test_sptrsv_low_precision(lg, torch_cuda, prec, tol):
+    A = MATS["cd16"]()
+    F = orc.parilu(A.row, A.col, A.val, 2, mode="sync")
+    b = np.random.default_rng(3).standard_normal(A.n)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec)
+        ctx.upload(A)
+        ctx.parilu0(2)
+        z = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        ctx.apply_precond(dev(torch_cuda, b), z)
+    ref = orc.trsv(*(lambda U: (U.ptr, U.idx, U.val))(F.U_csr()),
+                   orc.trsv(F.L.ptr, F.L.idx, F.L.val, b, True, True), False, False)
+    assert relmax(z.cpu().numpy(), ref) <= tol
+
+
+def _true_rel(A, x, b):
+    return np.linalg.norm(b - A.matvec(x)) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name,sweeps,m", [("lap64", 5, 30), ("cd16", 3, 50), ("cd_20x9x7", 3, 20)])
+@pytest.mark.parametrize("graph", [True, False])
+def test_fgmres_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph):
+    """Same factors, FP64: GPU FGMRES-Householder (compact-WY reflectors,
+    sync-free solves) reaches 1e-10 relative residual within +-2 directions
+    of the oracle, which mirrors LACE's FGMRES-Householder."""
+    A = MATS[name]()
+    b = A.matvec(np.ones(A.n)) if name == "lap64" else P.rhs_normal(A.n, 0)
+    F = orc.parilu(A.row, A.col, A.val, sweeps, mode="sync")
+    r = orc.fgmres({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                   search_max=m, restart_max=50, rtol=1e-10)
+    with lg.Context(0) as ctx:
+        ctx.set_options(use_graph=graph)
+        ctx.upload(A)
+        ctx.parilu0(sweeps)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=m, restart_max=50, rtol=1e-10)
+        x = xd.cpu().numpy()
+    assert res.converged and r.converged
+    assert abs(res.total_iterations - r.total_iterations) <= 2, (res.total_iterations, r.total_iterations)
+    assert abs(res.initial_residual - r.initial_residual) <= 1e-12 * r.initial_residual
+    assert _true_rel(A, x, b) <= 2e-10
+    assert np.linalg.norm(x - r.x) <= 1e-7 * np.linalg.norm(r.x)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+@pytest.mark.parametrize("mode", ["syncfree", "levels", "jacobi"])
+def test_fgmres_mixed_precision(lg, torch_cuda, prec, mode):
+    """FP32 (or BF16-stored) factors and solves inside the FP64 FGMRES reach
+    the same 1e-10 relative residual (the flexible basis absorbs the inexact
+    preconditioner)."""
+    A = MATS["cd16"]()
+    b = P.rhs_normal(A.n, 0)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync")
+    r = orc.fgmres({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                   search_max=50, restart_max=50, rtol=1e-10)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec, trsv=mode, jacobi_sweeps=12)
+        ctx.upload(A)
+        ctx.parilu0(3)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=50, rtol=1e-10)
+        x = xd.cpu().numpy()
+    assert res.converged
+    assert _true_rel(A, x, b) <= 2e-10
+    if mode != "jacobi" and prec == "fp32":
+        assert abs(res.total_iterations - r.total_iterations) <= 2
+
+
+def test_dropin_trefethen_linear_solver(lg):
+    """LACE's FGMRESHouseholderPreconditionedRestart test
+    (testing/test_linearSolver.cpp:621-726) through the drop-in entry points:
+    Trefethen_20, b = ones, x0 = 0, abs tol 1e-3, search 20, restart 20,
+    monitorOrthog on, exact solves; then ParCSRTRSV and no preconditioner."""
+    from lace_gb300 import dropin
+    A = P.trefethen(19)
+    Am = dropin.csr(A.row, A.col, A.val, A.n)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(Am, reduction=1e-15)
+    L = dropin.csr(lp, li, lv, A.n, dropin.Magma_CSRL)
+    U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
+    b = np.ones(A.n)
+    for choice in (0, 1, 2):
+        x, rc, log = dropin.fgmres_householder_restart(Am, b, np.zeros(A.n), L, U, search_max=20,
+                                                       restart_max=20, rtol=1e-3, tol_type=0,
+                                                       choice=choice, monitor_orthog=1)
+        assert rc == 0
+        assert np.linalg.norm(b - A.matvec(x)) <= 1e-3
+
+
+def test_dropin_parilu_vs_exact_ilu0(lg):
+    """LACE's test_iLU PariLUv0_3 (testing/test_iLU.cpp:185-223): residuals
+    within 1000x of the exact ILU(0) (MKL dcsrilu0 semantics; the oracle's
+    one-thread asynchronous sweep is exactly ILU(0))."""
+    from lace_gb300 import dropin
+    A = P.trefethen(19)
+    Am = dropin.csr(A.row, A.col, A.val, A.n)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(Am, reduction=1e-20)
+    G = orc.Factors(orc.Tri(lp, li, lv), orc.Tri(up, ui, uv), [])
+    res, nl = orc.zilures(A.row, A.col, A.val, G)
+    E = orc.parilu(A.row, A.col, A.val, 1, mode="async")
+    eres, enl = orc.zilures(A.row, A.col, A.val, E)
+    assert res <= 1000 * eres and nl <= 1000 * max(enl, 1e-300) + 1e-12
+    # and data_zilures on the GPU agrees with the oracle's nonlinear residual
+    L = dropin.csr(lp, li, lv, A.n, dropin.Magma_CSRL)
+    U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
+    r2, nl2, rc = dropin.zilures(Am, L, U)
+    assert rc == 0 and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-13
+
+
+def test_dropin_spmv_and_parcsrtrsv(lg):
+    from lace_gb300 import dropin
+    A = P.convdiff3d(8)
+    x = np.random.default_rng(0).standard_normal(A.n)
+    y, rc = dropin.spmv(2.0, dropin.csr(A.row, A.col, A.val, A.n), x)
+    assert rc == 0
+    assert np.allclose(y, 2.0 * A.matvec(x), rtol=1e-13, atol=1e-13)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync")
+    b = np.random.default_rng(1).standard_normal(A.n)
+    yl, it, rc = dropin.parcsrtrsv(dropin.MagmaLower, dropin.Magma_CSRL, dropin.Magma_UNITY,
+                                   F.L.ptr, F.L.idx, F.L.val, b, tol=1e-24)
+    assert rc == 0
+    ref = orc.trsv(F.L.ptr, F.L.idx, F.L.val, b, True, True)
+    assert relmax(yl, ref) <= 1e-12
+    Ur = F.U_csr()
+    yu, it, rc = dropin.parcsrtrsv(dropin.MagmaUpper, dropin.Magma_CSRU, dropin.Magma_VALUE,
+                                   Ur.ptr, Ur.idx, Ur.val, b, tol=1e-24)
+    assert rc == 0 and relmax(yu, orc.trsv(Ur.ptr, Ur.idx, Ur.val, b, False, False)) <= 1e-12
+    # wrong storage/fill combination: LACE returns -1 (src/trisolve.cpp:298-304)
+    _, _, rc = dropin.parcsrtrsv(dropin.MagmaLower, dropin.Magma_CSRU, dropin.Magma_UNITY,
+                                 F.L.ptr, F.L.idx, F.L.val, b)
+    assert rc == -1
