@@ -1,0 +1,366 @@
+"""Benchmark: time to a 1e-10 relative residual on one GB300.
+
+Workload (one "step" = one complete preconditioned solve of one system):
+  3D 7-point first-order upwind convection-diffusion, 128^3 grid
+  (n = 2,097,152, nnz = 14,581,760), cell Peclet 10, velocity (1, .5, .25);
+  b ~ N(0,1) seed 0, x0 = 0; ParILU(0) with 3 synchronous sweeps from the
+  A-initial guess; FGMRES-Householder(50) restarted, right-preconditioned by
+  exact (sync-free) triangular solves; stop at ||r|| <= 1e-10 ||r0||.
+Headline arm: FP32 factors and solves inside the FP64 FGMRES ("mixed");
+the all-FP64 GPU path is timed beside it.
+
+`value` is device time per solve with A resident in HBM (CUDA events on the
+solver stream).  `e2e` is the same solve through the LACE-named C ABI
+(data_PariLU_v0_3_prescribedSweeps + data_fgmres_householder_restart) from
+host buffers, copies included.  `--impl reference` times the CPU
+restatement of LACE's path (the oracle port; LACE's own build needs MKL
+and the LACE tree, neither of which exists on the GPU host) on all host
+cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = 128
+SWEEPS = 3
+M = 50
+RTOL = 1e-10
+RESTART_MAX = 20
+METRIC = "solve s to 1e-10 resid, mixed-prec vs FP64 on 1 GB300; SpMV/SpTRSV HBM GB/s"
+WORKLOAD = (f"convdiff3d {GRID}^3 7-pt upwind Pe10 (n={GRID**3}, nnz=14581760), ParILU(0) {SWEEPS} sync sweeps, "
+            f"FGMRES-Householder({M}) to 1e-10 rel, b~N(0,1) seed 0, x0=0")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def build_problem():
+    from lace_gb300 import problems as P
+    A = P.convdiff3d(GRID)
+    b = P.rhs_normal(A.n, 0)
+    return A, b
+
+
+def algorithmic_bytes(A, nnzL, nnzU, prec: str):
+    """Compulsory bytes (each array read or written once, int32 indices)."""
+    n = A.n
+    sv = 4 if prec != "fp64" else 8
+    sx = sv
+    # SpTRSV L (unit diagonal, not read): off-diagonals + row pointers + rhs (FP64 q) + x
+    bl = (nnzL - n) * (sv + 4) + n * 4 + n * 8 + n * sx
+    # SpTRSV U: off-diagonals + diagonal + row pointers + rhs (t) + x
+    bu = (nnzU - n) * (sv + 4) + n * (4 + sv) + n * sx + n * sx
+    spmv = A.nnz * (8 + 4) + n * (4 + 8 + 8)
+    return {"sptrsv_L": bl, "sptrsv_U": bu, "sptrsv_pair": bl + bu, "spmv": spmv}
+
+
+def run_ours(args):
+    import torch
+
+    import lace_gb300 as lg
+    from lace_gb300 import dropin
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    A, b = build_problem()
+    stream = torch.cuda.Stream()
+    ctx = lg.Context(local, stream=stream)
+    ctx.upload(A)
+    bd = torch.tensor(b, dtype=torch.float64, device="cuda")
+    xd = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+
+    def solve(prec):
+        ctx.set_options(precision=prec)
+        with torch.cuda.stream(stream):
+            xd.zero_()
+        ctx.parilu0(SWEEPS)
+        return ctx.fgmres(bd, xd, search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+
+    def timed(prec, k, w):
+        for _ in range(w):
+            solve(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        times = []
+        res = None
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ev0.record(stream)
+            res = solve(prec)
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1e3)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if world > 1:
+            torch.distributed.barrier()
+        return times, wall, res
+
+    with ClockSampler(local) as clk:
+        t_mixed, wall_mixed, r_mixed = timed("fp32", args.steps, args.warmup)
+    clocks = clk.summary()
+    x_mixed = xd.cpu().numpy()
+    t_fp64, wall_fp64, r_fp64 = timed("fp64", max(2, args.steps // 2), 1)
+    x_fp64 = xd.cpu().numpy()
+
+    def true_rel(x):
+        return float(np.linalg.norm(b - A.matvec(x)) / np.linalg.norm(b))
+
+    # ---- dominant kernel (the sync-free SpTRSV pair, L then U), timed alone on the solver stream
+    ctx.set_options(precision="fp32")
+    ctx.parilu0(SWEEPS)
+    q = torch.randn(A.n, dtype=torch.float64, device="cuda")
+    z = torch.empty_like(q)
+    for _ in range(3):
+        ctx.apply_precond(q, z)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    reps = 20
+    ev0.record(stream)
+    for _ in range(reps):
+        ctx.apply_precond(q, z)
+    ev1.record(stream)
+    ev1.synchronize()
+    trsv_s = ev0.elapsed_time(ev1) / 1e3 / reps
+    # SpMV (FP64 operator) alone
+    y = torch.empty_like(q)
+    for _ in range(3):
+        ctx.spmv(q, y)
+    ev0.record(stream)
+    for _ in range(reps):
+        ctx.spmv(q, y)
+    ev1.record(stream)
+    ev1.synchronize()
+    spmv_s = ev0.elapsed_time(ev1) / 1e3 / reps
+    Lp = np.diff(A.row)
+    nnzL = int(np.sum(A.col <= np.repeat(np.arange(A.n), Lp)))
+    nnzU = int(np.sum(A.col >= np.repeat(np.arange(A.n), Lp)))
+    ab = algorithmic_bytes(A, nnzL, nnzU, "fp32")
+    trsv_gbs = ab["sptrsv_pair"] / trsv_s / 1e9
+    spmv_gbs = ab["spmv"] / spmv_s / 1e9
+
+    # ---- e2e: the LACE-named C ABI from host buffers (copies inside)
+    e2e = None
+    if not args.skip_e2e:
+        dropin.set_options(precision="fp32")
+        Am = dropin.csr(A.row, A.col, A.val, A.n)
+        e2e_times = []
+        for it in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            (lp, li, lv), (up, ui, uv), info = dropin.parilu(Am, max_sweeps=SWEEPS)
+            L = dropin.csr(lp, li, lv, A.n, dropin.Magma_CSRL)
+            U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
+            x, rc, glog = dropin.fgmres_householder_restart(Am, b, np.zeros(A.n), L, U, search_max=M,
+                                                           restart_max=RESTART_MAX, rtol=RTOL, tol_type=1)
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                e2e_times.append(time.perf_counter() - t0)
+        dropin.set_options()
+        e2e_rel = true_rel(x)
+        h2d = 2 * (A.nnz * 8) + (len(lv) + len(uv)) * 8 + 2 * A.n * 8
+        d2h = (len(lv) + len(uv)) * 8 + A.n * 8
+        e2e = {"value": statistics.median(e2e_times), "unit": "s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "true_rel_resid": e2e_rel,
+               "path": "data_PariLU_v0_3_prescribedSweeps + data_fgmres_householder_restart (fp32 factors)"}
+
+    # ---- CPU baseline: oracle port (LACE's path restated in C, OpenMP), rank 0, N=1
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(A, b)
+
+    # launches per solve: 3 sweeps + 3 factor finishing + per cycle (residual, init,
+    # m x [2 trsv, pass A/B/C], x update); graph nodes after convergence launch and exit
+    cycles = r_mixed.restarts + 1
+    launches_per_solve = 2 * SWEEPS + 2 + cycles * (3 + M * 5)
+    med = statistics.median(t_mixed)
+    if world > 1:
+        tt = torch.tensor([med], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        med = float(tt.item())
+    out = {
+        "metric": METRIC,
+        "value": med,
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": med * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 factors+SpTRSV / fp64 FGMRES+SpMV",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": WORKLOAD, "precision": "mixed", "l2": "inputs larger than L2 (A 175 MB, "
+                   "Krylov basis 0.86 GB)", "parallelism": "replicas" if world > 1 else "single"},
+        "iterations": {"mixed": r_mixed.total_iterations, "fp64": r_fp64.total_iterations},
+        "true_rel_resid": {"mixed": true_rel(x_mixed), "fp64": true_rel(x_fp64)},
+        "fp64": {"value": statistics.median(t_fp64), "unit": "s"},
+        "speedup_mixed_vs_fp64": statistics.median(t_fp64) / med,
+        "kernels": {"sptrsv_pair_s": trsv_s, "sptrsv_pair_gbs": trsv_gbs, "spmv_s": spmv_s,
+                    "spmv_gbs": spmv_gbs},
+        "roofline": {"bound": "hbm", "kernel": "sptrsv_syncfree L+U (fp32)", "achieved": trsv_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": trsv_gbs / hbm_peak,
+                     "peak_source": peak_src, "algorithmic_bytes": ab["sptrsv_pair"],
+                     "traffic": args.traffic},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": int(launches_per_solve * args.steps),
+        "wall_s_timed": wall_mixed,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+
+
+def cpu_baseline(A, b):
+    """The oracle port on every host core: ParILU sweeps + FGMRES-Householder
+    with exact FP64 triangular solves, one full solve (the bounded sample is
+    the whole workload: it fits in tens of seconds)."""
+    from oracle import oracle as orc
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    t0 = time.perf_counter()
+    F = orc.parilu(A.row, A.col, A.val, SWEEPS, mode="sync")
+    r = orc.fgmres({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                   search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+    t = time.perf_counter() - t0
+    return {"value": t, "unit": "s", "cores": cores, "kind": "port",
+            "sample": f"one full solve ({r.total_iterations} FGMRES directions, FP64, exact sequential SpTRSV)",
+            "converged": r.converged}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    A, b = build_problem()
+    from oracle import oracle as orc
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    times = []
+    r = None
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        F = orc.parilu(A.row, A.col, A.val, SWEEPS, mode="sync")
+        r = orc.fgmres({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                       search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    med = statistics.median(times)
+    sample = f"one full solve per step ({r.total_iterations} FGMRES directions, FP64)"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": med, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": med * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": WORKLOAD, "precision": "fp64 (LACE's path is FP64)"},
+        "cpu_baseline": {"value": med, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": med, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per launch of the dominant kernel pair, if captured")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -260,6 +260,12 @@ typedef struct lace_gpu_options {
 
 void lace_gpu_default_options(lace_gpu_options *opt);
 
+/* Options used by the drop-in (LACE-named) entry points of section 1, e.g.
+ * FP32 factors for data_PariLU_v0_3 / data_fgmres_householder_restart.
+ * NULL restores the defaults (FP64, sync-free solves, CUDA graphs).
+ * No counterpart in LACE, whose calls carry no precision or mode knobs. */
+int lace_gpu_dropin_set_options(const lace_gpu_options *opt);
+
 /* stream: a cudaStream_t (NULL = a stream owned by the context) */
 int lace_gpu_ctx_create(lace_gpu_ctx **ctx, int device, void *stream);
 int lace_gpu_ctx_destroy(lace_gpu_ctx *ctx);

@@ -155,6 +155,7 @@ SIGNATURES = {
     "data_fgmres_householder": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_zilures": (_i, [DataMatrix, DataMatrix, DataMatrix, _DM, C.POINTER(_d), C.POINTER(_d)]),
     "lace_gpu_default_options": (None, [C.POINTER(GpuOptions)]),
+    "lace_gpu_dropin_set_options": (_i, [C.POINTER(GpuOptions)]),
     "lace_gpu_ctx_create": (_i, [C.POINTER(_p), _i, _p]),
     "lace_gpu_ctx_destroy": (_i, [_p]),
     "lace_gpu_set_options": (_i, [_p, C.POINTER(GpuOptions)]),

@@ -20,6 +20,18 @@ namespace {
 
 std::mutex g_mu;
 lace_gpu_ctx *g_ctx = nullptr;
+lace_gpu_options g_dopt;
+bool g_dopt_set = false;
+
+// options the drop-in entry points run with (precision of the factors and
+// solves, SpTRSV mode, graphs); LACE's own calls carry no such knobs
+lace_gpu_options dropin_opts() {
+  if (!g_dopt_set) {
+    lace_gpu_default_options(&g_dopt);
+    g_dopt_set = true;
+  }
+  return g_dopt;
+}
 
 int default_ctx(lace_gpu_ctx **out) {
   if (!g_ctx) {
@@ -68,38 +80,6 @@ bool is_csr(data_storage_t s) {
   return s == Magma_CSR || s == Magma_CUCSR || s == Magma_CSRL || s == Magma_CSRU;
 }
 
-// ||L0 U0 - A|| over pattern(L0 U0) for the A-initial guess (the initial
-// residual LACE's ParILU records via data_zilures, src/parilu_v0_3.cpp:30-34)
-double initial_full_residual(const data_d_matrix *A) {
-  const int n = A->num_rows;
-  std::vector<double> acc(n, 0.0);
-  std::vector<int> mark(n, -1), list;
-  list.reserve(64);
-  double res = 0.0;
-  for (int i = 0; i < n; ++i) {
-    list.clear();
-    for (int p = A->row[i]; p < A->row[i + 1]; ++p) {
-      const int k = A->col[p];
-      if (k > i) break;
-      const double lik = (k == i) ? 1.0 : A->val[p];
-      for (int q = A->row[k]; q < A->row[k + 1]; ++q) {
-        const int j = A->col[q];
-        if (j < k) continue;
-        if (mark[j] != i) {
-          mark[j] = i;
-          acc[j] = 0.0;
-          list.push_back(j);
-        }
-        acc[j] += lik * A->val[q];
-      }
-    }
-    for (int p = A->row[i]; p < A->row[i + 1]; ++p)
-      if (mark[A->col[p]] == i) acc[A->col[p]] -= A->val[p];
-    for (int j : list) res += acc[j] * acc[j];
-  }
-  return std::sqrt(res);
-}
-
 int fill_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
                  const std::vector<int> &idx, const std::vector<double> &val, int blocksize) {
   release_members(B);
@@ -142,8 +122,7 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   lace_gpu_ctx *c = nullptr;
   int rc = default_ctx(&c);
   if (rc) return fail(rc);
-  lace_gpu_options o;
-  lace_gpu_default_options(&o);
+  lace_gpu_options o = dropin_opts();
   lace_gpu_set_options(c, &o);
   const bool bcsr = A->storage_type == Magma_BCSR;
   const int n = A->num_rows;
@@ -157,7 +136,13 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
     rc = DEV_ERR_NOT_SUPPORTED;
   }
   if (rc) return fail(rc);
-  const double ares = bcsr ? 0.0 : initial_full_residual(A);
+  // residuals of the A-initial guess (src/parilu_v0_3.cpp:30-34), on the GPU
+  double ares = 0.0, nonlin0 = NAN;
+  if (!bcsr) {
+    rc = c->parilu(0, nullptr, nullptr, true, nullptr);
+    if (!rc) rc = c->ilu_residuals(&ares, &nonlin0);
+    if (rc) return fail(rc);
+  }
   double tol;
   int maxs;
   if (bcsr) {  // src/parilu_v0_3_bcsr.cpp:61,118: un-normalised step <= reduction
@@ -165,17 +150,13 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
     maxs = 100;
   } else if (mode == 0) {
     tol = reduction * ares;
-    maxs = 20;
+    // LACE caps its asynchronous sweeps at 20 (:45).  A synchronous sweep
+    // needs up to (dependency depth of L and U) sweeps to reach the same
+    // fixed point, so the cap is raised to that depth where it is larger.
+    maxs = std::max(20, c->nlevels[0] + c->nlevels[1] + 2);
   } else {
     tol = std::numeric_limits<double>::epsilon() * 4.0;
     maxs = log->maxSweeps;
-  }
-  double nonlin0 = NAN;
-  if (!bcsr) {
-    // nonlinear residual of the initial guess (0 sweeps)
-    rc = c->parilu(0, nullptr, &nonlin0, true, nullptr);
-    if (rc) return fail(rc);
-    nonlin0 *= c->anorm;
   }
   std::vector<double> steps;
   double step = 0.0, nonlin = 0.0;
@@ -186,9 +167,19 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   // download: L values (CSRL order), U values (CSCU order), FP64
   const int ld = bcsr ? A->blocksize * A->blocksize : 1;
   std::vector<double> lv((size_t)c->nnzL * ld), uv((size_t)c->nnzU * ld);
-  if (c->vtype() != VType::F64) return fail(DEV_ERR_NOT_SUPPORTED);
-  cudaMemcpy(lv.data(), c->Lv[c->cur].p, 8 * lv.size(), cudaMemcpyDeviceToHost);
-  cudaMemcpy(uv.data(), c->Ucv[c->cur].p, 8 * uv.size(), cudaMemcpyDeviceToHost);
+  if (c->vtype() != VType::F64) {
+    // FP32 / BF16 factors travel back as LACE's FP64 values
+    DBuf tl, tu;
+    if (tl.ensure(8 * lv.size()) || tu.ensure(8 * uv.size())) return fail(DEV_ERR_DEVICE_ALLOC);
+    launch_convert(c->stream, (int)lv.size(), c->vtype(), c->Lv[c->cur].p, VType::F64, tl.p);
+    launch_convert(c->stream, (int)uv.size(), c->vtype(), c->Ucv[c->cur].p, VType::F64, tu.p);
+    cudaMemcpyAsync(lv.data(), tl.p, 8 * lv.size(), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(uv.data(), tu.p, 8 * uv.size(), cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+  } else {
+    cudaMemcpy(lv.data(), c->Lv[c->cur].p, 8 * lv.size(), cudaMemcpyDeviceToHost);
+    cudaMemcpy(uv.data(), c->Ucv[c->cur].p, 8 * uv.size(), cudaMemcpyDeviceToHost);
+  }
   if (cudaGetLastError() != cudaSuccess) return fail(DEV_ERR_UNKNOWN);
   L->diagorder_type = Magma_UNITY;
   U->diagorder_type = Magma_VALUE;
@@ -357,11 +348,12 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
   lace_gpu_ctx *c = nullptr;
   int rc = default_ctx(&c);
   if (rc) return set_err(rc);
-  lace_gpu_options o;
-  lace_gpu_default_options(&o);
+  lace_gpu_options o = dropin_opts();
   o.monitor_orthog = par->monitorOrthog == 1;
   const int choice = par->user_csrtrsv_choice;
-  o.trsv_mode = choice == 1 ? LACE_TRSV_JACOBI : (choice == 2 ? LACE_TRSV_NONE : LACE_TRSV_SYNCFREE);
+  if (choice == 1) o.trsv_mode = LACE_TRSV_JACOBI;
+  else if (choice == 2) o.trsv_mode = LACE_TRSV_NONE;
+  else if (o.trsv_mode != LACE_TRSV_LEVELS) o.trsv_mode = LACE_TRSV_SYNCFREE;
   lace_gpu_set_options(c, &o);
   const int n = A->num_rows;
   rc = lace_gpu_upload_csr_host(c, n, A->row[n], A->row, A->col, A->val);
@@ -431,6 +423,19 @@ extern "C" int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U, d
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
   *nonlinres = std::sqrt(c->h_scal[41]);
   *res = *nonlinres;
+  return DEV_SUCCESS;
+}
+
+extern "C" int lace_gpu_dropin_set_options(const lace_gpu_options *opt) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!opt) {
+    lace_gpu_default_options(&g_dopt);
+  } else {
+    if (opt->precision < 0 || opt->precision > 2 || opt->trsv_mode < 0 || opt->trsv_mode > 3)
+      return set_err(DEV_ERR_ILLEGAL_VALUE);
+    g_dopt = *opt;
+  }
+  g_dopt_set = true;
   return DEV_SUCCESS;
 }
 

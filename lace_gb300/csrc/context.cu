@@ -200,9 +200,138 @@ int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int
   return nl;
 }
 
+int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
+  const int n = T.n;
+  const int CS = 32 * R;
+  const int nch = (n + CS - 1) / CS;
+  const int nblk = (nch + cpb - 1) / cpb;
+  std::vector<int> cblk(nch), lev(nch, 0);
+  std::vector<uint8_t> kind(nch, 0);
+  for (int p = 0; p < nch; ++p) cblk[lower ? p : nch - 1 - p] = p / cpb;
+  std::vector<std::vector<std::pair<int, int>>> reqs(nch);
+  std::vector<int> deps;
+  for (int p = 0; p < nch; ++p) {
+    const int c = lower ? p : nch - 1 - p;
+    deps.clear();
+    const int r0 = c * CS, r1 = std::min(n, r0 + CS);
+    for (int i = r0; i < r1; ++i) {
+      const int prev = lower ? i - 1 : i + 1;
+      for (int e = T.ptr[i]; e < T.ptr[i + 1]; ++e) {
+        const int j = T.idx[e];
+        if (j == i || (lower ? j > i : j < i)) continue;
+        const int cj = j / CS;
+        if (cj == c) {
+          if (j != prev) kind[c] = 1;
+        } else {
+          deps.push_back(cj);
+        }
+      }
+    }
+    std::sort(deps.begin(), deps.end());
+    deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
+    int l = 0;
+    for (int cj : deps) {
+      if (cblk[cj] == cblk[c]) {
+        l = std::max(l, lev[cj] + 1);
+      } else {
+        bool found = false;
+        for (auto &pr : reqs[c])
+          if (pr.first == cblk[cj]) {
+            pr.second = std::max(pr.second, lev[cj] + 1);
+            found = true;
+          }
+        if (!found) reqs[c].push_back({cblk[cj], lev[cj] + 1});
+      }
+    }
+    lev[c] = l;
+  }
+  std::vector<int> req_ptr(nch + 1, 0), req_blk, req_lvl;
+  for (int c = 0; c < nch; ++c) {
+    req_ptr[c + 1] = req_ptr[c] + (int)reqs[c].size();
+    for (auto &pr : reqs[c]) {
+      req_blk.push_back(pr.first);
+      req_lvl.push_back(pr.second);
+    }
+  }
+  // per block: chunks ordered by local level
+  std::vector<int> blk_lvl_ptr(nblk + 1, 0), lvl_ptr(1, 0), units;
+  units.reserve(nch);
+  int maxlev = 0;
+  for (int b = 0; b < nblk; ++b) {
+    const int p0 = b * cpb, p1 = std::min(nch, p0 + cpb);
+    int nl = 0;
+    for (int p = p0; p < p1; ++p) nl = std::max(nl, lev[lower ? p : nch - 1 - p] + 1);
+    maxlev = std::max(maxlev, nl);
+    std::vector<int> cnt(nl + 1, 0);
+    for (int p = p0; p < p1; ++p) cnt[lev[lower ? p : nch - 1 - p] + 1]++;
+    for (int l = 0; l < nl; ++l) cnt[l + 1] += cnt[l];
+    const int u0 = (int)units.size();
+    units.resize(u0 + (p1 - p0));
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int p = p0; p < p1; ++p) {
+      const int c = lower ? p : nch - 1 - p;
+      units[u0 + fill[lev[c]]++] = c;
+    }
+    blk_lvl_ptr[b + 1] = blk_lvl_ptr[b] + nl;
+    for (int l = 0; l < nl; ++l) lvl_ptr.push_back(u0 + cnt[l + 1]);
+  }
+  int rc = 0;
+  rc |= pb.blk_lvl_ptr.upload(blk_lvl_ptr.data(), 4 * blk_lvl_ptr.size(), s);
+  rc |= pb.lvl_ptr.upload(lvl_ptr.data(), 4 * lvl_ptr.size(), s);
+  rc |= pb.units.upload(units.data(), 4 * units.size(), s);
+  rc |= pb.chunk_blk.upload(cblk.data(), 4 * cblk.size(), s);
+  rc |= pb.req_ptr.upload(req_ptr.data(), 4 * req_ptr.size(), s);
+  rc |= pb.req_blk.upload(req_blk.data(), 4 * std::max<size_t>(1, req_blk.size()), s);
+  rc |= pb.req_lvl.upload(req_lvl.data(), 4 * std::max<size_t>(1, req_lvl.size()), s);
+  rc |= pb.kind.upload(kind.data(), kind.size(), s);
+  rc |= pb.progress.ensure(8 * (size_t)nblk);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  cudaMemsetAsync(pb.progress.p, 0, 8 * (size_t)nblk, s);
+  TriBlkPlan &d = pb.dev;
+  d.n = n;
+  d.nchunks = nch;
+  d.nblocks = nblk;
+  d.R = R;
+  d.cpb = cpb;
+  d.lower = lower ? 1 : 0;
+  d.blk_lvl_ptr = (const int *)pb.blk_lvl_ptr.p;
+  d.lvl_ptr = (const int *)pb.lvl_ptr.p;
+  d.units = (const int *)pb.units.p;
+  d.chunk_blk = (const int *)pb.chunk_blk.p;
+  d.req_ptr = (const int *)pb.req_ptr.p;
+  d.req_blk = (const int *)pb.req_blk.p;
+  d.req_lvl = (const int *)pb.req_lvl.p;
+  d.kind = (const uint8_t *)pb.kind.p;
+  d.progress = (unsigned long long *)pb.progress.p;
+  d.max_levels = maxlev;
+  pb.valid = true;
+  return 0;
+}
+
 }  // namespace lace
 
 using namespace lace;
+
+// the block-scheduled plan of one triangle with the current schedule shape
+int lace_gpu_ctx::ensure_plan(int which) {
+  PlanBufs &pb = plans[which];
+  if (pb.valid && pb.dev.R == plan_R && pb.dev.cpb == plan_cpb) {
+    pb.dev.warps = plan_warps;
+    return 0;
+  }
+  const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
+  const bool low[4] = {true, false, true, false};
+  int rc = build_blk_plan(*pats[which], low[which], plan_R, plan_cpb, pb, stream);
+  if (rc) return rc;
+  TriDev t = tri(which);
+  pb.dev.row = t.row;
+  pb.dev.col = t.col;
+  pb.dev.unit = t.unit;
+  pb.dev.warps = plan_warps;
+  const int per_sm = plan_warps == 1 ? 16 : (plan_warps <= 8 ? 4 : (plan_warps <= 16 ? 2 : 1));
+  pb.dev.grid = std::min(pb.dev.nblocks, num_sms() * per_sm);
+  return 0;
+}
 
 // ======================================================================
 // context lifetime
@@ -365,6 +494,7 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
   hUc = Uc;
   hLt = Lt;
   map_ur2uc_el.free();
+  for (auto &pb : plans) pb.valid = false;
   int rc = 0;
   rc |= Lrow.upload(L.ptr.data(), 4 * L.ptr.size(), stream);
   rc |= Lcol.upload(L.idx.data(), 4 * L.idx.size(), stream);
@@ -496,13 +626,25 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
                                         const int *col, const double *val) {
   if (!c || !row || (nnz > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
   cudaSetDevice(c->device);
-  int rc = validate_csr(n, nnz, row, col);
+  // same pattern as the resident matrix: only the values travel (the
+  // analysis - splits, maps, chunk kinds, level sets - is kept)
+  const bool same = c->bs == 0 && c->n_blk == n && c->nnzA == nnz && (int)c->hArow.size() == n + 1 &&
+                    memcmp(c->hArow.data(), row, 4 * (size_t)(n + 1)) == 0 &&
+                    memcmp(c->hAcol.data(), col, 4 * (size_t)nnz) == 0;
+  int rc = same ? 0 : validate_csr(n, nnz, row, col);
   if (rc) return set_err(rc);
-  if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) || c->Acol.upload(col, 4 * (size_t)nnz, c->stream) ||
-      c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
-    return set_err(DEV_ERR_DEVICE_ALLOC);
-  rc = c->upload_common(n, nnz, row, col, 0);
-  if (rc) return set_err(rc);
+  if (same) {
+    if (c->Aval.upload(val, 8 * (size_t)nnz, c->stream)) return set_err(DEV_ERR_DEVICE_ALLOC);
+  } else {
+    if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) ||
+        c->Acol.upload(col, 4 * (size_t)nnz, c->stream) || c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
+      return set_err(DEV_ERR_DEVICE_ALLOC);
+    rc = c->upload_common(n, nnz, row, col, 0);
+    if (rc) return set_err(rc);
+    c->hArow.assign(row, row + n + 1);
+    c->hAcol.assign(col, col + nnz);
+  }
+  c->factors_ready = false;
   double s = 0.0;
   for (int p = 0; p < nnz; ++p) s += val[p] * val[p];
   c->anorm = std::sqrt(s);
@@ -536,6 +678,8 @@ extern "C" int lace_gpu_upload_bcsr_host(lace_gpu_ctx *c, int nb, int bs, int nb
     return set_err(DEV_ERR_DEVICE_ALLOC);
   rc = c->upload_common(nb, nblk, row, col, bs);
   if (rc) return set_err(rc);
+  c->hArow.clear();
+  c->hAcol.clear();
   double s = 0.0;
   for (size_t p = 0; p < (size_t)nblk * ld; ++p) s += val[p] * val[p];
   c->anorm = std::sqrt(s);
@@ -720,8 +864,10 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
                         dstep + (s % 32));
     cur = 1 - cur;
     if (sync_each || s % 32 == 31 || s == sweeps - 1) {
-      const int cnt = s % 32 + 1;
-      LCHK(cudaMemcpyAsync(h_scal, dstep, 8 * cnt, cudaMemcpyDeviceToHost, stream));
+      // entries of this batch not yet read: one when reading every sweep
+      const int first = sync_each ? s % 32 : (s / 32) * 32 % 32;
+      const int cnt = s % 32 + 1 - first;
+      LCHK(cudaMemcpyAsync(h_scal, dstep + first, 8 * cnt, cudaMemcpyDeviceToHost, stream));
       LCHK(cudaStreamSynchronize(stream));
       if (steps)
         for (int k = 0; k < cnt; ++k) steps->push_back(h_scal[k] / anorm);
@@ -744,6 +890,23 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
   LCHK(cudaStreamSynchronize(stream));
   if (h_status() & kStatusBreakdown) return DEV_ERR_BADPRECOND;
   return DEV_SUCCESS;
+}
+
+// LACE's data_zilures pair for the current factors (CSR only): res over
+// pattern(LU) and nonlinres over S(A), both un-normalised
+int lace_gpu_ctx::ilu_residuals(double *res, double *nonlin) {
+  if (bs || !factors_ready) return DEV_ERR_NOT_SUPPORTED;
+  IluArgs a = ilu_args();
+  const VType t = vtype();
+  double *d = (double *)scal_buf.p + 40;
+  launch_ilu_residual(stream, a, t, Lv[cur].p, Ucv[cur].p, d);
+  launch_lu_fro(stream, a, t, (const int *)Urow.p, (const int *)Ucol.p, Lv[cur].p, Urv.p, Ucv[cur].p, d + 2);
+  LCHK(cudaMemcpyAsync(h_scal + 40, d, 4 * 8, cudaMemcpyDeviceToHost, stream));
+  LCHK(cudaStreamSynchronize(stream));
+  const double nl2 = h_scal[40], fro = h_scal[42], onS = h_scal[43];
+  if (nonlin) *nonlin = std::sqrt(nl2);
+  if (res) *res = std::sqrt(std::max(0.0, nl2 + fro - onS));
+  return 0;
 }
 
 int lace_gpu_ctx::h_status() {
@@ -807,11 +970,14 @@ int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int o
       launch_convert(stream, n, in_f32 ? VType::F32 : VType::F64, b, out_f32 ? VType::F32 : VType::F64, x);
       break;
     default:
-      if (bs)
+      if (bs) {
         launch_bcsr_sptrsv(stream, t, bs, vt, which == 1 ? dinv.p : nullptr, b, in_f32, x, out_f32, cb,
                            0, honor_done);
-      else
-        launch_sptrsv_syncfree(stream, t, vt, b, in_f32, x, out_f32, cb, 0, honor_done);
+      } else {
+        int rc = ensure_plan(which);
+        if (rc) return rc;
+        launch_sptrsv_blk(stream, plans[which].dev, t.val, vt, b, in_f32, x, out_f32, cb, which, honor_done);
+      }
   }
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
@@ -829,10 +995,6 @@ int lace_gpu_ctx::ensure_vectors() {
 
 int lace_gpu_ctx::autotune_trsv() {
   if (bs || opt.trsv_mode != LACE_TRSV_SYNCFREE) return 0;
-  if (opt.trsv_rows_per_lane > 0) {
-    rows_per_lane = opt.trsv_rows_per_lane;
-    return 0;
-  }
   if (trsv_tuned) return 0;
   int rc = ensure_vectors();
   if (rc) return rc;
@@ -842,10 +1004,29 @@ int lace_gpu_ctx::autotune_trsv() {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int bestR = 4;
-  for (int R : {1, 2, 4, 8}) {
-    rows_per_lane = R;
+  int bR = 4, bC = 1, bW = 1;
+  // schedule shapes: (rows per lane, chunks per block, warps per CTA); a
+  // block of one chunk on one warp is the warp-level sync-free solve
+  struct Cand {
+    int R, cpb, w;
+  };
+  std::vector<Cand> cands = {{4, 1, 1}, {1, 1, 1}, {4, 32, 16}, {4, 128, 16}, {4, 512, 16},
+                             {4, 2048, 16}, {1, 128, 16}, {1, 512, 16}, {1, 2048, 16}};
+  if (opt.trsv_rows_per_lane > 0) {
+    std::vector<Cand> keep;
+    for (auto c : cands)
+      if (c.R == 4) keep.push_back({opt.trsv_rows_per_lane, c.cpb, c.w});
+    cands = keep;
+  }
+  const int nch_min = (n + 31) / 32;
+  for (auto cd : cands) {
+    if (cd.cpb > 1 && cd.cpb * 32 * cd.R > 2 * n) continue;  // one block would hold everything
+    plan_R = cd.R;
+    plan_cpb = cd.cpb;
+    plan_warps = cd.w;
+    if ((rc = ensure_plan(0)) || (rc = ensure_plan(1))) return rc;
     solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+    solve_tri(1, vec_t.p, f32, vec_t2.p, f32, false, vec_r.p);
     cudaEventRecord(e0, stream);
     for (int r = 0; r < 2; ++r) {
       solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
@@ -855,16 +1036,24 @@ int lace_gpu_ctx::autotune_trsv() {
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
+    if (verbose) printf("trsv autotune R=%d cpb=%d warps=%d: %.3f ms per pair\n", cd.R, cd.cpb, cd.w, ms / 2);
     if (ms < best) {
       best = ms;
-      bestR = R;
+      bR = cd.R;
+      bC = cd.cpb;
+      bW = cd.w;
     }
   }
+  (void)nch_min;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  rows_per_lane = bestR;
+  plan_R = bR;
+  plan_cpb = bC;
+  plan_warps = bW;
+  rows_per_lane = bR;
   trsv_tuned = true;
   drop_graphs();
+  if (h_status() & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 
@@ -1020,6 +1209,12 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   int rc = ensure_krylov(m, opt.monitor_orthog != 0);
   if (!rc) rc = autotune_trsv();
   if (!rc && adjoint) rc = ensure_AT();
+  // solve plans are built on the host: before any graph capture
+  if (!rc && !bs && opt.trsv_mode == LACE_TRSV_SYNCFREE) {
+    rc = ensure_plan(adjoint ? 2 : 0);
+    if (!rc) rc = ensure_plan(adjoint ? 3 : 1);
+  }
+  if (!rc && cudaStreamSynchronize(stream) != cudaSuccess) rc = DEV_ERR_UNKNOWN;
   if (rc) return rc;
   ArnoldiArgs a = arnoldi_args(m, adjoint);
   Cycle *cy = a.cy;

@@ -27,6 +27,17 @@ struct Pattern {
   std::vector<int> ptr, idx;
 };
 
+// device arrays of one triangle's block-scheduled solve plan
+struct PlanBufs {
+  DBuf blk_lvl_ptr, lvl_ptr, units, chunk_blk, req_ptr, req_blk, req_lvl, kind, progress;
+  TriBlkPlan dev;
+  bool valid = false;
+};
+
+// host construction of a plan: chunks of 32*R rows, blocks of cpb chunks (in
+// solve order), local levels inside blocks, cross-block requirements
+int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, cudaStream_t s);
+
 extern thread_local int g_last_error;
 int set_err(int code);
 int cuda_code(cudaError_t e);
@@ -50,6 +61,7 @@ struct lace_gpu_ctx {
   int nnzA = 0;    // entries (blocks) of A
   double anorm = 0.0;
   DBuf Arow, Acol, Aval;
+  std::vector<int> hArow, hAcol;  // host copy of the resident CSR pattern
   // A^T for the adjoint
   bool AT_ready = false;
   DBuf ATrow, ATcol, ATval, map_at2a;
@@ -71,6 +83,9 @@ struct lace_gpu_ctx {
   int nlevels[4] = {0, 0, 0, 0};
   int rows_per_lane = 4;
   bool trsv_tuned = false;
+  lace::PlanBufs plans[4];
+  int plan_R = 4, plan_cpb = 1, plan_warps = 1;  // autotuned schedule shape
+  int ensure_plan(int which);
   int lanes = 8;
 
   // Krylov workspace
@@ -110,6 +125,7 @@ struct lace_gpu_ctx {
   int parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
              std::vector<double> *steps, double stop_below = -1.0);
   int h_status();
+  int ilu_residuals(double *res, double *nonlin);
   int solve_tri(int which, const void *b, int in_f32, void *x, int out_f32, bool honor_done,
                 void *tmp);
   int ensure_vectors();

@@ -115,6 +115,10 @@ void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *
 // ||(A - LU)|_S||_F^2 to *out (device)
 void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
                          double *out);
+// out2 = {||LU||_F^2, sum over S(A) of (LU)_ij^2}; Urow/Ucol/Ur: U in CSR,
+// a.Ucp/a.Uri + Uc: U in CSC (same values)
+void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
+                   const void *L, const void *Ur, const void *Uc, double *out2);
 // gather: dst[p] = src[perm[p]] with type conversion
 void launch_gather(cudaStream_t s, int count, const int *perm, VType ts, const void *src, VType td,
                    void *dst);
@@ -129,6 +133,22 @@ void launch_block_diag_inverse(cudaStream_t s, int nb, int bs, const int *Urow, 
 // x = T^{-1} b for one triangle; b/x typed by in_f32/out_f32 (else double).
 // compute precision follows the factor value type (double for F64, float
 // otherwise).  ctrl may be null (stand-alone call).
+// Block-scheduled sync-free solve plan of one triangle (device arrays; see
+// sptrsv_blk.cu).  Built on the host by build_blk_plan (context.cu).
+struct TriBlkPlan {
+  int n = 0, nchunks = 0, nblocks = 0;
+  int R = 4, cpb = 1, warps = 1, grid = 1;
+  int unit = 0, lower = 1;
+  const int *row = nullptr, *col = nullptr;
+  const int *blk_lvl_ptr = nullptr, *lvl_ptr = nullptr, *units = nullptr, *chunk_blk = nullptr;
+  const int *req_ptr = nullptr, *req_blk = nullptr, *req_lvl = nullptr;
+  const uint8_t *kind = nullptr;
+  unsigned long long *progress = nullptr;
+  int max_levels = 0;  // largest number of local levels of a block
+};
+void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
+                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done);
+
 // honor_done: return at once when ctrl->done is set (inside an Arnoldi cycle)
 void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
                             void *x, int out_f32, Control *ctrl, int grid_hint, bool honor_done);

@@ -372,9 +372,11 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const double nrm2 = sred[jp1];
+    // j+1 == n: the Krylov space is exhausted (LACE guards with search < n,
+    // :476); the new reflector is empty and H(j+1,j) = 0
+    const double nrm2 = jp1 < n ? sred[jp1] : 0.0;
     const double wn = sqrt(nrm2);
-    const double wj1 = w[jp1];
+    const double wj1 = jp1 < n ? w[jp1] : 0.0;
     const double dd = mysgn(wj1) * wn;  // LACE :477-478
     const double alpha = sqrt(2.0 * (nrm2 + fabs(wj1) * wn));
     const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
@@ -387,7 +389,7 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   __syncthreads();
   // d = V_j^T v_{j+1}; rho = row j+1 of V_{j+1}
   for (int k = threadIdx.x; k < jp1; k += kTPB) {
-    const double vk = V[(size_t)k * ldv + jp1];
+    const double vk = jp1 < n ? V[(size_t)k * ldv + jp1] : 0.0;
     sd[k] = (sred[k] + s_dd * vk) * s_ia;
     srho[k] = vk;
   }

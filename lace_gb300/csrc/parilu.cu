@@ -18,6 +18,12 @@ namespace lace {
 
 constexpr int kPTPB = 256;
 
+static int sweep_grid_pub(int rows) {
+  int g = (rows + kPTPB - 1) / kPTPB;
+  int cap = num_sms() * 8;
+  return g < 1 ? 1 : (g > cap ? cap : g);
+}
+
 __device__ __forceinline__ double block_sum_p(double v) {
   __shared__ double scratch[kPTPB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -124,6 +130,101 @@ __global__ void __launch_bounds__(kPTPB) k_ilu_residual(
     }
   }
   finish_sum(acc, partials, counter, out);
+}
+
+// ||LU||_F^2 and sum over S(A) of (LU)_ij^2, thread per row: row i of LU is
+// sum_k l_ik U(k,:), so ||(LU)(i,:)||^2 = sum_{k,k'} l_ik l_ik' <U(k,:),U(k',:)>
+// (sparse dots of U's CSR rows).  With the S(A) part of the ILU residual this
+// gives LACE's full residual ||LU - A|| over pattern(LU) (control/norms.cpp:
+// 389-398) without forming LU:  res^2 = sum_S (LU-A)^2 + ||LU||^2 - sum_S LU^2.
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_lu_fro(
+    int n, const int *__restrict__ Arow, const int *__restrict__ Acol, const int *__restrict__ Lrow,
+    const int *__restrict__ Lcol, const FT *__restrict__ L, const int *__restrict__ Urow,
+    const int *__restrict__ Ucol, const FT *__restrict__ Ur, const int *__restrict__ Ucp,
+    const int *__restrict__ Uri, const FT *__restrict__ Uc, double *partials, int *counter,
+    double *out2) {
+  double fro = 0.0, onS = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lb = Lrow[i], le = Lrow[i + 1];
+    for (int a = lb; a < le; ++a) {
+      const int k = Lcol[a];
+      const double lk = (k == i) ? 1.0 : (double)cvt<CT>(L[a]);
+      for (int b = a; b < le; ++b) {
+        const int k2 = Lcol[b];
+        const double lk2 = (k2 == i) ? 1.0 : (double)cvt<CT>(L[b]);
+        double dot = 0.0;
+        int p = Urow[k], q = Urow[k2];
+        const int pe = Urow[k + 1], qe = Urow[k2 + 1];
+        while (p < pe && q < qe) {
+          const int cp = Ucol[p], cq = Ucol[q];
+          if (cp == cq) {
+            dot = fma((double)cvt<CT>(Ur[p]), (double)cvt<CT>(Ur[q]), dot);
+            ++p;
+            ++q;
+          } else if (cp < cq) {
+            ++p;
+          } else {
+            ++q;
+          }
+        }
+        fro = fma((a == b ? 1.0 : 2.0) * lk * lk2, dot, fro);
+      }
+    }
+    for (int p = Arow[i]; p < Arow[i + 1]; ++p) {
+      const int j = Acol[p];
+      double t = 0.0;
+      int il = lb, iu = Ucp[j];
+      const int ue = Ucp[j + 1];
+      while (il < le && iu < ue) {
+        const int jl = Lcol[il], ju = Uri[iu];
+        if (jl == ju) {
+          t = fma(jl == i ? 1.0 : (double)cvt<CT>(L[il]), (double)cvt<CT>(Uc[iu]), t);
+          ++il;
+          ++iu;
+        } else if (jl < ju) {
+          ++il;
+        } else {
+          ++iu;
+        }
+      }
+      onS = fma(t, t, onS);
+    }
+  }
+  // two sums: fold each through the deterministic last-block protocol
+  double t1 = block_sum_p(fro);
+  double t2 = block_sum_p(onS);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = t1;
+    partials[2 * blockIdx.x + 1] = t2;
+  }
+  if (!arrive_last(counter)) return;
+  if (threadIdx.x == 0) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) {
+      s1 += partials[2 * b];
+      s2 += partials[2 * b + 1];
+    }
+    out2[0] = s1;
+    out2[1] = s2;
+  }
+}
+
+void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
+                   const void *L, const void *Ur, const void *Uc, double *out2) {
+  const int grid = sweep_grid_pub(a.n);
+  if (t == VType::F64)
+    k_lu_fro<double, double><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const double *)L, Urow,
+                                                    Ucol, (const double *)Ur, a.Ucp, a.Uri, (const double *)Uc,
+                                                    a.partials, a.counter, out2);
+  else if (t == VType::F32)
+    k_lu_fro<float, float><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const float *)L, Urow,
+                                                  Ucol, (const float *)Ur, a.Ucp, a.Uri, (const float *)Uc,
+                                                  a.partials, a.counter, out2);
+  else
+    k_lu_fro<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+        a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const __nv_bfloat16 *)L, Urow, Ucol, (const __nv_bfloat16 *)Ur,
+        a.Ucp, a.Uri, (const __nv_bfloat16 *)Uc, a.partials, a.counter, out2);
 }
 
 // ---------------------------------------------------------------- BCSR

@@ -25,6 +25,23 @@ _libc = C.CDLL(None)
 _libc.free.argtypes = [C.c_void_p]
 
 
+def set_options(precision: str = "fp64", trsv: str = "syncfree", jacobi_sweeps: int = 8,
+                use_graph: bool = True) -> None:
+    """lace_gpu_dropin_set_options: how the LACE-named calls run."""
+    from . import PREC, TRSV, GpuOptions
+    o = GpuOptions()
+    f = lib()
+    f.lace_gpu_default_options(C.byref(o))
+    o.precision = PREC[precision]
+    o.trsv_mode = TRSV[trsv]
+    o.jacobi_sweeps = jacobi_sweeps
+    o.use_graph = int(use_graph)
+    rc = f.lace_gpu_dropin_set_options(C.byref(o))
+    if rc:
+        from . import LaceError
+        raise LaceError(rc, "lace_gpu_dropin_set_options")
+
+
 class Mat:
     """A DataMatrix plus the numpy arrays it points into."""
 

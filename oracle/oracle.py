@@ -345,6 +345,78 @@ def block_inverse(a: np.ndarray) -> np.ndarray:
     return out.reshape(bs, bs)
 
 
+# ------------------------------------------------------------- BCSR
+
+@dataclass
+class BlockFactors:
+    L: Tri          # block CSRL: identity diagonal blocks last; val [nblkL, bs*bs]
+    U: Tri          # block CSCU: diagonal block last per block column; blocks untransposed
+    bs: int
+    steps: list
+
+    def U_rows(self) -> Tri:
+        nb = len(self.U.ptr) - 1
+        ptr, idx, _, perm = transpose(self.U.ptr, self.U.idx, None, nb)
+        return Tri(ptr, idx, self.U.val[perm])
+
+    def dinv(self) -> np.ndarray:
+        """inverses of U's diagonal blocks (block row order)."""
+        Ur = self.U_rows()
+        nb = len(Ur.ptr) - 1
+        out = np.zeros((nb, self.bs * self.bs))
+        for I in range(nb):
+            out[I] = block_inverse(Ur.val[Ur.ptr[I]].reshape(self.bs, self.bs)).ravel()
+        return out
+
+
+def bcsr_parilu(B, sweeps: int, mode: str = "sync", stop_below: float | None = None) -> BlockFactors:
+    """Block ParILU(0) from the A-initial guess (BCSRL with identity diagonal
+    blocks, BCSCU), src/parilu_v0_3_bcsr.cpp:22-32 and :118-254.  stop_below:
+    LACE's BCSR stop (un-normalised step <= reduction, :118)."""
+    bs, ld = B.bs, B.bs * B.bs
+    rid = B.rowidx()
+    A = np.ascontiguousarray(np.asarray(B.val).reshape(B.nblk, ld))
+    keepL = B.col <= rid
+    Lptr = np.zeros(B.nb + 1, dtype=np.int32)
+    np.cumsum(np.bincount(rid[keepL], minlength=B.nb), out=Lptr[1:])
+    Lidx = _i(B.col[keepL])
+    Lval = A[keepL].copy()
+    Lval[B.col[keepL] == rid[keepL]] = np.eye(bs).ravel()
+    keepU = B.col >= rid
+    Urp = np.zeros(B.nb + 1, dtype=np.int32)
+    np.cumsum(np.bincount(rid[keepU], minlength=B.nb), out=Urp[1:])
+    up, ui, _, perm = transpose(Urp, _i(B.col[keepU]), None, B.nb)
+    Uval = A[keepU][perm].copy()
+    F = BlockFactors(Tri(Lptr, Lidx, Lval), Tri(up, ui, Uval), bs, [])
+    lb = lib()
+    Lc, Uc = Lval.ravel().copy(), Uval.ravel().copy()
+    Ln, Un = Lc.copy(), Uc.copy()
+    it = 0
+    while it < sweeps:
+        if mode == "async":
+            s = lb.orc_bcsr_parilu_sweep(0, bs, B.nblk, rid, _i(B.col), A.ravel().copy(), Lptr, Lidx, Lc, Lc,
+                                         up, ui, Uc, Uc)
+        else:
+            s = lb.orc_bcsr_parilu_sweep(1, bs, B.nblk, rid, _i(B.col), A.ravel().copy(), Lptr, Lidx, Lc, Ln,
+                                         up, ui, Uc, Un)
+            Lc, Ln = Ln, Lc
+            Uc, Un = Un, Uc
+            Ln[:] = Lc
+            Un[:] = Uc
+        F.steps.append(s)
+        it += 1
+        if stop_below is not None and not s > stop_below:
+            break
+    F.L.val = Lc.reshape(-1, ld)
+    F.U.val = Uc.reshape(-1, ld)
+    return F
+
+
+def bcsr_precond(F: BlockFactors, f32: bool = False) -> dict:
+    Ur = F.U_rows()
+    return {"kind": "bcsr_f32" if f32 else "bcsr", "t1": F.L, "t2": Ur, "bdinv": F.dinv()}
+
+
 # ------------------------------------------------------------ FGMRES
 
 @dataclass

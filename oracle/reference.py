@@ -137,6 +137,11 @@ class Mat:
             pass
 
 
+def set_storage(A: Mat, storage: int) -> None:
+    """A->storage_type = storage (the first member of data_d_matrix)."""
+    C.cast(A.h, C.POINTER(C.c_int))[0] = storage
+
+
 def convert(A: Mat, old, new, diagorder=0) -> Mat:
     return Mat(A.L.ref_convert(A.h, old, new, diagorder), A.L)
 

@@ -1,0 +1,150 @@
+"""GPU parity for the block (BCSR 5x5) path and the adjoint (backward) entry.
+
+BCSR: SpMV, block ParILU sweeps, block SpTRSV and FGMRES against the oracle's
+block restatement (FP64 within 1e-12; FP32 factors reach the same 1e-10
+relative residual).
+Adjoint: dL/db and dL/dA from lace_gpu_solve_backward against central finite
+differences (step 1e-6, random unit directions, agreement 1e-6 relative) and
+against the oracle's FP64 adjoint solve.
+"""
+import numpy as np
+import pytest
+
+from lace_gb300 import problems as P
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lg(torch_cuda):
+    import lace_gb300
+    lace_gb300.lib()
+    return lace_gb300
+
+
+def dev(torch, a):
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_bcsr_spmv(lg, torch_cuda):
+    B = P.bcsr3d(6, 5, 4, seed=2)
+    x = np.random.default_rng(0).standard_normal(B.n)
+    with lg.Context(0) as ctx:
+        ctx.upload(B)
+        y = torch_cuda.zeros(B.n, dtype=torch_cuda.float64, device="cuda")
+        ctx.spmv(dev(torch_cuda, x), y)
+    ref = orc.bcsr_spmv(B.row, B.col, B.val, B.bs, x)
+    assert relmax(y.cpu().numpy(), ref) <= 1e-14
+
+
+def test_bcsr_dropin_parilu_matches_oracle(lg):
+    """data_PariLU_v0_3 with A->storage_type == Magma_BCSR dispatches to the
+    block sweep (LACE: src/parilu_v0_3_bcsr.cpp); values equal the oracle's
+    synchronous block sweeps after the same count."""
+    from lace_gb300 import dropin
+    B = P.bcsr3d(5, seed=1)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(dropin.bcsr(B), reduction=1e-24)
+    F = orc.bcsr_parilu(B, info["sweeps"], mode="sync")
+    assert np.array_equal(lp, F.L.ptr) and np.array_equal(li, F.L.idx)
+    assert np.array_equal(up, F.U.ptr) and np.array_equal(ui, F.U.idx)
+    assert relmax(lv, F.L.val.ravel()) <= 1e-12
+    assert relmax(uv, F.U.val.ravel()) <= 1e-12
+    # converged (step below the reduction) to the one-thread block ILU(0)
+    E = orc.bcsr_parilu(B, 1, mode="async")
+    assert relmax(lv, E.L.val.ravel()) <= 1e-10 and relmax(uv, E.U.val.ravel()) <= 1e-10
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_bcsr_fgmres(lg, torch_cuda, prec):
+    B = P.bcsr3d(8, seed=4)
+    b = P.rhs_normal(B.n, 0)
+    F = orc.bcsr_parilu(B, 3, mode="sync")
+    op = {"kind": "bcsr", "bs": B.bs, "row": B.row, "col": B.col, "val": B.val}
+    r = orc.fgmres(op, orc.bcsr_precond(F), b, search_max=50, restart_max=20, rtol=1e-10)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec)
+        ctx.upload(B)
+        ctx.parilu0(3)
+        xd = torch_cuda.zeros(B.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=20, rtol=1e-10)
+        x = xd.cpu().numpy()
+        # block triangular solves against the oracle's
+        z = torch_cuda.zeros(B.n, dtype=torch_cuda.float64, device="cuda")
+        q = np.random.default_rng(2).standard_normal(B.n)
+        ctx.apply_precond(dev(torch_cuda, q), z)
+    Ur = F.U_rows()
+    t = np.zeros(B.n)
+    lib = orc.lib()
+    lib.orc_bcsr_trsv_lower_unit(B.nb, B.bs, F.L.ptr, F.L.idx, np.ascontiguousarray(F.L.val.ravel()), q, t)
+    zr = np.zeros(B.n)
+    lib.orc_bcsr_trsv_upper(B.nb, B.bs, Ur.ptr, Ur.idx, np.ascontiguousarray(Ur.val.ravel()),
+                            np.ascontiguousarray(F.dinv().ravel()), t, zr)
+    assert relmax(z.cpu().numpy(), zr) <= (1e-12 if prec == "fp64" else 1e-4)
+    assert res.converged and r.converged
+    Bc = B.to_csr()
+    assert np.linalg.norm(b - Bc.matvec(x)) <= 2e-10 * np.linalg.norm(b)
+    assert abs(res.total_iterations - r.total_iterations) <= 2
+
+
+# ------------------------------------------------------------------ adjoint
+
+def _solve(lg, torch, ctx, A, b, sweeps=40):
+    ctx.upload(A)
+    ctx.parilu0(sweeps)
+    x = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    r = ctx.fgmres(dev(torch, b), x, search_max=50, restart_max=40, rtol=1e-14)
+    assert r.converged
+    return x
+
+
+def test_adjoint_against_finite_differences(lg, torch_cuda):
+    """L(x) = 0.5||x - x_t||^2 with A x = b (convection-diffusion, 8^3):
+    gradients w.r.t. b and A's values vs central FD (h = 1e-6) along random
+    unit directions; backward solve through FP32 transposed factors."""
+    A = P.convdiff3d(8)
+    rng = np.random.default_rng(1)
+    xt = rng.standard_normal(A.n)
+    b = P.rhs_normal(A.n, 0)
+    torch = torch_cuda
+
+    def loss(Aval, bvec):
+        with lg.Context(0) as c:
+            c.set_options(precision="fp64")
+            x = _solve(lg, torch, c, P.CSR(A.n, A.row, A.col, Aval), bvec)
+            xv = x.cpu().numpy()
+        return 0.5 * float(np.sum((xv - xt) ** 2)), xv
+
+    L0, x0 = loss(A.val, b)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision="fp32")
+        ctx.upload(A)
+        ctx.parilu0(3)
+        xd = dev(torch, x0)
+        dLdx = dev(torch, x0 - xt)
+        gb = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+        gA = torch.zeros(A.nnz, dtype=torch.float64, device="cuda")
+        ctx.backward(xd, dLdx, gb, gA, search_max=50, restart_max=40, rtol=1e-13)
+        gb, gA = gb.cpu().numpy(), gA.cpu().numpy()
+    # FP64 CPU adjoint: A^T lambda = x - x_t with the oracle's FGMRES on A^T
+    atp, ati, atv, _ = orc.transpose(A.row, A.col, A.val, A.n)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync")
+    ra = orc.fgmres({"kind": "csr", "row": atp, "col": ati, "val": atv}, orc.ilu_precond_adjoint(F), x0 - xt,
+                    search_max=50, restart_max=40, rtol=1e-13)
+    assert ra.converged
+    assert relmax(gb, ra.x) <= 1e-8
+    h = 1e-6
+    for k in range(8):
+        d = rng.standard_normal(A.n)
+        d /= np.linalg.norm(d)
+        fd = (loss(A.val, b + h * d)[0] - loss(A.val, b - h * d)[0]) / (2 * h)
+        assert abs(fd - gb @ d) <= 1e-6 * max(abs(fd), 1e-3 * np.linalg.norm(gb))
+    for k in range(6):
+        d = rng.standard_normal(A.nnz)
+        d /= np.linalg.norm(d)
+        fd = (loss(A.val + h * d, b)[0] - loss(A.val - h * d, b)[0]) / (2 * h)
+        assert abs(fd - gA @ d) <= 1e-6 * max(abs(fd), 1e-3 * np.linalg.norm(gA))
