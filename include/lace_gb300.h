@@ -334,18 +334,24 @@ const char *lace_gpu_error_string(int code);
  * ---------------------------------------------------------------------- */
 typedef struct lace_gpu_batch lace_gpu_batch;
 
-/* Host arrays: system s has n[s] rows, its CSR arrays start at
- * row_off[s] / nnz_off[s] in the concatenated row/col/val arrays (row
- * pointers local to the system).  nrhs right-hand sides per system. */
+/* Host arrays: system s has n[s] rows starting at global row row_off[s]
+ * (row_off[0] = 0, row_off[s+1] = row_off[s] + n[s]); `row` concatenates
+ * the systems' local row-pointer arrays (n[s]+1 entries each, so system s's
+ * starts at row + row_off[s] + s); its column indices and values start at
+ * col + nnz_off[s] / val + nnz_off[s] and are local to the system.  nrhs
+ * right-hand sides per system (1..64).  The context `ctx` becomes the
+ * batch's working context (its options decide the factor precision). */
 int lace_gpu_batch_create(lace_gpu_batch **batch, lace_gpu_ctx *ctx, int nsys,
                           const int *n, const int *row_off, const int *nnz_off,
                           const int *row, const int *col, const double *val,
                           int nrhs);
 int lace_gpu_batch_destroy(lace_gpu_batch *batch);
-/* ParILU sweeps for every system, then FGMRES-Householder(search_max) on
- * every (system, rhs) pair to rtol (relative).  b, x: device arrays holding,
- * per system, nrhs consecutive vectors of length n[s] (system-major, in the
- * order of row_off).  iters_out (host, nsys*nrhs, may be NULL). */
+/* ParILU sweeps for every system, then FGMRES-Householder(search_max <= 64)
+ * on every (system, rhs) pair to its own relative tolerance rtol.  b, x:
+ * device arrays of nrhs vectors of length N = sum n[s], rhs-major: entry i of
+ * system s for right-hand side r is at [r*N + row_off[s] + i].  x holds the
+ * initial guesses.  iters_out (host, nsys*nrhs, system-major, may be NULL):
+ * search directions used per (system, rhs). */
 int lace_gpu_batch_solve(lace_gpu_batch *batch, int sweeps, int search_max,
                          int restart_max, double rtol, const double *b,
                          double *x, int *iters_out);

@@ -253,6 +253,10 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
       req_lvl.push_back(pr.second);
     }
   }
+  if (req_blk.empty()) {  // keep the device arrays non-empty (never read)
+    req_blk.push_back(0);
+    req_lvl.push_back(0);
+  }
   // per block: chunks ordered by local level
   std::vector<int> blk_lvl_ptr(nblk + 1, 0), lvl_ptr(1, 0), units;
   units.reserve(nch);
@@ -281,8 +285,8 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
   rc |= pb.units.upload(units.data(), 4 * units.size(), s);
   rc |= pb.chunk_blk.upload(cblk.data(), 4 * cblk.size(), s);
   rc |= pb.req_ptr.upload(req_ptr.data(), 4 * req_ptr.size(), s);
-  rc |= pb.req_blk.upload(req_blk.data(), 4 * std::max<size_t>(1, req_blk.size()), s);
-  rc |= pb.req_lvl.upload(req_lvl.data(), 4 * std::max<size_t>(1, req_lvl.size()), s);
+  rc |= pb.req_blk.upload(req_blk.data(), 4 * req_blk.size(), s);
+  rc |= pb.req_lvl.upload(req_lvl.data(), 4 * req_lvl.size(), s);
   rc |= pb.kind.upload(kind.data(), kind.size(), s);
   rc |= pb.progress.ensure(8 * (size_t)nblk);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
@@ -359,6 +363,7 @@ extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream)
   LCHK(cudaSetDevice(device));
   lace_gpu_ctx *c = new lace_gpu_ctx();
   c->device = device;
+  c->verbose = getenv("LACE_GB300_VERBOSE") != nullptr;
   lace_gpu_default_options(&c->opt);
   if (stream) {
     c->stream = (cudaStream_t)stream;

@@ -7,9 +7,10 @@
 //   pass B : w <- w - V (T^T s)  (LACE :376-469, all reflectors at once),
 //            fused with d' = V^T w over rows > j and ||w_{j+1:}||^2; the last
 //            block forms the new reflector scalars (LACE :476-511), extends T,
-//            applies the Givens rotations and updates g (LACE :658-701), and
-//            on convergence solves the small least-squares system (:714-729)
+//            applies the Givens rotations, updates g and tests convergence
+//            (LACE :658-714)
 //   pass C : v_{j+1} and q = P_0...P_{j+1} e_{j+1} (LACE :519-617) in one read
+//   x update (end of cycle): small least-squares solve + x += Z y (:721-744)
 // Every kernel returns at once when Control::done is set, so a whole cycle can
 // be launched (or replayed from a CUDA graph) without host round trips.
 #include <math.h>
@@ -196,6 +197,19 @@ __device__ __forceinline__ double block_sum(double v, double *scratch) {
   return t;  // valid in thread 0
 }
 
+// last block: sred[k] = sum over blocks of partials[b*kLdT + k], k < count;
+// warp w takes k = w, w+8, ..., its lanes stride over the blocks (fixed
+// order, so the result is deterministic)
+__device__ __forceinline__ void fold_partials(const double *partials, int count, double *sred) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = wid; k < count; k += kTPB / 32) {
+    double s = 0.0;
+    for (int bb = lane; bb < (int)gridDim.x; bb += 32) s += partials[(size_t)bb * kLdT + k];
+    s = warp_sum(s);
+    if (lane == 0) sred[k] = s;
+  }
+}
+
 // ------------------------------------------------------- cycle start
 
 // r = b - A x (into a.w) and ||r||; last block sets up the first reflector
@@ -295,11 +309,7 @@ __global__ void __launch_bounds__(kTPB) k_passA(int n, OpView op, const ZT *__re
   for (int k = threadIdx.x; k < jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
   if (!arrive_last(&ctrl->block_count[1])) return;
   // s = V^T w  -> y = T^T s
-  for (int k = threadIdx.x; k < jp1; k += kTPB) {
-    double s = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb) s += partials[(size_t)bb * kLdT + k];
-    sred[k] = s;
-  }
+  fold_partials(partials, jp1, sred);
   __syncthreads();
   for (int k = threadIdx.x; k < jp1; k += kTPB) {
     double y = 0.0;
@@ -361,14 +371,17 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   for (int k = threadIdx.x; k <= jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
   if (!arrive_last(&ctrl->block_count[2])) return;
 
-  // ---- last block: new reflector, T extension, Givens, LS solve
+  // ---- last block: new reflector, T extension, Givens rotations
   __shared__ double sd[kLdT];
   __shared__ double srho[kLdT];
+  __shared__ double sh[kLdT], scs[kLdT], ssn[kLdT];
   __shared__ double s_dd, s_ia, s_vjj;
-  for (int k = threadIdx.x; k <= jp1; k += kTPB) {
-    double s = 0.0;
-    for (int bb = 0; bb < (int)gridDim.x; ++bb) s += partials[(size_t)bb * kLdT + k];
-    sred[k] = s;
+  fold_partials(partials, jp1 + 1, sred);
+  // Hessenberg column j and the rotations so far, staged in shared memory
+  for (int k = threadIdx.x; k <= j; k += kTPB) {
+    sh[k] = w[k];
+    scs[k] = cy->cs[k];
+    ssn[k] = cy->sn[k];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -415,38 +428,34 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   }
   if (threadIdx.x == 0) {
     // Hessenberg column j: h_k = w_k (k <= j), h_{j+1} = -dd  (LACE :658-701)
-    double *R = cy->R + (size_t)j * kLdT;
-    for (int k = 0; k <= j; ++k) R[k] = w[k];
     for (int k = 0; k < j; ++k) {
-      const double t0 = R[k], t1 = R[k + 1];
-      R[k + 1] = -cy->sn[k] * t0 + cy->cs[k] * t1;
-      R[k] = cy->cs[k] * t0 + cy->sn[k] * t1;
+      const double t0 = sh[k], t1 = sh[k + 1];
+      sh[k + 1] = -ssn[k] * t0 + scs[k] * t1;
+      sh[k] = scs[k] * t0 + ssn[k] * t1;
     }
     const double dd = s_dd;
     double c, s;
-    givens_rot(R[j], -dd, 4.9406564584124654e-324, &c, &s);
+    givens_rot(sh[j], -dd, 4.9406564584124654e-324, &c, &s);
     cy->cs[j] = c;
     cy->sn[j] = s;
-    R[j] = c * R[j] - s * dd;
-    cy->g[jp1] = -s * cy->g[j];
-    cy->g[j] = c * cy->g[j];
-    const double resid = fabs(cy->g[jp1]);
+    sh[j] = c * sh[j] - s * dd;
+    const double gj = cy->g[j];
+    cy->g[jp1] = -s * gj;
+    cy->g[j] = c * gj;
+    const double resid = fabs(-s * gj);
     cy->hist[j] = resid;
     ctrl->resid = resid;
     const bool conv = resid < ctrl->rtol_abs;
     if (conv || j == m - 1 || !(resid == resid)) {  // LACE :714 (+ opt4's non-finite stop)
-      // back-substitution, LACE :721-729
-      double *y = cy->yls;
-      for (int i = 0; i <= j; ++i) y[i] = cy->g[i] / cy->R[i + i * kLdT];
-      for (int jj = j; jj > 0; --jj)
-        for (int i = jj - 1; i >= 0; --i)
-          y[i] = y[i] - cy->R[i + jj * kLdT] * y[jj] / cy->R[i + i * kLdT];
-      ctrl->nsteps = jp1;
+      ctrl->nsteps = jp1;  // the least-squares solve runs in the x update
       ctrl->converged = conv ? 1 : 0;
       if (!(resid == resid)) ctrl->status |= kStatusBreakdown;
       ctrl->done = 1;
     }
   }
+  __syncthreads();
+  double *R = cy->R + (size_t)j * kLdT;
+  for (int k = threadIdx.x; k <= j; k += kTPB) R[k] = sh[k];
 }
 
 // ------------------------------------------------------------- pass C
@@ -505,14 +514,37 @@ void launch_orthog_monitor(cudaStream_t s, const ArnoldiArgs &a, int j, double *
 
 // ------------------------------------------------------------- x update
 
+// x += Z y with y the solution of the small triangular system R y = g
+// (LACE :721-744).  Every block solves it redundantly from R and g in L2
+// (O(j^2) flops, shared memory), which costs less than one more launch.
+constexpr int kPackMax = 64;  // cycles up to this length solve from shared memory
 template <typename ZT>
 __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ Z, size_t ldz,
-                                                  double *__restrict__ x, const Cycle *cy,
+                                                  double *__restrict__ x, Cycle *cy,
                                                   const Control *ctrl) {
   const int ns = ctrl->nsteps;
   if (!ctrl->done || ns == 0) return;
   __shared__ double sy[kLdT];
-  for (int k = threadIdx.x; k < ns; k += kTPB) sy[k] = cy->yls[k];
+  __shared__ double sR[kPackMax * (kPackMax + 1) / 2];
+  const bool packed = ns <= kPackMax;
+  if (packed) {
+    // column jj of the upper triangle at offset jj*(jj+1)/2
+    for (int jj = 0; jj < ns; ++jj)
+      for (int i = threadIdx.x; i <= jj; i += kTPB) sR[jj * (jj + 1) / 2 + i] = cy->R[i + jj * kLdT];
+  }
+  for (int k = threadIdx.x; k < ns; k += kTPB) sy[k] = cy->g[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int jj = ns - 1; jj >= 0; --jj) {
+      const double rjj = packed ? sR[jj * (jj + 1) / 2 + jj] : cy->R[jj + jj * kLdT];
+      const double yj = sy[jj] / rjj;
+      sy[jj] = yj;
+      for (int i = 0; i < jj; ++i)
+        sy[i] = fma(-(packed ? sR[jj * (jj + 1) / 2 + i] : cy->R[i + jj * kLdT]), yj, sy[i]);
+    }
+    if (blockIdx.x == 0)
+      for (int k = 0; k < ns; ++k) cy->yls[k] = sy[k];
+  }
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double s = x[i];

@@ -68,20 +68,28 @@ struct BlkPlanDev {
   unsigned long long *progress;  // per block: (epoch << 32) | levels done
 };
 
+// blockIdx.y selects one of several right-hand sides (vectors vstride
+// elements apart); each has its own tickets (tickets[rhs]) and progress
+// counters (progress + rhs * nblocks); tickets[gridDim.y] counts exiting CTAs.
 template <typename CT, typename VT, int R, bool LOWER>
-__global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b, int in_f32, void *x, int out_f32,
-                             int *tickets, int *epoch_slot, const int *done_flag, int *status) {
+__global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_, int in_f32, void *x_,
+                                                    int out_f32, size_t vstride, int *tickets,
+                                                    int *epoch_slot, const int *done_flag, int *status) {
   if (done_flag != nullptr && *(volatile const int *)done_flag) return;
   constexpr int CS = 32 * R;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
+  const int rhs = blockIdx.y;
+  const void *b = (const char *)b_ + (size_t)rhs * vstride * (in_f32 ? 4 : 8);
+  void *x = (char *)x_ + (size_t)rhs * vstride * (out_f32 ? 4 : 8);
+  P.progress += (size_t)rhs * P.nblocks;
   const unsigned long long ep = (unsigned long long)(unsigned)(*(volatile int *)epoch_slot + 1);
   __shared__ int s_blk;
   const VT *val = (const VT *)P.val;
   while (true) {
     __syncthreads();
-    if (threadIdx.x == 0) s_blk = atomicAdd(&tickets[0], 1);
+    if (threadIdx.x == 0) s_blk = atomicAdd(&tickets[rhs], 1);
     __syncthreads();
     const int bk = s_blk;
     if (bk >= P.nblocks) break;
@@ -203,41 +211,69 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b,
   }
   // the CTA that leaves last re-arms the tickets and publishes the epoch
   if (threadIdx.x == 0) {
-    const int e = atomicAdd(&tickets[1], 1);
-    if (e == (int)gridDim.x - 1) {
-      tickets[0] = 0;
-      tickets[1] = 0;
+    const int nrhs = gridDim.y;
+    const int e = atomicAdd(&tickets[nrhs], 1);
+    if (e == (int)(gridDim.x * gridDim.y) - 1) {
+      for (int r = 0; r <= nrhs; ++r) tickets[r] = 0;
       *epoch_slot = (int)ep;
       __threadfence();
     }
   }
 }
 
+struct BlkArgs {
+  const void *b;
+  int in_f32;
+  void *x;
+  int out_f32;
+  size_t vstride;
+  int nrhs;
+  int *tickets, *epoch_slot, *status;
+  const int *dfl;
+};
+
 template <typename CT, typename VT, int R>
-static void blk_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const void *b, int in_f32,
-                       void *x, int out_f32, int *tickets, int *epoch_slot, const int *dfl, int *status) {
+static void blk_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a) {
+  dim3 g(grid, a.nrhs);
   if (P.lower)
-    k_sptrsv_blk<CT, VT, R, true><<<grid, 32 * warps, 0, s>>>(P, b, in_f32, x, out_f32, tickets, epoch_slot, dfl,
-                                                              status);
+    k_sptrsv_blk<CT, VT, R, true><<<g, 32 * warps, 0, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets,
+                                                           a.epoch_slot, a.dfl, a.status);
   else
-    k_sptrsv_blk<CT, VT, R, false><<<grid, 32 * warps, 0, s>>>(P, b, in_f32, x, out_f32, tickets, epoch_slot, dfl,
-                                                               status);
+    k_sptrsv_blk<CT, VT, R, false><<<g, 32 * warps, 0, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets,
+                                                            a.epoch_slot, a.dfl, a.status);
 }
 
 template <typename CT, typename VT>
-static void blk_launch_r(cudaStream_t s, int R, const BlkPlanDev &P, int warps, int grid, const void *b,
-                         int in_f32, void *x, int out_f32, int *tickets, int *epoch_slot, const int *dfl,
-                         int *status) {
+static void blk_launch_r(cudaStream_t s, int R, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a) {
   switch (R) {
-    case 1: blk_launch<CT, VT, 1>(s, P, warps, grid, b, in_f32, x, out_f32, tickets, epoch_slot, dfl, status); break;
-    case 2: blk_launch<CT, VT, 2>(s, P, warps, grid, b, in_f32, x, out_f32, tickets, epoch_slot, dfl, status); break;
-    case 8: blk_launch<CT, VT, 8>(s, P, warps, grid, b, in_f32, x, out_f32, tickets, epoch_slot, dfl, status); break;
-    default: blk_launch<CT, VT, 4>(s, P, warps, grid, b, in_f32, x, out_f32, tickets, epoch_slot, dfl, status); break;
+    case 1: blk_launch<CT, VT, 1>(s, P, warps, grid, a); break;
+    case 2: blk_launch<CT, VT, 2>(s, P, warps, grid, a); break;
+    case 8: blk_launch<CT, VT, 8>(s, P, warps, grid, a); break;
+    default: blk_launch<CT, VT, 4>(s, P, warps, grid, a); break;
   }
 }
 
-void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
-                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done) {
+static BlkPlanDev plan_dev(const TriBlkPlan &pl, const void *val);
+
+// several right-hand sides at once: b/x hold nrhs vectors vstride apart;
+// tickets has nrhs+1 ints, progress nrhs*nblocks counters (both zeroed)
+void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
+                             int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets,
+                             unsigned long long *progress, int *epoch_slot, int *status, const int *done_flag) {
+  BlkPlanDev P = plan_dev(pl, val);
+  P.progress = progress;
+  int grid = pl.grid;
+  if (grid > pl.nblocks) grid = pl.nblocks;
+  if (grid < 1) grid = 1;
+  BlkArgs a{b, in_f32, x, out_f32, vstride, nrhs, tickets, epoch_slot, status, done_flag};
+  switch (vt) {
+    case VType::F64: blk_launch_r<double, double>(s, pl.R, P, pl.warps, grid, a); break;
+    case VType::F32: blk_launch_r<float, float>(s, pl.R, P, pl.warps, grid, a); break;
+    case VType::BF16: blk_launch_r<float, __nv_bfloat16>(s, pl.R, P, pl.warps, grid, a); break;
+  }
+}
+
+static BlkPlanDev plan_dev(const TriBlkPlan &pl, const void *val) {
   BlkPlanDev P;
   P.n = pl.n;
   P.nchunks = pl.nchunks;
@@ -256,18 +292,13 @@ void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VT
   P.req_lvl = pl.req_lvl;
   P.kind = pl.kind;
   P.progress = pl.progress;
-  int grid = pl.grid;
-  if (grid > pl.nblocks) grid = pl.nblocks;
-  if (grid < 1) grid = 1;
-  const int *dfl = honor_done ? &ctrl->done : nullptr;
-  int *tickets = ctrl->tickets[slot];
-  int *ep = &ctrl->trsv_epoch[slot];
-  int *st = &ctrl->status;
-  switch (vt) {
-    case VType::F64: blk_launch_r<double, double>(s, pl.R, P, pl.warps, grid, b, in_f32, x, out_f32, tickets, ep, dfl, st); break;
-    case VType::F32: blk_launch_r<float, float>(s, pl.R, P, pl.warps, grid, b, in_f32, x, out_f32, tickets, ep, dfl, st); break;
-    case VType::BF16: blk_launch_r<float, __nv_bfloat16>(s, pl.R, P, pl.warps, grid, b, in_f32, x, out_f32, tickets, ep, dfl, st); break;
-  }
+  return P;
+}
+
+void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
+                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done) {
+  launch_sptrsv_blk_multi(s, pl, val, vt, b, in_f32, x, out_f32, 0, 1, ctrl->tickets[slot], pl.progress,
+                          &ctrl->trsv_epoch[slot], &ctrl->status, honor_done ? &ctrl->done : nullptr);
 }
 
 }  // namespace lace

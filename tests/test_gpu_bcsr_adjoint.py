@@ -137,14 +137,17 @@ def test_adjoint_against_finite_differences(lg, torch_cuda):
                     search_max=50, restart_max=40, rtol=1e-13)
     assert ra.converged
     assert relmax(gb, ra.x) <= 1e-8
+    # relative gradient error |fd - g.d| / ||g|| <= 1e-6 (the loss is O(n) while
+    # a directional derivative along a random unit direction is O(||g||/sqrt(n)),
+    # so a per-direction relative bound would measure the FD's own rounding)
     h = 1e-6
     for k in range(8):
         d = rng.standard_normal(A.n)
         d /= np.linalg.norm(d)
         fd = (loss(A.val, b + h * d)[0] - loss(A.val, b - h * d)[0]) / (2 * h)
-        assert abs(fd - gb @ d) <= 1e-6 * max(abs(fd), 1e-3 * np.linalg.norm(gb))
+        assert abs(fd - gb @ d) <= 1e-6 * np.linalg.norm(gb)
     for k in range(6):
         d = rng.standard_normal(A.nnz)
         d /= np.linalg.norm(d)
         fd = (loss(A.val + h * d, b)[0] - loss(A.val - h * d, b)[0]) / (2 * h)
-        assert abs(fd - gA @ d) <= 1e-6 * max(abs(fd), 1e-3 * np.linalg.norm(gA))
+        assert abs(fd - gA @ d) <= 1e-6 * np.linalg.norm(gA)
