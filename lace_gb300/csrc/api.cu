@@ -158,10 +158,16 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
     tol = std::numeric_limits<double>::epsilon() * 4.0;
     maxs = log->maxSweeps;
   }
+  // A synchronous sweep can take a small step while still away from the fixed
+  // point (LACE's in-place sweep reaches it in one pass in its one-thread
+  // order).  When the dependency depth is small, run at least depth+1 sweeps:
+  // the synchronous iteration is then exact, like LACE's.
+  const int depth = c->nlevels[0] + c->nlevels[1];
+  const int min_sweeps = (mode == 0 && !bcsr && depth + 1 <= 64) ? std::min(depth + 1, maxs) : 0;
   std::vector<double> steps;
   double step = 0.0, nonlin = 0.0;
   auto t0 = std::chrono::steady_clock::now();
-  rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol);
+  rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol, min_sweeps);
   const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rc) return fail(rc);
   // download: L values (CSRL order), U values (CSCU order), FP64

@@ -258,11 +258,12 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
     req_lvl.push_back(0);
   }
   // per block: chunks ordered by local level
-  std::vector<int> blk_lvl_ptr(nblk + 1, 0), lvl_ptr(1, 0), units;
+  std::vector<int> blk_lvl_ptr(nblk + 1, 0), lvl_ptr(1, 0), units, blk_row0(nblk);
   units.reserve(nch);
   int maxlev = 0;
   for (int b = 0; b < nblk; ++b) {
     const int p0 = b * cpb, p1 = std::min(nch, p0 + cpb);
+    blk_row0[b] = (lower ? p0 : nch - p1) * CS;
     int nl = 0;
     for (int p = p0; p < p1; ++p) nl = std::max(nl, lev[lower ? p : nch - 1 - p] + 1);
     maxlev = std::max(maxlev, nl);
@@ -284,6 +285,7 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
   rc |= pb.lvl_ptr.upload(lvl_ptr.data(), 4 * lvl_ptr.size(), s);
   rc |= pb.units.upload(units.data(), 4 * units.size(), s);
   rc |= pb.chunk_blk.upload(cblk.data(), 4 * cblk.size(), s);
+  rc |= pb.blk_row0.upload(blk_row0.data(), 4 * blk_row0.size(), s);
   rc |= pb.req_ptr.upload(req_ptr.data(), 4 * req_ptr.size(), s);
   rc |= pb.req_blk.upload(req_blk.data(), 4 * req_blk.size(), s);
   rc |= pb.req_lvl.upload(req_lvl.data(), 4 * req_lvl.size(), s);
@@ -302,6 +304,7 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
   d.lvl_ptr = (const int *)pb.lvl_ptr.p;
   d.units = (const int *)pb.units.p;
   d.chunk_blk = (const int *)pb.chunk_blk.p;
+  d.blk_row0 = (const int *)pb.blk_row0.p;
   d.req_ptr = (const int *)pb.req_ptr.p;
   d.req_blk = (const int *)pb.req_blk.p;
   d.req_lvl = (const int *)pb.req_lvl.p;
@@ -856,7 +859,7 @@ int lace_gpu_ctx::init_factors() {
 }
 
 int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
-                         std::vector<double> *steps, double stop_below) {
+                         std::vector<double> *steps, double stop_below, int min_sweeps) {
   if (!n_blk) return DEV_ERR_NOT_INITIALIZED;
   int rc = init_factors();
   if (rc) return rc;
@@ -877,7 +880,7 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
       if (steps)
         for (int k = 0; k < cnt; ++k) steps->push_back(h_scal[k] / anorm);
       if (step_out) *step_out = h_scal[cnt - 1] / anorm;
-      if (sync_each && !(h_scal[cnt - 1] / anorm > stop_below)) break;
+      if (sync_each && s + 1 >= min_sweeps && !(h_scal[cnt - 1] / anorm > stop_below)) break;
     }
   }
   rc = finish_factors();
@@ -1015,8 +1018,11 @@ int lace_gpu_ctx::autotune_trsv() {
   struct Cand {
     int R, cpb, w;
   };
-  std::vector<Cand> cands = {{4, 1, 1}, {1, 1, 1}, {4, 32, 16}, {4, 128, 16}, {4, 512, 16},
-                             {4, 2048, 16}, {1, 128, 16}, {1, 512, 16}, {1, 2048, 16}};
+  // blocks up to the shared-memory window (160 KB of solved rows: 40960 rows
+  // in FP32, 20480 in FP64) keep every in-block dependency on chip
+  std::vector<Cand> cands = {{4, 1, 1},     {1, 1, 1},     {4, 32, 8},     {4, 128, 16},
+                             {4, 256, 16},  {1, 256, 16},  {1, 512, 16},   {1, 1024, 16},
+                             {4, 512, 16},  {1, 2048, 16}};
   if (opt.trsv_rows_per_lane > 0) {
     std::vector<Cand> keep;
     for (auto c : cands)
@@ -1177,7 +1183,7 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
   a.w = (double *)vec_w.p;
   a.q = (double *)vec_q.p;
   a.partials = (double *)part_buf.p;
-  a.grid = num_sms() * 4;
+  a.grid = num_sms() * 8;
   a.cy = (Cycle *)cycle_buf.p;
   a.ctrl = ctrl();
   a.m = m;

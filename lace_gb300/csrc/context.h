@@ -29,7 +29,7 @@ struct Pattern {
 
 // device arrays of one triangle's block-scheduled solve plan
 struct PlanBufs {
-  DBuf blk_lvl_ptr, lvl_ptr, units, chunk_blk, req_ptr, req_blk, req_lvl, kind, progress;
+  DBuf blk_lvl_ptr, lvl_ptr, units, chunk_blk, blk_row0, req_ptr, req_blk, req_lvl, kind, progress;
   TriBlkPlan dev;
   bool valid = false;
 };
@@ -123,7 +123,7 @@ struct lace_gpu_ctx {
   // up to `sweeps` sweeps; with sync_each, stops once the normalised step is
   // <= stop_below (LACE's stopping tests); steps receives every sweep's step
   int parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
-             std::vector<double> *steps, double stop_below = -1.0);
+             std::vector<double> *steps, double stop_below = -1.0, int min_sweeps = 0);
   int h_status();
   int ilu_residuals(double *res, double *nonlin);
   int solve_tri(int which, const void *b, int in_f32, void *x, int out_f32, bool honor_done,

@@ -141,6 +141,7 @@ struct TriBlkPlan {
   int unit = 0, lower = 1;
   const int *row = nullptr, *col = nullptr;
   const int *blk_lvl_ptr = nullptr, *lvl_ptr = nullptr, *units = nullptr, *chunk_blk = nullptr;
+  const int *blk_row0 = nullptr;  // lowest row of each block
   const int *req_ptr = nullptr, *req_blk = nullptr, *req_lvl = nullptr;
   const uint8_t *kind = nullptr;
   unsigned long long *progress = nullptr;

@@ -160,14 +160,31 @@ __device__ __forceinline__ void tile_dots(const double *__restrict__ V, size_t l
                                           int n, int base, int tr, int lo, const double *sw,
                                           double (&acc)[kSlots]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int t = lane; t < tr; t += 32) {
-    const int i = base + t;
-    if (i >= n || i < lo) continue;
-    const double wi = sw[t];
+  // the 8 rows of this lane, masked rows contribute 0 (their load address is
+  // redirected to the tile's first row, which is always valid)
+  double wv[8];
+  int iv[8];
 #pragma unroll
-    for (int sl = 0; sl < kSlots; ++sl) {
-      const int k = sl * 8 + wid;
-      if (k < ncols) acc[sl] = fma(V[(size_t)k * ldv + i], wi, acc[sl]);
+  for (int r = 0; r < 8; ++r) {
+    const int t = lane + 32 * r;
+    const int i = base + t;
+    const bool ok = t < tr && i < n && i >= lo;
+    wv[r] = ok ? sw[t] : 0.0;
+    iv[r] = ok ? i : base;
+  }
+#pragma unroll
+  for (int sl = 0; sl < kSlots; ++sl) {
+    if (sl * 8 >= ncols) break;  // uniform over the block
+    const int k = sl * 8 + wid;
+    if (k < ncols) {
+      const double *Vk = V + (size_t)k * ldv;
+      double a0 = 0.0, a1 = 0.0;
+#pragma unroll
+      for (int r = 0; r < 8; r += 2) {
+        a0 = fma(Vk[iv[r]], wv[r], a0);
+        a1 = fma(Vk[iv[r + 1]], wv[r + 1], a1);
+      }
+      acc[sl] += a0 + a1;
     }
   }
 }
@@ -354,8 +371,16 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   for (int base = blockIdx.x * kTPB; base < n; base += gridDim.x * kTPB) {
     const int i = base + threadIdx.x;
     if (i < n) {
-      double s = w[i];
-      for (int k = 0; k < jp1; ++k) s = fma(-V[(size_t)k * ldv + i], sy[k], s);
+      double s0 = w[i], s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      int k = 0;
+      for (; k + 4 <= jp1; k += 4) {
+        s0 = fma(-V[(size_t)k * ldv + i], sy[k], s0);
+        s1 = fma(-V[(size_t)(k + 1) * ldv + i], sy[k + 1], s1);
+        s2 = fma(-V[(size_t)(k + 2) * ldv + i], sy[k + 2], s2);
+        s3 = fma(-V[(size_t)(k + 3) * ldv + i], sy[k + 3], s3);
+      }
+      for (; k < jp1; ++k) s0 = fma(-V[(size_t)k * ldv + i], sy[k], s0);
+      const double s = (s0 + s1) + (s2 + s3);
       w[i] = s;
       sw[threadIdx.x] = s;
       if (i > j) nrm = fma(s, s, nrm);
@@ -472,9 +497,16 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, s
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
     V[(size_t)jp1 * ldv + i] = v;
-    double acc = (i == jp1 ? 1.0 : 0.0) - v * sc[jp1];
-    for (int k = 0; k < jp1; ++k) acc = fma(-V[(size_t)k * ldv + i], sc[k], acc);
-    q[i] = acc;
+    double a0 = (i == jp1 ? 1.0 : 0.0) - v * sc[jp1], a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int k = 0;
+    for (; k + 4 <= jp1; k += 4) {
+      a0 = fma(-V[(size_t)k * ldv + i], sc[k], a0);
+      a1 = fma(-V[(size_t)(k + 1) * ldv + i], sc[k + 1], a1);
+      a2 = fma(-V[(size_t)(k + 2) * ldv + i], sc[k + 2], a2);
+      a3 = fma(-V[(size_t)(k + 3) * ldv + i], sc[k + 3], a3);
+    }
+    for (; k < jp1; ++k) a0 = fma(-V[(size_t)k * ldv + i], sc[k], a0);
+    q[i] = (a0 + a1) + (a2 + a3);
   }
 }
 
@@ -547,9 +579,16 @@ __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ 
   }
   __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double s = x[i];
-    for (int k = 0; k < ns; ++k) s = fma((double)Z[(size_t)k * ldz + i], sy[k], s);  // LACE :735-744
-    x[i] = s;
+    double s0 = x[i], s1 = 0.0, s2 = 0.0, s3 = 0.0;  // LACE :735-744
+    int k = 0;
+    for (; k + 4 <= ns; k += 4) {
+      s0 = fma((double)Z[(size_t)k * ldz + i], sy[k], s0);
+      s1 = fma((double)Z[(size_t)(k + 1) * ldz + i], sy[k + 1], s1);
+      s2 = fma((double)Z[(size_t)(k + 2) * ldz + i], sy[k + 2], s2);
+      s3 = fma((double)Z[(size_t)(k + 3) * ldz + i], sy[k + 3], s3);
+    }
+    for (; k < ns; ++k) s0 = fma((double)Z[(size_t)k * ldz + i], sy[k], s0);
+    x[i] = (s0 + s1) + (s2 + s3);
   }
 }
 
@@ -564,7 +603,8 @@ static int rowgrid(int n) {
 
 void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x) {
   OpView op = opview(a);
-  switch (a.bs ? 8 : a.lanes) {
+  switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
+    case 1: k_cycle_residual<1><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
     case 4: k_cycle_residual<4><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
     case 16: k_cycle_residual<16><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
     case 32: k_cycle_residual<32><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
@@ -580,7 +620,8 @@ template <typename ZT>
 static void passA_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
   OpView op = opview(a);
   const ZT *z = (const ZT *)a.Z + (size_t)j * a.ldz;
-  switch (a.bs ? 8 : a.lanes) {
+  switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
+    case 1: k_passA<1, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
     case 4: k_passA<4, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
     case 16: k_passA<16, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
     case 32: k_passA<32, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;

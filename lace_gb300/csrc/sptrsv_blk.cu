@@ -52,6 +52,9 @@ __device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned l
 }
 __device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
+// shared memory a CTA may use for its block's solved rows
+constexpr int kSptrsvSmemMax = 160 * 1024;
+
 struct BlkPlanDev {
   int n, nchunks, nblocks;
   const int *row, *col;
@@ -61,25 +64,38 @@ struct BlkPlanDev {
   const int *lvl_ptr;       // level -> offset into units
   const int *units;         // chunk ids ordered by (block, level)
   const int *chunk_blk;     // chunk -> block (solve order index)
+  const int *blk_row0;      // block -> lowest row it holds
   const int *req_ptr;       // chunk -> offsets into req_blk / req_lvl
   const int *req_blk;       // blocks a chunk waits on
   const int *req_lvl;       // ... and how many levels of them
   const uint8_t *kind;      // 0 scan, 1 serial
   unsigned long long *progress;  // per block: (epoch << 32) | levels done
+  int win;                  // rows of a block kept in shared memory (0: none)
 };
 
 // blockIdx.y selects one of several right-hand sides (vectors vstride
 // elements apart); each has its own tickets (tickets[rhs]) and progress
 // counters (progress + rhs * nblocks); tickets[gridDim.y] counts exiting CTAs.
+//
+// Every row a block solves is also kept in shared memory (P.win rows from the
+// block's lowest row), so a dependency inside the block is a shared-memory
+// read after the level barrier; other blocks' rows are read from L2 after
+// their progress is seen.  With several warps the last one only publishes the
+// block's progress (one release store per level), so the fence latency stays
+// off the warps that solve the next level.
 template <typename CT, typename VT, int R, bool LOWER>
 __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_, int in_f32, void *x_,
                                                     int out_f32, size_t vstride, int *tickets,
                                                     int *epoch_slot, const int *done_flag, int *status) {
   if (done_flag != nullptr && *(volatile const int *)done_flag) return;
+  extern __shared__ unsigned char smem_raw[];
+  CT *xs = reinterpret_cast<CT *>(smem_raw);
   constexpr int CS = 32 * R;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const bool publisher_warp = nwarps > 1 && warp == nwarps - 1;
+  const int nw = nwarps > 1 ? nwarps - 1 : 1;  // warps that solve
   const int rhs = blockIdx.y;
   const void *b = (const char *)b_ + (size_t)rhs * vstride * (in_f32 ? 4 : 8);
   void *x = (char *)x_ + (size_t)rhs * vstride * (out_f32 ? 4 : 8);
@@ -94,119 +110,129 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_
     const int bk = s_blk;
     if (bk >= P.nblocks) break;
     const int l0 = P.blk_lvl_ptr[bk], l1 = P.blk_lvl_ptr[bk + 1];
+    const int row0 = P.blk_row0[bk];
     for (int lv = l0; lv < l1; ++lv) {
-      for (int u = P.lvl_ptr[lv] + warp; u < P.lvl_ptr[lv + 1]; u += nw) {
-        const int c = P.units[u];
-        // cross-block requirements: one lane per required block
-        const int r0 = P.req_ptr[c], nr = P.req_ptr[c + 1] - r0;
-        for (int q = lane; q < nr; q += 32) {
-          const int ob = P.req_blk[r0 + q];
-          const unsigned long long need = (ep << 32) | (unsigned)P.req_lvl[r0 + q];
-          int spins = 0;
-          while (ld_relaxed_u64(&P.progress[ob]) < need) {
-            if (++spins > kMaxSpins) {
-              atomicOr(status, kStatusSpinTimeout);
-              break;
+      if (!publisher_warp) {
+        for (int u = P.lvl_ptr[lv] + warp; u < P.lvl_ptr[lv + 1]; u += nw) {
+          const int c = P.units[u];
+          // cross-block requirements: one lane per required block
+          const int r0 = P.req_ptr[c], nr = P.req_ptr[c + 1] - r0;
+          for (int q = lane; q < nr; q += 32) {
+            const int ob = P.req_blk[r0 + q];
+            const unsigned long long need = (ep << 32) | (unsigned)P.req_lvl[r0 + q];
+            int spins = 0;
+            while (ld_relaxed_u64(&P.progress[ob]) < need) {
+              if (++spins > kMaxSpins) {
+                atomicOr(status, kStatusSpinTimeout);
+                break;
+              }
+              if (spins > 32) __nanosleep(32);
             }
-            if (spins > 32) __nanosleep(32);
           }
-        }
-        __syncwarp();
-        if (nr > 0) fence_acquire();
-        const int base = c * CS;
-        const int cnt = min(CS, P.n - base);
-        const bool serial = P.kind[c] != 0;
-        CT A[R], B[R], X[R];
-        int rows[R];
+          __syncwarp();
+          if (nr > 0) fence_acquire();
+          const int base = c * CS;
+          const int cnt = min(CS, P.n - base);
+          const bool serial = P.kind[c] != 0;
+          CT A[R], B[R], X[R];
+          int rows[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int pos = lane * R + r;
-          A[r] = (CT)1;
-          B[r] = (CT)0;
-          rows[r] = -1;
-          if (pos >= cnt) continue;
-          const int i = LOWER ? base + pos : base + cnt - 1 - pos;
-          rows[r] = i;
-          const int prev = LOWER ? i - 1 : i + 1;
-          CT acc = ld_in<CT>(b, in_f32, i);
-          CT d = (CT)1, ap = (CT)0;
-          for (int e = P.row[i]; e < P.row[i + 1]; ++e) {
-            const int jc = P.col[e];
-            if (jc == i) {
-              if (!P.unit) d = cvt<CT>(val[e]);
-              continue;
+          for (int r = 0; r < R; ++r) {
+            const int pos = lane * R + r;
+            A[r] = (CT)1;
+            B[r] = (CT)0;
+            rows[r] = -1;
+            if (pos >= cnt) continue;
+            const int i = LOWER ? base + pos : base + cnt - 1 - pos;
+            rows[r] = i;
+            const int prev = LOWER ? i - 1 : i + 1;
+            CT acc = ld_in<CT>(b, in_f32, i);
+            CT d = (CT)1, ap = (CT)0;
+            for (int e = P.row[i]; e < P.row[i + 1]; ++e) {
+              const int jc = P.col[e];
+              if (jc == i) {
+                if (!P.unit) d = cvt<CT>(val[e]);
+                continue;
+              }
+              if (LOWER ? (jc > i) : (jc < i)) continue;
+              const int cj = jc / CS;
+              if (cj == c) {
+                if (!serial && pos > 0 && jc == prev) ap = cvt<CT>(val[e]);
+                continue;
+              }
+              const unsigned slot = (unsigned)(jc - row0);
+              CT xv;
+              if (slot < (unsigned)P.win && P.chunk_blk[cj] == bk)
+                xv = ((volatile CT *)xs)[slot];
+              else
+                xv = ld_x_l2<CT>(x, out_f32, jc);
+              acc -= cvt<CT>(val[e]) * xv;
             }
-            if (LOWER ? (jc > i) : (jc < i)) continue;
-            const int cj = jc / CS;
-            if (cj == c) {
-              if (!serial && pos > 0 && jc == prev) ap = cvt<CT>(val[e]);
-              continue;
+            if (!serial) {
+              A[r] = -ap / d;
+              B[r] = acc / d;
+            } else {
+              A[r] = d;
+              B[r] = acc;
             }
-            const CT xv = (P.chunk_blk[cj] == bk) ? ld_x_cta<CT>(x, out_f32, jc) : ld_x_l2<CT>(x, out_f32, jc);
-            acc -= cvt<CT>(val[e]) * xv;
           }
           if (!serial) {
-            A[r] = -ap / d;
-            B[r] = acc / d;
-          } else {
-            A[r] = d;
-            B[r] = acc;
-          }
-        }
-        if (!serial) {
-          CT ca = (CT)1, cb = (CT)0;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            cb = A[r] * cb + B[r];
-            ca = A[r] * ca;
-          }
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
-            const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
-            if (lane >= o) {
-              cb = ca * pb + cb;
-              ca = ca * pa;
-            }
-          }
-          CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
-          if (lane == 0) xin = (CT)0;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            xin = A[r] * xin + B[r];
-            X[r] = xin;
-          }
-        } else {
-          for (int p = 0; p < cnt; ++p) {
-            const int owner = p / R, rr = p % R;
-            CT xp = (CT)0;
-#pragma unroll
-            for (int r = 0; r < R; ++r)
-              if (lane == owner && r == rr) xp = B[r] / A[r];
-            xp = __shfl_sync(0xffffffffu, xp, owner);
-            const int rowp = LOWER ? base + p : base + cnt - 1 - p;
+            CT ca = (CT)1, cb = (CT)0;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-              const int pos = lane * R + r;
-              if (pos == p) X[r] = xp;
-              if (pos > p && pos < cnt) {
-                const int i = rows[r];
-                for (int e = P.row[i]; e < P.row[i + 1]; ++e)
-                  if (P.col[e] == rowp) B[r] -= cvt<CT>(val[e]) * xp;
+              cb = A[r] * cb + B[r];
+              ca = A[r] * ca;
+            }
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
+              const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
+              if (lane >= o) {
+                cb = ca * pb + cb;
+                ca = ca * pa;
+              }
+            }
+            CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
+            if (lane == 0) xin = (CT)0;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              xin = A[r] * xin + B[r];
+              X[r] = xin;
+            }
+          } else {
+            for (int p = 0; p < cnt; ++p) {
+              const int owner = p / R, rr = p % R;
+              CT xp = (CT)0;
+#pragma unroll
+              for (int r = 0; r < R; ++r)
+                if (lane == owner && r == rr) xp = B[r] / A[r];
+              xp = __shfl_sync(0xffffffffu, xp, owner);
+              const int rowp = LOWER ? base + p : base + cnt - 1 - p;
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const int pos = lane * R + r;
+                if (pos == p) X[r] = xp;
+                if (pos > p && pos < cnt) {
+                  const int i = rows[r];
+                  for (int e = P.row[i]; e < P.row[i + 1]; ++e)
+                    if (P.col[e] == rowp) B[r] -= cvt<CT>(val[e]) * xp;
+                }
               }
             }
           }
-        }
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-          if (rows[r] >= 0) st_out<CT>(x, out_f32, rows[r], X[r]);
+          for (int r = 0; r < R; ++r)
+            if (rows[r] >= 0) {
+              st_out<CT>(x, out_f32, rows[r], X[r]);
+              const unsigned slot = (unsigned)(rows[r] - row0);
+              if (slot < (unsigned)P.win) xs[slot] = X[r];
+            }
+        }
       }
-      // level done: make it visible to the CTA, then to other CTAs
+      // level done: visible to the CTA now, to other CTAs after the release
       __syncthreads();
-      if (threadIdx.x == 0) {
-        __threadfence();
+      if ((publisher_warp || nwarps == 1) && lane == 0)
         st_release_u64(&P.progress[bk], (ep << 32) | (unsigned)(lv - l0 + 1));
-      }
     }
   }
   // the CTA that leaves last re-arms the tickets and publishes the epoch
@@ -235,12 +261,18 @@ struct BlkArgs {
 template <typename CT, typename VT, int R>
 static void blk_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a) {
   dim3 g(grid, a.nrhs);
-  if (P.lower)
-    k_sptrsv_blk<CT, VT, R, true><<<g, 32 * warps, 0, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets,
-                                                           a.epoch_slot, a.dfl, a.status);
-  else
-    k_sptrsv_blk<CT, VT, R, false><<<g, 32 * warps, 0, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets,
-                                                            a.epoch_slot, a.dfl, a.status);
+  const size_t sm = (size_t)P.win * sizeof(CT);
+  if (P.lower) {
+    auto fn = k_sptrsv_blk<CT, VT, R, true>;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    fn<<<g, 32 * warps, sm, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets, a.epoch_slot, a.dfl,
+                                 a.status);
+  } else {
+    auto fn = k_sptrsv_blk<CT, VT, R, false>;
+    if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    fn<<<g, 32 * warps, sm, s>>>(P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets, a.epoch_slot, a.dfl,
+                                 a.status);
+  }
 }
 
 template <typename CT, typename VT>
@@ -262,6 +294,10 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
                              unsigned long long *progress, int *epoch_slot, int *status, const int *done_flag) {
   BlkPlanDev P = plan_dev(pl, val);
   P.progress = progress;
+  // rows of a block kept in shared memory: the whole block when it fits
+  const size_t rows = (size_t)pl.cpb * 32 * pl.R;
+  const size_t esz = vt == VType::F64 ? 8 : 4;
+  P.win = rows * esz <= (size_t)kSptrsvSmemMax ? (int)rows : 0;
   int grid = pl.grid;
   if (grid > pl.nblocks) grid = pl.nblocks;
   if (grid < 1) grid = 1;
@@ -292,6 +328,8 @@ static BlkPlanDev plan_dev(const TriBlkPlan &pl, const void *val) {
   P.req_lvl = pl.req_lvl;
   P.kind = pl.kind;
   P.progress = pl.progress;
+  P.blk_row0 = pl.blk_row0;
+  P.win = 0;
   return P;
 }
 
