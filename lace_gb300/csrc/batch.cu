@@ -21,9 +21,6 @@
 
 namespace lace {
 
-void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
-                             int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets,
-                             unsigned long long *progress, int *epoch_slot, int *status, const int *done_flag);
 
 constexpr int kBT = 256;      // rows per tile, threads per block
 constexpr int kBMaxM = 64;    // largest search_max of the batched solver
@@ -391,7 +388,7 @@ struct lace_gpu_batch {
   lace::DBuf Srow, Scol, Sval;
   lace::DBuf tseg, tvoff, tmrow, tlen, tlrow0, st0, snt;
   int ntiles = 0;
-  lace::DBuf segbuf, V, Z, w, q, t, part, tick[2], prog[2];
+  lace::DBuf segbuf, V, Z, w, q, t, part, tick[2];
   size_t ldv = 0;
   int ld = 0;
   lace::Seg S{};
@@ -520,13 +517,10 @@ static int batch_workspace(lace_gpu_batch *B, int m) {
   rc |= B->segbuf.ensure(8 * dbl + 4 * 4 * ns);
   for (int k = 0; k < 2; ++k) {
     rc |= B->tick[k].ensure(4 * (size_t)(B->nrhs + 1));
-    const TriBlkPlan &pl = B->ctx->plans[k].dev;
-    rc |= B->prog[k].ensure(8 * (size_t)std::max(1, pl.nblocks) * B->nrhs);
   }
   if (rc) return DEV_ERR_DEVICE_ALLOC;
   for (int k = 0; k < 2; ++k) {
     cudaMemsetAsync(B->tick[k].p, 0, B->tick[k].bytes, B->ctx->stream);
-    cudaMemsetAsync(B->prog[k].p, 0, B->prog[k].bytes, B->ctx->stream);
   }
   double *d = (double *)B->segbuf.p;
   lace::Seg &S = B->S;
@@ -572,11 +566,9 @@ static int batch_cycle_body(lace_gpu_batch *B, int m) {
     void *zj = (char *)B->Z.p + (size_t)j * ldz * (f32 ? 4 : 8);
     TriDev tl = c->tri(0), tu = c->tri(1);
     launch_sptrsv_blk_multi(s, c->plans[0].dev, tl.val, vt, B->q.p, 0, B->t.p, f32, B->N, B->nrhs,
-                            (int *)B->tick[0].p, (unsigned long long *)B->prog[0].p, &c->ctrl()->trsv_epoch[0],
-                            &c->ctrl()->status, nullptr);
+                            (int *)B->tick[0].p, &c->ctrl()->status, nullptr);
     launch_sptrsv_blk_multi(s, c->plans[1].dev, tu.val, vt, B->t.p, f32, zj, f32, B->N, B->nrhs,
-                            (int *)B->tick[1].p, (unsigned long long *)B->prog[1].p, &c->ctrl()->trsv_epoch[1],
-                            &c->ctrl()->status, nullptr);
+                            (int *)B->tick[1].p, &c->ctrl()->status, nullptr);
     if (f32)
       k_bpassA<float><<<grid, kBT, 0, s>>>(B->T, A, (const float *)zj, (double *)B->w.p, (const double *)B->V.p,
                                           B->ldv, j, (double *)B->part.p, B->S);

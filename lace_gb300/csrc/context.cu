@@ -201,6 +201,7 @@ int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int
 }
 
 int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
+  if (cpb < 1 || cpb > kBlkMaxUnits) return DEV_ERR_ILLEGAL_VALUE;
   const int n = T.n;
   const int CS = 32 * R;
   const int nch = (n + CS - 1) / CS;
@@ -208,7 +209,6 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
   std::vector<int> cblk(nch), lev(nch, 0);
   std::vector<uint8_t> kind(nch, 0);
   for (int p = 0; p < nch; ++p) cblk[lower ? p : nch - 1 - p] = p / cpb;
-  std::vector<std::vector<std::pair<int, int>>> reqs(nch);
   std::vector<int> deps;
   for (int p = 0; p < nch; ++p) {
     const int c = lower ? p : nch - 1 - p;
@@ -227,72 +227,36 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
         }
       }
     }
-    std::sort(deps.begin(), deps.end());
-    deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
     int l = 0;
-    for (int cj : deps) {
-      if (cblk[cj] == cblk[c]) {
-        l = std::max(l, lev[cj] + 1);
-      } else {
-        bool found = false;
-        for (auto &pr : reqs[c])
-          if (pr.first == cblk[cj]) {
-            pr.second = std::max(pr.second, lev[cj] + 1);
-            found = true;
-          }
-        if (!found) reqs[c].push_back({cblk[cj], lev[cj] + 1});
-      }
-    }
+    for (int cj : deps)
+      if (cblk[cj] == cblk[c]) l = std::max(l, lev[cj] + 1);
     lev[c] = l;
   }
-  std::vector<int> req_ptr(nch + 1, 0), req_blk, req_lvl;
-  for (int c = 0; c < nch; ++c) {
-    req_ptr[c + 1] = req_ptr[c] + (int)reqs[c].size();
-    for (auto &pr : reqs[c]) {
-      req_blk.push_back(pr.first);
-      req_lvl.push_back(pr.second);
-    }
-  }
-  if (req_blk.empty()) {  // keep the device arrays non-empty (never read)
-    req_blk.push_back(0);
-    req_lvl.push_back(0);
-  }
   // per block: chunks ordered by local level
-  std::vector<int> blk_lvl_ptr(nblk + 1, 0), lvl_ptr(1, 0), units, blk_row0(nblk);
-  units.reserve(nch);
-  int maxlev = 0;
+  std::vector<int4> blk(nblk), urec;
+  urec.reserve(nch);
+  int max_units = 0;
   for (int b = 0; b < nblk; ++b) {
     const int p0 = b * cpb, p1 = std::min(nch, p0 + cpb);
-    blk_row0[b] = (lower ? p0 : nch - p1) * CS;
     int nl = 0;
     for (int p = p0; p < p1; ++p) nl = std::max(nl, lev[lower ? p : nch - 1 - p] + 1);
-    maxlev = std::max(maxlev, nl);
     std::vector<int> cnt(nl + 1, 0);
     for (int p = p0; p < p1; ++p) cnt[lev[lower ? p : nch - 1 - p] + 1]++;
     for (int l = 0; l < nl; ++l) cnt[l + 1] += cnt[l];
-    const int u0 = (int)units.size();
-    units.resize(u0 + (p1 - p0));
-    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    std::vector<int> order(p1 - p0);
     for (int p = p0; p < p1; ++p) {
       const int c = lower ? p : nch - 1 - p;
-      units[u0 + fill[lev[c]]++] = c;
+      order[cnt[lev[c]]++] = c;
     }
-    blk_lvl_ptr[b + 1] = blk_lvl_ptr[b] + nl;
-    for (int l = 0; l < nl; ++l) lvl_ptr.push_back(u0 + cnt[l + 1]);
+    const int u0 = (int)urec.size();
+    for (int c : order) urec.push_back(make_int4(c, lev[c] | ((int)kind[c] << 30), 0, 0));
+    blk[b] = make_int4(u0, (int)urec.size(), nl, (lower ? p0 : nch - p1) * CS);
+    max_units = std::max(max_units, p1 - p0);
   }
   int rc = 0;
-  rc |= pb.blk_lvl_ptr.upload(blk_lvl_ptr.data(), 4 * blk_lvl_ptr.size(), s);
-  rc |= pb.lvl_ptr.upload(lvl_ptr.data(), 4 * lvl_ptr.size(), s);
-  rc |= pb.units.upload(units.data(), 4 * units.size(), s);
-  rc |= pb.chunk_blk.upload(cblk.data(), 4 * cblk.size(), s);
-  rc |= pb.blk_row0.upload(blk_row0.data(), 4 * blk_row0.size(), s);
-  rc |= pb.req_ptr.upload(req_ptr.data(), 4 * req_ptr.size(), s);
-  rc |= pb.req_blk.upload(req_blk.data(), 4 * req_blk.size(), s);
-  rc |= pb.req_lvl.upload(req_lvl.data(), 4 * req_lvl.size(), s);
-  rc |= pb.kind.upload(kind.data(), kind.size(), s);
-  rc |= pb.progress.ensure(8 * (size_t)nblk);
+  rc |= pb.blk.upload(blk.data(), sizeof(int4) * blk.size(), s);
+  rc |= pb.urec.upload(urec.data(), sizeof(int4) * urec.size(), s);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
-  cudaMemsetAsync(pb.progress.p, 0, 8 * (size_t)nblk, s);
   TriBlkPlan &d = pb.dev;
   d.n = n;
   d.nchunks = nch;
@@ -300,17 +264,9 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
   d.R = R;
   d.cpb = cpb;
   d.lower = lower ? 1 : 0;
-  d.blk_lvl_ptr = (const int *)pb.blk_lvl_ptr.p;
-  d.lvl_ptr = (const int *)pb.lvl_ptr.p;
-  d.units = (const int *)pb.units.p;
-  d.chunk_blk = (const int *)pb.chunk_blk.p;
-  d.blk_row0 = (const int *)pb.blk_row0.p;
-  d.req_ptr = (const int *)pb.req_ptr.p;
-  d.req_blk = (const int *)pb.req_blk.p;
-  d.req_lvl = (const int *)pb.req_lvl.p;
-  d.kind = (const uint8_t *)pb.kind.p;
-  d.progress = (unsigned long long *)pb.progress.p;
-  d.max_levels = maxlev;
+  d.blk = (const int4 *)pb.blk.p;
+  d.urec = (const int4 *)pb.urec.p;
+  d.max_units = max_units;
   pb.valid = true;
   return 0;
 }
@@ -984,6 +940,10 @@ int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int o
       } else {
         int rc = ensure_plan(which);
         if (rc) return rc;
+        if (b == x) {  // the solve fills x before it reads b
+          cudaMemcpyAsync(tmp, b, (size_t)n * (in_f32 ? 4 : 8), cudaMemcpyDeviceToDevice, stream);
+          b = tmp;
+        }
         launch_sptrsv_blk(stream, plans[which].dev, t.val, vt, b, in_f32, x, out_f32, cb, which, honor_done);
       }
   }
@@ -1019,10 +979,11 @@ int lace_gpu_ctx::autotune_trsv() {
     int R, cpb, w;
   };
   // blocks up to the shared-memory window (160 KB of solved rows: 40960 rows
-  // in FP32, 20480 in FP64) keep every in-block dependency on chip
-  std::vector<Cand> cands = {{4, 1, 1},     {1, 1, 1},     {4, 32, 8},     {4, 128, 16},
-                             {4, 256, 16},  {1, 256, 16},  {1, 512, 16},   {1, 1024, 16},
-                             {4, 512, 16},  {1, 2048, 16}};
+  // in FP32, 20480 in FP64) keep every in-block dependency on chip; a block
+  // holds at most 1024 chunks (its unit records are staged in shared memory)
+  std::vector<Cand> cands = {{4, 1, 1},    {1, 1, 1},    {4, 32, 8},    {1, 64, 8},
+                             {1, 128, 16}, {1, 256, 16}, {1, 512, 16},  {1, 1024, 16},
+                             {2, 256, 16}, {4, 64, 16},  {4, 128, 16},  {4, 256, 16}};
   if (opt.trsv_rows_per_lane > 0) {
     std::vector<Cand> keep;
     for (auto c : cands)
@@ -1063,6 +1024,7 @@ int lace_gpu_ctx::autotune_trsv() {
   plan_warps = bW;
   rows_per_lane = bR;
   trsv_tuned = true;
+  cudaMemsetAsync(&ctrl()->status, 0, 4, stream);
   drop_graphs();
   if (h_status() & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
@@ -1077,6 +1039,7 @@ extern "C" int lace_gpu_sptrsv(lace_gpu_ctx *c, int which, const double *b, doub
   int rc = c->ensure_vectors();
   if (!rc) rc = c->autotune_trsv();
   if (rc) return set_err(rc);
+  cudaMemsetAsync(&c->ctrl()->status, 0, 4, c->stream);
   const bool f32 = c->vtype() != VType::F64;
   if (f32) {
     rc = c->solve_tri(which, b, 0, c->vec_t.p, 1, false, c->vec_t2.p);
@@ -1098,6 +1061,7 @@ extern "C" int lace_gpu_apply_precond(lace_gpu_ctx *c, const double *q, double *
   int rc = c->ensure_vectors();
   if (!rc) rc = c->autotune_trsv();
   if (rc) return set_err(rc);
+  cudaMemsetAsync(&c->ctrl()->status, 0, 4, c->stream);
   const int f32 = c->vtype() != VType::F64;
   rc = c->solve_tri(0, q, 0, c->vec_t.p, f32, false, c->vec_t2.p);
   if (!rc) {

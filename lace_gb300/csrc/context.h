@@ -29,7 +29,7 @@ struct Pattern {
 
 // device arrays of one triangle's block-scheduled solve plan
 struct PlanBufs {
-  DBuf blk_lvl_ptr, lvl_ptr, units, chunk_blk, blk_row0, req_ptr, req_blk, req_lvl, kind, progress;
+  DBuf blk, urec;
   TriBlkPlan dev;
   bool valid = false;
 };

@@ -135,20 +135,27 @@ void launch_block_diag_inverse(cudaStream_t s, int nb, int bs, const int *Urow, 
 // otherwise).  ctrl may be null (stand-alone call).
 // Block-scheduled sync-free solve plan of one triangle (device arrays; see
 // sptrsv_blk.cu).  Built on the host by build_blk_plan (context.cu).
+// most chunks a block of a plan may hold (the solve stages a block's unit
+// records in shared memory)
+constexpr int kBlkMaxUnits = 1024;
 struct TriBlkPlan {
   int n = 0, nchunks = 0, nblocks = 0;
   int R = 4, cpb = 1, warps = 1, grid = 1;
   int unit = 0, lower = 1;
   const int *row = nullptr, *col = nullptr;
-  const int *blk_lvl_ptr = nullptr, *lvl_ptr = nullptr, *units = nullptr, *chunk_blk = nullptr;
-  const int *blk_row0 = nullptr;  // lowest row of each block
-  const int *req_ptr = nullptr, *req_blk = nullptr, *req_lvl = nullptr;
-  const uint8_t *kind = nullptr;
-  unsigned long long *progress = nullptr;
-  int max_levels = 0;  // largest number of local levels of a block
+  // per block (solve order): {first unit, end unit, local levels, lowest row}
+  const int4 *blk = nullptr;
+  // per unit (blocks in solve order, a block's chunks by local level):
+  // {chunk, local level | serial << 30, 0, 0}
+  const int4 *urec = nullptr;
+  int max_units = 0;  // most chunks in one block
 };
+// x must not overlap b (x is filled with the unsolved pattern first)
 void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
                        int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done);
+void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
+                             int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets, int *status,
+                             const int *done_flag);
 
 // honor_done: return at once when ctrl->done is set (inside an Arnoldi cycle)
 void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
