@@ -96,7 +96,7 @@ struct BlkPlanDev {
   int unit;
   const int4 *blk;   // {first unit, end unit, local levels, lowest row}
   const int4 *urec;  // {chunk, local level | serial << 30, 0, 0}
-  int win;           // rows of a block kept in shared memory (0: none)
+  int win;           // rows of a block kept in shared memory (0: none), plus a spare slot
   int rec_off;       // byte offset of the staged unit records in dynamic shared memory
 };
 
@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_
     const unsigned win = min(brows, (unsigned)P.win);
     for (int u = threadIdx.x; u < nunits; u += blockDim.x) s_rec[u] = P.urec[B.x + u];
     for (unsigned s = threadIdx.x; s < win; s += blockDim.x) xs[s] = unsolved_value<CT>();
+    if (threadIdx.x == 0) xs[win] = (CT)0;  // the spare slot: always solved
     __syncthreads();
     // a warp's chunks are k = warp, warp + nw, ...: ub is ready to solve;
     // the entries of the next one (rw, with its head rh) are in flight, and
@@ -297,39 +298,73 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_
         A[r] = serial ? (CT)0 : ub.aps[r];
         X[r] = (CT)0;
       }
-      // Wait for every dependency of the chunk with the whole warp in one
-      // loop: each pass reads all of them and forms the sums; the warp leaves
-      // when every lane saw all its dependencies solved.  (Lanes spinning on
-      // different branches of a diverged warp would wait for the scheduler to
-      // switch between them.)
+      // Wait for the chunk's dependencies with the whole warp in lock step
+      // (lanes spinning on different branches of a diverged warp would wait
+      // for the scheduler to switch between them): each pass reads all of a
+      // phase's dependencies and forms the sums, and the warp leaves when
+      // every lane saw them solved.  Phase A: rows of other blocks (and
+      // dependencies beyond the loaded entries), read through L2; they are
+      // usually solved before the warp gets here.  Phase B: rows of this block
+      // from the window, branch free - an entry that is not a window
+      // dependency reads the always-solved spare slot with weight 0.
+      bool far = false;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        Bv[r] = ub.bs[r];
+        far |= (ub.rest >> r) & 1;
+#pragma unroll
+        for (int t = 0; t < S; ++t) far |= ub.code[r][t] <= -2;
+      }
+      if (__any_sync(0xffffffffu, far)) {
+        for (int spins = 0;; ++spins) {
+          bool ok = true;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            CT acc = ub.bs[r];
+#pragma unroll
+            for (int t = 0; t < S; ++t)
+              if (ub.code[r][t] <= -2) acc -= ub.vs[r][t] * read_dep<CT>(xs, x, out_f32, ub.code[r][t], ok);
+            if (ub.rest & (1 << r))
+              for (int e = ub.e0[r] + S; e < ub.e1[r]; ++e) {
+                const int i = rows[r], jc = P.col[e];
+                if (jc == i || (LOWER ? (jc > i) : (jc < i)) || jc / CS == c) continue;
+                const unsigned slot = (unsigned)(jc - row0);
+                const int code = (slot < brows && slot < win) ? (int)slot : -jc - 2;
+                acc -= cvt<CT>(val[e]) * ub.rd[r] * read_dep<CT>(xs, x, out_f32, code, ok);
+              }
+            Bv[r] = acc;
+          }
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
+            if (lane == 0) atomicOr(status, kStatusSpinTimeout);  // the solve is reported as failed
+            break;
+          }
+          if (spins > 32) __nanosleep(32);
+        }
+      }
       for (int spins = 0;; ++spins) {
         bool ok = true;
+        CT acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          CT acc = ub.bs[r];
+          acc[r] = Bv[r];
 #pragma unroll
           for (int t = 0; t < S; ++t) {
             const int code = ub.code[r][t];
-            if (code != -1) acc -= ub.vs[r][t] * read_dep<CT>(xs, x, out_f32, code, ok);
+            const CT v = ((const volatile CT *)xs)[code >= 0 ? code : (int)win];
+            ok &= !is_unsolved(v);
+            acc[r] -= (code >= 0 ? ub.vs[r][t] : (CT)0) * v;
           }
-          // dependencies beyond the loaded entries (long rows)
-          if (ub.rest & (1 << r))
-            for (int e = ub.e0[r] + S; e < ub.e1[r]; ++e) {
-              const int i = rows[r], jc = P.col[e];
-              if (jc == i || (LOWER ? (jc > i) : (jc < i)) || jc / CS == c) continue;
-              const unsigned slot = (unsigned)(jc - row0);
-              const int code = (slot < brows && slot < win) ? (int)slot : -jc - 2;
-              acc -= cvt<CT>(val[e]) * ub.rd[r] * read_dep<CT>(xs, x, out_f32, code, ok);
-            }
-          Bv[r] = acc;
         }
-        if (__all_sync(0xffffffffu, ok)) break;
+        if (__all_sync(0xffffffffu, ok)) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) Bv[r] = acc[r];
+          break;
+        }
         if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
-          // give up (or another wait did): the solve is reported as failed
           if (lane == 0) atomicOr(status, kStatusSpinTimeout);
           break;
         }
-        if (spins > 256) __nanosleep(32);
       }
       if (!serial) {
         // x_p = A_p x_{p-1} + B_p along the chunk: a warp-wide affine scan
@@ -484,7 +519,7 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
   const size_t rows = (size_t)pl.cpb * 32 * pl.R;
   const size_t esz = vt == VType::F64 ? 8 : 4;
   P.win = rows * esz <= (size_t)kSptrsvSmemMax ? (int)rows : 0;
-  P.rec_off = (int)(((size_t)P.win * esz + 15) & ~(size_t)15);
+  P.rec_off = (int)(((size_t)(P.win + 1) * esz + 15) & ~(size_t)15);  // window + spare slot
   int grid = pl.grid;
   if (grid > pl.nblocks) grid = pl.nblocks;
   if (grid < 1) grid = 1;
