@@ -200,7 +200,7 @@ int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int
   return nl;
 }
 
-int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
+int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
   if (cpb < 1 || cpb > kBlkMaxUnits) return DEV_ERR_ILLEGAL_VALUE;
   const int n = T.n;
   const int CS = 32 * R;
@@ -253,20 +253,90 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
     blk[b] = make_int4(u0, (int)urec.size(), nl, (lower ? p0 : nch - p1) * CS);
     max_units = std::max(max_units, p1 - p0);
   }
+  // the plan's own layout: per unit, where each row's dependencies are read
+  // and which CSR entries give their values
+  const int S = blk_slots(R);
+  const size_t nu = urec.size();
+  const size_t rs = nu * (size_t)R * 32;
+  std::vector<int> ucode(rs * S, -1), umap(rs * S, -1), udiag(rs, -1), uprev(rs, -1), uflag(nu * 32, 0);
+  for (size_t u = 0; u < nu; ++u) {
+    const int c = urec[u].x;
+    const bool serial = kind[c] != 0;
+    const int4 B = blk[cblk[c]];
+    const int row0 = B.w, brows = (B.y - B.x) * CS;
+    const int base = c * CS, cnt = std::min(CS, n - base);
+    for (int lane = 0; lane < 32; ++lane)
+      for (int r = 0; r < R; ++r) {
+        const int pos = lane * R + r;
+        if (pos >= cnt) continue;
+        const int i = lower ? base + pos : base + cnt - 1 - pos;
+        const int prev = lower ? i - 1 : i + 1;
+        const size_t q = (u * R + r) * 32 + lane;
+        int next = 0;
+        for (int e = T.ptr[i]; e < T.ptr[i + 1]; ++e) {
+          const int j = T.idx[e];
+          if (j == i) {
+            if (!unit) udiag[q] = e;
+            continue;
+          }
+          if (lower ? j > i : j < i) continue;
+          if (j / CS == c) {
+            if (!serial && j == prev) uprev[q] = e;
+            continue;
+          }
+          if (next < S) {
+            const size_t qs = ((u * S + next) * R + r) * 32 + lane;
+            const int slot = j - row0;
+            ucode[qs] = (slot >= 0 && slot < brows) ? slot : -j - 2;
+            umap[qs] = e;
+          }
+          ++next;
+        }
+        if (next > S) {  // solved from the CSR arrays
+          uflag[u * 32 + lane] |= 1 << r;
+          for (int t = 0; t < S; ++t) {
+            const size_t qs = ((u * S + t) * R + r) * 32 + lane;
+            ucode[qs] = -1;
+            umap[qs] = -1;
+          }
+        }
+      }
+  }
   int rc = 0;
   rc |= pb.blk.upload(blk.data(), sizeof(int4) * blk.size(), s);
   rc |= pb.urec.upload(urec.data(), sizeof(int4) * urec.size(), s);
+  rc |= pb.ucode.upload(ucode.data(), 4 * ucode.size(), s);
+  rc |= pb.umap.upload(umap.data(), 4 * umap.size(), s);
+  rc |= pb.udiag.upload(udiag.data(), 4 * udiag.size(), s);
+  rc |= pb.uprev.upload(uprev.data(), 4 * uprev.size(), s);
+  rc |= pb.uflag.upload(uflag.data(), 4 * uflag.size(), s);
+  rc |= pb.uvs.ensure(8 * rs * S);
+  rc |= pb.uaps.ensure(8 * rs);
+  rc |= pb.urd.ensure(8 * rs);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
+  // the host vectors go out of scope: wait for the uploads
+  if (cudaStreamSynchronize(s) != cudaSuccess) return DEV_ERR_UNKNOWN;
   TriBlkPlan &d = pb.dev;
   d.n = n;
   d.nchunks = nch;
   d.nblocks = nblk;
+  d.nunits = (int)nu;
   d.R = R;
   d.cpb = cpb;
   d.lower = lower ? 1 : 0;
+  d.unit = unit ? 1 : 0;
   d.blk = (const int4 *)pb.blk.p;
   d.urec = (const int4 *)pb.urec.p;
   d.max_units = max_units;
+  d.ucode = (const int *)pb.ucode.p;
+  d.umap = (const int *)pb.umap.p;
+  d.udiag = (const int *)pb.udiag.p;
+  d.uprev = (const int *)pb.uprev.p;
+  d.uflag = (const int *)pb.uflag.p;
+  d.uvs = pb.uvs.p;
+  d.uaps = pb.uaps.p;
+  d.urd = pb.urd.p;
+  pb.vals_version = -1;
   pb.valid = true;
   return 0;
 }
@@ -275,25 +345,29 @@ int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, c
 
 using namespace lace;
 
-// the block-scheduled plan of one triangle with the current schedule shape
+// the block-scheduled plan of one triangle with the current schedule shape,
+// its values gathered from the current factor values
 int lace_gpu_ctx::ensure_plan(int which) {
   PlanBufs &pb = plans[which];
-  if (pb.valid && pb.dev.R == plan_R && pb.dev.cpb == plan_cpb) {
-    pb.dev.warps = plan_warps;
-    return 0;
-  }
-  const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
-  const bool low[4] = {true, false, true, false};
-  int rc = build_blk_plan(*pats[which], low[which], plan_R, plan_cpb, pb, stream);
-  if (rc) return rc;
   TriDev t = tri(which);
+  if (!(pb.valid && pb.dev.R == plan_R && pb.dev.cpb == plan_cpb)) {
+    const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
+    const bool low[4] = {true, false, true, false};
+    int rc = build_blk_plan(*pats[which], low[which], t.unit != 0, plan_R, plan_cpb, pb, stream);
+    if (rc) return rc;
+  }
   pb.dev.row = t.row;
   pb.dev.col = t.col;
-  pb.dev.unit = t.unit;
   pb.dev.warps = plan_warps;
   const int per_sm = plan_warps == 1 ? 16 : (plan_warps <= 8 ? 4 : (plan_warps <= 16 ? 2 : 1));
   pb.dev.grid = std::min(pb.dev.nblocks, num_sms() * per_sm);
-  return 0;
+  if (pb.vals_version != fact_version || pb.vals_type != (int)vtype() || pb.vals_src != t.val) {
+    launch_plan_values(stream, pb.dev, t.val, vtype());
+    pb.vals_version = fact_version;
+    pb.vals_type = (int)vtype();
+    pb.vals_src = t.val;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 
 // ======================================================================
@@ -544,6 +618,7 @@ int lace_gpu_ctx::set_factors_host(int nrows, const int *lrow, const int *lcol, 
   launch_gather(stream, nnzU, (const int *)m.p, VType::F64, tu.p, t, Ucv[0].p);
   launch_gather(stream, nnzL, (const int *)map_lt2l.p, VType::F64, tl.p, t, Ltv.p);
   factors_ready = true;
+  ++fact_version;
   if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
   return 0;
 }
@@ -798,6 +873,7 @@ int lace_gpu_ctx::finish_factors() {
                               &ctrl()->status);
   }
   factors_ready = true;
+  ++fact_version;
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 

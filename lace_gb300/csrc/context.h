@@ -29,14 +29,18 @@ struct Pattern {
 
 // device arrays of one triangle's block-scheduled solve plan
 struct PlanBufs {
-  DBuf blk, urec;
+  DBuf blk, urec, ucode, umap, udiag, uprev, uflag, uvs, uaps, urd;
   TriBlkPlan dev;
   bool valid = false;
+  // the factor values the plan's values were gathered from
+  int vals_version = -1;
+  int vals_type = -1;
+  const void *vals_src = nullptr;
 };
 
 // host construction of a plan: chunks of 32*R rows, blocks of cpb chunks (in
 // solve order), local levels inside blocks, cross-block requirements
-int build_blk_plan(const Pattern &T, bool lower, int R, int cpb, PlanBufs &pb, cudaStream_t s);
+int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s);
 
 extern thread_local int g_last_error;
 int set_err(int code);
@@ -75,6 +79,7 @@ struct lace_gpu_ctx {
   DBuf Lv[2], Ucv[2], Urv, Ltv, dinv;
   int cur = 0;
   bool factors_ready = false;
+  int fact_version = 0;  // bumped whenever the factor values change
 
   // SpTRSV per triangle (0 L, 1 U, 2 U^T, 3 L^T)
   DBuf kinds[4][4];  // [triangle][log2 rows-per-lane]

@@ -135,11 +135,13 @@ void launch_block_diag_inverse(cudaStream_t s, int nb, int bs, const int *Urow, 
 // otherwise).  ctrl may be null (stand-alone call).
 // Block-scheduled sync-free solve plan of one triangle (device arrays; see
 // sptrsv_blk.cu).  Built on the host by build_blk_plan (context.cu).
-// most chunks a block of a plan may hold (the solve stages a block's unit
-// records in shared memory)
+// most chunks a block of a plan may hold
 constexpr int kBlkMaxUnits = 1024;
+// dependencies outside its chunk a row keeps in the plan's own layout (rows
+// with more are solved from the CSR arrays)
+__host__ __device__ constexpr int blk_slots(int R) { return R == 1 ? 4 : (R == 2 ? 3 : 2); }
 struct TriBlkPlan {
-  int n = 0, nchunks = 0, nblocks = 0;
+  int n = 0, nchunks = 0, nblocks = 0, nunits = 0;
   int R = 4, cpb = 1, warps = 1, grid = 1;
   int unit = 0, lower = 1;
   const int *row = nullptr, *col = nullptr;
@@ -149,7 +151,22 @@ struct TriBlkPlan {
   // {chunk, local level | serial << 30, 0, 0}
   const int4 *urec = nullptr;
   int max_units = 0;  // most chunks in one block
+  // The plan's own layout of the solve, coalesced per warp.  Per unit u,
+  // slot t < S, row r < R, lane l: index ((u*S + t)*R + r)*32 + l for the
+  // slot arrays, (u*R + r)*32 + l for the per-row ones.
+  //   ucode: where the dependency is read: >= 0 row (code) of the block's
+  //          window, <= -2 row -(code+2) of the output, -1 none
+  //   umap, udiag, uprev: CSR entry of the dependency, the diagonal (-1 for a
+  //          unit diagonal) and the previous row of a scan chunk (or -1)
+  //   uflag: per unit and lane, bit r: row r has more than S dependencies
+  //          (its slots are empty; it is solved from the CSR arrays)
+  //   uvs, uaps, urd: values in the compute type, gathered from the factor
+  //          values: a_ij / a_ii, -a_{i,prev} / a_ii and 1 / a_ii
+  const int *ucode = nullptr, *umap = nullptr, *udiag = nullptr, *uprev = nullptr, *uflag = nullptr;
+  void *uvs = nullptr, *uaps = nullptr, *urd = nullptr;
 };
+// gather the plan's values (uvs, uaps, urd) from the triangle's values
+void launch_plan_values(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt);
 // x must not overlap b (x is filled with the unsolved pattern first)
 void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
                        int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done);

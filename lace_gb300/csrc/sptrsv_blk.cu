@@ -18,13 +18,14 @@
 // its dependencies in the block), so the lowest unsolved chunk can always
 // proceed.
 //
-// Each warp prepares its next chunks while other warps solve, three deep:
-// the chunk after next has its record and row pointers loaded, the next one
-// its entries and right-hand side, and when a chunk is done the next one is
-// classified (window slot or row of another block per entry) and scaled by
-// the reciprocal of the diagonal.  What is left on the dependency chain is
-// reading the dependencies, one fused multiply-add per entry, the scan, and
-// the stores.
+// The plan holds the solve in its own layout, coalesced per warp: for each
+// chunk, row and dependency slot where the dependency is read (window slot or
+// row of the output) and, gathered from the factor values whenever they
+// change, the entry scaled by the reciprocal of the diagonal (rows with more
+// dependencies than slots are solved from the CSR arrays).  A warp loads the
+// next chunk's data while it solves the current one, so what is left on the
+// dependency chain is reading the dependencies, one fused multiply-add per
+// entry, the scan, and the stores.
 //
 // For a lexicographic 7-point stencil with R = 4 (a chunk = one x-line) and
 // blocks of whole planes, every x-line is one scan, the j- and k-direction
@@ -82,177 +83,270 @@ __device__ __forceinline__ CT read_dep(const CT *xs, const void *x, int f32, int
   return v;
 }
 
-// CSR entries of a row loaded ahead of the row's turn; longer rows read the
-// rest when they are solved
-template <int R>
-struct BlkSlots {
-  static constexpr int S = R == 1 ? 6 : (R == 2 ? 4 : (R == 4 ? 3 : 2));
-};
-
 struct BlkPlanDev {
   int n, nblocks;
   const int *row, *col;
-  const void *val;
-  int unit;
-  const int4 *blk;   // {first unit, end unit, local levels, lowest row}
-  const int4 *urec;  // {chunk, local level | serial << 30, 0, 0}
-  int win;           // rows of a block kept in shared memory (0: none), plus a spare slot
-  int rec_off;       // byte offset of the staged unit records in dynamic shared memory
+  const void *val;  // CSR values (rows solved from the CSR arrays, serial chunks)
+  const int4 *blk;  // {first unit, end unit, local levels, lowest row}
+  const int4 *urec; // {chunk, local level | serial << 30, 0, 0}
+  const int *ucode, *uflag;
+  const void *uvs, *uaps, *urd;
+  int win;  // rows of a block kept in shared memory (0: none), plus a spare slot
 };
 
-// A chunk of the block whose record and row pointers are loaded.
-template <int R>
-struct UnitHead {
-  int k;  // index in the block's unit list; -1: none
-  int4 rec;
-  int e0[R], e1[R];
-};
-// Loaded entries of a chunk, before classification.
-template <typename VT, int R, int S>
-struct UnitRaw {
-  int cc[R][S];
-  VT vv[R][S];
-  unsigned long long braw[R];  // b_i: FP64 bits, or FP32 bits in the low word
-};
-// A chunk ready to solve.  Per row: bs = b/d, aps = -a_{i,prev}/d, rd = 1/d,
-// and the loaded entries scaled by 1/d with where their dependency is read:
-// code >= 0 a window slot, code <= -2 row -(code+2) of the output, -1 none.
-// Bit r of rest: row r has dependencies among the entries not loaded.
+// One chunk's solve data, loaded by its warp ahead of its turn, and the
+// record of the chunk this register set takes next (loaded one turn early, so
+// that the right-hand-side loads need not wait for it).
 template <typename CT, int R, int S>
-struct UnitReady {
-  int k;
-  int4 rec;
-  CT bs[R], aps[R], rd[R];
+struct Unit {
+  int k;  // index in the block's unit list; -1: none
+  int4 rec, nrec;
   int code[R][S];
   CT vs[R][S];
-  int e0[R], e1[R];
-  int rest;
+  CT aps[R], rd[R];
+  unsigned long long braw[R];  // b_i: FP64 bits, or FP32 bits in the low word
+  int flag;
 };
 
-template <int R, bool LOWER>
-__device__ __forceinline__ void unit_head(UnitHead<R> &h, int k, int nunits, const int4 *s_rec,
-                                          const BlkPlanDev &P, int lane) {
+// take chunk k (its record is d.nrec) and load the record of chunk k + step
+template <typename CT, int R, int S, bool LOWER>
+__device__ __forceinline__ void unit_load(Unit<CT, R, S> &d, int k, int step, int nunits, int ubase,
+                                          const BlkPlanDev &P, const void *b, int in_f32, int lane) {
   constexpr int CS = 32 * R;
-  h.k = k < nunits ? k : -1;
-  if (h.k < 0) return;
-  h.rec = s_rec[k];
-  const int base = h.rec.x * CS, cnt = min(CS, P.n - base);
+  d.k = k < nunits ? k : -1;
+  if (d.k < 0) return;
+  d.rec = d.nrec;
+  if (k + step < nunits) d.nrec = P.urec[(size_t)ubase + k + step];
+  const size_t u = (size_t)ubase + k;
+  const CT *uvs = (const CT *)P.uvs, *uaps = (const CT *)P.uaps, *urd = (const CT *)P.urd;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const size_t q = (u * R + r) * 32 + lane;
+    d.aps[r] = uaps[q];
+    d.rd[r] = urd[q];
+#pragma unroll
+    for (int t = 0; t < S; ++t) {
+      const size_t qs = ((u * S + t) * R + r) * 32 + lane;
+      d.code[r][t] = P.ucode[qs];
+      d.vs[r][t] = uvs[qs];
+    }
+  }
+  d.flag = P.uflag[u * 32 + lane];
+  const int base = d.rec.x * CS, cnt = min(CS, P.n - base);
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int pos = lane * R + r;
-    h.e0[r] = 0;
-    h.e1[r] = 0;
+    d.braw[r] = 0;
     if (pos < cnt) {
       const int i = LOWER ? base + pos : base + cnt - 1 - pos;
-      h.e0[r] = P.row[i];
-      h.e1[r] = P.row[i + 1];
+      if (in_f32) d.braw[r] = ((const unsigned *)b)[i];
+      else d.braw[r] = ((const unsigned long long *)b)[i];
     }
   }
 }
 
-template <typename VT, int R, int S, bool LOWER>
-__device__ __forceinline__ void unit_load(UnitRaw<VT, R, S> &w, const UnitHead<R> &h, const BlkPlanDev &P,
-                                          const void *b, int in_f32, int lane) {
+// Phase A of a chunk's wait: rows outside the window, read through L2 (OT:
+// the output's type).  Branch free over the slots - a slot without such a
+// dependency reads an always-solved zero in this CTA's shared memory - so
+// that the lanes' loads of one pass go out together.  Rows solved from the
+// CSR arrays are read after.
+template <typename CT, typename VT, typename OT, int R, int S, bool LOWER>
+__device__ __forceinline__ void far_wait(const Unit<CT, R, S> &d, const BlkPlanDev &P, const CT *xs, const void *x,
+                                         int row0, unsigned brows, unsigned win, int lane, const int *rows, int c,
+                                         CT *Bv, const double *s_zero, int *status) {
   constexpr int CS = 32 * R;
-  if (h.k < 0) return;
   const VT *val = (const VT *)P.val;
-  const int base = h.rec.x * CS, cnt = min(CS, P.n - base);
+  const OT *zero = (const OT *)s_zero;
+  const OT *src[R][S];
+  CT w[R][S], acc0[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int pos = lane * R + r;
-    w.braw[r] = 0;
-    if (pos < cnt) {
-      const int i = LOWER ? base + pos : base + cnt - 1 - pos;
-      if (in_f32) w.braw[r] = ((const unsigned *)b)[i];
-      else w.braw[r] = ((const unsigned long long *)b)[i];
-    }
+    acc0[r] = Bv[r];
 #pragma unroll
     for (int t = 0; t < S; ++t) {
-      const int e = h.e0[r] + t;
-      w.cc[r][t] = -1;
-      if (e < h.e1[r]) {
-        w.cc[r][t] = P.col[e];
-        w.vv[r][t] = val[e];
-      }
+      const int code = d.code[r][t];
+      const bool glob = code <= -2 || code >= (int)win;
+      src[r][t] = glob ? (const OT *)x + (code <= -2 ? -code - 2 : row0 + code) : zero;
+      w[r][t] = glob ? d.vs[r][t] : (CT)0;
     }
+  }
+  for (int spins = 0;; ++spins) {
+    bool ok = true;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      CT acc = acc0[r];
+#pragma unroll
+      for (int t = 0; t < S; ++t) {
+        const OT v = *(const volatile OT *)src[r][t];
+        ok &= !is_unsolved(v);
+        acc -= w[r][t] * (CT)v;
+      }
+      if ((d.flag >> r) & 1) {
+        const int i = rows[r];
+        for (int e = P.row[i]; e < P.row[i + 1]; ++e) {
+          const int jc = P.col[e];
+          if (jc == i || (LOWER ? (jc > i) : (jc < i)) || jc / CS == c) continue;
+          const unsigned slot = (unsigned)(jc - row0);
+          const int code = (slot < brows && slot < win) ? (int)slot : -jc - 2;
+          acc -= cvt<CT>(val[e]) * d.rd[r] * read_dep<CT>(xs, x, sizeof(OT) == 4, code, ok);
+        }
+      }
+      Bv[r] = acc;
+    }
+    if (__all_sync(0xffffffffu, ok)) break;
+    if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
+      if (lane == 0) atomicOr(status, kStatusSpinTimeout);  // the solve is reported as failed
+      break;
+    }
+    if (spins > 32) __nanosleep(32);
   }
 }
 
 template <typename CT, typename VT, int R, int S, bool LOWER>
-__device__ __forceinline__ void unit_classify(UnitReady<CT, R, S> &u, const UnitRaw<VT, R, S> &w,
-                                              const UnitHead<R> &h, const BlkPlanDev &P, int in_f32,
-                                              int lane, int row0, unsigned brows, unsigned win) {
+__device__ __forceinline__ void unit_solve(const Unit<CT, R, S> &d, const BlkPlanDev &P, CT *xs, void *x,
+                                           int in_f32, int out_f32, int row0, unsigned brows, unsigned win,
+                                           int lane, const double *s_zero, int *status) {
   constexpr int CS = 32 * R;
-  u.k = h.k;
-  u.rec = h.rec;
-  if (u.k < 0) return;
   const VT *val = (const VT *)P.val;
-  const int c = h.rec.x;
-  const bool serial = (h.rec.y >> 30) != 0;
-  const int base = c * CS, cnt = min(CS, P.n - base);
-  u.rest = 0;
+  const int c = d.rec.x;
+  const bool serial = (d.rec.y >> 30) != 0;
+  const int base = c * CS;
+  const int cnt = min(CS, P.n - base);
+  CT A[R], Bv[R], X[R];
+  int rows[R];
+  bool far = false;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int pos = lane * R + r;
-    const int i = LOWER ? base + pos : base + cnt - 1 - pos;
-    const int prev = LOWER ? i - 1 : i + 1;
-    u.e0[r] = h.e0[r];
-    u.e1[r] = h.e1[r];
-    CT d = (CT)1, ap = (CT)0;
-    auto where = [&](int jc, CT v) -> int {
-      if (jc == i) {
-        if (!P.unit) d = v;
-        return -1;
-      }
-      if (LOWER ? (jc > i) : (jc < i)) return -1;
-      if (jc / CS == c) {
-        if (!serial && jc == prev) ap = v;
-        return -1;
-      }
-      const unsigned slot = (unsigned)(jc - row0);
-      return (slot < brows && slot < win) ? (int)slot : -jc - 2;
-    };
+    rows[r] = pos < cnt ? (LOWER ? base + pos : base + cnt - 1 - pos) : -1;
+    A[r] = serial ? (CT)0 : d.aps[r];
+    const CT bb = in_f32 ? (CT)__uint_as_float((unsigned)d.braw[r]) : (CT)__longlong_as_double((long long)d.braw[r]);
+    Bv[r] = rows[r] >= 0 ? bb * d.rd[r] : (CT)0;
+    X[r] = (CT)0;
+    far |= (d.flag >> r) & 1;
 #pragma unroll
-    for (int t = 0; t < S; ++t) {
-      const CT v = cvt<CT>(w.vv[r][t]);
-      u.code[r][t] = w.cc[r][t] >= 0 ? where(w.cc[r][t], v) : -1;
-      u.vs[r][t] = v;
-    }
-    // the diagonal (last in a CSRL row) may lie beyond the loaded entries
-    for (int e = h.e0[r] + S; e < h.e1[r]; ++e)
-      if (where(P.col[e], cvt<CT>(val[e])) != -1) u.rest |= 1 << r;
-    const CT rd = P.unit ? (CT)1 : rcp_rn(d);
-    const CT bb = in_f32 ? (CT)__uint_as_float((unsigned)w.braw[r])
-                         : (CT)__longlong_as_double((long long)w.braw[r]);
-    u.rd[r] = rd;
-    u.bs[r] = pos < cnt ? bb * rd : (CT)0;
-    u.aps[r] = -ap * rd;
-#pragma unroll
-    for (int t = 0; t < S; ++t) u.vs[r][t] *= rd;
+    for (int t = 0; t < S; ++t) far |= d.code[r][t] <= -2 || d.code[r][t] >= (int)win;
   }
+  // Wait for the chunk's dependencies with the whole warp in lock step
+  // (lanes spinning on different branches of a diverged warp would wait for
+  // the scheduler to switch between them): each pass reads all of a phase's
+  // dependencies and forms the sums, and the warp leaves when every lane saw
+  // them solved.  Phase A: rows outside the window (other blocks) and rows
+  // solved from the CSR arrays, read through L2; they are usually solved
+  // before the warp gets here.  Phase B: rows of the window, branch free - an
+  // entry that is not a window dependency reads the always-solved spare slot
+  // with weight 0.
+  if (__any_sync(0xffffffffu, far)) {
+    if (out_f32) far_wait<CT, VT, float, R, S, LOWER>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status);
+    else far_wait<CT, VT, double, R, S, LOWER>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status);
+  }
+  for (int spins = 0;; ++spins) {
+    bool ok = true;
+    CT acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      acc[r] = Bv[r];
+#pragma unroll
+      for (int t = 0; t < S; ++t) {
+        const int code = d.code[r][t];
+        const bool in = (unsigned)code < win;
+        const CT v = ((const volatile CT *)xs)[in ? code : (int)win];
+        ok &= !is_unsolved(v);
+        acc[r] -= (in ? d.vs[r][t] : (CT)0) * v;
+      }
+    }
+    if (__all_sync(0xffffffffu, ok)) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) Bv[r] = acc[r];
+      break;
+    }
+    if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
+      if (lane == 0) atomicOr(status, kStatusSpinTimeout);
+      break;
+    }
+  }
+  if (!serial) {
+    // x_p = A_p x_{p-1} + B_p along the chunk: a warp-wide affine scan
+    CT ca = (CT)1, cb = (CT)0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      cb = A[r] * cb + Bv[r];
+      ca = A[r] * ca;
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
+      const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
+      if (lane >= o) {
+        cb = ca * pb + cb;
+        ca = ca * pa;
+      }
+    }
+    CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
+    if (lane == 0) xin = (CT)0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      xin = A[r] * xin + Bv[r];
+      X[r] = xin;
+    }
+  } else {
+    // position by position: the owner's value is final, the later rows of
+    // the chunk subtract it (entries from the CSR arrays)
+    int e0[R], e1[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      e0[r] = rows[r] >= 0 ? P.row[rows[r]] : 0;
+      e1[r] = rows[r] >= 0 ? P.row[rows[r] + 1] : 0;
+    }
+    for (int p = 0; p < cnt; ++p) {
+      const int owner = p / R, rr = p % R;
+      CT xp = (CT)0;
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (lane == owner && r == rr) xp = Bv[r];
+      xp = __shfl_sync(0xffffffffu, xp, owner);
+      const int rowp = LOWER ? base + p : base + cnt - 1 - p;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int pos = lane * R + r;
+        if (pos == p) X[r] = xp;
+        if (pos > p && pos < cnt)
+          for (int e = e0[r]; e < e1[r]; ++e)
+            if (P.col[e] == rowp) Bv[r] -= cvt<CT>(val[e]) * d.rd[r] * xp;
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (rows[r] >= 0) {
+      const CT v = as_solved(X[r]);
+      const unsigned slot = (unsigned)(rows[r] - row0);
+      if (slot < win) ((volatile CT *)xs)[slot] = v;
+      st_out<CT>(x, out_f32, rows[r], v);
+    }
 }
 
 // blockIdx.y selects one of several right-hand sides (vectors vstride
 // elements apart, each filled with the unsolved pattern beforehand); each has
 // its own ticket counter tickets[rhs]; tickets[gridDim.y] counts exiting CTAs.
 template <typename CT, typename VT, int R, bool LOWER>
-__global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_, int in_f32, void *x_,
+__global__ void __launch_bounds__(512, 1) k_sptrsv_blk(BlkPlanDev P, const void *b_, int in_f32, void *x_,
                                                     int out_f32, size_t vstride, int *tickets,
                                                     const int *done_flag, int *status) {
   if (done_flag != nullptr && *(volatile const int *)done_flag) return;
   constexpr int CS = 32 * R;
-  constexpr int S = BlkSlots<R>::S;
+  constexpr int S = blk_slots(R);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CT *xs = reinterpret_cast<CT *>(smem_raw);
-  int4 *s_rec = reinterpret_cast<int4 *>(smem_raw + P.rec_off);
   __shared__ int s_blk;
+  __shared__ double s_zero;  // always solved: read by dependency slots that read nothing
+  if (threadIdx.x == 0) s_zero = 0.0;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int rhs = blockIdx.y;
   const void *b = (const char *)b_ + (size_t)rhs * vstride * (in_f32 ? 4 : 8);
   void *x = (char *)x_ + (size_t)rhs * vstride * (out_f32 ? 4 : 8);
-  const VT *val = (const VT *)P.val;
   while (true) {
     __syncthreads();
     if (threadIdx.x == 0) s_blk = atomicAdd(&tickets[rhs], 1);
@@ -263,170 +357,22 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_
     const int nunits = B.y - B.x, row0 = B.w;
     const unsigned brows = (unsigned)(nunits * CS);
     const unsigned win = min(brows, (unsigned)P.win);
-    for (int u = threadIdx.x; u < nunits; u += blockDim.x) s_rec[u] = P.urec[B.x + u];
     for (unsigned s = threadIdx.x; s < win; s += blockDim.x) xs[s] = unsolved_value<CT>();
     if (threadIdx.x == 0) xs[win] = (CT)0;  // the spare slot: always solved
     __syncthreads();
-    // a warp's chunks are k = warp, warp + nw, ...: ub is ready to solve;
-    // the entries of the next one (rw, with its head rh) are in flight, and
-    // the record and row pointers of the one after that (hd)
-    UnitReady<CT, R, S> ub;
-    UnitRaw<VT, R, S> rw;
-    UnitHead<R> rh, hd;
-    {
-      UnitHead<R> h0;
-      unit_head<R, LOWER>(h0, warp, nunits, s_rec, P, lane);
-      unit_load<VT, R, S, LOWER>(rw, h0, P, b, in_f32, lane);
-      rh.k = -1;
-      if (h0.k >= 0) unit_head<R, LOWER>(rh, h0.k + nw, nunits, s_rec, P, lane);
-      unit_classify<CT, VT, R, S, LOWER>(ub, rw, h0, P, in_f32, lane, row0, brows, win);
-      unit_load<VT, R, S, LOWER>(rw, rh, P, b, in_f32, lane);
-      hd.k = -1;
-      if (rh.k >= 0) unit_head<R, LOWER>(hd, rh.k + nw, nunits, s_rec, P, lane);
-    }
-    while (ub.k >= 0) {
-      const int c = ub.rec.x;
-      const bool serial = (ub.rec.y >> 30) != 0;
-      const int base = c * CS;
-      const int cnt = min(CS, P.n - base);
-      CT A[R], Bv[R], X[R];
-      int rows[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int pos = lane * R + r;
-        rows[r] = pos < cnt ? (LOWER ? base + pos : base + cnt - 1 - pos) : -1;
-        A[r] = serial ? (CT)0 : ub.aps[r];
-        X[r] = (CT)0;
-      }
-      // Wait for the chunk's dependencies with the whole warp in lock step
-      // (lanes spinning on different branches of a diverged warp would wait
-      // for the scheduler to switch between them): each pass reads all of a
-      // phase's dependencies and forms the sums, and the warp leaves when
-      // every lane saw them solved.  Phase A: rows of other blocks (and
-      // dependencies beyond the loaded entries), read through L2; they are
-      // usually solved before the warp gets here.  Phase B: rows of this block
-      // from the window, branch free - an entry that is not a window
-      // dependency reads the always-solved spare slot with weight 0.
-      bool far = false;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        Bv[r] = ub.bs[r];
-        far |= (ub.rest >> r) & 1;
-#pragma unroll
-        for (int t = 0; t < S; ++t) far |= ub.code[r][t] <= -2;
-      }
-      if (__any_sync(0xffffffffu, far)) {
-        for (int spins = 0;; ++spins) {
-          bool ok = true;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            CT acc = ub.bs[r];
-#pragma unroll
-            for (int t = 0; t < S; ++t)
-              if (ub.code[r][t] <= -2) acc -= ub.vs[r][t] * read_dep<CT>(xs, x, out_f32, ub.code[r][t], ok);
-            if (ub.rest & (1 << r))
-              for (int e = ub.e0[r] + S; e < ub.e1[r]; ++e) {
-                const int i = rows[r], jc = P.col[e];
-                if (jc == i || (LOWER ? (jc > i) : (jc < i)) || jc / CS == c) continue;
-                const unsigned slot = (unsigned)(jc - row0);
-                const int code = (slot < brows && slot < win) ? (int)slot : -jc - 2;
-                acc -= cvt<CT>(val[e]) * ub.rd[r] * read_dep<CT>(xs, x, out_f32, code, ok);
-              }
-            Bv[r] = acc;
-          }
-          if (__all_sync(0xffffffffu, ok)) break;
-          if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
-            if (lane == 0) atomicOr(status, kStatusSpinTimeout);  // the solve is reported as failed
-            break;
-          }
-          if (spins > 32) __nanosleep(32);
-        }
-      }
-      for (int spins = 0;; ++spins) {
-        bool ok = true;
-        CT acc[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          acc[r] = Bv[r];
-#pragma unroll
-          for (int t = 0; t < S; ++t) {
-            const int code = ub.code[r][t];
-            const CT v = ((const volatile CT *)xs)[code >= 0 ? code : (int)win];
-            ok &= !is_unsolved(v);
-            acc[r] -= (code >= 0 ? ub.vs[r][t] : (CT)0) * v;
-          }
-        }
-        if (__all_sync(0xffffffffu, ok)) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) Bv[r] = acc[r];
-          break;
-        }
-        if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
-          if (lane == 0) atomicOr(status, kStatusSpinTimeout);
-          break;
-        }
-      }
-      if (!serial) {
-        // x_p = A_p x_{p-1} + B_p along the chunk: a warp-wide affine scan
-        CT ca = (CT)1, cb = (CT)0;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          cb = A[r] * cb + Bv[r];
-          ca = A[r] * ca;
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
-          const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
-          if (lane >= o) {
-            cb = ca * pb + cb;
-            ca = ca * pa;
-          }
-        }
-        CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
-        if (lane == 0) xin = (CT)0;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          xin = A[r] * xin + Bv[r];
-          X[r] = xin;
-        }
-      } else {
-        // position by position: the owner's value is final, the later rows
-        // of the chunk subtract it
-        for (int p = 0; p < cnt; ++p) {
-          const int owner = p / R, rr = p % R;
-          CT xp = (CT)0;
-#pragma unroll
-          for (int r = 0; r < R; ++r)
-            if (lane == owner && r == rr) xp = Bv[r];
-          xp = __shfl_sync(0xffffffffu, xp, owner);
-          const int rowp = LOWER ? base + p : base + cnt - 1 - p;
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const int pos = lane * R + r;
-            if (pos == p) X[r] = xp;
-            if (pos > p && pos < cnt)
-              for (int e = ub.e0[r]; e < ub.e1[r]; ++e)
-                if (P.col[e] == rowp) Bv[r] -= cvt<CT>(val[e]) * ub.rd[r] * xp;
-          }
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        if (rows[r] >= 0) {
-          const CT v = as_solved(X[r]);
-          const unsigned slot = (unsigned)(rows[r] - row0);
-          if (slot < win) ((volatile CT *)xs)[slot] = v;
-          st_out<CT>(x, out_f32, rows[r], v);
-        }
-      // advance the pipeline: classify the next chunk (its entries were
-      // loaded one chunk ago), load the entries of the one after, and the
-      // record and row pointers of the one after that
-      unit_classify<CT, VT, R, S, LOWER>(ub, rw, rh, P, in_f32, lane, row0, brows, win);
-      rh = hd;
-      unit_load<VT, R, S, LOWER>(rw, rh, P, b, in_f32, lane);
-      hd.k = -1;
-      if (rh.k >= 0) unit_head<R, LOWER>(hd, rh.k + nw, nunits, s_rec, P, lane);
+    // a warp's chunks are k = warp, warp + nw, ...; two register sets take
+    // turns, so a chunk's data is loaded while the chunk before it is solved
+    Unit<CT, R, S> d0, d1;
+    if (warp < nunits) d0.nrec = P.urec[B.x + warp];
+    if (warp + nw < nunits) d1.nrec = P.urec[B.x + warp + nw];
+    unit_load<CT, R, S, LOWER>(d0, warp, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+    unit_load<CT, R, S, LOWER>(d1, warp + nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+    while (d0.k >= 0) {
+      unit_solve<CT, VT, R, S, LOWER>(d0, P, xs, x, in_f32, out_f32, row0, brows, win, lane, &s_zero, status);
+      unit_load<CT, R, S, LOWER>(d0, d0.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+      if (d1.k < 0) break;
+      unit_solve<CT, VT, R, S, LOWER>(d1, P, xs, x, in_f32, out_f32, row0, brows, win, lane, &s_zero, status);
+      unit_load<CT, R, S, LOWER>(d1, d1.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
     }
   }
   // the CTA that leaves last re-arms the tickets
@@ -437,6 +383,50 @@ __global__ void __launch_bounds__(512) k_sptrsv_blk(BlkPlanDev P, const void *b_
       for (int r = 0; r <= nrhs; ++r) tickets[r] = 0;
       __threadfence();
     }
+  }
+}
+
+// the plan's values from the triangle's values: per row slot q, 1/a_ii (1 for
+// a unit diagonal), -a_{i,prev}/a_ii, and a_ij/a_ii per dependency slot
+template <typename VT, typename CT>
+__global__ void k_plan_values(size_t rs, int R, int S, const int *umap, const int *udiag, const int *uprev,
+                              const VT *val, CT *uvs, CT *uaps, CT *urd) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t per = (size_t)R * 32;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < rs; q += stride) {
+    const int dg = udiag[q], pv = uprev[q];
+    const CT rd = dg >= 0 ? (CT)1 / cvt<CT>(val[dg]) : (CT)1;
+    urd[q] = rd;
+    uaps[q] = pv >= 0 ? -cvt<CT>(val[pv]) * rd : (CT)0;
+    const size_t u = q / per, w = q % per;
+    for (int t = 0; t < S; ++t) {
+      const size_t qs = (u * S + t) * per + w;
+      const int e = umap[qs];
+      uvs[qs] = e >= 0 ? cvt<CT>(val[e]) * rd : (CT)0;
+    }
+  }
+}
+
+void launch_plan_values(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt) {
+  const size_t rs = (size_t)pl.nunits * pl.R * 32;
+  const int S = blk_slots(pl.R);
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 8, (rs + 255) / 256));
+  switch (vt) {
+    case VType::F64:
+      k_plan_values<double, double><<<grid, 256, 0, s>>>(rs, pl.R, S, pl.umap, pl.udiag, pl.uprev,
+                                                         (const double *)val, (double *)pl.uvs,
+                                                         (double *)pl.uaps, (double *)pl.urd);
+      break;
+    case VType::F32:
+      k_plan_values<float, float><<<grid, 256, 0, s>>>(rs, pl.R, S, pl.umap, pl.udiag, pl.uprev,
+                                                       (const float *)val, (float *)pl.uvs, (float *)pl.uaps,
+                                                       (float *)pl.urd);
+      break;
+    case VType::BF16:
+      k_plan_values<__nv_bfloat16, float><<<grid, 256, 0, s>>>(rs, pl.R, S, pl.umap, pl.udiag, pl.uprev,
+                                                               (const __nv_bfloat16 *)val, (float *)pl.uvs,
+                                                               (float *)pl.uaps, (float *)pl.urd);
+      break;
   }
 }
 
@@ -474,7 +464,7 @@ struct BlkArgs {
 template <typename CT, typename VT, int R>
 static void blk_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a) {
   dim3 g(grid, a.nrhs);
-  const size_t sm = (size_t)P.rec_off + (size_t)a.max_units * sizeof(int4);
+  const size_t sm = ((size_t)P.win + 1) * sizeof(CT);
   if (a.lower) {
     auto fn = k_sptrsv_blk<CT, VT, R, true>;
     if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -503,11 +493,14 @@ static BlkPlanDev plan_dev(const TriBlkPlan &pl, const void *val) {
   P.row = pl.row;
   P.col = pl.col;
   P.val = val;
-  P.unit = pl.unit;
   P.blk = pl.blk;
   P.urec = pl.urec;
+  P.ucode = pl.ucode;
+  P.uflag = pl.uflag;
+  P.uvs = pl.uvs;
+  P.uaps = pl.uaps;
+  P.urd = pl.urd;
   P.win = 0;
-  P.rec_off = 0;
   return P;
 }
 
@@ -519,7 +512,6 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
   const size_t rows = (size_t)pl.cpb * 32 * pl.R;
   const size_t esz = vt == VType::F64 ? 8 : 4;
   P.win = rows * esz <= (size_t)kSptrsvSmemMax ? (int)rows : 0;
-  P.rec_off = (int)(((size_t)(P.win + 1) * esz + 15) & ~(size_t)15);  // window + spare slot
   int grid = pl.grid;
   if (grid > pl.nblocks) grid = pl.nblocks;
   if (grid < 1) grid = 1;
