@@ -10,7 +10,8 @@
 //          map csr->csc (the CSR values are gathered after the sweeps)
 //   L^T    CSR of L's transpose (adjoint solves), with a position map
 //   per triangle: chunk kinds (u8), ready flags (i32), level lists (i32)
-//   Krylov V[ldv x (m+1)] f64 column-major (ldv = n rounded up to 32),
+//   Krylov V[ldv x (m+1)] f64 column-major (ldv = n rounded up to 32, plus
+//          32 so that columns are not a power of two bytes apart),
 //          Z[ldv x m] f32 (mixed precision) or f64, w/q/t vectors
 #include <algorithm>
 #include <chrono>
@@ -1073,11 +1074,13 @@ int lace_gpu_ctx::autotune_trsv() {
     plan_cpb = cd.cpb;
     plan_warps = cd.w;
     if ((rc = ensure_plan(0)) || (rc = ensure_plan(1))) return rc;
-    solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+    // the pair as the Arnoldi cycle runs it: q, intermediate and z all in
+    // the factor precision's vector type
+    solve_tri(0, vec_q.p, f32, vec_t.p, f32, false, vec_t2.p);
     solve_tri(1, vec_t.p, f32, vec_t2.p, f32, false, vec_r.p);
     cudaEventRecord(e0, stream);
     for (int r = 0; r < 2; ++r) {
-      solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+      solve_tri(0, vec_q.p, f32, vec_t.p, f32, false, vec_t2.p);
       solve_tri(1, vec_t.p, f32, vec_t2.p, f32, false, vec_r.p);
     }
     cudaEventRecord(e1, stream);
@@ -1162,11 +1165,14 @@ int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
   int rc = ensure_vectors();
   if (rc) return rc;
   const bool zf32 = vtype() != VType::F64;
-  ldv = ((size_t)n + 31) / 32 * 32;
-  if (m > ws_m || zf32 != ws_zf32) {
+  // columns a power of two bytes apart would put one row's entries of every
+  // column on the same memory channels
+  ldv = ((size_t)n + 31) / 32 * 32 + 32;
+  const size_t vbytes = 8 * ldv * (size_t)(m + 1), zbytes = (zf32 ? 4 : 8) * ldv * (size_t)m;
+  if (m > ws_m || zf32 != ws_zf32 || Vb.bytes < vbytes || Zb.bytes < zbytes) {
     drop_graphs();
-    rc |= Vb.ensure(8 * ldv * (size_t)(m + 1));
-    rc |= Zb.ensure((zf32 ? 4 : 8) * ldv * (size_t)m);
+    rc |= Vb.ensure(vbytes);
+    rc |= Zb.ensure(zbytes);
     if (rc) return DEV_ERR_DEVICE_ALLOC;
     ws_m = m;
     ws_zf32 = zf32;
@@ -1221,7 +1227,8 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
   a.ldz = ldv;
   a.z_f32 = ws_zf32 ? 1 : 0;
   a.w = (double *)vec_w.p;
-  a.q = (double *)vec_q.p;
+  a.q = vec_q.p;
+  a.q_f32 = vtype() != VType::F64 ? 1 : 0;
   a.partials = (double *)part_buf.p;
   a.grid = num_sms() * 8;
   a.cy = (Cycle *)cycle_buf.p;
@@ -1233,19 +1240,19 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
 // the search-direction loop of one cycle (LACE :311-759), all on the device
 int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) {
   const int t1 = adjoint ? 2 : 0, t2 = adjoint ? 3 : 1;
-  const int f32 = a.z_f32;
+  const int tf32 = vtype() != VType::F64;  // the intermediate vector of the two solves
   for (int j = 0; j < m; ++j) {
-    void *zj = (char *)a.Z + (size_t)j * a.ldz * (f32 ? 4 : 8);
-    int rc = solve_tri(t1, a.q, 0, vec_t.p, f32, true, vec_t2.p);
-    if (!rc) rc = solve_tri(t2, vec_t.p, f32, zj, f32, true, vec_t2.p);
+    void *zj = (char *)a.Z + (size_t)j * a.ldz * (a.z_f32 ? 4 : 8);
+    int rc = solve_tri(t1, a.q, a.q_f32, vec_t.p, tf32, true, vec_t2.p);
+    if (!rc) rc = solve_tri(t2, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p);
     if (rc) return rc;
     launch_passA(stream, a, j);
     launch_passB(stream, a, j);
     launch_passC(stream, a, j);
     if (opt.monitor_orthog && Qmon.p) {
       // q_{j+1} into the monitor basis, then ||I - Q^T Q|| over q_0..q_j
-      cudaMemcpyAsync((double *)Qmon.p + (size_t)(j + 1) * ldv, a.q, 8 * (size_t)n,
-                      cudaMemcpyDeviceToDevice, stream);
+      launch_convert(stream, n, a.q_f32 ? VType::F32 : VType::F64, a.q, VType::F64,
+                     (double *)Qmon.p + (size_t)(j + 1) * ldv);
       launch_orthog_monitor(stream, a, j, (double *)Qmon.p, ldv);
     }
   }
@@ -1291,7 +1298,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     launch_cycle_residual(stream, a, b, x);
     launch_cycle_init(stream, a);
     if (opt.monitor_orthog && Qmon.p)
-      cudaMemcpyAsync(Qmon.p, a.q, 8 * (size_t)n, cudaMemcpyDeviceToDevice, stream);
+      launch_convert(stream, n, a.q_f32 ? VType::F32 : VType::F64, a.q, VType::F64, Qmon.p);
     if (opt.use_graph) {
       auto it = graphs.find(key);
       if (it == graphs.end()) {

@@ -81,7 +81,8 @@ struct ArnoldiArgs {
   size_t ldz = 0;
   int z_f32 = 0;
   double *w = nullptr;   // work vector (A z, later the transformed column)
-  double *q = nullptr;   // next Krylov vector
+  void *q = nullptr;     // next Krylov vector (float when q_f32, else double)
+  int q_f32 = 0;
   double *partials = nullptr;  // grid-reduction scratch
   int grid = 0;          // blocks of the reducing kernels
   Cycle *cy = nullptr;

@@ -110,6 +110,29 @@ void launch_bcsr_spmv(cudaStream_t s, int nb, int bs, const int *row, const int 
 
 // --------------------------------------------------- row-tile machinery
 
+// FP32 -> FP64 exactly, with integer operations (conversions run on the FP64
+// unit, the scarce one on this part)
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  unsigned m = b & 0x7fffffu;
+  unsigned long long ef;
+  if (e == 0) {
+    if (m == 0) {
+      ef = 0;
+    } else {  // subnormal: normalise
+      const int sh = __clz((int)m) - 8;
+      m = (m << sh) & 0x7fffffu;
+      ef = (unsigned long long)(897 - sh) << 52;
+    }
+  } else {
+    ef = (unsigned long long)(e == 255 ? 2047u : e + 896u) << 52;
+  }
+  return __longlong_as_double(
+      (long long)(((unsigned long long)(b & 0x80000000u) << 32) | ef | ((unsigned long long)m << 29)));
+}
+
 // operator row i of the tile: CSR (LPR lanes per row) or BCSR (thread/row)
 struct OpView {
   int bs;
@@ -129,7 +152,7 @@ __device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, in
       double s = 0.0;
       if (i < n) {
         const int e = op.row[i + 1];
-        for (int p = op.row[i] + sub; p < e; p += LPR) s = fma(op.val[p], (double)z[op.col[p]], s);
+        for (int p = op.row[i] + sub; p < e; p += LPR) s = fma(op.val[p], to_f64(z[op.col[p]]), s);
       }
 #pragma unroll
       for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
@@ -145,7 +168,7 @@ __device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, in
         for (int p = op.row[I]; p < op.row[I + 1]; ++p) {
           const double *blk = op.val + (size_t)p * ld + r * bs;
           const ZT *zj = z + (size_t)op.col[p] * bs;
-          for (int c = 0; c < bs; ++c) s = fma(blk[c], (double)zj[c], s);
+          for (int c = 0; c < bs; ++c) s = fma(blk[c], to_f64(zj[c]), s);
         }
       }
       sw[t] = s;
@@ -156,9 +179,10 @@ __device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, in
 // acc[slot] += sum over tile rows (masked by lo) of V[k][i] * sw[t]  with
 // k = slot*8 + warp.  Lanes walk rows, warps walk columns: every V load is a
 // coalesced 256-byte row segment of one column.
+template <int NS>
 __device__ __forceinline__ void tile_dots(const double *__restrict__ V, size_t ldv, int ncols,
                                           int n, int base, int tr, int lo, const double *sw,
-                                          double (&acc)[kSlots]) {
+                                          double (&acc)[NS]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // the 8 rows of this lane, masked rows contribute 0 (their load address is
   // redirected to the tile's first row, which is always valid)
@@ -173,27 +197,27 @@ __device__ __forceinline__ void tile_dots(const double *__restrict__ V, size_t l
     iv[r] = ok ? i : base;
   }
 #pragma unroll
-  for (int sl = 0; sl < kSlots; ++sl) {
+  for (int sl = 0; sl < NS; ++sl) {
     if (sl * 8 >= ncols) break;  // uniform over the block
     const int k = sl * 8 + wid;
     if (k < ncols) {
+      // straight into the slot: FP64 additions cost as much as the products
       const double *Vk = V + (size_t)k * ldv;
-      double a0 = 0.0, a1 = 0.0;
+      double v[8];
 #pragma unroll
-      for (int r = 0; r < 8; r += 2) {
-        a0 = fma(Vk[iv[r]], wv[r], a0);
-        a1 = fma(Vk[iv[r + 1]], wv[r + 1], a1);
-      }
-      acc[sl] += a0 + a1;
+      for (int r = 0; r < 8; ++r) v[r] = Vk[iv[r]];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) acc[sl] = fma(v[r], wv[r], acc[sl]);
     }
   }
 }
 
 // block-reduce acc into sred[k] (k < ncols); plus optional extra scalar
-__device__ __forceinline__ void block_reduce_slots(double (&acc)[kSlots], int ncols, double *sred) {
+template <int NS>
+__device__ __forceinline__ void block_reduce_slots(double (&acc)[NS], int ncols, double *sred) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int sl = 0; sl < kSlots; ++sl) {
+  for (int sl = 0; sl < NS; ++sl) {
     const int k = sl * 8 + wid;
     if (sl * 8 < ncols) {  // warp-uniform
       double v = warp_sum(acc[sl]);
@@ -286,8 +310,9 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
 }
 
 // V[:,0] = (r + dd e_0)/alpha,  q = -r/dd
+template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
-                                                     double *__restrict__ V, double *__restrict__ q,
+                                                     double *__restrict__ V, QT *__restrict__ q,
                                                      const Cycle *cy, const Control *ctrl) {
   if (ctrl->done) return;
   const double dd = cy->dd0, ia = cy->inv_alpha0;
@@ -295,13 +320,85 @@ __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__rest
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double ri = r[i];
     V[i] = (i == 0 ? ri + dd : ri) * ia;
-    q[i] = -ri * rdd;
+    q[i] = (QT)(-ri * rdd);
   }
+}
+
+// sum_k V[k][i] c[k] over k < ncols: eight independent loads in flight
+__device__ __forceinline__ double vcomb8(const double *__restrict__ V, size_t ldv, int i, int ncols,
+                                         const double *c) {
+  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int k = 0;
+  for (; k + 8 <= ncols; k += 8) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = fma(V[(size_t)(k + u) * ldv + i], c[k + u], a[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+    if (k + u < ncols) a[u] = fma(V[(size_t)(k + u) * ldv + i], c[k + u], a[u]);
+  return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+}
+
+// FP64 -> FP32 with integer operations, rounding toward zero (the FP64 unit,
+// which also converts, is the scarce one).  Finite values only: below the
+// FP32 normal range they become 0, above it NaN.
+__device__ __forceinline__ float dtof_rz(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  const unsigned m = ((hi & 0xfffffu) << 3) | ((unsigned)b >> 29);
+  const unsigned mag = e <= 0 ? 0u : (e >= 255 ? 0x7fc00000u : (((unsigned)e << 23) | m));
+  return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
+// rows i, i+1 (i even): sum_k V[k][i..i+1] c[k] in FP32 (V converted with
+// dtof_rz), for vectors that only feed the FP32 preconditioner
+__device__ __forceinline__ float2 vcomb8x2f(const double *__restrict__ V, size_t ldv, int i, int ncols,
+                                           const float *c) {
+  float2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (int k = 0; k < ncols; k += 8) {
+    double2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) v[u] = __ldg(reinterpret_cast<const double2 *>(V + (size_t)(k + u) * ldv + i));
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) {
+        a[u & 3].x = fmaf(dtof_rz(v[u].x), c[k + u], a[u & 3].x);
+        a[u & 3].y = fmaf(dtof_rz(v[u].y), c[k + u], a[u & 3].y);
+      }
+  }
+  return make_float2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
+}
+
+// rows i, i+1 (i even, i+1 < n): sum_k V[k][i..i+1] c[k] over k < ncols with
+// 16-byte loads, a batch of eight columns in flight before any use
+__device__ __forceinline__ double2 vcomb8x2(const double *__restrict__ V, size_t ldv, int i, int ncols,
+                                           const double *c) {
+  // two accumulators per row: the FP64 unit is the scarce one, so few
+  // closing additions matter more than a short dependency chain
+  double2 a[2] = {{0.0, 0.0}, {0.0, 0.0}};
+  for (int k = 0; k < ncols; k += 8) {
+    // a partial batch skips its missing columns
+    double2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) v[u] = __ldg(reinterpret_cast<const double2 *>(V + (size_t)(k + u) * ldv + i));
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) {
+        a[u & 1].x = fma(v[u].x, c[k + u], a[u & 1].x);
+        a[u & 1].y = fma(v[u].y, c[k + u], a[u & 1].y);
+      }
+  }
+  return make_double2(a[0].x + a[1].x, a[0].y + a[1].y);
 }
 
 // ------------------------------------------------------------- pass A
 
-template <int LPR, typename ZT>
+// NS: dot-product slots per warp (8 NS >= j + 1), so that short bases keep
+// few accumulators in registers
+template <int LPR, typename ZT, int NS>
 __global__ void __launch_bounds__(kTPB) k_passA(int n, OpView op, const ZT *__restrict__ z,
                                                 double *__restrict__ w, const double *__restrict__ V,
                                                 size_t ldv, int jp1, double *partials, Cycle *cy,
@@ -310,18 +407,18 @@ __global__ void __launch_bounds__(kTPB) k_passA(int n, OpView op, const ZT *__re
   __shared__ double sw[kTPB];
   __shared__ double sred[kLdT];
   const int tr = (op.bs == 0) ? kTPB : (kTPB / op.bs) * op.bs;
-  double acc[kSlots];
+  double acc[NS];
 #pragma unroll
-  for (int sl = 0; sl < kSlots; ++sl) acc[sl] = 0.0;
+  for (int sl = 0; sl < NS; ++sl) acc[sl] = 0.0;
   for (int base = blockIdx.x * tr; base < n; base += gridDim.x * tr) {
     tile_apply<LPR, ZT>(op, n, base, tr, z, sw);
     __syncthreads();
     for (int t = threadIdx.x; t < tr; t += kTPB)
       if (base + t < n) w[base + t] = sw[t];
-    tile_dots(V, ldv, jp1, n, base, tr, 0, sw, acc);
+    tile_dots<NS>(V, ldv, jp1, n, base, tr, 0, sw, acc);
     __syncthreads();
   }
-  block_reduce_slots(acc, jp1, sred);
+  block_reduce_slots<NS>(acc, jp1, sred);
   __syncthreads();
   for (int k = threadIdx.x; k < jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
   if (!arrive_last(&ctrl->block_count[1])) return;
@@ -353,43 +450,47 @@ __device__ void givens_rot(double a, double b, double tol, double *c, double *s)
   }
 }
 
+template <int NS>
 __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict__ V, size_t ldv,
                                                 int j, int m, double *__restrict__ w,
                                                 double *partials, Cycle *cy, Control *ctrl) {
   if (ctrl->done) return;
-  __shared__ double sw[kTPB];
+  __shared__ double sw[2 * kTPB];
   __shared__ double sy[kLdT];
   __shared__ double sred[kLdT + 1];
   __shared__ double scratch[kTPB / 32];
   const int jp1 = j + 1;
   for (int k = threadIdx.x; k < jp1; k += kTPB) sy[k] = cy->y[k];
   __syncthreads();
-  double acc[kSlots];
+  double acc[NS];
 #pragma unroll
-  for (int sl = 0; sl < kSlots; ++sl) acc[sl] = 0.0;
+  for (int sl = 0; sl < NS; ++sl) acc[sl] = 0.0;
   double nrm = 0.0;
-  for (int base = blockIdx.x * kTPB; base < n; base += gridDim.x * kTPB) {
-    const int i = base + threadIdx.x;
-    if (i < n) {
-      double s0 = w[i], s1 = 0.0, s2 = 0.0, s3 = 0.0;
-      int k = 0;
-      for (; k + 4 <= jp1; k += 4) {
-        s0 = fma(-V[(size_t)k * ldv + i], sy[k], s0);
-        s1 = fma(-V[(size_t)(k + 1) * ldv + i], sy[k + 1], s1);
-        s2 = fma(-V[(size_t)(k + 2) * ldv + i], sy[k + 2], s2);
-        s3 = fma(-V[(size_t)(k + 3) * ldv + i], sy[k + 3], s3);
-      }
-      for (; k < jp1; ++k) s0 = fma(-V[(size_t)k * ldv + i], sy[k], s0);
-      const double s = (s0 + s1) + (s2 + s3);
-      w[i] = s;
-      sw[threadIdx.x] = s;
-      if (i > j) nrm = fma(s, s, nrm);
+  // w -= V y over tiles of 2*kTPB rows (a row pair per thread, 16-byte
+  // loads), then the tile's dot products with V for rows > j
+  for (int base = blockIdx.x * 2 * kTPB; base < n; base += gridDim.x * 2 * kTPB) {
+    const int i = base + 2 * threadIdx.x;
+    if (i + 1 < n) {
+      const double2 wv = *reinterpret_cast<const double2 *>(w + i);
+      const double2 c = vcomb8x2(V, ldv, i, jp1, sy);
+      const double s0 = wv.x - c.x, s1 = wv.y - c.y;
+      *reinterpret_cast<double2 *>(w + i) = make_double2(s0, s1);
+      sw[2 * threadIdx.x] = s0;
+      sw[2 * threadIdx.x + 1] = s1;
+      if (i > j) nrm = fma(s0, s0, nrm);
+      if (i + 1 > j) nrm = fma(s1, s1, nrm);
+    } else if (i < n) {
+      const double s0 = w[i] - vcomb8(V, ldv, i, jp1, sy);
+      w[i] = s0;
+      sw[2 * threadIdx.x] = s0;
+      if (i > j) nrm = fma(s0, s0, nrm);
     }
     __syncthreads();
-    tile_dots(V, ldv, jp1, n, base, kTPB, jp1, sw, acc);
+    tile_dots<NS>(V, ldv, jp1, n, base, kTPB, jp1, sw, acc);
+    tile_dots<NS>(V, ldv, jp1, n, base + kTPB, kTPB, jp1, sw + kTPB, acc);
     __syncthreads();
   }
-  block_reduce_slots(acc, jp1, sred);
+  block_reduce_slots<NS>(acc, jp1, sred);
   double tot = block_sum(nrm, scratch);
   if (threadIdx.x == 0) sred[jp1] = tot;
   __syncthreads();
@@ -485,28 +586,48 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
 
 // ------------------------------------------------------------- pass C
 
+// v_{j+1} (FP64) and q = e_{j+1} - V_{j+1} c, two rows per thread.  With an
+// FP32 q (mixed precision: q only feeds the FP32 preconditioner, which
+// rounds it to FP32 on its first read) the combination runs in FP32.
+template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, size_t ldv, int j,
-                                                const double *__restrict__ w, double *__restrict__ q,
+                                                const double *__restrict__ w, QT *__restrict__ q,
                                                 const Cycle *cy, const Control *ctrl) {
   if (ctrl->done) return;
+  constexpr bool kF32 = sizeof(QT) == 4;
   __shared__ double sc[kLdT];
+  __shared__ float scf[kLdT];
   const int jp1 = j + 1;
-  for (int k = threadIdx.x; k <= jp1; k += kTPB) sc[k] = cy->c[k];
+  for (int k = threadIdx.x; k <= jp1; k += kTPB) {
+    sc[k] = cy->c[k];
+    scf[k] = (float)sc[k];
+  }
   __syncthreads();
   const double dd = cy->dd, ia = cy->inv_alpha;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
-    V[(size_t)jp1 * ldv + i] = v;
-    double a0 = (i == jp1 ? 1.0 : 0.0) - v * sc[jp1], a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    int k = 0;
-    for (; k + 4 <= jp1; k += 4) {
-      a0 = fma(-V[(size_t)k * ldv + i], sc[k], a0);
-      a1 = fma(-V[(size_t)(k + 1) * ldv + i], sc[k + 1], a1);
-      a2 = fma(-V[(size_t)(k + 2) * ldv + i], sc[k + 2], a2);
-      a3 = fma(-V[(size_t)(k + 3) * ldv + i], sc[k + 3], a3);
+  double *vn = V + (size_t)jp1 * ldv;
+  const int npair = n / 2;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += gridDim.x * blockDim.x) {
+    const int i = 2 * p;
+    const double2 wv = *reinterpret_cast<const double2 *>(w + i);
+    const double v0 = (i > j) ? (i == jp1 ? wv.x + dd : wv.x) * ia : 0.0;
+    const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? wv.y + dd : wv.y) * ia : 0.0;
+    *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
+    if constexpr (kF32) {
+      const float2 s = vcomb8x2f(V, ldv, i, jp1, scf);
+      *reinterpret_cast<float2 *>(q + i) =
+          make_float2(((i == jp1 ? 1.f : 0.f) - dtof_rz(v0) * scf[jp1]) - s.x,
+                      ((i + 1 == jp1 ? 1.f : 0.f) - dtof_rz(v1) * scf[jp1]) - s.y);
+    } else {
+      const double2 s = vcomb8x2(V, ldv, i, jp1, sc);
+      *reinterpret_cast<double2 *>(q + i) = make_double2(((i == jp1 ? 1.0 : 0.0) - v0 * sc[jp1]) - s.x,
+                                                         ((i + 1 == jp1 ? 1.0 : 0.0) - v1 * sc[jp1]) - s.y);
     }
-    for (; k < jp1; ++k) a0 = fma(-V[(size_t)k * ldv + i], sc[k], a0);
-    q[i] = (a0 + a1) + (a2 + a3);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // the last row of an odd n
+    const int i = n - 1;
+    const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
+    vn[i] = v;
+    q[i] = (QT)(((i == jp1 ? 1.0 : 0.0) - v * sc[jp1]) - vcomb8(V, ldv, i, jp1, sc));
   }
 }
 
@@ -582,12 +703,12 @@ __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ 
     double s0 = x[i], s1 = 0.0, s2 = 0.0, s3 = 0.0;  // LACE :735-744
     int k = 0;
     for (; k + 4 <= ns; k += 4) {
-      s0 = fma((double)Z[(size_t)k * ldz + i], sy[k], s0);
-      s1 = fma((double)Z[(size_t)(k + 1) * ldz + i], sy[k + 1], s1);
-      s2 = fma((double)Z[(size_t)(k + 2) * ldz + i], sy[k + 2], s2);
-      s3 = fma((double)Z[(size_t)(k + 3) * ldz + i], sy[k + 3], s3);
+      s0 = fma(to_f64(Z[(size_t)k * ldz + i]), sy[k], s0);
+      s1 = fma(to_f64(Z[(size_t)(k + 1) * ldz + i]), sy[k + 1], s1);
+      s2 = fma(to_f64(Z[(size_t)(k + 2) * ldz + i]), sy[k + 2], s2);
+      s3 = fma(to_f64(Z[(size_t)(k + 3) * ldz + i]), sy[k + 3], s3);
     }
-    for (; k < ns; ++k) s0 = fma((double)Z[(size_t)k * ldz + i], sy[k], s0);
+    for (; k < ns; ++k) s0 = fma(to_f64(Z[(size_t)k * ldz + i]), sy[k], s0);
     x[i] = (s0 + s1) + (s2 + s3);
   }
 }
@@ -613,19 +734,37 @@ void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b
 }
 
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
-  k_cycle_init<<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.q, a.cy, a.ctrl);
+  if (a.q_f32)
+    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (float *)a.q, a.cy, a.ctrl);
+  else
+    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (double *)a.q, a.cy, a.ctrl);
+}
+
+// dot-product slots per warp for j+1 basis columns
+static int slots_for(int jp1) {
+  const int need = (jp1 + 7) / 8;
+  return need <= 2 ? 2 : (need <= 4 ? 4 : (need <= 8 ? 8 : kSlots));
+}
+
+template <typename ZT, int NS>
+static void passA_ns(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  OpView op = opview(a);
+  const ZT *z = (const ZT *)a.Z + (size_t)j * a.ldz;
+  switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
+    case 1: k_passA<1, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    case 16: k_passA<16, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    case 32: k_passA<32, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    default: k_passA<8, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+  }
 }
 
 template <typename ZT>
 static void passA_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
-  OpView op = opview(a);
-  const ZT *z = (const ZT *)a.Z + (size_t)j * a.ldz;
-  switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
-    case 1: k_passA<1, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
-    case 4: k_passA<4, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
-    case 16: k_passA<16, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
-    case 32: k_passA<32, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
-    default: k_passA<8, ZT><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+  switch (slots_for(j + 1)) {
+    case 2: passA_ns<ZT, 2>(s, a, j); break;
+    case 4: passA_ns<ZT, 4>(s, a, j); break;
+    case 8: passA_ns<ZT, 8>(s, a, j); break;
+    default: passA_ns<ZT, kSlots>(s, a, j); break;
   }
 }
 
@@ -635,11 +774,19 @@ void launch_passA(cudaStream_t s, const ArnoldiArgs &a, int j) {
 }
 
 void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j) {
-  k_passB<<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl);
+  switch (slots_for(j + 1)) {
+    case 2: k_passB<2><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
+    case 4: k_passB<4><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
+    case 8: k_passB<8><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
+    default: k_passB<kSlots><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
+  }
 }
 
 void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
-  k_passC<<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, a.q, a.cy, a.ctrl);
+  if (a.q_f32)
+    k_passC<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl);
+  else
+    k_passC<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (double *)a.q, a.cy, a.ctrl);
 }
 
 void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x) {
