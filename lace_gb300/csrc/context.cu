@@ -673,9 +673,11 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
                     memcmp(c->hAcol.data(), col, 4 * (size_t)nnz) == 0;
   int rc = same ? 0 : validate_csr(n, nnz, row, col);
   if (rc) return set_err(rc);
+  ++c->aval_version;
   if (same) {
     if (c->Aval.upload(val, 8 * (size_t)nnz, c->stream)) return set_err(DEV_ERR_DEVICE_ALLOC);
   } else {
+    c->sell_valid = false;
     if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) ||
         c->Acol.upload(col, 4 * (size_t)nnz, c->stream) || c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
       return set_err(DEV_ERR_DEVICE_ALLOC);
@@ -713,6 +715,8 @@ extern "C" int lace_gpu_upload_bcsr_host(lace_gpu_ctx *c, int nb, int bs, int nb
   int rc = validate_csr(nb, nblk, row, col);
   if (rc) return set_err(rc);
   const size_t ld = (size_t)bs * bs;
+  ++c->aval_version;
+  c->sell_valid = false;
   if (c->Arow.upload(row, 4 * (size_t)(nb + 1), c->stream) || c->Acol.upload(col, 4 * (size_t)nblk, c->stream) ||
       c->Aval.upload(val, 8 * (size_t)nblk * ld, c->stream))
     return set_err(DEV_ERR_DEVICE_ALLOC);
@@ -733,6 +737,7 @@ extern "C" int lace_gpu_update_values_device(lace_gpu_ctx *c, const double *val)
   if (!c || !val) return set_err(DEV_ERR_INVALID_PTR);
   const size_t ld = c->bs ? (size_t)c->bs * c->bs : 1;
   LCHK(cudaMemcpyAsync(c->Aval.p, val, 8 * (size_t)c->nnzA * ld, cudaMemcpyDeviceToDevice, c->stream));
+  ++c->aval_version;
   // ||A||_F on the device
   double *partials = (double *)c->part_ensure();
   if (!partials) return set_err(DEV_ERR_DEVICE_ALLOC);
@@ -1185,6 +1190,51 @@ int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
   return 0;
 }
 
+// A in sliced ELL (slices of 32 rows; within a slice, entry t of all rows
+// together), built from the host copy of the pattern; values gathered from
+// the resident CSR values whenever they change
+int lace_gpu_ctx::ensure_sell() {
+  if (bs || (int)hArow.size() != n + 1) return 0;  // CSR uploads only
+  if (!sell_valid) {
+    const int nsl = (n + 31) / 32;
+    std::vector<int> ptr(nsl + 1, 0);
+    for (int s = 0; s < nsl; ++s) {
+      int w = 0;
+      for (int i = 32 * s; i < std::min(n, 32 * s + 32); ++i) w = std::max(w, hArow[i + 1] - hArow[i]);
+      ptr[s + 1] = ptr[s] + 32 * w;
+    }
+    std::vector<int> col(std::max(1, ptr[nsl])), map(std::max(1, ptr[nsl]), -1);
+    for (int s = 0; s < nsl; ++s)
+      for (int l = 0; l < 32; ++l) {
+        const int i = 32 * s + l;
+        const int w = (ptr[s + 1] - ptr[s]) / 32;
+        for (int t = 0; t < w; ++t) {
+          const int q = ptr[s] + 32 * t + l;
+          const bool in = i < n && t < hArow[i + 1] - hArow[i];
+          col[q] = in ? hAcol[hArow[i] + t] : 0;
+          map[q] = in ? hArow[i] + t : -1;
+        }
+      }
+    int rc = 0;
+    rc |= sell_ptr.upload(ptr.data(), 4 * ptr.size(), stream);
+    rc |= sell_col.upload(col.data(), 4 * col.size(), stream);
+    rc |= sell_map.upload(map.data(), 4 * map.size(), stream);
+    rc |= sell_val.ensure(8 * col.size());
+    if (rc) return DEV_ERR_DEVICE_ALLOC;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+    sell_slots = (size_t)ptr[nsl];
+    sell_valid = true;
+    sell_version = -1;
+    drop_graphs();
+  }
+  if (sell_version != aval_version) {
+    launch_sell_values(stream, sell_slots, (const int *)sell_map.p, (const double *)Aval.p,
+                       (double *)sell_val.p);
+    sell_version = aval_version;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
 int lace_gpu_ctx::ensure_AT() {
   if (AT_ready) return 0;
   if (bs) return DEV_ERR_NOT_SUPPORTED;
@@ -1219,6 +1269,11 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
     a.row = (const int *)Arow.p;
     a.col = (const int *)Acol.p;
     a.val = (const double *)Aval.p;
+    if (sell_valid && !bs) {
+      a.sell_ptr = (const int *)sell_ptr.p;
+      a.sell_col = (const int *)sell_col.p;
+      a.sell_val = (const double *)sell_val.p;
+    }
   }
   a.lanes = lanes;
   a.V = (double *)Vb.p;
@@ -1267,6 +1322,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   int rc = ensure_krylov(m, opt.monitor_orthog != 0);
   if (!rc) rc = autotune_trsv();
   if (!rc && adjoint) rc = ensure_AT();
+  if (!rc && !adjoint) rc = ensure_sell();
   // solve plans are built on the host: before any graph capture
   if (!rc && !bs && opt.trsv_mode == LACE_TRSV_SYNCFREE) {
     rc = ensure_plan(adjoint ? 2 : 0);

@@ -66,6 +66,14 @@ struct lace_gpu_ctx {
   double anorm = 0.0;
   DBuf Arow, Acol, Aval;
   std::vector<int> hArow, hAcol;  // host copy of the resident CSR pattern
+  int aval_version = 0;  // bumped whenever A's values change
+  // A in sliced ELL for the Arnoldi operator (CSR only): slice offsets, columns,
+  // source CSR entry of each slot (-1: padding) and the gathered values
+  DBuf sell_ptr, sell_col, sell_map, sell_val;
+  size_t sell_slots = 0;
+  bool sell_valid = false;
+  int sell_version = -1;
+  int ensure_sell();
   // A^T for the adjoint
   bool AT_ready = false;
   DBuf ATrow, ATcol, ATval, map_at2a;

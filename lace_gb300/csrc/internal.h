@@ -75,6 +75,11 @@ struct ArnoldiArgs {
   const int *row = nullptr, *col = nullptr;
   const double *val = nullptr;
   int lanes = 8;
+  // the same operator in sliced ELL (slices of 32 rows, entry t of the
+  // slice's rows stored together: index sell_ptr[s] + 32 t + lane); null when
+  // absent
+  const int *sell_ptr = nullptr, *sell_col = nullptr;
+  const double *sell_val = nullptr;
   double *V = nullptr;   // reflectors, n x (m+1) column-major
   size_t ldv = 0;
   void *Z = nullptr;     // preconditioned vectors, n x m (float or double)
@@ -120,6 +125,8 @@ void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *
 // a.Ucp/a.Uri + Uc: U in CSC (same values)
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
                    const void *L, const void *Ur, const void *Uc, double *out2);
+// the sliced-ELL values of the operator: dst[q] = map[q] >= 0 ? src[map[q]] : 0
+void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst);
 // gather: dst[p] = src[perm[p]] with type conversion
 void launch_gather(cudaStream_t s, int count, const int *perm, VType ts, const void *src, VType td,
                    void *dst);

@@ -16,6 +16,8 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
+
 #include "internal.h"
 
 namespace lace {
@@ -138,12 +140,41 @@ struct OpView {
   int bs;
   const int *row, *col;
   const double *val;
+  const int *sell_ptr, *sell_col;  // sliced ELL (CSR row pointers give the row lengths)
+  const double *sell_val;
 };
 
 template <int LPR, typename ZT>
 __device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, int tr,
                                            const ZT *__restrict__ z, double *sw) {
-  if (op.bs == 0) {
+  if (op.bs == 0 && op.sell_ptr != nullptr) {
+    // sliced ELL: warp w takes the 32-row slices w, w+8, ... of the tile; entry
+    // t of the slice's rows is one coalesced load, four entries in flight
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int t0 = wid * 32; t0 < tr; t0 += kTPB) {
+      const int i = base + t0 + lane;
+      double s = 0.0;
+      if (i < n) {
+        const int len = op.row[i + 1] - op.row[i];
+        const int *cp = op.sell_col + op.sell_ptr[(base + t0) >> 5] + lane;
+        const double *vp = op.sell_val + (cp - op.sell_col);
+        for (int t = 0; t < len; t += 4) {
+          int c[4];
+          double v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (t + u < len) {
+              c[u] = cp[32 * (t + u)];
+              v[u] = vp[32 * (t + u)];
+            }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (t + u < len) s = fma(v[u], to_f64(z[c[u]]), s);
+        }
+      }
+      sw[t0 + lane] = s;
+    }
+  } else if (op.bs == 0) {
     const int sub = threadIdx.x & (LPR - 1);
     const int grp = threadIdx.x / LPR;
     constexpr int G = kTPB / LPR;
@@ -715,7 +746,23 @@ __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ 
 
 // ------------------------------------------------------------ launchers
 
-static OpView opview(const ArnoldiArgs &a) { return OpView{a.bs, a.row, a.col, a.val}; }
+static OpView opview(const ArnoldiArgs &a) {
+  return OpView{a.bs, a.row, a.col, a.val, a.sell_ptr, a.sell_col, a.sell_val};
+}
+
+__global__ void k_sell_values(size_t count, const int *__restrict__ map, const double *__restrict__ src,
+                              double *__restrict__ dst) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (size_t)gridDim.x * blockDim.x) {
+    const int e = map[q];
+    dst[q] = e >= 0 ? src[e] : 0.0;
+  }
+}
+
+void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst) {
+  if (count == 0) return;
+  const int grid = (int)std::min<size_t>((size_t)num_sms() * 8, (count + 255) / 256);
+  k_sell_values<<<grid, 256, 0, s>>>(count, map, src, dst);
+}
 
 static int rowgrid(int n) {
   int g = (n + kTPB - 1) / kTPB;
