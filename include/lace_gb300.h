@@ -300,6 +300,14 @@ int lace_gpu_spmv(lace_gpu_ctx *ctx, double alpha, const double *x,
 /* z = M^{-1} q with the current factors and options (device FP64) */
 int lace_gpu_apply_precond(lace_gpu_ctx *ctx, const double *q, double *z);
 
+/* z = M^{-1} q as one step of the FGMRES cycle applies it, enqueued on the
+ * context's stream without waiting: q and z are device vectors in the
+ * vector type of the factor precision (float for FP32/BF16 factors, double
+ * for FP64).  For timing the preconditioner kernels; the preconditioner must
+ * have been applied once (lace_gpu_apply_precond) since the factors changed,
+ * and a spin-wait timeout shows in the next lace_gpu_apply_precond or solve. */
+int lace_gpu_precond_enqueue(lace_gpu_ctx *ctx, const void *q, void *z);
+
 /* one triangle: which 0 = L (unit lower), 1 = U (upper), 2 = U^T (lower),
  * 3 = L^T (unit upper); device FP64 in/out (converted internally) */
 int lace_gpu_sptrsv(lace_gpu_ctx *ctx, int which, const double *b, double *x);

@@ -127,6 +127,12 @@ class Context:
     def apply_precond(self, q, z) -> None:
         _chk(self._lib.lace_gpu_apply_precond(self.h, _ptr(q), _ptr(z)), "apply_precond")
 
+    def precond_enqueue(self, q, z) -> None:
+        """z = M^{-1} q as the FGMRES cycle applies it (q, z in the factor
+        precision's vector type: float32 unless precision is fp64), enqueued
+        on the context's stream without waiting - for timing."""
+        _chk(self._lib.lace_gpu_precond_enqueue(self.h, _ptr(q), _ptr(z)), "precond_enqueue")
+
     def fgmres(self, b, x, search_max: int = 30, restart_max: int = 20, rtol: float = 1e-10,
                tol_type: int = 1) -> GmresResult:
         par = GmresParam()

@@ -1138,6 +1138,16 @@ extern "C" int lace_gpu_sptrsv(lace_gpu_ctx *c, int which, const double *b, doub
   return DEV_SUCCESS;
 }
 
+extern "C" int lace_gpu_precond_enqueue(lace_gpu_ctx *c, const void *q, void *z) {
+  if (!c || !q || !z) return set_err(DEV_ERR_INVALID_PTR);
+  if (!c->factors_ready || !c->trsv_tuned) return set_err(DEV_ERR_NOT_INITIALIZED);
+  cudaSetDevice(c->device);
+  const int f32 = c->vtype() != VType::F64;
+  int rc = c->solve_tri(0, q, f32, c->vec_t.p, f32, false, c->vec_t2.p);
+  if (!rc) rc = c->solve_tri(1, c->vec_t.p, f32, z, f32, false, c->vec_t2.p);
+  return rc ? set_err(rc) : DEV_SUCCESS;
+}
+
 extern "C" int lace_gpu_apply_precond(lace_gpu_ctx *c, const double *q, double *z) {
   if (!c || !q || !z) return set_err(DEV_ERR_INVALID_PTR);
   if (!c->factors_ready) return set_err(DEV_ERR_NOT_INITIALIZED);
