@@ -308,6 +308,30 @@ int lace_gpu_apply_precond(lace_gpu_ctx *ctx, const double *q, double *z);
  * and a spin-wait timeout shows in the next lace_gpu_apply_precond or solve. */
 int lace_gpu_precond_enqueue(lace_gpu_ctx *ctx, const void *q, void *z);
 
+/* Largest num_rows lace_gpu_parcsrtrsv_noalloc accepts. */
+#define LACE_GPU_NOALLOC_MAX_ROWS 262144
+
+/* data_parcsrtrsv on DEVICE arrays, allocating no memory.  No counterpart in
+ * the reference: it is for callers that cannot allocate device memory - code
+ * whose device memory belongs to its own pool or arena, which forbids further
+ * allocations, and code in a latency-critical loop, where cudaMalloc/cudaFree
+ * would synchronise the whole device.  Same arguments, rule for uplo /
+ * storage / diag, sweeps and result as data_parcsrtrsv, but Aval, row, col,
+ * rhsval and yval (start vector in, solution out) are device pointers, and
+ * the sweeps run on `stream` (NULL: the default stream); the call returns
+ * when the solve is done.  Its scratch is one fixed device array (about
+ * 2 MB, held by every GPU that loads the library): num_rows above
+ * LACE_GPU_NOALLOC_MAX_ROWS returns DEV_ERR_NOT_SUPPORTED.  The first call on
+ * a device sets the scratch up (looks up its address and clears its counter)
+ * and should come before any stream capture.  Every call uses the same
+ * scratch: calls that overlap on the GPU (from several threads or streams)
+ * race and give wrong results. */
+int lace_gpu_parcsrtrsv_noalloc(const data_uplo_t uplo, const data_storage_t storage,
+                                const data_diagorder_t diag, const int num_rows,
+                                const dataType *Aval, const int *row, const int *col,
+                                const dataType *rhsval, dataType *yval, const dataType tol,
+                                int *iter, void *stream);
+
 /* one triangle: which 0 = L (unit lower), 1 = U (upper), 2 = U^T (lower),
  * 3 = L^T (unit upper); device FP64 in/out (converted internally) */
 int lace_gpu_sptrsv(lace_gpu_ctx *ctx, int which, const double *b, double *x);
