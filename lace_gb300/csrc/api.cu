@@ -46,6 +46,22 @@ int default_ctx(lace_gpu_ctx **out) {
   return 0;
 }
 
+// wall time of the phases of a drop-in call, printed when the context is verbose
+struct PhaseClock {
+  bool on;
+  const char *what;
+  std::chrono::steady_clock::time_point t0, t;
+  PhaseClock(bool on_, const char *what_) : on(on_), what(what_) { t0 = t = std::chrono::steady_clock::now(); }
+  void mark(const char *phase) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    printf("%% %s %-28s %8.2f ms (%8.2f ms)\n", what, phase,
+           std::chrono::duration<double, std::milli>(now - t).count(),
+           std::chrono::duration<double, std::milli>(now - t0).count());
+    t = now;
+  }
+};
+
 template <typename T>
 T *lace_alloc(size_t count) {
   // LACE_CALLOC (include/dense_types.h:430-449): posix_memalign(64), zeroed
@@ -54,6 +70,18 @@ T *lace_alloc(size_t count) {
   size_t padded = (bytes / 64 + 1) * 64;
   if (posix_memalign(&p, 64, padded) != 0) return nullptr;
   memset(p, 0, padded);
+  return (T *)p;
+}
+
+// the same allocation for `count` elements the caller writes at once: only
+// the padding past them is zeroed here
+template <typename T>
+T *lace_alloc_filled(size_t count) {
+  void *p = nullptr;
+  size_t bytes = count * sizeof(T);
+  size_t padded = (bytes / 64 + 1) * 64;
+  if (posix_memalign(&p, 64, padded) != 0) return nullptr;
+  memset((char *)p + bytes, 0, padded - bytes);
   return (T *)p;
 }
 
@@ -80,31 +108,36 @@ bool is_csr(data_storage_t s) {
   return s == Magma_CSR || s == Magma_CUCSR || s == Magma_CSRL || s == Magma_CSRU;
 }
 
-int fill_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
-                 const std::vector<int> &idx, const std::vector<double> &val, int blocksize) {
+// an output container from the factor pattern and FP64 values on the device
+// (copied straight into the container's array; the stream is synchronised
+// before returning)
+int fill_csr_out_dev(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
+                     const std::vector<int> &idx, const void *dval, int blocksize, cudaStream_t s) {
   release_members(B);
   const int ld = blocksize > 0 ? blocksize * blocksize : 1;
+  const size_t nval = idx.size() * ld;
   B->storage_type = st;
   B->major = MagmaRowMajor;
   B->fill_mode = fill;
   B->num_rows = n;
   B->num_cols = n;
-  B->row = lace_alloc<int>(n + 1);
-  B->col = lace_alloc<int>(idx.size() + 1);
-  B->val = lace_alloc<double>(idx.size() * ld + 1);
+  B->row = lace_alloc_filled<int>(ptr.size());
+  B->col = lace_alloc_filled<int>(idx.size());
+  B->val = lace_alloc_filled<double>(nval);
   if (!B->row || !B->col || !B->val) return DEV_ERR_HOST_ALLOC;
+  if (cudaMemcpyAsync(B->val, dval, 8 * nval, cudaMemcpyDeviceToHost, s) != cudaSuccess) return DEV_ERR_UNKNOWN;
   memcpy(B->row, ptr.data(), 4 * ptr.size());
   memcpy(B->col, idx.data(), 4 * idx.size());
-  memcpy(B->val, val.data(), 8 * val.size());
   if (blocksize > 0) {
     B->blocksize = blocksize;
     B->ldblock = ld;
     B->numblocks = (int)idx.size();
-    B->nnz = (int)idx.size() * ld;
+    B->nnz = (int)nval;
   } else {
     B->nnz = (int)idx.size();
   }
   B->true_nnz = B->nnz;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return DEV_ERR_UNKNOWN;
   return 0;
 }
 
@@ -124,6 +157,7 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   if (rc) return fail(rc);
   lace_gpu_options o = dropin_opts();
   lace_gpu_set_options(c, &o);
+  PhaseClock pc(c->verbose, "parilu");
   const bool bcsr = A->storage_type == Magma_BCSR;
   const int n = A->num_rows;
   if (bcsr) {
@@ -136,6 +170,7 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
     rc = DEV_ERR_NOT_SUPPORTED;
   }
   if (rc) return fail(rc);
+  pc.mark("upload A");
   // residuals of the A-initial guess (src/parilu_v0_3.cpp:30-34), on the GPU
   double ares = 0.0, nonlin0 = NAN;
   if (!bcsr) {
@@ -170,32 +205,32 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol, min_sweeps);
   const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rc) return fail(rc);
-  // download: L values (CSRL order), U values (CSCU order), FP64
+  pc.mark("residuals + sweeps");
+  // L values (CSRL order) and U values (CSCU order) as FP64, copied straight
+  // into the output containers
   const int ld = bcsr ? A->blocksize * A->blocksize : 1;
-  std::vector<double> lv((size_t)c->nnzL * ld), uv((size_t)c->nnzU * ld);
+  const size_t nl = (size_t)c->nnzL * ld, nu = (size_t)c->nnzU * ld;
+  DBuf tl, tu;
+  const void *dl = c->Lv[c->cur].p, *du = c->Ucv[c->cur].p;
   if (c->vtype() != VType::F64) {
     // FP32 / BF16 factors travel back as LACE's FP64 values
-    DBuf tl, tu;
-    if (tl.ensure(8 * lv.size()) || tu.ensure(8 * uv.size())) return fail(DEV_ERR_DEVICE_ALLOC);
-    launch_convert(c->stream, (int)lv.size(), c->vtype(), c->Lv[c->cur].p, VType::F64, tl.p);
-    launch_convert(c->stream, (int)uv.size(), c->vtype(), c->Ucv[c->cur].p, VType::F64, tu.p);
-    cudaMemcpyAsync(lv.data(), tl.p, 8 * lv.size(), cudaMemcpyDeviceToHost, c->stream);
-    cudaMemcpyAsync(uv.data(), tu.p, 8 * uv.size(), cudaMemcpyDeviceToHost, c->stream);
-    cudaStreamSynchronize(c->stream);
-  } else {
-    cudaMemcpy(lv.data(), c->Lv[c->cur].p, 8 * lv.size(), cudaMemcpyDeviceToHost);
-    cudaMemcpy(uv.data(), c->Ucv[c->cur].p, 8 * uv.size(), cudaMemcpyDeviceToHost);
+    if (tl.ensure(8 * nl) || tu.ensure(8 * nu)) return fail(DEV_ERR_DEVICE_ALLOC);
+    launch_convert(c->stream, (int)nl, c->vtype(), dl, VType::F64, tl.p);
+    launch_convert(c->stream, (int)nu, c->vtype(), du, VType::F64, tu.p);
+    dl = tl.p;
+    du = tu.p;
   }
   if (cudaGetLastError() != cudaSuccess) return fail(DEV_ERR_UNKNOWN);
   L->diagorder_type = Magma_UNITY;
   U->diagorder_type = Magma_VALUE;
-  rc = fill_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, lv,
-                    bcsr ? A->blocksize : 0);
+  rc = fill_csr_out_dev(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, dl,
+                        bcsr ? A->blocksize : 0, c->stream);
   if (!rc)
-    rc = fill_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, uv,
-                      bcsr ? A->blocksize : 0);
+    rc = fill_csr_out_dev(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, du,
+                          bcsr ? A->blocksize : 0, c->stream);
   if (rc) return fail(rc);
   U->major = MagmaColMajor;
+  pc.mark("fill L, U");
   log->sweeps = (int)steps.size();
   log->tol = tol;
   log->finalStep = steps.empty() ? 0.0 : steps.back();
@@ -361,16 +396,27 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
   else if (choice == 2) o.trsv_mode = LACE_TRSV_NONE;
   else if (o.trsv_mode != LACE_TRSV_LEVELS) o.trsv_mode = LACE_TRSV_SYNCFREE;
   lace_gpu_set_options(c, &o);
+  PhaseClock pc(c->verbose, "fgmres");
   const int n = A->num_rows;
   rc = lace_gpu_upload_csr_host(c, n, A->row[n], A->row, A->col, A->val);
   if (rc) return set_err(rc);
+  pc.mark("upload A");
   if (choice != 2) {
     if (!L || !U) return set_err(DEV_ERR_INVALID_PTR);
-    std::vector<int> up, ui;
-    std::vector<double> uv;
-    u_as_csr(U, up, ui, uv);
-    rc = c->set_factors_host(n, L->row, L->col, L->val, up.data(), ui.data(), uv.data());
+    // factors as ParILU returned them (U in CSC, the context's own patterns):
+    // values go up as they are; anything else is converted on the host
+    rc = 1;
+    if ((U->storage_type == Magma_CSCU || U->storage_type == Magma_CSC) && L->num_rows == n && U->num_rows == n)
+      rc = c->set_factors_csc_host(n, L->row, L->col, L->val, U->row, U->col, U->val);
+    if (rc == 1) {
+      std::vector<int> up, ui;
+      std::vector<double> uv;
+      u_as_csr(U, up, ui, uv);
+      pc.mark("U as CSR");
+      rc = c->set_factors_host(n, L->row, L->col, L->val, up.data(), ui.data(), uv.data());
+    }
     if (rc) return set_err(rc);
+    pc.mark("set factors");
   }
   DBuf db, dx;
   if (upload_vec(db, b->val, n, c->stream) || upload_vec(dx, x0->val, n, c->stream))
@@ -379,8 +425,10 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
   rc = c->fgmres((const double *)db.p, (double *)dx.p, par->search_max, restart_max, par->tol_type,
                  par->rtol, false, log, &total, nullptr);
   if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
+  pc.mark("b, x0 + solve");
   if (cudaMemcpy(x0->val, dx.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
     return set_err(DEV_ERR_UNKNOWN);
+  pc.mark("download x");
   log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (c->verbose)
     printf("gmres_search_directions = %d;\ngmres_total_search_directions = %d;\n", log->search_directions,

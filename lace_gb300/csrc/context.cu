@@ -577,6 +577,49 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
   return 0;
 }
 
+int lace_gpu_ctx::device_anorm() {
+  const size_t ld = bs ? (size_t)bs * bs : 1;
+  const size_t count = (size_t)nnzA * ld;
+  double *partials = (double *)part_ensure();
+  const void *z = zeros(count);
+  if (!partials || !z) return DEV_ERR_DEVICE_ALLOC;
+  launch_sqdiff(stream, (int)count, Aval.p, z, 0, partials, (int *)cnt_buf.p + 8, (double *)scal_buf.p + 8);
+  if (cudaMemcpyAsync(h_scal + 8, (double *)scal_buf.p + 8, 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return DEV_ERR_UNKNOWN;
+  anorm = std::sqrt(h_scal[8]);
+  return 0;
+}
+
+int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lcol, const double *lval,
+                                       const int *ucp, const int *uri, const double *ucval) {
+  if (bs || nrows != n || (int)hL.ptr.size() != n + 1 || (int)hUc.ptr.size() != n + 1) return 1;
+  if (memcmp(hL.ptr.data(), lrow, 4 * (size_t)(n + 1)) != 0 ||
+      memcmp(hUc.ptr.data(), ucp, 4 * (size_t)(n + 1)) != 0 || lrow[n] != nnzL || ucp[n] != nnzU ||
+      memcmp(hL.idx.data(), lcol, 4 * (size_t)nnzL) != 0 || memcmp(hUc.idx.data(), uri, 4 * (size_t)nnzU) != 0)
+    return 1;
+  int rc = alloc_factor_values();
+  if (rc) return rc;
+  const VType t = vtype();
+  cur = 0;
+  if (t == VType::F64) {
+    if (cudaMemcpyAsync(Lv[0].p, lval, 8 * (size_t)nnzL, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(Ucv[0].p, ucval, 8 * (size_t)nnzU, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      return DEV_ERR_UNKNOWN;
+  } else {
+    DBuf tl, tu;
+    if (tl.upload(lval, 8 * (size_t)nnzL, stream) || tu.upload(ucval, 8 * (size_t)nnzU, stream))
+      return DEV_ERR_DEVICE_ALLOC;
+    launch_convert(stream, nnzL, VType::F64, tl.p, t, Lv[0].p);
+    launch_convert(stream, nnzU, VType::F64, tu.p, t, Ucv[0].p);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;  // before tl, tu go
+  }
+  rc = finish_factors();  // U's CSR image and L^T, gathered on the GPU
+  if (rc) return rc;
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  return 0;
+}
+
 // caller-supplied factors (host, FP64): L CSRL, U CSR (diagonal first).  The
 // factor analysis is redone only when the patterns differ from the current
 // ones.  Values are stored in the context's precision.
@@ -687,11 +730,9 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
     c->hAcol.assign(col, col + nnz);
   }
   c->factors_ready = false;
-  double s = 0.0;
-  for (int p = 0; p < nnz; ++p) s += val[p] * val[p];
-  c->anorm = std::sqrt(s);
+  rc = c->device_anorm();
+  if (rc) return set_err(rc);
   c->AT_ready = false;
-  LCHK(cudaStreamSynchronize(c->stream));
   return c->autotune_spmv();
 }
 

@@ -120,6 +120,14 @@ struct lace_gpu_ctx {
   int analyse_factors(const lace::Pattern &L, const lace::Pattern &Ur);
   int set_factors_host(int nrows, const int *lrow, const int *lcol, const double *lval,
                        const int *urow, const int *ucol, const double *uval);
+  // the same from U in CSC order (diagonal last in each column), when L's and
+  // U's patterns are the context's own (as ParILU returned them): the values
+  // are uploaded as they are and U's CSR image is gathered on the GPU.
+  // Returns 1 (nothing done) when the patterns differ.
+  int set_factors_csc_host(int nrows, const int *lrow, const int *lcol, const double *lval,
+                           const int *ucp, const int *uri, const double *ucval);
+  // ||A||_F from the resident values, on the GPU
+  int device_anorm();
   std::vector<int> uc2ur_h;  // CSC position of U -> CSR position
   int upload_common(int n_, int nnz_, const int *row, const int *col, int bs_);
   void set_rows_per_lane(int R);

@@ -9,6 +9,7 @@ posix_memalign (as LACE_CALLOC does); `free_matrix` releases them with free().
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -160,6 +161,43 @@ def parilu(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None, gpu_
     free_matrix(L)
     free_matrix(U)
     return la, ua, info
+
+
+class LibMat(Mat):
+    """A container the library filled (ParILU's L or U); its arrays are
+    released with free(), as data_zmfree does, when the object goes away."""
+
+    def __init__(self, m: DataMatrix):
+        super().__init__()
+        self.m = m
+        weakref.finalize(self, free_matrix, m)
+
+    def arrays(self):
+        return matrix_arrays(self.m)
+
+
+def parilu_mats(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None):
+    """data_PariLU_v0_3 (max_sweeps None) or data_PariLU_v0_3_prescribedSweeps,
+    returning the filled containers themselves (L in CSRL, U in CSCU) to pass
+    on to fgmres_householder_restart as a C caller would, without copies."""
+    L = DataMatrix()
+    U = DataMatrix()
+    L.storage_type = Magma_CSRL
+    U.storage_type = Magma_CSCU
+    log = PrecondLog()
+    f = lib()
+    if max_sweeps is None:
+        f.data_PariLU_v0_3(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log))
+    else:
+        log.maxSweeps = max_sweeps
+        f.data_PariLU_v0_3_prescribedSweeps(A.ref, C.byref(L), C.byref(U), reduction, C.byref(log))
+    if log.sweeps < 0:
+        from . import LaceError
+        raise LaceError(f.lace_gpu_last_error(), "data_PariLU_v0_3")
+    info = {k: getattr(log, k) for k in ("sweeps", "tol", "finalStep", "A_Frobenius", "precond_generation_time",
+                                         "initial_residual", "initial_nonlinear_residual",
+                                         "nonlinear_residual", "omp_num_threads")}
+    return LibMat(L), LibMat(U), info
 
 
 def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
