@@ -256,6 +256,14 @@ typedef struct lace_gpu_options {
   int spmv_lanes;       /* lanes per CSR row; 0 = autotune               */
   int trsv_rows_per_lane; /* sync-free chunk = 32 * this rows; 0 = auto  */
   int monitor_orthog;   /* ||I - Q^T Q||_inf after every step (slow)     */
+  /* Sync-free solve schedule.  0 = autotune; trsv_chunks_per_block > 0 pins
+   * it (with trsv_rows_per_lane, 0 meaning 1): chunks per block (<= 1024),
+   * warps per CTA (1-16, 0 = 16) and CTAs per thread-block cluster (1, 2, 4
+   * or 8; 0 = 1; a cluster the device or the shared memory cannot hold runs
+   * as 1). */
+  int trsv_chunks_per_block;
+  int trsv_warps;
+  int trsv_cluster;
 } lace_gpu_options;
 
 void lace_gpu_default_options(lace_gpu_options *opt);

@@ -68,7 +68,8 @@ def lib() -> C.CDLL:
 class GpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("trsv_mode", C.c_int), ("jacobi_sweeps", C.c_int),
                 ("jacobi_tol", C.c_double), ("use_graph", C.c_int), ("spmv_lanes", C.c_int),
-                ("trsv_rows_per_lane", C.c_int), ("monitor_orthog", C.c_int)]
+                ("trsv_rows_per_lane", C.c_int), ("monitor_orthog", C.c_int),
+                ("trsv_chunks_per_block", C.c_int), ("trsv_warps", C.c_int), ("trsv_cluster", C.c_int)]
 
 
 def _padded(fields):

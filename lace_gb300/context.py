@@ -67,7 +67,10 @@ class Context:
     def set_options(self, precision: str | None = None, trsv: str | None = None,
                     jacobi_sweeps: int | None = None, use_graph: bool | None = None,
                     spmv_lanes: int | None = None, rows_per_lane: int | None = None,
-                    monitor_orthog: bool | None = None) -> "Context":
+                    monitor_orthog: bool | None = None, schedule: tuple | None = None) -> "Context":
+        """schedule: (chunks per block, warps, cluster) pins the sync-free
+        solve's schedule (see lace_gpu_options); (0, 0, 0) returns it to the
+        autotune."""
         o = self.opts
         if precision is not None:
             o.precision = PREC[precision]
@@ -83,6 +86,8 @@ class Context:
             o.trsv_rows_per_lane = int(rows_per_lane)
         if monitor_orthog is not None:
             o.monitor_orthog = int(bool(monitor_orthog))
+        if schedule is not None:
+            o.trsv_chunks_per_block, o.trsv_warps, o.trsv_cluster = (int(v) for v in schedule)
         _chk(self._lib.lace_gpu_set_options(self.h, C.byref(o)), "set_options")
         return self
 

@@ -15,6 +15,7 @@
 //          Z[ldv x m] f32 (mixed precision) or f64, w/q/t vectors
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -228,26 +229,35 @@ int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, Plan
         }
       }
     }
+    // the level over all dependencies, in this block or an earlier one: the
+    // step of the whole solve's wavefront at which the chunk can go
     int l = 0;
-    for (int cj : deps)
-      if (cblk[cj] == cblk[c]) l = std::max(l, lev[cj] + 1);
+    for (int cj : deps) l = std::max(l, lev[cj] + 1);
     lev[c] = l;
   }
-  // per block: chunks ordered by local level
+  // per block: chunks ordered by level (then by position).  A block that
+  // straddles two stretches of the wavefront (the end of one plane of a
+  // stencil and the start of the next) then has its warps take the chunks in
+  // the order they become ready; an in-block dependency always has a lower
+  // level, so the order stays topological.
   std::vector<int4> blk(nblk), urec;
   urec.reserve(nch);
   int max_units = 0;
   for (int b = 0; b < nblk; ++b) {
     const int p0 = b * cpb, p1 = std::min(nch, p0 + cpb);
-    int nl = 0;
-    for (int p = p0; p < p1; ++p) nl = std::max(nl, lev[lower ? p : nch - 1 - p] + 1);
+    int lmin = INT_MAX, lmax = 0;
+    for (int p = p0; p < p1; ++p) {
+      lmin = std::min(lmin, lev[lower ? p : nch - 1 - p]);
+      lmax = std::max(lmax, lev[lower ? p : nch - 1 - p]);
+    }
+    const int nl = lmax - lmin + 1;
     std::vector<int> cnt(nl + 1, 0);
-    for (int p = p0; p < p1; ++p) cnt[lev[lower ? p : nch - 1 - p] + 1]++;
+    for (int p = p0; p < p1; ++p) cnt[lev[lower ? p : nch - 1 - p] - lmin + 1]++;
     for (int l = 0; l < nl; ++l) cnt[l + 1] += cnt[l];
     std::vector<int> order(p1 - p0);
     for (int p = p0; p < p1; ++p) {
       const int c = lower ? p : nch - 1 - p;
-      order[cnt[lev[c]]++] = c;
+      order[cnt[lev[c] - lmin]++] = c;
     }
     const int u0 = (int)urec.size();
     for (int c : order) urec.push_back(make_int4(c, lev[c] | ((int)kind[c] << 30), 0, 0));
@@ -360,6 +370,7 @@ int lace_gpu_ctx::ensure_plan(int which) {
   pb.dev.row = t.row;
   pb.dev.col = t.col;
   pb.dev.warps = plan_warps;
+  pb.dev.cl = plan_cl;
   const int per_sm = plan_warps == 1 ? 16 : (plan_warps <= 8 ? 4 : (plan_warps <= 16 ? 2 : 1));
   pb.dev.grid = std::min(pb.dev.nblocks, num_sms() * per_sm);
   if (pb.vals_version != fact_version || pb.vals_type != (int)vtype() || pb.vals_src != t.val) {
@@ -384,6 +395,9 @@ extern "C" void lace_gpu_default_options(lace_gpu_options *o) {
   o->spmv_lanes = 0;
   o->trsv_rows_per_lane = 0;
   o->monitor_orthog = 0;
+  o->trsv_chunks_per_block = 0;
+  o->trsv_warps = 0;
+  o->trsv_cluster = 0;
 }
 
 extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream) {
@@ -457,7 +471,16 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
   if (!c || !o) return set_err(DEV_ERR_INVALID_PTR);
   if (o->precision < 0 || o->precision > 2 || o->trsv_mode < 0 || o->trsv_mode > 3)
     return set_err(DEV_ERR_ILLEGAL_VALUE);
+  if (o->trsv_chunks_per_block < 0 || o->trsv_chunks_per_block > kBlkMaxUnits || o->trsv_warps < 0 ||
+      o->trsv_warps > 16 ||
+      !(o->trsv_cluster == 0 || o->trsv_cluster == 1 || o->trsv_cluster == 2 || o->trsv_cluster == 4 ||
+        o->trsv_cluster == 8))
+    return set_err(DEV_ERR_ILLEGAL_VALUE);
   const bool prec_changed = o->precision != c->opt.precision;
+  // a new schedule choice: tuned again before the next solve
+  if (o->trsv_rows_per_lane != c->opt.trsv_rows_per_lane || o->trsv_chunks_per_block != c->opt.trsv_chunks_per_block ||
+      o->trsv_warps != c->opt.trsv_warps || o->trsv_cluster != c->opt.trsv_cluster)
+    c->trsv_tuned = false;
   c->opt = *o;
   c->drop_graphs();
   if (prec_changed) c->factors_ready = false;
@@ -1095,22 +1118,29 @@ int lace_gpu_ctx::autotune_trsv() {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int bR = 4, bC = 1, bW = 1;
-  // schedule shapes: (rows per lane, chunks per block, warps per CTA); a
-  // block of one chunk on one warp is the warp-level sync-free solve
+  int bR = 4, bC = 1, bW = 1, bL = 1;
+  // schedule shapes: (rows per lane, chunks per block, warps per CTA, CTAs
+  // per cluster); a block of one chunk on one warp is the warp-level
+  // sync-free solve; in a cluster, consecutive blocks pass their rows on in
+  // distributed shared memory
   struct Cand {
-    int R, cpb, w;
+    int R, cpb, w, cl;
   };
   // blocks up to the shared-memory window (160 KB of solved rows: 40960 rows
   // in FP32, 20480 in FP64) keep every in-block dependency on chip; a block
   // holds at most 1024 chunks (its unit records are staged in shared memory)
-  std::vector<Cand> cands = {{4, 1, 1},    {1, 1, 1},    {4, 32, 8},    {1, 64, 8},
-                             {1, 128, 16}, {1, 256, 16}, {1, 512, 16},  {1, 1024, 16},
-                             {2, 256, 16}, {4, 64, 16},  {4, 128, 16},  {4, 256, 16}};
-  if (opt.trsv_rows_per_lane > 0) {
+  std::vector<Cand> cands = {{4, 1, 1, 1},    {1, 1, 1, 1},    {4, 32, 8, 1},   {1, 64, 8, 1},
+                             {1, 128, 16, 1},  {1, 256, 16, 1},  {1, 512, 16, 1}, {1, 1024, 16, 1},
+                             {2, 256, 16, 1},  {4, 64, 16, 1},   {4, 128, 16, 1}, {4, 256, 16, 1},
+                             {1, 256, 16, 2},  {1, 256, 16, 4},  {1, 384, 16, 4}, {1, 512, 16, 4},
+                             {1, 512, 16, 8},  {2, 256, 16, 4}};
+  if (opt.trsv_chunks_per_block > 0) {
+    cands = {{opt.trsv_rows_per_lane > 0 ? opt.trsv_rows_per_lane : 1, opt.trsv_chunks_per_block,
+              opt.trsv_warps > 0 ? opt.trsv_warps : 16, opt.trsv_cluster > 0 ? opt.trsv_cluster : 1}};
+  } else if (opt.trsv_rows_per_lane > 0) {
     std::vector<Cand> keep;
     for (auto c : cands)
-      if (c.R == 4) keep.push_back({opt.trsv_rows_per_lane, c.cpb, c.w});
+      if (c.R == 4) keep.push_back({opt.trsv_rows_per_lane, c.cpb, c.w, c.cl});
     cands = keep;
   }
   const int nch_min = (n + 31) / 32;
@@ -1119,7 +1149,14 @@ int lace_gpu_ctx::autotune_trsv() {
     plan_R = cd.R;
     plan_cpb = cd.cpb;
     plan_warps = cd.w;
+    plan_cl = cd.cl;
     if ((rc = ensure_plan(0)) || (rc = ensure_plan(1))) return rc;
+    if (cd.cl > 1 && !(sptrsv_cluster_supported(plans[0].dev, vtype()) &&
+                       sptrsv_cluster_supported(plans[1].dev, vtype()))) {
+      if (cands.size() > 1) continue;
+      plan_cl = cd.cl = 1;  // a pinned schedule runs without the cluster
+      if ((rc = ensure_plan(0)) || (rc = ensure_plan(1))) return rc;
+    }
     // the pair as the Arnoldi cycle runs it: q, intermediate and z all in
     // the factor precision's vector type
     solve_tri(0, vec_q.p, f32, vec_t.p, f32, false, vec_t2.p);
@@ -1133,12 +1170,21 @@ int lace_gpu_ctx::autotune_trsv() {
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    if (verbose) printf("trsv autotune R=%d cpb=%d warps=%d: %.3f ms per pair\n", cd.R, cd.cpb, cd.w, ms / 2);
+    // a shape whose solves gave up waiting is not a candidate
+    const int st = h_status();
+    if (st & kStatusSpinTimeout) {
+      cudaMemsetAsync(&ctrl()->status, 0, 4, stream);
+      ms = 1e30f;
+    }
+    if (verbose)
+      printf("trsv autotune R=%d cpb=%d warps=%d cluster=%d: %.3f ms per pair%s\n", cd.R, cd.cpb, cd.w, cd.cl,
+             ms / 2, (st & kStatusSpinTimeout) ? " (wait timed out)" : "");
     if (ms < best) {
       best = ms;
       bR = cd.R;
       bC = cd.cpb;
       bW = cd.w;
+      bL = cd.cl;
     }
   }
   (void)nch_min;
@@ -1147,11 +1193,12 @@ int lace_gpu_ctx::autotune_trsv() {
   plan_R = bR;
   plan_cpb = bC;
   plan_warps = bW;
+  plan_cl = bL;
   rows_per_lane = bR;
   trsv_tuned = true;
   cudaMemsetAsync(&ctrl()->status, 0, 4, stream);
   drop_graphs();
-  if (h_status() & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
+  if (best >= 1e30f) return DEV_ERR_INTERNAL_LIMIT;  // no shape finished its solves
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 

@@ -39,7 +39,7 @@ struct PlanBufs {
 };
 
 // host construction of a plan: chunks of 32*R rows, blocks of cpb chunks (in
-// solve order), local levels inside blocks, cross-block requirements
+// solve order), chunks of a block in wavefront-level order, cross-block requirements
 int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s);
 
 extern thread_local int g_last_error;
@@ -97,7 +97,7 @@ struct lace_gpu_ctx {
   int rows_per_lane = 4;
   bool trsv_tuned = false;
   lace::PlanBufs plans[4];
-  int plan_R = 4, plan_cpb = 1, plan_warps = 1;  // autotuned schedule shape
+  int plan_R = 4, plan_cpb = 1, plan_warps = 1, plan_cl = 1;  // autotuned schedule shape
   int ensure_plan(int which);
   int lanes = 8;
 

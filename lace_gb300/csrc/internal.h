@@ -153,12 +153,13 @@ struct TriBlkPlan {
   int R = 4, cpb = 1, warps = 1, grid = 1;
   int unit = 0, lower = 1;
   const int *row = nullptr, *col = nullptr;
-  // per block (solve order): {first unit, end unit, local levels, lowest row}
+  // per block (solve order): {first unit, end unit, levels spanned, lowest row}
   const int4 *blk = nullptr;
-  // per unit (blocks in solve order, a block's chunks by local level):
-  // {chunk, local level | serial << 30, 0, 0}
+  // per unit (blocks in solve order, a block's chunks by level):
+  // {chunk, level | serial << 30, 0, 0}
   const int4 *urec = nullptr;
   int max_units = 0;  // most chunks in one block
+  int cl = 1;         // CTAs per thread-block cluster (consecutive blocks pass rows on in shared memory)
   // The plan's own layout of the solve, coalesced per warp.  Per unit u,
   // slot t < S, row r < R, lane l: index ((u*S + t)*R + r)*32 + l for the
   // slot arrays, (u*R + r)*32 + l for the per-row ones.
@@ -173,6 +174,9 @@ struct TriBlkPlan {
   const int *ucode = nullptr, *umap = nullptr, *udiag = nullptr, *uprev = nullptr, *uflag = nullptr;
   void *uvs = nullptr, *uaps = nullptr, *urd = nullptr;
 };
+// 1 when the plan's cluster shape can be launched on this device with the
+// value type's window (some cluster of it fits)
+int sptrsv_cluster_supported(const TriBlkPlan &pl, VType vt);
 // gather the plan's values (uvs, uaps, urd) from the triangle's values
 void launch_plan_values(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt);
 // x must not overlap b (x is filled with the unsolved pattern first)

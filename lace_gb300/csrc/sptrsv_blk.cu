@@ -14,9 +14,11 @@
 // way.  A row waits for a dependency by reading it until the pattern is gone:
 // from the window when the dependency is in the same block, from L2
 // otherwise.  There are no per-level barriers: warps take the block's chunks
-// round robin in local-level order (a chunk's level is one more than that of
-// its dependencies in the block), so the lowest unsolved chunk can always
-// proceed.
+// round robin in level order (a chunk's level is one more than the highest
+// level of its dependencies, in any block: its step in the wavefront of the
+// whole solve), so the lowest unsolved chunk can always proceed, and a block
+// that holds parts of two stretches of the wavefront takes its chunks in the
+// order they become ready.
 //
 // The plan holds the solve in its own layout, coalesced per warp: for each
 // chunk, row and dependency slot where the dependency is read (window slot or
@@ -33,6 +35,8 @@
 // first plane reads rows of another CTA.
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "internal.h"
 
 namespace lace {
@@ -43,8 +47,10 @@ __device__ __forceinline__ void st_out(void *x, int out_f32, int i, T v) {
   else ((volatile double *)x)[i] = (double)v;
 }
 
-// shared memory a CTA may use for its block's solved rows
+// shared memory a CTA may use for its block's solved rows; a CTA of a
+// cluster also holds the previous block's rows
 constexpr int kSptrsvSmemMax = 160 * 1024;
+constexpr size_t kSptrsvClusterSmemMax = 200 * 1024;
 
 __device__ __forceinline__ bool is_unsolved(float v) { return __float_as_uint(v) == 0xffffffffu; }
 __device__ __forceinline__ bool is_unsolved(double v) { return __double_as_longlong(v) == -1ll; }
@@ -87,11 +93,22 @@ struct BlkPlanDev {
   int n, nblocks;
   const int *row, *col;
   const void *val;  // CSR values (rows solved from the CSR arrays, serial chunks)
-  const int4 *blk;  // {first unit, end unit, local levels, lowest row}
-  const int4 *urec; // {chunk, local level | serial << 30, 0, 0}
+  const int4 *blk;  // {first unit, end unit, levels spanned, lowest row}
+  const int4 *urec; // {chunk, level | serial << 30, 0, 0}
   const int *ucode, *uflag;
   const void *uvs, *uaps, *urd;
   int win;  // rows of a block kept in shared memory (0: none), plus a spare slot
+};
+
+// The rows of the previous block of a thread-block cluster, which the CTA
+// that solves them writes into this CTA's shared memory (the halo, from slot
+// base on), and where this CTA writes its own rows for the next one.
+template <typename CT>
+struct Halo {
+  int prev_row0;       // lowest row of the previous block
+  unsigned prev_rows;  // its rows (0: no previous block in the cluster)
+  unsigned base;       // first halo slot in shared memory
+  CT *remote;          // the next CTA's shared memory (nullptr: none)
 };
 
 // One chunk's solve data, loaded by its warp ahead of its turn, and the
@@ -150,10 +167,17 @@ __device__ __forceinline__ void unit_load(Unit<CT, R, S> &d, int k, int step, in
 // dependency reads an always-solved zero in this CTA's shared memory - so
 // that the lanes' loads of one pass go out together.  Rows solved from the
 // CSR arrays are read after.
-template <typename CT, typename VT, typename OT, int R, int S, bool LOWER>
+// A far dependency (code <= -2) in the previous block of the cluster is read
+// from the halo instead.
+template <bool HALO, typename CT>
+__device__ __forceinline__ bool in_halo(int code, const Halo<CT> &h) {
+  return HALO && code <= -2 && (unsigned)(-code - 2 - h.prev_row0) < h.prev_rows;
+}
+
+template <typename CT, typename VT, typename OT, int R, int S, bool LOWER, bool HALO>
 __device__ __forceinline__ void far_wait(const Unit<CT, R, S> &d, const BlkPlanDev &P, const CT *xs, const void *x,
                                          int row0, unsigned brows, unsigned win, int lane, const int *rows, int c,
-                                         CT *Bv, const double *s_zero, int *status) {
+                                         CT *Bv, const double *s_zero, int *status, const Halo<CT> &h) {
   constexpr int CS = 32 * R;
   const VT *val = (const VT *)P.val;
   const OT *zero = (const OT *)s_zero;
@@ -165,7 +189,7 @@ __device__ __forceinline__ void far_wait(const Unit<CT, R, S> &d, const BlkPlanD
 #pragma unroll
     for (int t = 0; t < S; ++t) {
       const int code = d.code[r][t];
-      const bool glob = code <= -2 || code >= (int)win;
+      const bool glob = (code <= -2 && !in_halo<HALO>(code, h)) || code >= (int)win;
       src[r][t] = glob ? (const OT *)x + (code <= -2 ? -code - 2 : row0 + code) : zero;
       w[r][t] = glob ? d.vs[r][t] : (CT)0;
     }
@@ -202,10 +226,10 @@ __device__ __forceinline__ void far_wait(const Unit<CT, R, S> &d, const BlkPlanD
   }
 }
 
-template <typename CT, typename VT, int R, int S, bool LOWER>
+template <typename CT, typename VT, int R, int S, bool LOWER, bool HALO>
 __device__ __forceinline__ void unit_solve(const Unit<CT, R, S> &d, const BlkPlanDev &P, CT *xs, void *x,
                                            int in_f32, int out_f32, int row0, unsigned brows, unsigned win,
-                                           int lane, const double *s_zero, int *status) {
+                                           int lane, const double *s_zero, int *status, const Halo<CT> &h) {
   constexpr int CS = 32 * R;
   const VT *val = (const VT *)P.val;
   const int c = d.rec.x;
@@ -225,7 +249,25 @@ __device__ __forceinline__ void unit_solve(const Unit<CT, R, S> &d, const BlkPla
     X[r] = (CT)0;
     far |= (d.flag >> r) & 1;
 #pragma unroll
-    for (int t = 0; t < S; ++t) far |= d.code[r][t] <= -2 || d.code[r][t] >= (int)win;
+    for (int t = 0; t < S; ++t)
+      far |= (d.code[r][t] <= -2 && !in_halo<HALO>(d.code[r][t], h)) || d.code[r][t] >= (int)win;
+  }
+  // The scan's multipliers depend on the factor values only, so they are
+  // formed before the wait: m[k] is the product of A over the rows of the
+  // 2^k lanes before this lane's partial, and after the wait a round of the
+  // scan is one shuffle and one multiply-add.
+  CT m[5];
+  if (!serial) {
+    CT ca = (CT)1;
+#pragma unroll
+    for (int r = 0; r < R; ++r) ca = A[r] * ca;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int o = 1 << k;
+      const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
+      m[k] = ca;
+      if (lane >= o) ca = ca * pa;
+    }
   }
   // Wait for the chunk's dependencies with the whole warp in lock step
   // (lanes spinning on different branches of a diverged warp would wait for
@@ -233,61 +275,73 @@ __device__ __forceinline__ void unit_solve(const Unit<CT, R, S> &d, const BlkPla
   // dependencies and forms the sums, and the warp leaves when every lane saw
   // them solved.  Phase A: rows outside the window (other blocks) and rows
   // solved from the CSR arrays, read through L2; they are usually solved
-  // before the warp gets here.  Phase B: rows of the window, branch free - an
-  // entry that is not a window dependency reads the always-solved spare slot
+  // before the warp gets here.  Phase B: rows of the window (and of the halo),
+  // branch free - an entry that is neither reads the always-solved spare slot
   // with weight 0.
   if (__any_sync(0xffffffffu, far)) {
-    if (out_f32) far_wait<CT, VT, float, R, S, LOWER>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status);
-    else far_wait<CT, VT, double, R, S, LOWER>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status);
+    if (out_f32)
+      far_wait<CT, VT, float, R, S, LOWER, HALO>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status, h);
+    else
+      far_wait<CT, VT, double, R, S, LOWER, HALO>(d, P, xs, x, row0, brows, win, lane, rows, c, Bv, s_zero, status, h);
   }
-  for (int spins = 0;; ++spins) {
-    bool ok = true;
-    CT acc[R];
+  // the slots read in phase B (window, halo, or the spare slot with weight 0)
+  int idx[R][S];
+  CT wv[R][S];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      acc[r] = Bv[r];
+  for (int r = 0; r < R; ++r)
 #pragma unroll
-      for (int t = 0; t < S; ++t) {
-        const int code = d.code[r][t];
-        const bool in = (unsigned)code < win;
-        const CT v = ((const volatile CT *)xs)[in ? code : (int)win];
-        ok &= !is_unsolved(v);
-        acc[r] -= (in ? d.vs[r][t] : (CT)0) * v;
+    for (int t = 0; t < S; ++t) {
+      const int code = d.code[r][t];
+      const bool in = (unsigned)code < win;
+      idx[r][t] = in ? code : (int)win;
+      wv[r][t] = in ? d.vs[r][t] : (CT)0;
+      if (in_halo<HALO>(code, h)) {
+        idx[r][t] = (int)h.base + (-code - 2 - h.prev_row0);
+        wv[r][t] = d.vs[r][t];
       }
     }
-    if (__all_sync(0xffffffffu, ok)) {
+  CT v[R][S];
+  for (int spins = 0;; ++spins) {
+    bool ok = true;
 #pragma unroll
-      for (int r = 0; r < R; ++r) Bv[r] = acc[r];
-      break;
-    }
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int t = 0; t < S; ++t) {
+        v[r][t] = ((const volatile CT *)xs)[idx[r][t]];
+        ok &= !is_unsolved(v[r][t]);
+      }
+    if (__all_sync(0xffffffffu, ok)) break;
     if (spins > kMaxSpins || ((spins & 1023) == 1023 && (*(const volatile int *)status & kStatusSpinTimeout))) {
       if (lane == 0) atomicOr(status, kStatusSpinTimeout);
       break;
     }
   }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int t = 0; t < S; ++t) Bv[r] -= wv[r][t] * v[r][t];
   if (!serial) {
     // x_p = A_p x_{p-1} + B_p along the chunk: a warp-wide affine scan
-    CT ca = (CT)1, cb = (CT)0;
+    // (inclusive over the lanes' partials)
+    CT cb = (CT)0;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      cb = A[r] * cb + Bv[r];
-      ca = A[r] * ca;
+    for (int r = 0; r < R; ++r) cb = A[r] * cb + Bv[r];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const CT pb = __shfl_up_sync(0xffffffffu, cb, 1 << k);
+      if (lane >= (1 << k)) cb = m[k] * pb + cb;
     }
+    if (R == 1) {
+      X[0] = cb;
+    } else {
+      // the lane's rows from the partial before it
+      CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
+      if (lane == 0) xin = (CT)0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
-      const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
-      if (lane >= o) {
-        cb = ca * pb + cb;
-        ca = ca * pa;
+      for (int r = 0; r < R; ++r) {
+        xin = A[r] * xin + Bv[r];
+        X[r] = xin;
       }
-    }
-    CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
-    if (lane == 0) xin = (CT)0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      xin = A[r] * xin + Bv[r];
-      X[r] = xin;
     }
   } else {
     // position by position: the owner's value is final, the later rows of
@@ -322,8 +376,47 @@ __device__ __forceinline__ void unit_solve(const Unit<CT, R, S> &d, const BlkPla
       const CT v = as_solved(X[r]);
       const unsigned slot = (unsigned)(rows[r] - row0);
       if (slot < win) ((volatile CT *)xs)[slot] = v;
+      if (HALO && h.remote != nullptr) ((volatile CT *)h.remote)[h.base + slot] = v;  // the next CTA's halo
       st_out<CT>(x, out_f32, rows[r], v);
     }
+}
+
+// The chunks of one block: a warp's chunks are k = warp, warp + nw, ...; two
+// register sets take turns, so a chunk's data is loaded while the chunk
+// before it is solved.
+template <typename CT, typename VT, int R, bool LOWER, bool HALO>
+__device__ __forceinline__ void solve_block(const BlkPlanDev &P, const int4 &B, CT *xs, const void *b, int in_f32,
+                                            void *x, int out_f32, int warp, int nw, int lane, const double *s_zero,
+                                            int *status, const Halo<CT> &h) {
+  constexpr int CS = 32 * R;
+  constexpr int S = blk_slots(R);
+  const int nunits = B.y - B.x, row0 = B.w;
+  const unsigned brows = (unsigned)(nunits * CS);
+  const unsigned win = min(brows, (unsigned)P.win);
+  Unit<CT, R, S> d0, d1;
+  if (warp < nunits) d0.nrec = P.urec[B.x + warp];
+  if (warp + nw < nunits) d1.nrec = P.urec[B.x + warp + nw];
+  unit_load<CT, R, S, LOWER>(d0, warp, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+  unit_load<CT, R, S, LOWER>(d1, warp + nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+  while (d0.k >= 0) {
+    unit_solve<CT, VT, R, S, LOWER, HALO>(d0, P, xs, x, in_f32, out_f32, row0, brows, win, lane, s_zero, status, h);
+    unit_load<CT, R, S, LOWER>(d0, d0.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+    if (d1.k < 0) break;
+    unit_solve<CT, VT, R, S, LOWER, HALO>(d1, P, xs, x, in_f32, out_f32, row0, brows, win, lane, s_zero, status, h);
+    unit_load<CT, R, S, LOWER>(d1, d1.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
+  }
+}
+
+// the CTA that leaves last re-arms the tickets
+__device__ __forceinline__ void rearm_tickets(int *tickets) {
+  if (threadIdx.x == 0) {
+    const int nrhs = gridDim.y;
+    const int e = atomicAdd(&tickets[nrhs], 1);
+    if (e == (int)(gridDim.x * gridDim.y) - 1) {
+      for (int r = 0; r <= nrhs; ++r) tickets[r] = 0;
+      __threadfence();
+    }
+  }
 }
 
 // blockIdx.y selects one of several right-hand sides (vectors vstride
@@ -335,7 +428,6 @@ __global__ void __launch_bounds__(512, 1) k_sptrsv_blk(BlkPlanDev P, const void 
                                                     const int *done_flag, int *status) {
   if (done_flag != nullptr && *(volatile const int *)done_flag) return;
   constexpr int CS = 32 * R;
-  constexpr int S = blk_slots(R);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CT *xs = reinterpret_cast<CT *>(smem_raw);
   __shared__ int s_blk;
@@ -354,36 +446,85 @@ __global__ void __launch_bounds__(512, 1) k_sptrsv_blk(BlkPlanDev P, const void 
     const int bk = s_blk;
     if (bk >= P.nblocks) break;
     const int4 B = P.blk[bk];
-    const int nunits = B.y - B.x, row0 = B.w;
-    const unsigned brows = (unsigned)(nunits * CS);
+    const unsigned brows = (unsigned)((B.y - B.x) * CS);
     const unsigned win = min(brows, (unsigned)P.win);
     for (unsigned s = threadIdx.x; s < win; s += blockDim.x) xs[s] = unsolved_value<CT>();
     if (threadIdx.x == 0) xs[win] = (CT)0;  // the spare slot: always solved
     __syncthreads();
-    // a warp's chunks are k = warp, warp + nw, ...; two register sets take
-    // turns, so a chunk's data is loaded while the chunk before it is solved
-    Unit<CT, R, S> d0, d1;
-    if (warp < nunits) d0.nrec = P.urec[B.x + warp];
-    if (warp + nw < nunits) d1.nrec = P.urec[B.x + warp + nw];
-    unit_load<CT, R, S, LOWER>(d0, warp, 2 * nw, nunits, B.x, P, b, in_f32, lane);
-    unit_load<CT, R, S, LOWER>(d1, warp + nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
-    while (d0.k >= 0) {
-      unit_solve<CT, VT, R, S, LOWER>(d0, P, xs, x, in_f32, out_f32, row0, brows, win, lane, &s_zero, status);
-      unit_load<CT, R, S, LOWER>(d0, d0.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
-      if (d1.k < 0) break;
-      unit_solve<CT, VT, R, S, LOWER>(d1, P, xs, x, in_f32, out_f32, row0, brows, win, lane, &s_zero, status);
-      unit_load<CT, R, S, LOWER>(d1, d1.k + 2 * nw, 2 * nw, nunits, B.x, P, b, in_f32, lane);
-    }
+    solve_block<CT, VT, R, LOWER, false>(P, B, xs, b, in_f32, x, out_f32, warp, nw, lane, &s_zero, status,
+                                         Halo<CT>{0, 0u, 0u, nullptr});
   }
-  // the CTA that leaves last re-arms the tickets
-  if (threadIdx.x == 0) {
-    const int nrhs = gridDim.y;
-    const int e = atomicAdd(&tickets[nrhs], 1);
-    if (e == (int)(gridDim.x * gridDim.y) - 1) {
-      for (int r = 0; r <= nrhs; ++r) tickets[r] = 0;
-      __threadfence();
+  rearm_tickets(tickets);
+}
+
+// The thread-block cluster variant.  A cluster of C CTAs takes C consecutive
+// blocks with one ticket (rank r the r-th), and every CTA but the last in the
+// cluster writes each row it solves into the next CTA's halo through
+// distributed shared memory, so the block after it reads the rows it depends
+// on there instead of through L2.  Shared memory: the window (P.win rows and
+// the spare slot), then the halo (P.win rows).  Cluster barriers separate
+// the groups: a CTA fills its window and halo with the unsolved pattern only
+// after every CTA of the cluster finished the previous group, and starts
+// solving only after every CTA of the cluster filled its own.  Rank 0 hands
+// the ticket to every CTA's own shared memory before the barrier, so that no
+// CTA touches another's shared memory after the last barrier (a CTA may then
+// leave).  A rank waits only for blocks before its own, which earlier ranks
+// and clusters holding earlier tickets solve, so every wait ends.
+template <typename CT, typename VT, int R, bool LOWER>
+__global__ void __launch_bounds__(512, 1) k_sptrsv_cl(BlkPlanDev P, const void *b_, int in_f32, void *x_,
+                                                   int out_f32, size_t vstride, int *tickets,
+                                                   const int *done_flag, int *status) {
+  // the same flag for every CTA: the whole cluster returns or none does
+  if (done_flag != nullptr && *(volatile const int *)done_flag) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  constexpr int CS = 32 * R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CT *xs = reinterpret_cast<CT *>(smem_raw);
+  __shared__ int s_grp;
+  __shared__ double s_zero;
+  if (threadIdx.x == 0) s_zero = 0.0;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const int rhs = blockIdx.y;
+  const int rank = (int)cl.block_rank(), csize = (int)cl.num_blocks();
+  const void *b = (const char *)b_ + (size_t)rhs * vstride * (in_f32 ? 4 : 8);
+  void *x = (char *)x_ + (size_t)rhs * vstride * (out_f32 ? 4 : 8);
+  const unsigned hbase = (unsigned)P.win + 1;
+  CT *next_xs = rank + 1 < csize ? cl.map_shared_rank(xs, rank + 1) : nullptr;
+  cl.sync();  // every CTA of the cluster runs before one writes to another
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) {
+      const int g = atomicAdd(&tickets[rhs], 1);
+      for (int r = 0; r < csize; ++r) *(volatile int *)cl.map_shared_rank(&s_grp, r) = g;
     }
+    cl.sync();  // the ticket is out; every CTA is done with the previous group
+    const int grp = *(const volatile int *)&s_grp;
+    if (grp * csize >= P.nblocks) break;  // the same for the whole cluster
+    const int bk = grp * csize + rank;
+    const bool active = bk < P.nblocks;
+    int4 B = make_int4(0, 0, 0, 0);
+    Halo<CT> h{0, 0u, hbase, nullptr};
+    if (active) {
+      B = P.blk[bk];
+      const unsigned brows = (unsigned)((B.y - B.x) * CS);
+      const unsigned win = min(brows, (unsigned)P.win);
+      for (unsigned s = threadIdx.x; s < win; s += blockDim.x) xs[s] = unsolved_value<CT>();
+      if (threadIdx.x == 0) xs[win] = (CT)0;  // the spare slot: always solved
+      if (rank > 0) {
+        const int4 Bp = P.blk[bk - 1];
+        h.prev_row0 = Bp.w;
+        h.prev_rows = (unsigned)((Bp.y - Bp.x) * CS);
+        for (unsigned s = threadIdx.x; s < h.prev_rows; s += blockDim.x) xs[hbase + s] = unsolved_value<CT>();
+      }
+      if (rank + 1 < csize && bk + 1 < P.nblocks) h.remote = next_xs;
+    }
+    cl.sync();  // every halo is filled before any CTA writes into one
+    if (active)
+      solve_block<CT, VT, R, LOWER, true>(P, B, xs, b, in_f32, x, out_f32, warp, nw, lane, &s_zero, status, h);
   }
+  rearm_tickets(tickets);
 }
 
 // the plan's values from the triangle's values: per row slot q, 1/a_ii (1 for
@@ -459,10 +600,44 @@ struct BlkArgs {
   int *tickets, *status;
   const int *dfl;
   int max_units, lower;
+  int cl;  // CTAs per thread-block cluster (1: the plain kernel)
 };
+
+template <typename CT, typename VT, int R, bool LOWER>
+static cudaError_t cl_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a,
+                             bool query_only, int *clusters) {
+  auto fn = k_sptrsv_cl<CT, VT, R, LOWER>;
+  const size_t sm = (2 * (size_t)P.win + 1) * sizeof(CT);
+  if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, a.nrhs);
+  cfg.blockDim = dim3(32 * warps);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)a.cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (query_only) return cudaOccupancyMaxActiveClusters(clusters, fn, &cfg);
+  return cudaLaunchKernelEx(&cfg, fn, P, a.b, a.in_f32, a.x, a.out_f32, a.vstride, a.tickets, a.dfl, a.status);
+}
+
+template <typename CT, typename VT, int R>
+static cudaError_t cl_launch_l(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a,
+                               bool query_only, int *clusters) {
+  return a.lower ? cl_launch<CT, VT, R, true>(s, P, warps, grid, a, query_only, clusters)
+                 : cl_launch<CT, VT, R, false>(s, P, warps, grid, a, query_only, clusters);
+}
 
 template <typename CT, typename VT, int R>
 static void blk_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int grid, const BlkArgs &a) {
+  if (R <= 4 && a.cl > 1) {
+    cl_launch_l<CT, VT, (R <= 4 ? R : 4)>(s, P, warps, grid, a, false, nullptr);
+    return;
+  }
   dim3 g(grid, a.nrhs);
   const size_t sm = ((size_t)P.win + 1) * sizeof(CT);
   if (a.lower) {
@@ -504,21 +679,68 @@ static BlkPlanDev plan_dev(const TriBlkPlan &pl, const void *val) {
   return P;
 }
 
+// shared memory of a block's window; the cluster variant needs twice that
+// (window and halo) and a window that holds the whole block
+static int window_rows(const TriBlkPlan &pl, VType vt) {
+  const size_t rows = (size_t)pl.cpb * 32 * pl.R;
+  const size_t esz = vt == VType::F64 ? 8 : 4;
+  return rows * esz <= (size_t)kSptrsvSmemMax ? (int)rows : 0;
+}
+
+static int cluster_size(const TriBlkPlan &pl, VType vt) {
+  if (pl.cl <= 1 || pl.R > 4) return 1;
+  const size_t esz = vt == VType::F64 ? 8 : 4;
+  const int win = window_rows(pl, vt);
+  if (win == 0 || (2 * (size_t)win + 1) * esz > kSptrsvClusterSmemMax) return 1;
+  return pl.cl;
+}
+
+int sptrsv_cluster_supported(const TriBlkPlan &pl, VType vt) {
+  if (cluster_size(pl, vt) <= 1) return 0;
+  BlkPlanDev P = plan_dev(pl, nullptr);
+  P.win = window_rows(pl, vt);
+  BlkArgs a{nullptr, 0, nullptr, 0, 0, 1, nullptr, nullptr, nullptr, pl.max_units, pl.lower, pl.cl};
+  int clusters = 0;
+  cudaError_t e = cudaSuccess;
+  switch (vt) {
+    case VType::F64:
+      e = pl.R == 1 ? cl_launch_l<double, double, 1>(0, P, pl.warps, pl.cl, a, true, &clusters)
+                    : (pl.R == 2 ? cl_launch_l<double, double, 2>(0, P, pl.warps, pl.cl, a, true, &clusters)
+                                 : cl_launch_l<double, double, 4>(0, P, pl.warps, pl.cl, a, true, &clusters));
+      break;
+    default:
+      e = pl.R == 1 ? cl_launch_l<float, float, 1>(0, P, pl.warps, pl.cl, a, true, &clusters)
+                    : (pl.R == 2 ? cl_launch_l<float, float, 2>(0, P, pl.warps, pl.cl, a, true, &clusters)
+                                 : cl_launch_l<float, float, 4>(0, P, pl.warps, pl.cl, a, true, &clusters));
+      break;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return clusters > 0 ? 1 : 0;
+}
+
 void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
                              int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets, int *status,
                              const int *done_flag) {
   BlkPlanDev P = plan_dev(pl, val);
   // rows of a block kept in shared memory: the whole block when it fits
-  const size_t rows = (size_t)pl.cpb * 32 * pl.R;
-  const size_t esz = vt == VType::F64 ? 8 : 4;
-  P.win = rows * esz <= (size_t)kSptrsvSmemMax ? (int)rows : 0;
+  P.win = window_rows(pl, vt);
+  const int cl = cluster_size(pl, vt);
   int grid = pl.grid;
-  if (grid > pl.nblocks) grid = pl.nblocks;
-  if (grid < 1) grid = 1;
+  if (cl > 1) {
+    // whole clusters, at most one per group of cl blocks
+    const int groups = (pl.nblocks + cl - 1) / cl;
+    grid = std::max(1, std::min(groups, std::max(1, grid / cl))) * cl;
+  } else {
+    if (grid > pl.nblocks) grid = pl.nblocks;
+    if (grid < 1) grid = 1;
+  }
   const size_t vec16 = ((size_t)pl.n * (out_f32 ? 4 : 8) + 15) / 16;
   const int fgrid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 4, (vec16 + 255) / 256));
   k_fill_unsolved<<<fgrid, 256, 0, s>>>(x, out_f32, pl.n, vstride, nrhs, done_flag);
-  BlkArgs a{b, in_f32, x, out_f32, vstride, nrhs, tickets, status, done_flag, pl.max_units, pl.lower};
+  BlkArgs a{b, in_f32, x, out_f32, vstride, nrhs, tickets, status, done_flag, pl.max_units, pl.lower, cl};
   switch (vt) {
     case VType::F64: blk_launch_r<double, double>(s, pl.R, P, pl.warps, grid, a); break;
     case VType::F32: blk_launch_r<float, float>(s, pl.R, P, pl.warps, grid, a); break;

@@ -145,6 +145,67 @@ def test_sptrsv_low_precision(lg, torch_cuda, prec, tol):
     assert relmax(z.cpu().numpy(), ref) <= tol
 
 
+def _random_band(n, per_row, band, seed):
+    """Symmetric pattern with per_row random neighbours up to band rows away
+    (a chunk then reads rows of many other chunks and blocks), diagonally
+    dominant."""
+    rng = np.random.default_rng(seed)
+    i = np.repeat(np.arange(n), per_row)
+    j = i - rng.integers(1, band + 1, size=i.shape[0])
+    keep = j >= 0
+    i, j = i[keep], j[keep]
+    v = -rng.uniform(0.1, 1.0, size=i.shape[0])
+    A = P._assemble(n, [i, j, np.arange(n)], [j, i, np.arange(n)], [v, v, np.zeros(n)])
+    # one entry per (row, col)
+    r = np.repeat(np.arange(n), np.diff(A.row))
+    key = r.astype(np.int64) * n + A.col
+    _, first = np.unique(key, return_index=True)
+    first.sort()
+    rows, cols, vals = r[first], A.col[first], A.val[first]
+    diag = np.bincount(rows, weights=np.abs(vals), minlength=n) + 1.0
+    vals = np.where(rows == cols, diag[rows], vals)
+    return P._assemble(n, [rows], [cols], [vals])
+
+
+SCHED_MATS = {
+    "cd16": MATS["cd16"],
+    "cd_20x9x7": MATS["cd_20x9x7"],
+    "aniso77": MATS["aniso77"],
+    "band3000": lambda: _random_band(3000, 2, 200, 5),
+}
+
+
+# (rows per lane, chunks per block, warps, CTAs per cluster)
+SCHEDULES = [(1, 8, 4, 1), (1, 8, 4, 2), (1, 8, 4, 4), (1, 16, 8, 8), (1, 3, 2, 4), (1, 5, 16, 8), (2, 4, 4, 4),
+             (4, 4, 4, 2), (4, 2, 2, 1), (8, 2, 4, 2)]
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-4)])
+@pytest.mark.parametrize("sched", SCHEDULES, ids=lambda s: "R%d_cpb%d_w%d_cl%d" % s)
+@pytest.mark.parametrize("name", list(SCHED_MATS))
+def test_sptrsv_schedules(lg, torch_cuda, name, sched, prec, tol):
+    """Every pinned schedule of the block solve (plain and cluster kernels,
+    blocks that do not divide the chunks, groups that do not fill a cluster,
+    an R = 8 cluster request that runs without one): all four triangles
+    against the oracle's sequential solve, within 1e-12 relative in FP64 and
+    1e-4 in FP32."""
+    A = SCHED_MATS[name]()
+    F = orc.parilu(A.row, A.col, A.val, 2, mode="sync")
+    b = np.random.default_rng(11).standard_normal(A.n)
+    R, cpb, w, cl = sched
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec, rows_per_lane=R, schedule=(cpb, w, cl))
+        ctx.upload(A)
+        ctx.parilu0(2)
+        for which in range(4):
+            xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+            ctx.sptrsv(which, dev(torch_cuda, b), xd)
+            T, lower, unit = _oracle_tri(F, which)
+            ref = orc.trsv(T.ptr, T.idx, T.val, b, lower, unit)
+            err = relmax(xd.cpu().numpy(), ref)
+            assert err <= tol, (which, err)
+
+
 def _true_rel(A, x, b):
     return np.linalg.norm(b - A.matvec(x)) / np.linalg.norm(b)
 
