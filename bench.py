@@ -157,8 +157,13 @@ def run_ours(args):
     bd = torch.tensor(b, dtype=torch.float64, device="cuda")
     xd = torch.zeros(A.n, dtype=torch.float64, device="cuda")
 
+    pin = {}
+    if args.trsv_schedule:
+        R, cpb, w, cl = (int(v) for v in args.trsv_schedule.split(","))
+        pin = {"rows_per_lane": R, "schedule": (cpb, w, cl)}
+
     def solve(prec):
-        ctx.set_options(precision=prec)
+        ctx.set_options(precision=prec, **pin)
         with torch.cuda.stream(stream):
             xd.zero_()
         ctx.parilu0(SWEEPS)
@@ -200,7 +205,7 @@ def run_ours(args):
     # ---- dominant kernel: the preconditioner pair of one FGMRES step (fill +
     # L solve + fill + U solve, FP32 vectors), enqueued back to back on the
     # solver stream and timed there with CUDA events
-    ctx.set_options(precision="fp32")
+    ctx.set_options(precision="fp32", **pin)
     ctx.parilu0(SWEEPS)
     q = torch.randn(A.n, dtype=torch.float64, device="cuda")
     z = torch.empty_like(q)
@@ -222,6 +227,7 @@ def run_ours(args):
     torch.cuda.nvtx.range_pop()
     trsv_s = ev0.elapsed_time(ev1) / 1e3 / reps
     ctx.apply_precond(q, z)  # surfaces a spin-wait timeout of the timed pairs, if any
+    sched = dict(zip(("rows_per_lane", "chunks_per_block", "warps", "cluster"), ctx.trsv_schedule()))
     # SpMV (FP64 operator) alone
     y = torch.empty_like(q)
     for _ in range(3):
@@ -307,7 +313,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "SpTRSV pair of one FGMRES step (L + U, fp32, fills included)",
                      "achieved": trsv_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": trsv_gbs / hbm_peak,
                      "peak_source": peak_src + " (burst copy)", "algorithmic_bytes": ab["sptrsv_pair"],
-                     "traffic": traffic},
+                     "traffic": traffic, "schedule": sched},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks,
@@ -375,6 +381,10 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel pair, if captured")
+    ap.add_argument("--trsv-schedule", default=None,
+                    help="R,chunks,warps,cluster: pin the sync-free solve schedule (the autotune's choice is "
+                         "reported as roofline.schedule) - for profiling the same kernels under ncu, whose "
+                         "launch overhead would change the autotune's choice")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":

@@ -308,6 +308,12 @@ int lace_gpu_spmv(lace_gpu_ctx *ctx, double alpha, const double *x,
 /* z = M^{-1} q with the current factors and options (device FP64) */
 int lace_gpu_apply_precond(lace_gpu_ctx *ctx, const double *q, double *z);
 
+/* The sync-free solve schedule in use, once the first solve has tuned it:
+ * out[0] rows per lane, out[1] chunks per block, out[2] warps per CTA,
+ * out[3] CTAs per thread-block cluster (1: none).  DEV_ERR_NOT_INITIALIZED
+ * before.  No counterpart in LACE. */
+int lace_gpu_get_trsv_schedule(lace_gpu_ctx *ctx, int *out);
+
 /* z = M^{-1} q as one step of the FGMRES cycle applies it, enqueued on the
  * context's stream without waiting: q and z are device vectors in the
  * vector type of the factor precision (float for FP32/BF16 factors, double

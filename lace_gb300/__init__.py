@@ -169,6 +169,7 @@ SIGNATURES = {
     "lace_gpu_spmv": (_i, [_p, _d, _p, _d, _p]),
     "lace_gpu_apply_precond": (_i, [_p, _p, _p]),
     "lace_gpu_precond_enqueue": (_i, [_p, _p, _p]),
+    "lace_gpu_get_trsv_schedule": (_i, [_p, _p]),
     "lace_gpu_parcsrtrsv_noalloc": (_i, [_i, _i, _i, _i, _p, _p, _p, _p, _p, _d, _p, _p]),
     "lace_gpu_sptrsv": (_i, [_p, _i, _p, _p]),
     "lace_gpu_fgmres_householder": (_i, [_p, _p, _p, C.POINTER(GmresParam), C.POINTER(GmresLog),

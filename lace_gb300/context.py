@@ -132,6 +132,13 @@ class Context:
     def apply_precond(self, q, z) -> None:
         _chk(self._lib.lace_gpu_apply_precond(self.h, _ptr(q), _ptr(z)), "apply_precond")
 
+    def trsv_schedule(self) -> tuple:
+        """(rows per lane, chunks per block, warps per CTA, CTAs per cluster)
+        of the sync-free solves, once the first solve has tuned it."""
+        out = (C.c_int * 4)()
+        _chk(self._lib.lace_gpu_get_trsv_schedule(self.h, out), "get_trsv_schedule")
+        return tuple(out)
+
     def precond_enqueue(self, q, z) -> None:
         """z = M^{-1} q as the FGMRES cycle applies it (q, z in the factor
         precision's vector type: float32 unless precision is fp64), enqueued

@@ -483,7 +483,10 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
     c->trsv_tuned = false;
   c->opt = *o;
   c->drop_graphs();
-  if (prec_changed) c->factors_ready = false;
+  if (prec_changed) {
+    c->factors_ready = false;
+    c->trsv_tuned = false;  // the window and the best schedule depend on the value type
+  }
   if (o->trsv_rows_per_lane > 0) c->set_rows_per_lane(o->trsv_rows_per_lane);
   if (o->spmv_lanes > 0) c->lanes = o->spmv_lanes;
   return DEV_SUCCESS;
@@ -1234,6 +1237,16 @@ extern "C" int lace_gpu_precond_enqueue(lace_gpu_ctx *c, const void *q, void *z)
   int rc = c->solve_tri(0, q, f32, c->vec_t.p, f32, false, c->vec_t2.p);
   if (!rc) rc = c->solve_tri(1, c->vec_t.p, f32, z, f32, false, c->vec_t2.p);
   return rc ? set_err(rc) : DEV_SUCCESS;
+}
+
+extern "C" int lace_gpu_get_trsv_schedule(lace_gpu_ctx *c, int *out) {
+  if (!c || !out) return set_err(DEV_ERR_INVALID_PTR);
+  if (!c->trsv_tuned) return set_err(DEV_ERR_NOT_INITIALIZED);
+  out[0] = c->plan_R;
+  out[1] = c->plan_cpb;
+  out[2] = c->plan_warps;
+  out[3] = c->plan_cl;
+  return DEV_SUCCESS;
 }
 
 extern "C" int lace_gpu_apply_precond(lace_gpu_ctx *c, const double *q, double *z) {
