@@ -10,9 +10,11 @@
 #include <cstring>
 #include <limits>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "context.h"
+#include "hostpar.h"
 
 using namespace lace;
 
@@ -108,11 +110,12 @@ bool is_csr(data_storage_t s) {
   return s == Magma_CSR || s == Magma_CUCSR || s == Magma_CSRL || s == Magma_CSRU;
 }
 
-// an output container from the factor pattern and FP64 values on the device
-// (copied straight into the container's array; the stream is synchronised
-// before returning)
-int fill_csr_out_dev(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
-                     const std::vector<int> &idx, const void *dval, int blocksize, cudaStream_t s) {
+// An output container from the factor pattern, in two steps: the host part
+// (allocation, the pattern, the values' pages mapped) needs nothing from the
+// GPU and can run while it works; the FP64 values on the device then go
+// straight into the container's array.
+int prepare_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
+                    const std::vector<int> &idx, int blocksize) {
   release_members(B);
   const int ld = blocksize > 0 ? blocksize * blocksize : 1;
   const size_t nval = idx.size() * ld;
@@ -125,9 +128,11 @@ int fill_csr_out_dev(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int 
   B->col = lace_alloc_filled<int>(idx.size());
   B->val = lace_alloc_filled<double>(nval);
   if (!B->row || !B->col || !B->val) return DEV_ERR_HOST_ALLOC;
-  if (cudaMemcpyAsync(B->val, dval, 8 * nval, cudaMemcpyDeviceToHost, s) != cudaSuccess) return DEV_ERR_UNKNOWN;
-  memcpy(B->row, ptr.data(), 4 * ptr.size());
-  memcpy(B->col, idx.data(), 4 * idx.size());
+  // the values' pages mapped by host threads now, so that the copy into them
+  // runs at full speed (faults taken inside it cost several times more)
+  par_zero(B->val, 8 * nval);
+  par_copy(B->row, ptr.data(), 4 * ptr.size());
+  par_copy(B->col, idx.data(), 4 * idx.size());
   if (blocksize > 0) {
     B->blocksize = blocksize;
     B->ldblock = ld;
@@ -137,8 +142,12 @@ int fill_csr_out_dev(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int 
     B->nnz = (int)idx.size();
   }
   B->true_nnz = B->nnz;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return DEV_ERR_UNKNOWN;
   return 0;
+}
+
+// the values (nval FP64 on the device) into a prepared container; enqueued
+int finish_csr_out(data_d_matrix *B, const void *dval, size_t nval, cudaStream_t s) {
+  return cudaMemcpyAsync(B->val, dval, 8 * nval, cudaMemcpyDeviceToHost, s) == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 
 // mode 0: data_PariLU_v0_3 stop rule (step <= reduction*Ares, <= 20 sweeps,
@@ -201,33 +210,43 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   const int min_sweeps = (mode == 0 && !bcsr && depth + 1 <= 64) ? std::min(depth + 1, maxs) : 0;
   std::vector<double> steps;
   double step = 0.0, nonlin = 0.0;
+  // the output containers' host part is prepared while the GPU sweeps
+  L->diagorder_type = Magma_UNITY;
+  U->diagorder_type = Magma_VALUE;
+  int prep_rc = 0;
+  std::thread prep([&] {
+    prep_rc = prepare_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx,
+                              bcsr ? A->blocksize : 0);
+    if (!prep_rc)
+      prep_rc = prepare_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx,
+                                bcsr ? A->blocksize : 0);
+  });
   auto t0 = std::chrono::steady_clock::now();
   rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol, min_sweeps);
   const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  prep.join();
   if (rc) return fail(rc);
+  if (prep_rc) return fail(prep_rc);
   pc.mark("residuals + sweeps");
   // L values (CSRL order) and U values (CSCU order) as FP64, copied straight
   // into the output containers
   const int ld = bcsr ? A->blocksize * A->blocksize : 1;
   const size_t nl = (size_t)c->nnzL * ld, nu = (size_t)c->nnzU * ld;
-  DBuf tl, tu;
   const void *dl = c->Lv[c->cur].p, *du = c->Ucv[c->cur].p;
   if (c->vtype() != VType::F64) {
-    // FP32 / BF16 factors travel back as LACE's FP64 values
-    if (tl.ensure(8 * nl) || tu.ensure(8 * nu)) return fail(DEV_ERR_DEVICE_ALLOC);
-    launch_convert(c->stream, (int)nl, c->vtype(), dl, VType::F64, tl.p);
-    launch_convert(c->stream, (int)nu, c->vtype(), du, VType::F64, tu.p);
-    dl = tl.p;
-    du = tu.p;
+    // FP32 / BF16 factors travel back as LACE's FP64 values, through the
+    // context's staging buffer (no allocation per call)
+    if (c->stage64.ensure(8 * (nl + nu))) return fail(DEV_ERR_DEVICE_ALLOC);
+    double *tl = (double *)c->stage64.p, *tu = tl + nl;
+    launch_convert(c->stream, (int)nl, c->vtype(), dl, VType::F64, tl);
+    launch_convert(c->stream, (int)nu, c->vtype(), du, VType::F64, tu);
+    dl = tl;
+    du = tu;
   }
   if (cudaGetLastError() != cudaSuccess) return fail(DEV_ERR_UNKNOWN);
-  L->diagorder_type = Magma_UNITY;
-  U->diagorder_type = Magma_VALUE;
-  rc = fill_csr_out_dev(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, dl,
-                        bcsr ? A->blocksize : 0, c->stream);
-  if (!rc)
-    rc = fill_csr_out_dev(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, du,
-                          bcsr ? A->blocksize : 0, c->stream);
+  rc = finish_csr_out(L, dl, nl, c->stream);
+  if (!rc) rc = finish_csr_out(U, du, nu, c->stream);
+  if (!rc && cudaStreamSynchronize(c->stream) != cudaSuccess) rc = DEV_ERR_UNKNOWN;
   if (rc) return fail(rc);
   U->major = MagmaColMajor;
   pc.mark("fill L, U");
@@ -418,15 +437,15 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
     if (rc) return set_err(rc);
     pc.mark("set factors");
   }
-  DBuf db, dx;
-  if (upload_vec(db, b->val, n, c->stream) || upload_vec(dx, x0->val, n, c->stream))
+  // b and x0 in buffers the context keeps (no allocation per call)
+  if (upload_vec(c->dropin_b, b->val, n, c->stream) || upload_vec(c->dropin_x, x0->val, n, c->stream))
     return set_err(DEV_ERR_DEVICE_ALLOC);
   int total = 0;
-  rc = c->fgmres((const double *)db.p, (double *)dx.p, par->search_max, restart_max, par->tol_type,
-                 par->rtol, false, log, &total, nullptr);
+  rc = c->fgmres((const double *)c->dropin_b.p, (double *)c->dropin_x.p, par->search_max, restart_max,
+                 par->tol_type, par->rtol, false, log, &total, nullptr);
   if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
   pc.mark("b, x0 + solve");
-  if (cudaMemcpy(x0->val, dx.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpy(x0->val, c->dropin_x.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
     return set_err(DEV_ERR_UNKNOWN);
   pc.mark("download x");
   log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

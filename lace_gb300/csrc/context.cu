@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "context.h"
+#include "hostpar.h"
 
 namespace lace {
 
@@ -620,9 +621,9 @@ int lace_gpu_ctx::device_anorm() {
 int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lcol, const double *lval,
                                        const int *ucp, const int *uri, const double *ucval) {
   if (bs || nrows != n || (int)hL.ptr.size() != n + 1 || (int)hUc.ptr.size() != n + 1) return 1;
-  if (memcmp(hL.ptr.data(), lrow, 4 * (size_t)(n + 1)) != 0 ||
-      memcmp(hUc.ptr.data(), ucp, 4 * (size_t)(n + 1)) != 0 || lrow[n] != nnzL || ucp[n] != nnzU ||
-      memcmp(hL.idx.data(), lcol, 4 * (size_t)nnzL) != 0 || memcmp(hUc.idx.data(), uri, 4 * (size_t)nnzU) != 0)
+  if (!par_equal(hL.ptr.data(), lrow, 4 * (size_t)(n + 1)) || !par_equal(hUc.ptr.data(), ucp, 4 * (size_t)(n + 1)) ||
+      lrow[n] != nnzL || ucp[n] != nnzU || !par_equal(hL.idx.data(), lcol, 4 * (size_t)nnzL) ||
+      !par_equal(hUc.idx.data(), uri, 4 * (size_t)nnzU))
     return 1;
   int rc = alloc_factor_values();
   if (rc) return rc;
@@ -633,12 +634,15 @@ int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lc
         cudaMemcpyAsync(Ucv[0].p, ucval, 8 * (size_t)nnzU, cudaMemcpyHostToDevice, stream) != cudaSuccess)
       return DEV_ERR_UNKNOWN;
   } else {
-    DBuf tl, tu;
-    if (tl.upload(lval, 8 * (size_t)nnzL, stream) || tu.upload(ucval, 8 * (size_t)nnzU, stream))
-      return DEV_ERR_DEVICE_ALLOC;
-    launch_convert(stream, nnzL, VType::F64, tl.p, t, Lv[0].p);
-    launch_convert(stream, nnzU, VType::F64, tu.p, t, Ucv[0].p);
-    if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;  // before tl, tu go
+    // FP64 values through a staging buffer the context keeps (no allocation
+    // per call), converted on the GPU
+    if (stage64.ensure(8 * (size_t)(nnzL + nnzU))) return DEV_ERR_DEVICE_ALLOC;
+    double *tl = (double *)stage64.p, *tu = tl + nnzL;
+    if (cudaMemcpyAsync(tl, lval, 8 * (size_t)nnzL, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(tu, ucval, 8 * (size_t)nnzU, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      return DEV_ERR_UNKNOWN;
+    launch_convert(stream, nnzL, VType::F64, tl, t, Lv[0].p);
+    launch_convert(stream, nnzU, VType::F64, tu, t, Ucv[0].p);
   }
   rc = finish_factors();  // U's CSR image and L^T, gathered on the GPU
   if (rc) return rc;
@@ -738,8 +742,8 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
   // same pattern as the resident matrix: only the values travel (the
   // analysis - splits, maps, chunk kinds, level sets - is kept)
   const bool same = c->bs == 0 && c->n_blk == n && c->nnzA == nnz && (int)c->hArow.size() == n + 1 &&
-                    memcmp(c->hArow.data(), row, 4 * (size_t)(n + 1)) == 0 &&
-                    memcmp(c->hAcol.data(), col, 4 * (size_t)nnz) == 0;
+                    par_equal(c->hArow.data(), row, 4 * (size_t)(n + 1)) &&
+                    par_equal(c->hAcol.data(), col, 4 * (size_t)nnz);
   int rc = same ? 0 : validate_csr(n, nnz, row, col);
   if (rc) return set_err(rc);
   ++c->aval_version;

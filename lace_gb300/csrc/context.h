@@ -108,6 +108,8 @@ struct lace_gpu_ctx {
   DBuf Vb, Zb, Qmon, vec_w, vec_q, vec_t, vec_t2, vec_r;
   DBuf part_buf, zero_buf;
   DBuf ctrl_buf, cycle_buf, scal_buf, cnt_buf;
+  DBuf stage64;           // FP64 factor values on their way to FP32/BF16
+  DBuf dropin_b, dropin_x;  // right-hand side and solution of the drop-in FGMRES
   lace::Control *h_ctrl = nullptr;
   double *h_scal = nullptr;
   std::map<std::tuple<int, int, int, int, int, int, int, int>, cudaGraphExec_t> graphs;

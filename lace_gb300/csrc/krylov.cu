@@ -787,6 +787,20 @@ void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
     k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (double *)a.q, a.cy, a.ctrl);
 }
 
+// One wave: as many blocks as are resident at once (the passes loop over
+// their row tiles), so no partly filled last wave, and the last block folds
+// few partial sums.  Never more than the ArnoldiArgs grid the partial-sum
+// buffer is sized for.
+template <typename K>
+static int wave_grid(K kernel, int cap) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTPB, 0) != cudaSuccess || per_sm <= 0) {
+    cudaGetLastError();
+    return cap;
+  }
+  return std::max(1, std::min(cap, per_sm * num_sms()));
+}
+
 // dot-product slots per warp for j+1 basis columns
 static int slots_for(int jp1) {
   const int need = (jp1 + 7) / 8;
@@ -798,7 +812,11 @@ static void passA_ns(cudaStream_t s, const ArnoldiArgs &a, int j) {
   OpView op = opview(a);
   const ZT *z = (const ZT *)a.Z + (size_t)j * a.ldz;
   switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
-    case 1: k_passA<1, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
+    case 1: {
+      static const int g = wave_grid(k_passA<1, ZT, NS>, a.grid);
+      k_passA<1, ZT, NS><<<g, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl);
+      break;
+    }
     case 16: k_passA<16, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
     case 32: k_passA<32, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
     default: k_passA<8, ZT, NS><<<a.grid, kTPB, 0, s>>>(a.n, op, z, a.w, a.V, a.ldv, j + 1, a.partials, a.cy, a.ctrl); break;
@@ -820,20 +838,30 @@ void launch_passA(cudaStream_t s, const ArnoldiArgs &a, int j) {
   else passA_t<double>(s, a, j);
 }
 
+template <int NS>
+static void passB_ns(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  static const int g = wave_grid(k_passB<NS>, a.grid);
+  k_passB<NS><<<g, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl);
+}
+
 void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j) {
   switch (slots_for(j + 1)) {
-    case 2: k_passB<2><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
-    case 4: k_passB<4><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
-    case 8: k_passB<8><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
-    default: k_passB<kSlots><<<a.grid, kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.m, a.w, a.partials, a.cy, a.ctrl); break;
+    case 2: passB_ns<2>(s, a, j); break;
+    case 4: passB_ns<4>(s, a, j); break;
+    case 8: passB_ns<8>(s, a, j); break;
+    default: passB_ns<kSlots>(s, a, j); break;
   }
 }
 
 void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
-  if (a.q_f32)
-    k_passC<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl);
-  else
-    k_passC<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (double *)a.q, a.cy, a.ctrl);
+  if (a.q_f32) {
+    static const int g = wave_grid(k_passC<float>, num_sms() * 8);
+    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl);
+  } else {
+    static const int g = wave_grid(k_passC<double>, num_sms() * 8);
+    k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (double *)a.q, a.cy,
+                                                                  a.ctrl);
+  }
 }
 
 void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x) {

@@ -91,7 +91,9 @@ def bcsr(A) -> Mat:
     return M
 
 
-def dense(v) -> Mat:
+def dense(v, copy: bool = True) -> Mat:
+    """A Magma_DENSE column; copy=False wraps a float64 array the call only
+    reads (no copy when it is already contiguous)."""
     v = np.asarray(v, dtype=np.float64)
     M = Mat()
     M.m.storage_type = Magma_DENSE
@@ -100,7 +102,7 @@ def dense(v) -> Mat:
     M.m.nnz = len(v)
     M.m.ld = len(v)
     M.m.major = MagmaColMajor
-    M.m.val = M._own(v.copy(), np.float64)
+    M.m.val = M._own(v.copy() if copy else v, np.float64)
     return M
 
 
@@ -202,7 +204,7 @@ def parilu_mats(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None)
 
 def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
                                rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, single_cycle=False):
-    bv = dense(b)
+    bv = dense(b, copy=False)
     xv = dense(x0)
     par = GmresParam()
     par.search_max = search_max
@@ -218,8 +220,11 @@ def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, sear
     Ur = U.ref if U is not None else None
     fn = f.data_fgmres_householder if single_cycle else f.data_fgmres_householder_restart
     rc = fn(A.ref, bv.ref, xv.ref, Lr, Ur, C.byref(par), C.byref(log))
-    return vector_values(xv), rc, {k: getattr(log, k) for k in ("restarts", "search_directions", "solve_time",
-                                                                "initial_residual", "final_residual")}
+    # the solution is written into x0's array in place: hand that array back
+    own = xv.keep[-1]
+    x = own if xv.m.val == own.ctypes.data else vector_values(xv)
+    return x, rc, {k: getattr(log, k) for k in ("restarts", "search_directions", "solve_time",
+                                                 "initial_residual", "final_residual")}
 
 
 def spmv(alpha: float, A: Mat, x, beta: float = 0.0, y=None):
