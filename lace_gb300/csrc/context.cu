@@ -113,6 +113,14 @@ static void init_from_A(cudaStream_t s, int count, const int *map, const double 
   }
 }
 
+// *diff |= (a differs from b anywhere in count ints)
+__global__ void k_pattern_diff(size_t count, const int *__restrict__ a, const int *__restrict__ b, int *diff) {
+  bool d = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+    d |= a[i] != b[i];
+  if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(diff, 1);
+}
+
 // dLdA_ij = -lambda_i x_j on A's pattern (CSR order)
 __global__ void k_grad_A(int n, const int *__restrict__ row, const int *__restrict__ col,
                          const double *__restrict__ lam, const double *__restrict__ x,
@@ -618,13 +626,46 @@ int lace_gpu_ctx::device_anorm() {
   return 0;
 }
 
+// Whether the caller's host arrays h[k] (count[k] ints) equal the resident
+// device arrays dev[k]: the host arrays go up (about 0.4 ms for A's pattern of
+// the 128^3 system) and are compared on the GPU, instead of against host
+// copies by the CPU.
+int lace_gpu_ctx::same_on_device(int parts, const int *const *h, const int *const *dev, const size_t *count,
+                                 bool *same) {
+  size_t tot = 0;
+  for (int k = 0; k < parts; ++k) tot += count[k];
+  if (pat_stage.ensure(4 * tot + 16)) return DEV_ERR_DEVICE_ALLOC;
+  int *flag = (int *)pat_stage.p, *stage = flag + 4;
+  if (cudaMemsetAsync(flag, 0, 4, stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  size_t off = 0;
+  for (int k = 0; k < parts; ++k) {
+    if (count[k] && cudaMemcpyAsync(stage + off, h[k], 4 * count[k], cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      return DEV_ERR_UNKNOWN;
+    const int grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 8, (count[k] + 255) / 256));
+    if (count[k]) k_pattern_diff<<<grid, 256, 0, stream>>>(count[k], stage + off, dev[k], flag);
+    off += count[k];
+  }
+  int f = 1;
+  if (cudaMemcpyAsync(&f, flag, 4, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return DEV_ERR_UNKNOWN;
+  *same = f == 0;
+  return 0;
+}
+
 int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lcol, const double *lval,
                                        const int *ucp, const int *uri, const double *ucval) {
   if (bs || nrows != n || (int)hL.ptr.size() != n + 1 || (int)hUc.ptr.size() != n + 1) return 1;
-  if (!par_equal(hL.ptr.data(), lrow, 4 * (size_t)(n + 1)) || !par_equal(hUc.ptr.data(), ucp, 4 * (size_t)(n + 1)) ||
-      lrow[n] != nnzL || ucp[n] != nnzU || !par_equal(hL.idx.data(), lcol, 4 * (size_t)nnzL) ||
-      !par_equal(hUc.idx.data(), uri, 4 * (size_t)nnzU))
-    return 1;
+  if (lrow[n] != nnzL || ucp[n] != nnzU) return 1;
+  {
+    const int *h[4] = {lrow, ucp, lcol, uri};
+    const int *d[4] = {(const int *)Lrow.p, (const int *)Ucp.p, (const int *)Lcol.p, (const int *)Uri.p};
+    const size_t cnt[4] = {(size_t)n + 1, (size_t)n + 1, (size_t)nnzL, (size_t)nnzU};
+    bool same = false;
+    const int rc = same_on_device(4, h, d, cnt, &same);
+    if (rc) return rc;
+    if (!same) return 1;
+  }
   int rc = alloc_factor_values();
   if (rc) return rc;
   const VType t = vtype();
@@ -741,9 +782,14 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
   cudaSetDevice(c->device);
   // same pattern as the resident matrix: only the values travel (the
   // analysis - splits, maps, chunk kinds, level sets - is kept)
-  const bool same = c->bs == 0 && c->n_blk == n && c->nnzA == nnz && (int)c->hArow.size() == n + 1 &&
-                    par_equal(c->hArow.data(), row, 4 * (size_t)(n + 1)) &&
-                    par_equal(c->hAcol.data(), col, 4 * (size_t)nnz);
+  bool same = c->bs == 0 && c->n_blk == n && c->nnzA == nnz && (int)c->hArow.size() == n + 1 && row[n] == nnz;
+  if (same) {  // compared with the resident pattern on the GPU
+    const int *h[2] = {row, col};
+    const int *d[2] = {(const int *)c->Arow.p, (const int *)c->Acol.p};
+    const size_t cnt[2] = {(size_t)n + 1, (size_t)nnz};
+    const int rc = c->same_on_device(2, h, d, cnt, &same);
+    if (rc) return set_err(rc);
+  }
   int rc = same ? 0 : validate_csr(n, nnz, row, col);
   if (rc) return set_err(rc);
   ++c->aval_version;

@@ -130,6 +130,8 @@ struct lace_gpu_ctx {
                            const int *ucp, const int *uri, const double *ucval);
   // ||A||_F from the resident values, on the GPU
   int device_anorm();
+  DBuf pat_stage;  // a caller's pattern on its way to be compared with the resident one
+  int same_on_device(int parts, const int *const *h, const int *const *dev, const size_t *count, bool *same);
   std::vector<int> uc2ur_h;  // CSC position of U -> CSR position
   int upload_common(int n_, int nnz_, const int *row, const int *col, int bs_);
   void set_rows_per_lane(int R);

@@ -38,6 +38,29 @@ MATS = {
 }
 
 
+def test_reupload_pattern_check(lg, torch_cuda):
+    """Uploads to one context: a new pattern with the same n and nnz (a 16x4
+    grid after a 4x16 one) is analysed afresh, the same pattern with new
+    values is not; SpMV and the preconditioned solve follow either way."""
+    A1 = P.laplace2d(16, 4)
+    A2 = P.laplace2d(4, 16)
+    assert A1.n == A2.n and len(A1.col) == len(A2.col) and not np.array_equal(A1.col, A2.col)
+    A3 = P.CSR(A2.n, A2.row, A2.col, A2.val * 1.5)
+    x = np.random.default_rng(2).standard_normal(A1.n)
+    with lg.Context(0) as ctx:
+        for A in (A1, A2, A3, A1):
+            ctx.upload(A)
+            y = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+            ctx.spmv(dev(torch_cuda, x), y)
+            assert relmax(y.cpu().numpy(), A.matvec(x)) <= 1e-14
+            ctx.parilu0(2)
+            F = orc.parilu(A.row, A.col, A.val, 2, mode="sync")
+            z = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+            ctx.sptrsv(0, dev(torch_cuda, x), z)
+            ref = orc.trsv(F.L.ptr, F.L.idx, F.L.val, x, True, True)
+            assert relmax(z.cpu().numpy(), ref) <= 1e-12
+
+
 @pytest.mark.parametrize("name", list(MATS))
 @pytest.mark.parametrize("lanes", [0, 2, 4, 8, 16, 32])
 def test_spmv(lg, torch_cuda, name, lanes):
