@@ -429,26 +429,32 @@ __device__ __forceinline__ double2 vcomb8x2(const double *__restrict__ V, size_t
 
 // NS: dot-product slots per warp (8 NS >= j + 1), so that short bases keep
 // few accumulators in registers
+// five blocks per SM for up to 16 basis columns (a few bytes of spill;
+// measured slightly faster than four)
 template <int LPR, typename ZT, int NS>
-__global__ void __launch_bounds__(kTPB) k_passA(int n, OpView op, const ZT *__restrict__ z,
+__global__ void __launch_bounds__(kTPB, NS <= 2 ? 5 : 1) k_passA(int n, OpView op, const ZT *__restrict__ z,
                                                 double *__restrict__ w, const double *__restrict__ V,
                                                 size_t ldv, int jp1, double *partials, Cycle *cy,
                                                 Control *ctrl) {
   if (ctrl->done) return;
-  __shared__ double sw[kTPB];
+  // two tile buffers: a tile's products are written while slower warps still
+  // read the previous tile's, so one barrier per tile
+  __shared__ double swb[2][kTPB];
+  int buf = 0;
   __shared__ double sred[kLdT];
   const int tr = (op.bs == 0) ? kTPB : (kTPB / op.bs) * op.bs;
   double acc[NS];
 #pragma unroll
   for (int sl = 0; sl < NS; ++sl) acc[sl] = 0.0;
-  for (int base = blockIdx.x * tr; base < n; base += gridDim.x * tr) {
+  for (int base = blockIdx.x * tr; base < n; base += gridDim.x * tr, buf ^= 1) {
+    double *sw = swb[buf];
     tile_apply<LPR, ZT>(op, n, base, tr, z, sw);
     __syncthreads();
     for (int t = threadIdx.x; t < tr; t += kTPB)
       if (base + t < n) w[base + t] = sw[t];
     tile_dots<NS>(V, ldv, jp1, n, base, tr, 0, sw, acc);
-    __syncthreads();
   }
+  __syncthreads();
   block_reduce_slots<NS>(acc, jp1, sred);
   __syncthreads();
   for (int k = threadIdx.x; k < jp1; k += kTPB) partials[(size_t)blockIdx.x * kLdT + k] = sred[k];
@@ -481,12 +487,15 @@ __device__ void givens_rot(double a, double b, double tol, double *c, double *s)
   }
 }
 
+// three blocks per SM for up to 32 basis columns (a few bytes of spill; the
+// occupancy matters more: measured 2.8 % faster FGMRES)
 template <int NS>
-__global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict__ V, size_t ldv,
+__global__ void __launch_bounds__(kTPB, NS <= 4 ? 3 : 1) k_passB(int n, const double *__restrict__ V, size_t ldv,
                                                 int j, int m, double *__restrict__ w,
                                                 double *partials, Cycle *cy, Control *ctrl) {
   if (ctrl->done) return;
-  __shared__ double sw[2 * kTPB];
+  __shared__ double swb[2][2 * kTPB];  // two tile buffers, one barrier per tile (as in pass A)
+  int buf = 0;
   __shared__ double sy[kLdT];
   __shared__ double sred[kLdT + 1];
   __shared__ double scratch[kTPB / 32];
@@ -499,7 +508,8 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
   double nrm = 0.0;
   // w -= V y over tiles of 2*kTPB rows (a row pair per thread, 16-byte
   // loads), then the tile's dot products with V for rows > j
-  for (int base = blockIdx.x * 2 * kTPB; base < n; base += gridDim.x * 2 * kTPB) {
+  for (int base = blockIdx.x * 2 * kTPB; base < n; base += gridDim.x * 2 * kTPB, buf ^= 1) {
+    double *sw = swb[buf];
     const int i = base + 2 * threadIdx.x;
     if (i + 1 < n) {
       const double2 wv = *reinterpret_cast<const double2 *>(w + i);
@@ -519,7 +529,6 @@ __global__ void __launch_bounds__(kTPB) k_passB(int n, const double *__restrict_
     __syncthreads();
     tile_dots<NS>(V, ldv, jp1, n, base, kTPB, jp1, sw, acc);
     tile_dots<NS>(V, ldv, jp1, n, base + kTPB, kTPB, jp1, sw + kTPB, acc);
-    __syncthreads();
   }
   block_reduce_slots<NS>(acc, jp1, sred);
   double tot = block_sum(nrm, scratch);
