@@ -1104,8 +1104,13 @@ extern "C" int lace_gpu_spmv(lace_gpu_ctx *c, double alpha, const double *x, dou
 }
 
 // one triangle solve with the configured mode; in/out typed
+bool lace_gpu_ctx::syncfree_blocks() const {
+  return bs == 0 && opt.trsv_mode != LACE_TRSV_LEVELS && opt.trsv_mode != LACE_TRSV_JACOBI &&
+         opt.trsv_mode != LACE_TRSV_NONE;
+}
+
 int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int out_f32,
-                            bool honor_done, void *tmp) {
+                            bool honor_done, void *tmp, bool prefilled) {
   TriDev t = tri(which);
   const VType vt = vtype();
   Control *cb = ctrl();
@@ -1143,7 +1148,8 @@ int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int o
           cudaMemcpyAsync(tmp, b, (size_t)n * (in_f32 ? 4 : 8), cudaMemcpyDeviceToDevice, stream);
           b = tmp;
         }
-        launch_sptrsv_blk(stream, plans[which].dev, t.val, vt, b, in_f32, x, out_f32, cb, which, honor_done);
+        launch_sptrsv_blk(stream, plans[which].dev, t.val, vt, b, in_f32, x, out_f32, cb, which, honor_done,
+                          prefilled && b != x);
       }
   }
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
@@ -1450,6 +1456,9 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
   a.cy = (Cycle *)cycle_buf.p;
   a.ctrl = ctrl();
   a.m = m;
+  a.prefill = syncfree_blocks() ? 1 : 0;
+  a.fill_t = vec_t.p;
+  a.fill_t_f32 = vtype() != VType::F64 ? 1 : 0;
   return a;
 }
 
@@ -1459,8 +1468,9 @@ int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) 
   const int tf32 = vtype() != VType::F64;  // the intermediate vector of the two solves
   for (int j = 0; j < m; ++j) {
     void *zj = (char *)a.Z + (size_t)j * a.ldz * (a.z_f32 ? 4 : 8);
-    int rc = solve_tri(t1, a.q, a.q_f32, vec_t.p, tf32, true, vec_t2.p);
-    if (!rc) rc = solve_tri(t2, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p);
+    // both outputs were marked unsolved by the kernel before (a.prefill)
+    int rc = solve_tri(t1, a.q, a.q_f32, vec_t.p, tf32, true, vec_t2.p, a.prefill != 0);
+    if (!rc) rc = solve_tri(t2, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p, a.prefill != 0);
     if (rc) return rc;
     launch_passA(stream, a, j);
     launch_passB(stream, a, j);

@@ -151,8 +151,10 @@ struct lace_gpu_ctx {
              std::vector<double> *steps, double stop_below = -1.0, int min_sweeps = 0);
   int h_status();
   int ilu_residuals(double *res, double *nonlin);
+  // prefilled: x already holds the unsolved pattern (sync-free block solves)
   int solve_tri(int which, const void *b, int in_f32, void *x, int out_f32, bool honor_done,
-                void *tmp);
+                void *tmp, bool prefilled = false);
+  bool syncfree_blocks() const;  // the solves are the block-scheduled sync-free ones
   int ensure_vectors();
   int ensure_krylov(int m, bool monitor);
   int ensure_AT();

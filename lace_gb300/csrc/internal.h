@@ -93,6 +93,14 @@ struct ArnoldiArgs {
   Cycle *cy = nullptr;
   Control *ctrl = nullptr;
   int m = 0;
+  // The step's two sync-free solves poll their outputs until the unsolved
+  // pattern is gone; with prefill set, the kernel before them (the cycle's
+  // first vector, else pass C of the previous step) writes the pattern into
+  // the L solve's output (fill_t) and the next column of Z as it goes, and the
+  // solves launch without their own fill.
+  int prefill = 0;
+  void *fill_t = nullptr;
+  int fill_t_f32 = 0;
 };
 
 void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x);
@@ -180,11 +188,13 @@ int sptrsv_cluster_supported(const TriBlkPlan &pl, VType vt);
 // gather the plan's values (uvs, uaps, urd) from the triangle's values
 void launch_plan_values(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt);
 // x must not overlap b (x is filled with the unsolved pattern first)
+// prefilled: x already holds the unsolved pattern (no fill launched)
 void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
-                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done);
+                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done,
+                       bool prefilled = false);
 void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
                              int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets, int *status,
-                             const int *done_flag);
+                             const int *done_flag, bool prefilled = false);
 
 // honor_done: return at once when ctrl->done is set (inside an Arnoldi cycle)
 void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,

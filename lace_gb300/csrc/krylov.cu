@@ -341,10 +341,28 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
 }
 
 // V[:,0] = (r + dd e_0)/alpha,  q = -r/dd
+// the unsolved pattern (all ones) into row i of an FP32 or FP64 vector: the
+// sync-free solve that writes the vector polls it until the pattern is gone
+__device__ __forceinline__ void mark_unsolved(void *x, int f32, size_t i) {
+  if (f32) reinterpret_cast<unsigned *>(x)[i] = ~0u;
+  else reinterpret_cast<unsigned long long *>(x)[i] = ~0ull;
+}
+
+// the vectors the next step's two solves write, marked unsolved (null: none)
+struct Prefill {
+  void *t, *z;
+  int t_f32, z_f32;
+};
+
+__device__ __forceinline__ void prefill_row(const Prefill &f, size_t i) {
+  if (f.t) mark_unsolved(f.t, f.t_f32, i);
+  if (f.z) mark_unsolved(f.z, f.z_f32, i);
+}
+
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
                                                      double *__restrict__ V, QT *__restrict__ q,
-                                                     const Cycle *cy, const Control *ctrl) {
+                                                     const Cycle *cy, const Control *ctrl, Prefill pf) {
   if (ctrl->done) return;
   const double dd = cy->dd0, ia = cy->inv_alpha0;
   const double rdd = 1.0 / dd;
@@ -352,6 +370,7 @@ __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__rest
     const double ri = r[i];
     V[i] = (i == 0 ? ri + dd : ri) * ia;
     q[i] = (QT)(-ri * rdd);
+    prefill_row(pf, i);
   }
 }
 
@@ -632,7 +651,7 @@ __global__ void __launch_bounds__(kTPB, NS <= 4 ? 3 : 1) k_passB(int n, const do
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, size_t ldv, int j,
                                                 const double *__restrict__ w, QT *__restrict__ q,
-                                                const Cycle *cy, const Control *ctrl) {
+                                                const Cycle *cy, const Control *ctrl, Prefill pf) {
   if (ctrl->done) return;
   constexpr bool kF32 = sizeof(QT) == 4;
   __shared__ double sc[kLdT];
@@ -662,12 +681,15 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, s
       *reinterpret_cast<double2 *>(q + i) = make_double2(((i == jp1 ? 1.0 : 0.0) - v0 * sc[jp1]) - s.x,
                                                          ((i + 1 == jp1 ? 1.0 : 0.0) - v1 * sc[jp1]) - s.y);
     }
+    prefill_row(pf, i);
+    prefill_row(pf, i + 1);
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // the last row of an odd n
     const int i = n - 1;
     const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
     vn[i] = v;
     q[i] = (QT)(((i == jp1 ? 1.0 : 0.0) - v * sc[jp1]) - vcomb8(V, ldv, i, jp1, sc));
+    prefill_row(pf, i);
   }
 }
 
@@ -789,11 +811,19 @@ void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b
   }
 }
 
+// the outputs of step j's two solves (the L solve's vector and column j of Z)
+static Prefill prefill_for(const ArnoldiArgs &a, int j) {
+  if (!a.prefill || j >= a.m) return Prefill{nullptr, nullptr, 0, 0};
+  void *zj = (char *)a.Z + (size_t)j * a.ldz * (a.z_f32 ? 4 : 8);
+  return Prefill{a.fill_t, zj, a.fill_t_f32, a.z_f32};
+}
+
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
+  const Prefill pf = prefill_for(a, 0);
   if (a.q_f32)
-    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (float *)a.q, a.cy, a.ctrl);
+    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (float *)a.q, a.cy, a.ctrl, pf);
   else
-    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (double *)a.q, a.cy, a.ctrl);
+    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (double *)a.q, a.cy, a.ctrl, pf);
 }
 
 // One wave: as many blocks as are resident at once (the passes loop over
@@ -863,13 +893,15 @@ void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j) {
 }
 
 void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  const Prefill pf = prefill_for(a, j + 1);  // for the next step's solves
   if (a.q_f32) {
     static const int g = wave_grid(k_passC<float>, num_sms() * 8);
-    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl);
+    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl,
+                                                                pf);
   } else {
     static const int g = wave_grid(k_passC<double>, num_sms() * 8);
     k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (double *)a.q, a.cy,
-                                                                  a.ctrl);
+                                                                  a.ctrl, pf);
   }
 }
 

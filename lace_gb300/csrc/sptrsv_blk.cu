@@ -723,7 +723,7 @@ int sptrsv_cluster_supported(const TriBlkPlan &pl, VType vt) {
 
 void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
                              int in_f32, void *x, int out_f32, size_t vstride, int nrhs, int *tickets, int *status,
-                             const int *done_flag) {
+                             const int *done_flag, bool prefilled) {
   BlkPlanDev P = plan_dev(pl, val);
   // rows of a block kept in shared memory: the whole block when it fits
   P.win = window_rows(pl, vt);
@@ -737,9 +737,11 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
     if (grid > pl.nblocks) grid = pl.nblocks;
     if (grid < 1) grid = 1;
   }
-  const size_t vec16 = ((size_t)pl.n * (out_f32 ? 4 : 8) + 15) / 16;
-  const int fgrid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 4, (vec16 + 255) / 256));
-  k_fill_unsolved<<<fgrid, 256, 0, s>>>(x, out_f32, pl.n, vstride, nrhs, done_flag);
+  if (!prefilled) {
+    const size_t vec16 = ((size_t)pl.n * (out_f32 ? 4 : 8) + 15) / 16;
+    const int fgrid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 4, (vec16 + 255) / 256));
+    k_fill_unsolved<<<fgrid, 256, 0, s>>>(x, out_f32, pl.n, vstride, nrhs, done_flag);
+  }
   BlkArgs a{b, in_f32, x, out_f32, vstride, nrhs, tickets, status, done_flag, pl.max_units, pl.lower, cl};
   switch (vt) {
     case VType::F64: blk_launch_r<double, double>(s, pl.R, P, pl.warps, grid, a); break;
@@ -749,9 +751,9 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
 }
 
 void launch_sptrsv_blk(cudaStream_t s, const TriBlkPlan &pl, const void *val, VType vt, const void *b,
-                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done) {
+                       int in_f32, void *x, int out_f32, Control *ctrl, int slot, bool honor_done, bool prefilled) {
   launch_sptrsv_blk_multi(s, pl, val, vt, b, in_f32, x, out_f32, 0, 1, ctrl->tickets[slot], &ctrl->status,
-                          honor_done ? &ctrl->done : nullptr);
+                          honor_done ? &ctrl->done : nullptr, prefilled);
 }
 
 }  // namespace lace
