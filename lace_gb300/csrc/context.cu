@@ -22,6 +22,7 @@
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -166,25 +167,6 @@ void transpose_pattern(const Pattern &P, Pattern &T, std::vector<int> &t2p) {
     }
 }
 
-// chunk kinds for the sync-free solve: 0 = every in-chunk dependency is the
-// previous row in solve order (affine scan), 1 = serial
-void chunk_kinds(const Pattern &T, bool lower, int R, std::vector<uint8_t> &kind) {
-  const int CS = 32 * R;
-  const int n = T.n;
-  const int nch = (n + CS - 1) / CS;
-  kind.assign(nch, 0);
-  for (int i = 0; i < n; ++i) {
-    const int c = i / CS;
-    const int prev = lower ? i - 1 : i + 1;
-    for (int p = T.ptr[i]; p < T.ptr[i + 1]; ++p) {
-      const int j = T.idx[p];
-      if (j == i) continue;
-      if (lower ? j > i : j < i) continue;
-      if (j / CS == c && j != prev) kind[c] = 1;
-    }
-  }
-}
-
 int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int> &lrows) {
   const int n = T.n;
   std::vector<int> lev(n, 0);
@@ -211,7 +193,7 @@ int levels(const Pattern &T, bool lower, std::vector<int> &lptr, std::vector<int
   return nl;
 }
 
-int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
+int build_blk_plan_host(const Pattern &T, bool lower, bool unit, int R, int cpb, HostPlan &hp) {
   if (cpb < 1 || cpb > kBlkMaxUnits) return DEV_ERR_ILLEGAL_VALUE;
   const int n = T.n;
   const int CS = 32 * R;
@@ -249,7 +231,9 @@ int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, Plan
   // stencil and the start of the next) then has its warps take the chunks in
   // the order they become ready; an in-block dependency always has a lower
   // level, so the order stays topological.
-  std::vector<int4> blk(nblk), urec;
+  std::vector<int4> &blk = hp.blk, &urec = hp.urec;
+  blk.assign(nblk, int4{});
+  urec.clear();
   urec.reserve(nch);
   int max_units = 0;
   for (int b = 0; b < nblk; ++b) {
@@ -278,7 +262,12 @@ int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, Plan
   const int S = blk_slots(R);
   const size_t nu = urec.size();
   const size_t rs = nu * (size_t)R * 32;
-  std::vector<int> ucode(rs * S, -1), umap(rs * S, -1), udiag(rs, -1), uprev(rs, -1), uflag(nu * 32, 0);
+  std::vector<int> &ucode = hp.ucode, &umap = hp.umap, &udiag = hp.udiag, &uprev = hp.uprev, &uflag = hp.uflag;
+  ucode.assign(rs * S, -1);
+  umap.assign(rs * S, -1);
+  udiag.assign(rs, -1);
+  uprev.assign(rs, -1);
+  uflag.assign(nu * 32, 0);
   for (size_t u = 0; u < nu; ++u) {
     const int c = urec[u].x;
     const bool serial = kind[c] != 0;
@@ -322,32 +311,45 @@ int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, Plan
         }
       }
   }
+  hp.n = n;
+  hp.nch = nch;
+  hp.R = R;
+  hp.cpb = cpb;
+  hp.lower = lower;
+  hp.unit = unit;
+  hp.max_units = max_units;
+  return 0;
+}
+
+int upload_blk_plan(const HostPlan &hp, PlanBufs &pb, cudaStream_t s) {
+  const int S = blk_slots(hp.R);
+  const size_t nu = hp.urec.size(), rs = nu * (size_t)hp.R * 32;
   int rc = 0;
-  rc |= pb.blk.upload(blk.data(), sizeof(int4) * blk.size(), s);
-  rc |= pb.urec.upload(urec.data(), sizeof(int4) * urec.size(), s);
-  rc |= pb.ucode.upload(ucode.data(), 4 * ucode.size(), s);
-  rc |= pb.umap.upload(umap.data(), 4 * umap.size(), s);
-  rc |= pb.udiag.upload(udiag.data(), 4 * udiag.size(), s);
-  rc |= pb.uprev.upload(uprev.data(), 4 * uprev.size(), s);
-  rc |= pb.uflag.upload(uflag.data(), 4 * uflag.size(), s);
+  rc |= pb.blk.upload(hp.blk.data(), sizeof(int4) * hp.blk.size(), s);
+  rc |= pb.urec.upload(hp.urec.data(), sizeof(int4) * hp.urec.size(), s);
+  rc |= pb.ucode.upload(hp.ucode.data(), 4 * hp.ucode.size(), s);
+  rc |= pb.umap.upload(hp.umap.data(), 4 * hp.umap.size(), s);
+  rc |= pb.udiag.upload(hp.udiag.data(), 4 * hp.udiag.size(), s);
+  rc |= pb.uprev.upload(hp.uprev.data(), 4 * hp.uprev.size(), s);
+  rc |= pb.uflag.upload(hp.uflag.data(), 4 * hp.uflag.size(), s);
   rc |= pb.uvs.ensure(8 * rs * S);
   rc |= pb.uaps.ensure(8 * rs);
   rc |= pb.urd.ensure(8 * rs);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
-  // the host vectors go out of scope: wait for the uploads
+  // the caller's host vectors may go: wait for the uploads
   if (cudaStreamSynchronize(s) != cudaSuccess) return DEV_ERR_UNKNOWN;
   TriBlkPlan &d = pb.dev;
-  d.n = n;
-  d.nchunks = nch;
-  d.nblocks = nblk;
+  d.n = hp.n;
+  d.nchunks = hp.nch;
+  d.nblocks = (int)hp.blk.size();
   d.nunits = (int)nu;
-  d.R = R;
-  d.cpb = cpb;
-  d.lower = lower ? 1 : 0;
-  d.unit = unit ? 1 : 0;
+  d.R = hp.R;
+  d.cpb = hp.cpb;
+  d.lower = hp.lower ? 1 : 0;
+  d.unit = hp.unit ? 1 : 0;
   d.blk = (const int4 *)pb.blk.p;
   d.urec = (const int4 *)pb.urec.p;
-  d.max_units = max_units;
+  d.max_units = hp.max_units;
   d.ucode = (const int *)pb.ucode.p;
   d.umap = (const int *)pb.umap.p;
   d.udiag = (const int *)pb.udiag.p;
@@ -359,6 +361,12 @@ int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, Plan
   pb.vals_version = -1;
   pb.valid = true;
   return 0;
+}
+
+int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
+  HostPlan hp;
+  const int rc = build_blk_plan_host(T, lower, unit, R, cpb, hp);
+  return rc ? rc : upload_blk_plan(hp, pb, s);
 }
 
 }  // namespace lace
@@ -373,7 +381,14 @@ int lace_gpu_ctx::ensure_plan(int which) {
   if (!(pb.valid && pb.dev.R == plan_R && pb.dev.cpb == plan_cpb)) {
     const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
     const bool low[4] = {true, false, true, false};
-    int rc = build_blk_plan(*pats[which], low[which], t.unit != 0, plan_R, plan_cpb, pb, stream);
+    int rc;
+    auto it = prebuilt.find(std::make_tuple(which, plan_R, plan_cpb));
+    if (it != prebuilt.end()) {
+      rc = upload_blk_plan(it->second, pb, stream);
+      prebuilt.erase(it);  // uploaded: its host memory goes
+    } else {
+      rc = build_blk_plan(*pats[which], low[which], t.unit != 0, plan_R, plan_cpb, pb, stream);
+    }
     if (rc) return rc;
   }
   pb.dev.row = t.row;
@@ -581,24 +596,23 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
   rc |= map_ur2uc.upload(ur2uc.data(), 4 * ur2uc.size(), stream);
   rc |= map_lt2l.upload(lt2l.data(), 4 * lt2l.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
-  // level sets of the four triangles (level-scheduled option + reporting)
+  // level sets of the four triangles (level-scheduled option, sweep caps),
+  // one host thread each
   const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
   const bool low[4] = {true, false, true, false};
+  std::vector<int> lp[4], lr[4];
+  {
+    std::thread th[4];
+    for (int t = 0; t < 4; ++t) th[t] = std::thread([&, t] { nlevels[t] = levels(*pats[t], low[t], lp[t], lr[t]); });
+    for (auto &x : th) x.join();
+  }
   for (int t = 0; t < 4; ++t) {
-    std::vector<int> lp, lr;
-    nlevels[t] = levels(*pats[t], low[t], lp, lr);
-    rc |= lvl_ptr[t].upload(lp.data(), 4 * lp.size(), stream);
-    rc |= lvl_rows[t].upload(lr.data(), 4 * lr.size(), stream);
-    // ready flags: one per chunk at the smallest chunk size; zero = never set
-    const int maxch = (L.n + 31) / 32 + 1;
+    rc |= lvl_ptr[t].upload(lp[t].data(), 4 * lp[t].size(), stream);
+    rc |= lvl_rows[t].upload(lr[t].data(), 4 * lr[t].size(), stream);
+    // ready flags of the BCSR solve: one per block row; zero = never set
+    const int maxch = L.n + 1;
     rc |= ready[t].ensure(4 * (size_t)maxch);
     if (!rc) cudaMemsetAsync(ready[t].p, 0, 4 * (size_t)maxch, stream);
-    for (int ri = 0; ri < 4; ++ri) {
-      const int R = 1 << ri;
-      std::vector<uint8_t> k;
-      chunk_kinds(*pats[t], low[t], R, k);
-      rc |= kinds[t][ri].upload(k.data(), k.size(), stream);
-    }
   }
   // the epochs of the new ready arrays restart with the zeroed flags
   Control zero;
@@ -750,9 +764,6 @@ TriDev lace_gpu_ctx::tri(int which) const {
   t.n = bs ? n_blk * bs : n_blk;
   t.slot = which;
   t.ready = (int *)ready[which].p;
-  int ri = 0;
-  while ((1 << ri) < rows_per_lane) ++ri;
-  t.kind = (const uint8_t *)kinds[which][ri].p;
   t.rows_per_lane = rows_per_lane;
   t.nchunks = (n_blk + 32 * rows_per_lane - 1) / (32 * rows_per_lane);
   t.lvl_ptr = (const int *)lvl_ptr[which].p;
@@ -1203,8 +1214,47 @@ int lace_gpu_ctx::autotune_trsv() {
     cands = keep;
   }
   const int nch_min = (n + 31) / 32;
-  for (auto cd : cands) {
-    if (cd.cpb > 1 && cd.cpb * 32 * cd.R > 2 * n) continue;  // one block would hold everything
+  // one block would hold everything
+  cands.erase(std::remove_if(cands.begin(), cands.end(),
+                             [&](const Cand &c) { return c.cpb > 1 && c.cpb * 32 * c.R > 2 * n && cands.size() > 1; }),
+              cands.end());
+  // The host halves of the candidates' plans (L and U) are built in parallel
+  // ahead of their turn, in batches of about 4 GB of host memory.
+  const size_t plan_bytes = (size_t)n * 48 + ((size_t)1 << 20);
+  const size_t batch = std::max<size_t>(2, std::min<size_t>(16, ((size_t)4 << 30) / plan_bytes));
+  // candidates of one plan shape next to each other: the plan is built once
+  std::stable_sort(cands.begin(), cands.end(),
+                   [](const Cand &a, const Cand &b) { return a.R != b.R ? a.R < b.R : a.cpb < b.cpb; });
+  auto have = [&](int w, int R, int cpb) {
+    return prebuilt.count(std::make_tuple(w, R, cpb)) || (plans[w].valid && plans[w].dev.R == R && plans[w].dev.cpb == cpb);
+  };
+  auto prebuild_from = [&](size_t first) {
+    std::vector<std::tuple<int, int, int>> keys;
+    for (size_t c = first; c < cands.size() && keys.size() < batch; ++c)
+      for (int w = 0; w < 2; ++w) {
+        const auto k = std::make_tuple(w, cands[c].R, cands[c].cpb);
+        if (!have(w, cands[c].R, cands[c].cpb) && std::find(keys.begin(), keys.end(), k) == keys.end())
+          keys.push_back(k);
+      }
+    std::vector<HostPlan *> out;
+    for (auto &k : keys) out.push_back(&prebuilt[k]);  // map nodes stay put
+    const Pattern *pats[2] = {&hL, &hU};
+    std::vector<int> err(keys.size(), 0);
+    std::vector<std::thread> th;
+    for (size_t i = 0; i < keys.size(); ++i)
+      th.emplace_back([&, i] {
+        const int w = std::get<0>(keys[i]);
+        err[i] = build_blk_plan_host(*pats[w], w == 0, w == 0, std::get<1>(keys[i]), std::get<2>(keys[i]), *out[i]);
+      });
+    for (auto &x : th) x.join();
+    for (int e : err)
+      if (e) return e;
+    return 0;
+  };
+  for (size_t ci = 0; ci < cands.size(); ++ci) {
+    Cand cd = cands[ci];
+    if (!have(0, cd.R, cd.cpb) || !have(1, cd.R, cd.cpb))
+      if ((rc = prebuild_from(ci))) return rc;
     plan_R = cd.R;
     plan_cpb = cd.cpb;
     plan_warps = cd.w;
@@ -1247,6 +1297,7 @@ int lace_gpu_ctx::autotune_trsv() {
     }
   }
   (void)nch_min;
+  prebuilt.clear();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   plan_R = bR;

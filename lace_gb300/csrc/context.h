@@ -38,8 +38,19 @@ struct PlanBufs {
   const void *vals_src = nullptr;
 };
 
+// host part of a plan (what build_blk_plan_host fills, upload_blk_plan sends)
+struct HostPlan {
+  int n = 0, nch = 0, R = 1, cpb = 1, max_units = 0;
+  bool lower = true, unit = false;
+  std::vector<int4> blk, urec;
+  std::vector<int> ucode, umap, udiag, uprev, uflag;
+};
+
 // host construction of a plan: chunks of 32*R rows, blocks of cpb chunks (in
-// solve order), chunks of a block in wavefront-level order, cross-block requirements
+// solve order), chunks of a block in wavefront-level order, cross-block
+// requirements; then its upload
+int build_blk_plan_host(const Pattern &T, bool lower, bool unit, int R, int cpb, HostPlan &hp);
+int upload_blk_plan(const HostPlan &hp, PlanBufs &pb, cudaStream_t s);
 int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s);
 
 extern thread_local int g_last_error;
@@ -90,7 +101,6 @@ struct lace_gpu_ctx {
   int fact_version = 0;  // bumped whenever the factor values change
 
   // SpTRSV per triangle (0 L, 1 U, 2 U^T, 3 L^T)
-  DBuf kinds[4][4];  // [triangle][log2 rows-per-lane]
   DBuf ready[4];
   DBuf lvl_ptr[4], lvl_rows[4];
   int nlevels[4] = {0, 0, 0, 0};
@@ -99,6 +109,8 @@ struct lace_gpu_ctx {
   lace::PlanBufs plans[4];
   int plan_R = 4, plan_cpb = 1, plan_warps = 1, plan_cl = 1;  // autotuned schedule shape
   int ensure_plan(int which);
+  // host plans the autotune built in parallel, keyed (triangle, R, chunks per block)
+  std::map<std::tuple<int, int, int>, lace::HostPlan> prebuilt;
   int lanes = 8;
 
   // Krylov workspace

@@ -45,7 +45,6 @@ struct TriDev {
   const void *val = nullptr;  // double / float / bf16 per precision
   int lower = 1;
   int unit = 0;
-  const uint8_t *kind = nullptr;  // per chunk: 0 scan, 1 serial
   int rows_per_lane = 4;
   int nchunks = 0;
   int *ready = nullptr;
@@ -197,8 +196,6 @@ void launch_sptrsv_blk_multi(cudaStream_t s, const TriBlkPlan &pl, const void *v
                              const int *done_flag, bool prefilled = false);
 
 // honor_done: return at once when ctrl->done is set (inside an Arnoldi cycle)
-void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
-                            void *x, int out_f32, Control *ctrl, int grid_hint, bool honor_done);
 void launch_sptrsv_levels(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
                           void *x, int out_f32, Control *ctrl, bool honor_done);
 // one synchronous Jacobi sweep y_new = D^{-1}(b - (T - D) y_old); step partial sums

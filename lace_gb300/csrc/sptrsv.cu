@@ -4,18 +4,12 @@
 // (src/fgmres_householder_restart.cpp:320-332); the Jacobi sweep replaces
 // data_parcsrtrsv (src/trisolve.cpp:256-351) in synchronous form.
 //
-// Sync-free solve.  Rows are grouped into chunks of 32*R consecutive rows;
-// one warp owns a chunk, lane l the R consecutive rows l*R .. l*R+R-1 (in
-// solve direction).  Warps take chunks in dependency order from an atomic
-// ticket, so a warp only ever waits for chunks already held by running
-// warps: no co-residency assumption, no deadlock.  Dependencies on other
-// chunks are waited for through a per-chunk ready flag (acquire/release,
-// bounded spin).  Inside a chunk, when every row depends on no row of its own
-// chunk except the previous one ("scan" chunks - e.g. the x-lines of a
-// lexicographic stencil), the chunk is solved as a first-order linear
-// recurrence x_p = a_p x_{p-1} + b_p with a warp-wide affine scan; other
-// chunks ("serial" chunks) are resolved position by position with shuffles.
-// Flags carry an epoch that advances every launch, so they are never reset.
+// Here: the level-scheduled solve, the Jacobi sweeps and the BCSR solve (the
+// default CSR solve, block-scheduled and sync-free, is in sptrsv_blk.cu).  The
+// BCSR solve takes block rows in dependency order from an atomic ticket, so a
+// warp only ever waits for block rows already held by running warps, and
+// waits for them through per-block-row ready flags (acquire/release, bounded
+// spin) that carry an epoch advancing every launch, so they are never reset.
 #include "internal.h"
 
 namespace lace {
@@ -55,182 +49,6 @@ __device__ __forceinline__ void wait_flag(const int *flag, int epoch, int *statu
       return;
     }
     if (spins > 64) __nanosleep(64);
-  }
-}
-
-template <typename CT, typename VT, int R, bool LOWER>
-__global__ void __launch_bounds__(kSTPB) k_sptrsv_sf(int n, int nchunks, const int *__restrict__ row,
-                                                     const int *__restrict__ col,
-                                                     const VT *__restrict__ val, int unit,
-                                                     const void *b, int in_f32, void *x, int out_f32,
-                                                     const uint8_t *__restrict__ kind, int *ready,
-                                                     int *tickets, int *epoch_slot, const int *done_flag,
-                                                     int *status) {
-  if (done_flag != nullptr && *(volatile const int *)done_flag) return;
-  constexpr int CS = 32 * R;
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int epoch = *(volatile int *)epoch_slot + 1;
-  while (true) {
-    int t = 0;
-    if (lane == 0) t = atomicAdd(&tickets[0], 1);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= nchunks) break;
-    const int c = LOWER ? t : nchunks - 1 - t;
-    const int base = c * CS;
-    const int cnt = min(CS, n - base);
-    const bool serial = kind[c] != 0;
-    CT A[R], B[R], X[R];
-    int rows[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int pos = lane * R + r;
-      A[r] = (CT)1;  // identity map for positions beyond the chunk end
-      B[r] = (CT)0;
-      rows[r] = -1;
-      if (pos >= cnt) continue;
-      const int i = LOWER ? base + pos : base + cnt - 1 - pos;
-      rows[r] = i;
-      const int prev = LOWER ? i - 1 : i + 1;
-      CT acc = ldin<CT>(b, in_f32, i);
-      CT d = (CT)1, ap = (CT)0;
-      for (int e = row[i]; e < row[i + 1]; ++e) {
-        const int jc = col[e];
-        if (jc == i) {
-          if (!unit) d = cvt<CT>(val[e]);
-          continue;
-        }
-        if (LOWER ? (jc > i) : (jc < i)) continue;  // other triangle: not part of T
-        const int cj = jc / CS;
-        if (cj == c) {
-          // same chunk: the previous position is folded into the scan; any
-          // other in-chunk dependency makes this a serial chunk (below)
-          if (!serial && pos > 0 && jc == prev) ap = cvt<CT>(val[e]);
-          continue;
-        }
-        wait_flag(&ready[cj], epoch, status);
-        acc -= cvt<CT>(val[e]) * ldx<CT>(x, out_f32, jc);
-      }
-      if (!serial) {
-        A[r] = -ap / d;
-        B[r] = acc / d;
-      } else {
-        A[r] = d;    // serial path keeps (acc, d)
-        B[r] = acc;
-      }
-    }
-    if (!serial) {
-      // lane-local composition of its R maps, then an inclusive warp scan:
-      // (a2,b2) o (a1,b1) = (a2 a1, a2 b1 + b2)
-      CT ca = (CT)1, cb = (CT)0;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        cb = A[r] * cb + B[r];
-        ca = A[r] * ca;
-      }
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const CT pa = __shfl_up_sync(0xffffffffu, ca, o);
-        const CT pb = __shfl_up_sync(0xffffffffu, cb, o);
-        if (lane >= o) {
-          cb = ca * pb + cb;
-          ca = ca * pa;
-        }
-      }
-      // value entering this lane = x at the last position of the previous lane
-      CT xin = __shfl_up_sync(0xffffffffu, cb, 1);
-      if (lane == 0) xin = (CT)0;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        xin = A[r] * xin + B[r];
-        X[r] = xin;
-      }
-    } else {
-      // position-by-position: the owner finalises x_p, broadcasts it, and
-      // every later position subtracts its coefficient on row(p)
-      for (int p = 0; p < cnt; ++p) {
-        const int owner = p / R, rr = p % R;
-        CT xp = (CT)0;
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-          if (lane == owner && r == rr) xp = B[r] / A[r];
-        xp = __shfl_sync(0xffffffffu, xp, owner);
-        const int rowp = LOWER ? base + p : base + cnt - 1 - p;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int pos = lane * R + r;
-          if (pos == p) X[r] = xp;
-          if (pos > p && pos < cnt) {
-            const int i = rows[r];
-            for (int e = row[i]; e < row[i + 1]; ++e)
-              if (col[e] == rowp) B[r] -= cvt<CT>(val[e]) * xp;
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (rows[r] >= 0) stout<CT>(x, out_f32, rows[r], X[r]);
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) st_release(&ready[c], epoch);
-  }
-  // the warp that leaves last re-arms the tickets and publishes the epoch
-  if (lane == 0) {
-    const int e = atomicAdd(&tickets[1], 1);
-    if (e == nwarps - 1) {
-      tickets[0] = 0;
-      tickets[1] = 0;
-      *epoch_slot = epoch;
-      __threadfence();
-    }
-  }
-}
-
-template <typename CT, typename VT, int R>
-static void sf_launch(cudaStream_t s, const TriDev &t, const void *b, int in_f32, void *x,
-                      int out_f32, const int *ctrl, int *tickets, int *epoch_slot, int *status,
-                      int grid) {
-  if (t.lower)
-    k_sptrsv_sf<CT, VT, R, true><<<grid, kSTPB, 0, s>>>(t.n, t.nchunks, t.row, t.col, (const VT *)t.val,
-                                                        t.unit, b, in_f32, x, out_f32, t.kind, t.ready,
-                                                        tickets, epoch_slot, ctrl, status);
-  else
-    k_sptrsv_sf<CT, VT, R, false><<<grid, kSTPB, 0, s>>>(t.n, t.nchunks, t.row, t.col, (const VT *)t.val,
-                                                         t.unit, b, in_f32, x, out_f32, t.kind, t.ready,
-                                                         tickets, epoch_slot, ctrl, status);
-}
-
-template <typename CT, typename VT>
-static void sf_launch_r(cudaStream_t s, const TriDev &t, const void *b, int in_f32, void *x,
-                        int out_f32, const int *ctrl, int *tickets, int *epoch_slot, int *status,
-                        int grid) {
-  switch (t.rows_per_lane) {
-    case 1: sf_launch<CT, VT, 1>(s, t, b, in_f32, x, out_f32, ctrl, tickets, epoch_slot, status, grid); break;
-    case 2: sf_launch<CT, VT, 2>(s, t, b, in_f32, x, out_f32, ctrl, tickets, epoch_slot, status, grid); break;
-    case 8: sf_launch<CT, VT, 8>(s, t, b, in_f32, x, out_f32, ctrl, tickets, epoch_slot, status, grid); break;
-    default: sf_launch<CT, VT, 4>(s, t, b, in_f32, x, out_f32, ctrl, tickets, epoch_slot, status, grid); break;
-  }
-}
-
-// the control block carries the tickets / epochs; a stand-alone call (no
-// Arnoldi control) still needs one, so the caller always passes a Control
-void launch_sptrsv_syncfree(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
-                            void *x, int out_f32, Control *ctrl, int grid_hint, bool honor_done) {
-  int *tickets = ctrl->tickets[t.slot];
-  int *epoch_slot = &ctrl->trsv_epoch[t.slot];
-  int *status = &ctrl->status;
-  int warps_needed = t.nchunks;
-  int grid = grid_hint > 0 ? grid_hint : num_sms() * 8;
-  int maxgrid = (warps_needed * 32 + kSTPB - 1) / kSTPB;
-  if (grid > maxgrid) grid = maxgrid;
-  if (grid < 1) grid = 1;
-  // a stand-alone solve must not skip on a finished Arnoldi cycle
-  const int *skip = honor_done ? &ctrl->done : nullptr;
-  switch (vt) {
-    case VType::F64: sf_launch_r<double, double>(s, t, b, in_f32, x, out_f32, skip, tickets, epoch_slot, status, grid); break;
-    case VType::F32: sf_launch_r<float, float>(s, t, b, in_f32, x, out_f32, skip, tickets, epoch_slot, status, grid); break;
-    case VType::BF16: sf_launch_r<float, __nv_bfloat16>(s, t, b, in_f32, x, out_f32, skip, tickets, epoch_slot, status, grid); break;
   }
 }
 
