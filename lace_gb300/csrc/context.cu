@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <thread>
 #include <tuple>
@@ -137,17 +138,34 @@ __global__ void k_grad_A(int n, const int *__restrict__ row, const int *__restri
 int validate_csr(int n, int nnz, const int *row, const int *col) {
   if (n < 0 || nnz < 0) return DEV_ERR_ILLEGAL_VALUE;
   if (row[0] != 0 || row[n] != nnz) return DEV_ERR_ILLEGAL_VALUE;
-  for (int i = 0; i < n; ++i) {
-    if (row[i + 1] < row[i]) return DEV_ERR_ILLEGAL_VALUE;
-    bool diag = false;
-    for (int p = row[i]; p < row[i + 1]; ++p) {
-      if (col[p] < 0 || col[p] >= n) return DEV_ERR_ILLEGAL_VALUE;
-      if (p > row[i] && col[p] <= col[p - 1]) return DEV_ERR_NOT_SUPPORTED;  // unsorted / duplicate
-      if (col[p] == i) diag = true;
+  // rows checked in parallel ranges; the first faulty row decides the code
+  std::mutex mu;
+  int bad_row = n, bad_code = 0;
+  par_for((size_t)n, 65536, [&](size_t b, size_t e) {
+    for (int i = (int)b; i < (int)e; ++i) {
+      int code = 0;
+      if (row[i + 1] < row[i]) {
+        code = DEV_ERR_ILLEGAL_VALUE;
+      } else {
+        bool diag = false;
+        for (int p = row[i]; p < row[i + 1] && !code; ++p) {
+          if (col[p] < 0 || col[p] >= n) code = DEV_ERR_ILLEGAL_VALUE;
+          else if (p > row[i] && col[p] <= col[p - 1]) code = DEV_ERR_NOT_SUPPORTED;  // unsorted / duplicate
+          else if (col[p] == i) diag = true;
+        }
+        if (!code && !diag) code = DEV_ERR_NOT_SUPPORTED;  // ParILU needs every diagonal entry
+      }
+      if (code) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (i < bad_row) {
+          bad_row = i;
+          bad_code = code;
+        }
+        return;
+      }
     }
-    if (!diag) return DEV_ERR_NOT_SUPPORTED;  // ParILU needs every diagonal entry
-  }
-  return 0;
+  });
+  return bad_code;
 }
 
 void transpose_pattern(const Pattern &P, Pattern &T, std::vector<int> &t2p) {
@@ -520,46 +538,71 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
 // upload + analysis
 // ======================================================================
 
+// wall time of setup phases, printed when the context is verbose
+struct SetupClock {
+  bool on;
+  std::chrono::steady_clock::time_point t;
+  explicit SetupClock(bool on_) : on(on_), t(std::chrono::steady_clock::now()) {}
+  void mark(const char *what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    printf("%% setup %-30s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
+  SetupClock sc(verbose);
   n_blk = n_;
   bs = bs_;
-  Pattern A;
-  A.n = n_;
-  A.ptr.assign(row, row + n_ + 1);
-  A.idx.assign(col, col + row[n_]);
-  // L = strict lower + diagonal last (CSRL), U = diagonal + upper (CSRU)
+  // L = strict lower + diagonal last (CSRL), U = diagonal + upper (CSRU):
+  // counted per row, then filled, both over parallel row ranges
   Pattern L, Ur;
   L.n = Ur.n = n_;
   L.ptr.assign(n_ + 1, 0);
   Ur.ptr.assign(n_ + 1, 0);
-  std::vector<int> l2a, ur2a;
+  par_for((size_t)n_, 65536, [&](size_t b, size_t e) {
+    for (int i = (int)b; i < (int)e; ++i) {
+      int cl = 1, cu = 0;  // the unit diagonal of L
+      for (int p = row[i]; p < row[i + 1]; ++p) {
+        if (col[p] < i) ++cl;
+        else ++cu;
+      }
+      L.ptr[i + 1] = cl;
+      Ur.ptr[i + 1] = cu;
+    }
+  });
   for (int i = 0; i < n_; ++i) {
-    int dpos = -1;
-    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
-      const int j = A.idx[p];
-      if (j < i) {
-        L.idx.push_back(j);
-        l2a.push_back(p);
-      } else if (j == i) {
-        dpos = p;
-      }
-    }
-    L.idx.push_back(i);
-    l2a.push_back(-1);  // unit diagonal
-    L.ptr[i + 1] = (int)L.idx.size();
-    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
-      const int j = A.idx[p];
-      if (j > i || p == dpos) {
-        Ur.idx.push_back(j);
-        ur2a.push_back(p);
-      }
-    }
-    Ur.ptr[i + 1] = (int)Ur.idx.size();
+    L.ptr[i + 1] += L.ptr[i];
+    Ur.ptr[i + 1] += Ur.ptr[i];
   }
+  std::vector<int> l2a(L.ptr[n_]), ur2a(Ur.ptr[n_]);
+  L.idx.resize(L.ptr[n_]);
+  Ur.idx.resize(Ur.ptr[n_]);
+  par_for((size_t)n_, 65536, [&](size_t b, size_t e) {
+    for (int i = (int)b; i < (int)e; ++i) {
+      int ql = L.ptr[i], qu = Ur.ptr[i];
+      for (int p = row[i]; p < row[i + 1]; ++p) {
+        const int j = col[p];
+        if (j < i) {
+          L.idx[ql] = j;
+          l2a[ql++] = p;
+        } else {
+          Ur.idx[qu] = j;
+          ur2a[qu++] = p;
+        }
+      }
+      L.idx[ql] = i;
+      l2a[ql] = -1;  // unit diagonal
+    }
+  });
+  sc.mark("L/U split");
   int rc = analyse_factors(L, Ur);
   if (rc) return rc;
   std::vector<int> uc2a(hUc.idx.size());
-  for (size_t q = 0; q < uc2a.size(); ++q) uc2a[q] = ur2a[uc2ur_h[q]];
+  par_for(uc2a.size(), 1 << 20, [&](size_t b, size_t e) {
+    for (size_t q = b; q < e; ++q) uc2a[q] = ur2a[uc2ur_h[q]];
+  });
   rc |= map_l2a.upload(l2a.data(), 4 * l2a.size(), stream);
   rc |= map_uc2a.upload(uc2a.data(), 4 * uc2a.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
@@ -570,32 +613,39 @@ int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
 // factor patterns L (CSRL) and U (CSRU) -> CSC of U, L^T, maps, chunk kinds,
 // level sets, ready flags
 int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
+  SetupClock sc(verbose);
   Pattern Uc, Lt;
   std::vector<int> lt2l;
-  transpose_pattern(Ur, Uc, uc2ur_h);
-  transpose_pattern(L, Lt, lt2l);
+  {  // the two transposes on two host threads
+    std::thread tu([&] { transpose_pattern(Ur, Uc, uc2ur_h); });
+    transpose_pattern(L, Lt, lt2l);
+    tu.join();
+  }
+  sc.mark("transposes");
   std::vector<int> ur2uc(uc2ur_h.size());
   for (size_t q = 0; q < uc2ur_h.size(); ++q) ur2uc[uc2ur_h[q]] = (int)q;
   nnzL = (int)L.idx.size();
   nnzU = (int)Ur.idx.size();
   hL = L;
   hU = Ur;
-  hUc = Uc;
-  hLt = Lt;
+  hUc = std::move(Uc);
+  hLt = std::move(Lt);
+  sc.mark("maps, pattern copies");
   map_ur2uc_el.free();
   for (auto &pb : plans) pb.valid = false;
   int rc = 0;
   rc |= Lrow.upload(L.ptr.data(), 4 * L.ptr.size(), stream);
   rc |= Lcol.upload(L.idx.data(), 4 * L.idx.size(), stream);
-  rc |= Ucp.upload(Uc.ptr.data(), 4 * Uc.ptr.size(), stream);
-  rc |= Uri.upload(Uc.idx.data(), 4 * Uc.idx.size(), stream);
+  rc |= Ucp.upload(hUc.ptr.data(), 4 * hUc.ptr.size(), stream);
+  rc |= Uri.upload(hUc.idx.data(), 4 * hUc.idx.size(), stream);
   rc |= Urow.upload(Ur.ptr.data(), 4 * Ur.ptr.size(), stream);
   rc |= Ucol.upload(Ur.idx.data(), 4 * Ur.idx.size(), stream);
-  rc |= Ltp.upload(Lt.ptr.data(), 4 * Lt.ptr.size(), stream);
-  rc |= Lti.upload(Lt.idx.data(), 4 * Lt.idx.size(), stream);
+  rc |= Ltp.upload(hLt.ptr.data(), 4 * hLt.ptr.size(), stream);
+  rc |= Lti.upload(hLt.idx.data(), 4 * hLt.idx.size(), stream);
   rc |= map_ur2uc.upload(ur2uc.data(), 4 * ur2uc.size(), stream);
   rc |= map_lt2l.upload(lt2l.data(), 4 * lt2l.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
+  sc.mark("pattern uploads");
   // level sets of the four triangles (level-scheduled option, sweep caps),
   // one host thread each
   const Pattern *pats[4] = {&hL, &hU, &hUc, &hLt};
@@ -614,6 +664,7 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
     rc |= ready[t].ensure(4 * (size_t)maxch);
     if (!rc) cudaMemsetAsync(ready[t].p, 0, 4 * (size_t)maxch, stream);
   }
+  sc.mark("level sets");
   // the epochs of the new ready arrays restart with the zeroed flags
   Control zero;
   memset(&zero, 0, sizeof(zero));
@@ -811,16 +862,22 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
     if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) ||
         c->Acol.upload(col, 4 * (size_t)nnz, c->stream) || c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
       return set_err(DEV_ERR_DEVICE_ALLOC);
+    SetupClock sc(c->verbose);
     rc = c->upload_common(n, nnz, row, col, 0);
     if (rc) return set_err(rc);
+    sc.mark("analysis");
     c->hArow.assign(row, row + n + 1);
     c->hAcol.assign(col, col + nnz);
+    sc.mark("host copy of the pattern");
   }
   c->factors_ready = false;
   rc = c->device_anorm();
   if (rc) return set_err(rc);
   c->AT_ready = false;
-  return c->autotune_spmv();
+  SetupClock sc(c->verbose && !same);
+  rc = c->autotune_spmv();
+  sc.mark("SpMV autotune");
+  return rc;
 }
 
 extern "C" int lace_gpu_upload_csr_device(lace_gpu_ctx *c, int n, int nnz, const int *row,
@@ -1414,25 +1471,31 @@ int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
 int lace_gpu_ctx::ensure_sell() {
   if (bs || (int)hArow.size() != n + 1) return 0;  // CSR uploads only
   if (!sell_valid) {
+    // slice widths, their offsets, then the slices, over parallel ranges
     const int nsl = (n + 31) / 32;
     std::vector<int> ptr(nsl + 1, 0);
-    for (int s = 0; s < nsl; ++s) {
-      int w = 0;
-      for (int i = 32 * s; i < std::min(n, 32 * s + 32); ++i) w = std::max(w, hArow[i + 1] - hArow[i]);
-      ptr[s + 1] = ptr[s] + 32 * w;
-    }
-    std::vector<int> col(std::max(1, ptr[nsl])), map(std::max(1, ptr[nsl]), -1);
-    for (int s = 0; s < nsl; ++s)
-      for (int l = 0; l < 32; ++l) {
-        const int i = 32 * s + l;
-        const int w = (ptr[s + 1] - ptr[s]) / 32;
-        for (int t = 0; t < w; ++t) {
-          const int q = ptr[s] + 32 * t + l;
-          const bool in = i < n && t < hArow[i + 1] - hArow[i];
-          col[q] = in ? hAcol[hArow[i] + t] : 0;
-          map[q] = in ? hArow[i] + t : -1;
-        }
+    par_for((size_t)nsl, 8192, [&](size_t b, size_t e) {
+      for (int s = (int)b; s < (int)e; ++s) {
+        int w = 0;
+        for (int i = 32 * s; i < std::min(n, 32 * s + 32); ++i) w = std::max(w, hArow[i + 1] - hArow[i]);
+        ptr[s + 1] = 32 * w;
       }
+    });
+    for (int s = 0; s < nsl; ++s) ptr[s + 1] += ptr[s];
+    std::vector<int> col(std::max(1, ptr[nsl])), map(std::max(1, ptr[nsl]), -1);
+    par_for((size_t)nsl, 8192, [&](size_t b, size_t e) {
+      for (int s = (int)b; s < (int)e; ++s)
+        for (int l = 0; l < 32; ++l) {
+          const int i = 32 * s + l;
+          const int w = (ptr[s + 1] - ptr[s]) / 32;
+          for (int t = 0; t < w; ++t) {
+            const int q = ptr[s] + 32 * t + l;
+            const bool in = i < n && t < hArow[i + 1] - hArow[i];
+            col[q] = in ? hAcol[hArow[i] + t] : 0;
+            map[q] = in ? hArow[i] + t : -1;
+          }
+        }
+    });
     int rc = 0;
     rc |= sell_ptr.upload(ptr.data(), 4 * ptr.size(), stream);
     rc |= sell_col.upload(col.data(), 4 * col.size(), stream);
@@ -1541,10 +1604,14 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
                          std::vector<double> *hist) {
   if (m < 1 || m > kMaxM) return DEV_ERR_NOT_SUPPORTED;
   if (!factors_ready && opt.trsv_mode != LACE_TRSV_NONE) return DEV_ERR_NOT_INITIALIZED;
+  SetupClock sc(verbose);
   int rc = ensure_krylov(m, opt.monitor_orthog != 0);
+  sc.mark("Krylov workspace");
   if (!rc) rc = autotune_trsv();
+  sc.mark("SpTRSV autotune");
   if (!rc && adjoint) rc = ensure_AT();
   if (!rc && !adjoint) rc = ensure_sell();
+  sc.mark("operator (A^T or sliced ELL)");
   // solve plans are built on the host: before any graph capture
   if (!rc && !bs && opt.trsv_mode == LACE_TRSV_SYNCFREE) {
     rc = ensure_plan(adjoint ? 2 : 0);
@@ -1580,6 +1647,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     if (opt.use_graph) {
       auto it = graphs.find(key);
       if (it == graphs.end()) {
+        SetupClock gc(verbose);
         cudaGraph_t g;
         LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         rc = enqueue_cycle_body(a, m, adjoint);
@@ -1589,10 +1657,12 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
           return rc;
         }
         LCHK(ce);
+        gc.mark("cycle graph capture");
         cudaGraphExec_t ge;
         ce = cudaGraphInstantiate(&ge, g, 0);
         cudaGraphDestroy(g);
         LCHK(ce);
+        gc.mark("cycle graph instantiation");
         it = graphs.emplace(key, ge).first;
       }
       LCHK(cudaGraphLaunch(it->second, stream));

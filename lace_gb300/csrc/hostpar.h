@@ -42,6 +42,27 @@ void par_ranges(size_t bytes, F f) {
   for (auto &x : th) x.join();
 }
 
+// f(begin, end) over [0, count) cut into one range per thread (`grain`
+// items per thread at least), the calling thread taking the first
+template <typename F>
+void par_for(size_t count, size_t grain, F f) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::max<size_t>(1, std::min<size_t>({(size_t)16, (size_t)hw, count / std::max<size_t>(1, grain)}));
+  if (nt <= 1) {
+    if (count) f((size_t)0, count);
+    return;
+  }
+  const size_t per = (count + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (size_t t = 1; t < nt; ++t) {
+    const size_t b = per * t;
+    if (b >= count) break;
+    th.emplace_back(f, b, std::min(count, b + per));
+  }
+  f((size_t)0, std::min(count, per));
+  for (auto &x : th) x.join();
+}
+
 inline bool par_equal(const void *a, const void *b, size_t bytes) {
   const int nt = host_threads(bytes);
   std::vector<char> diff(nt + 1, 0);
