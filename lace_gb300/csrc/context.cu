@@ -1449,10 +1449,12 @@ int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
   // column on the same memory channels
   ldv = ((size_t)n + 31) / 32 * 32 + 32;
   const size_t vbytes = 8 * ldv * (size_t)(m + 1), zbytes = (zf32 ? 4 : 8) * ldv * (size_t)m;
-  if (m > ws_m || zf32 != ws_zf32 || Vb.bytes < vbytes || Zb.bytes < zbytes) {
+  const size_t vfbytes = zf32 ? 4 * ldv * (size_t)(m + 1) : 0;
+  if (m > ws_m || zf32 != ws_zf32 || Vb.bytes < vbytes || Zb.bytes < zbytes || Vfb.bytes < vfbytes) {
     drop_graphs();
     rc |= Vb.ensure(vbytes);
     rc |= Zb.ensure(zbytes);
+    if (zf32) rc |= Vfb.ensure(vfbytes);
     if (rc) return DEV_ERR_DEVICE_ALLOC;
     ws_m = m;
     ws_zf32 = zf32;
@@ -1559,6 +1561,7 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
   a.lanes = lanes;
   a.V = (double *)Vb.p;
   a.ldv = ldv;
+  a.Vf = vtype() != VType::F64 ? (float *)Vfb.p : nullptr;
   a.Z = Zb.p;
   a.ldz = ldv;
   a.z_f32 = ws_zf32 ? 1 : 0;

@@ -117,7 +117,7 @@ struct lace_gpu_ctx {
   int ws_m = 0;
   bool ws_zf32 = false;
   size_t ldv = 0;
-  DBuf Vb, Zb, Qmon, vec_w, vec_q, vec_t, vec_t2, vec_r;
+  DBuf Vb, Vfb, Zb, Qmon, vec_w, vec_q, vec_t, vec_t2, vec_r;
   DBuf part_buf, zero_buf;
   DBuf ctrl_buf, cycle_buf, scal_buf, cnt_buf;
   DBuf stage64;           // FP64 factor values on their way to FP32/BF16

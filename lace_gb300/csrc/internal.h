@@ -81,6 +81,10 @@ struct ArnoldiArgs {
   const double *sell_val = nullptr;
   double *V = nullptr;   // reflectors, n x (m+1) column-major
   size_t ldv = 0;
+  // the reflectors again in FP32 (rounded toward zero, same leading
+  // dimension), when the next Krylov vector q is FP32: pass C forms q from
+  // them, reading half the bytes; null otherwise
+  float *Vf = nullptr;
   void *Z = nullptr;     // preconditioned vectors, n x m (float or double)
   size_t ldz = 0;
   int z_f32 = 0;

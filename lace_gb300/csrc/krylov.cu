@@ -341,6 +341,18 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
 }
 
 // V[:,0] = (r + dd e_0)/alpha,  q = -r/dd
+// FP64 -> FP32 with integer operations, rounding toward zero (the FP64 unit,
+// which also converts, is the scarce one).  Finite values only: below the
+// FP32 normal range they become 0, above it NaN.
+__device__ __forceinline__ float dtof_rz(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  const unsigned m = ((hi & 0xfffffu) << 3) | ((unsigned)b >> 29);
+  const unsigned mag = e <= 0 ? 0u : (e >= 255 ? 0x7fc00000u : (((unsigned)e << 23) | m));
+  return __uint_as_float((hi & 0x80000000u) | mag);
+}
+
 // the unsolved pattern (all ones) into row i of an FP32 or FP64 vector: the
 // sync-free solve that writes the vector polls it until the pattern is gone
 __device__ __forceinline__ void mark_unsolved(void *x, int f32, size_t i) {
@@ -361,14 +373,17 @@ __device__ __forceinline__ void prefill_row(const Prefill &f, size_t i) {
 
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
-                                                     double *__restrict__ V, QT *__restrict__ q,
-                                                     const Cycle *cy, const Control *ctrl, Prefill pf) {
+                                                     double *__restrict__ V, float *__restrict__ Vf,
+                                                     QT *__restrict__ q, const Cycle *cy, const Control *ctrl,
+                                                     Prefill pf) {
   if (ctrl->done) return;
   const double dd = cy->dd0, ia = cy->inv_alpha0;
   const double rdd = 1.0 / dd;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double ri = r[i];
-    V[i] = (i == 0 ? ri + dd : ri) * ia;
+    const double v = (i == 0 ? ri + dd : ri) * ia;
+    V[i] = v;
+    if (Vf) Vf[i] = dtof_rz(v);
     q[i] = (QT)(-ri * rdd);
     prefill_row(pf, i);
   }
@@ -389,33 +404,22 @@ __device__ __forceinline__ double vcomb8(const double *__restrict__ V, size_t ld
   return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
 }
 
-// FP64 -> FP32 with integer operations, rounding toward zero (the FP64 unit,
-// which also converts, is the scarce one).  Finite values only: below the
-// FP32 normal range they become 0, above it NaN.
-__device__ __forceinline__ float dtof_rz(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-  const unsigned m = ((hi & 0xfffffu) << 3) | ((unsigned)b >> 29);
-  const unsigned mag = e <= 0 ? 0u : (e >= 255 ? 0x7fc00000u : (((unsigned)e << 23) | m));
-  return __uint_as_float((hi & 0x80000000u) | mag);
-}
 
-// rows i, i+1 (i even): sum_k V[k][i..i+1] c[k] in FP32 (V converted with
-// dtof_rz), for vectors that only feed the FP32 preconditioner
-__device__ __forceinline__ float2 vcomb8x2f(const double *__restrict__ V, size_t ldv, int i, int ncols,
+// rows i, i+1 (i even): sum_k Vf[k][i..i+1] c[k] in FP32 from the FP32 copy
+// of the reflectors, for vectors that only feed the FP32 preconditioner
+__device__ __forceinline__ float2 vcomb8x2f(const float *__restrict__ Vf, size_t ldv, int i, int ncols,
                                            const float *c) {
   float2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   for (int k = 0; k < ncols; k += 8) {
-    double2 v[8];
+    float2 v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u)
-      if (k + u < ncols) v[u] = __ldg(reinterpret_cast<const double2 *>(V + (size_t)(k + u) * ldv + i));
+      if (k + u < ncols) v[u] = __ldg(reinterpret_cast<const float2 *>(Vf + (size_t)(k + u) * ldv + i));
 #pragma unroll
     for (int u = 0; u < 8; ++u)
       if (k + u < ncols) {
-        a[u & 3].x = fmaf(dtof_rz(v[u].x), c[k + u], a[u & 3].x);
-        a[u & 3].y = fmaf(dtof_rz(v[u].y), c[k + u], a[u & 3].y);
+        a[u & 3].x = fmaf(v[u].x, c[k + u], a[u & 3].x);
+        a[u & 3].y = fmaf(v[u].y, c[k + u], a[u & 3].y);
       }
   }
   return make_float2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
@@ -649,9 +653,10 @@ __global__ void __launch_bounds__(kTPB, NS <= 4 ? 3 : 1) k_passB(int n, const do
 // FP32 q (mixed precision: q only feeds the FP32 preconditioner, which
 // rounds it to FP32 on its first read) the combination runs in FP32.
 template <typename QT>
-__global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, size_t ldv, int j,
-                                                const double *__restrict__ w, QT *__restrict__ q,
-                                                const Cycle *cy, const Control *ctrl, Prefill pf) {
+__global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, float *__restrict__ Vf,
+                                                size_t ldv, int j, const double *__restrict__ w,
+                                                QT *__restrict__ q, const Cycle *cy, const Control *ctrl,
+                                                Prefill pf) {
   if (ctrl->done) return;
   constexpr bool kF32 = sizeof(QT) == 4;
   __shared__ double sc[kLdT];
@@ -672,10 +677,11 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, s
     const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? wv.y + dd : wv.y) * ia : 0.0;
     *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
     if constexpr (kF32) {
-      const float2 s = vcomb8x2f(V, ldv, i, jp1, scf);
-      *reinterpret_cast<float2 *>(q + i) =
-          make_float2(((i == jp1 ? 1.f : 0.f) - dtof_rz(v0) * scf[jp1]) - s.x,
-                      ((i + 1 == jp1 ? 1.f : 0.f) - dtof_rz(v1) * scf[jp1]) - s.y);
+      const float2 vf = make_float2(dtof_rz(v0), dtof_rz(v1));
+      *reinterpret_cast<float2 *>(Vf + (size_t)jp1 * ldv + i) = vf;  // the FP32 copy of v_{j+1}
+      const float2 s = vcomb8x2f(Vf, ldv, i, jp1, scf);
+      *reinterpret_cast<float2 *>(q + i) = make_float2(((i == jp1 ? 1.f : 0.f) - vf.x * scf[jp1]) - s.x,
+                                                       ((i + 1 == jp1 ? 1.f : 0.f) - vf.y * scf[jp1]) - s.y);
     } else {
       const double2 s = vcomb8x2(V, ldv, i, jp1, sc);
       *reinterpret_cast<double2 *>(q + i) = make_double2(((i == jp1 ? 1.0 : 0.0) - v0 * sc[jp1]) - s.x,
@@ -688,6 +694,7 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, s
     const int i = n - 1;
     const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
     vn[i] = v;
+    if (kF32) Vf[(size_t)jp1 * ldv + i] = dtof_rz(v);
     q[i] = (QT)(((i == jp1 ? 1.0 : 0.0) - v * sc[jp1]) - vcomb8(V, ldv, i, jp1, sc));
     prefill_row(pf, i);
   }
@@ -821,9 +828,9 @@ static Prefill prefill_for(const ArnoldiArgs &a, int j) {
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
   const Prefill pf = prefill_for(a, 0);
   if (a.q_f32)
-    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (float *)a.q, a.cy, a.ctrl, pf);
+    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.Vf, (float *)a.q, a.cy, a.ctrl, pf);
   else
-    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, (double *)a.q, a.cy, a.ctrl, pf);
+    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, nullptr, (double *)a.q, a.cy, a.ctrl, pf);
 }
 
 // One wave: as many blocks as are resident at once (the passes loop over
@@ -896,12 +903,12 @@ void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
   const Prefill pf = prefill_for(a, j + 1);  // for the next step's solves
   if (a.q_f32) {
     static const int g = wave_grid(k_passC<float>, num_sms() * 8);
-    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (float *)a.q, a.cy, a.ctrl,
-                                                                pf);
+    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.Vf, a.ldv, j, a.w, (float *)a.q, a.cy,
+                                                                a.ctrl, pf);
   } else {
     static const int g = wave_grid(k_passC<double>, num_sms() * 8);
-    k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, j, a.w, (double *)a.q, a.cy,
-                                                                  a.ctrl, pf);
+    k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, nullptr, a.ldv, j, a.w, (double *)a.q,
+                                                                  a.cy, a.ctrl, pf);
   }
 }
 
