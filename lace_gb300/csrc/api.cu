@@ -145,6 +145,37 @@ int prepare_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n
   return 0;
 }
 
+// The output containers' host part for L (CSRL) and U (CSCU) of the
+// context's factor patterns, on two host threads (each spreading its bulk
+// work further), running while the GPU works.
+struct OutPrep {
+  std::thread tl, tu;
+  int rcl = 0, rcu = 0;
+  double ms = 0.0;
+  std::chrono::steady_clock::time_point t0;
+  bool started = false;
+  void start(data_d_matrix *L, data_d_matrix *U, const lace_gpu_ctx *c, bool bcsr, int n, int blocksize) {
+    L->diagorder_type = Magma_UNITY;
+    U->diagorder_type = Magma_VALUE;
+    t0 = std::chrono::steady_clock::now();
+    tl = std::thread([this, L, c, bcsr, n, blocksize] {
+      rcl = prepare_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, blocksize);
+    });
+    tu = std::thread([this, U, c, bcsr, n, blocksize] {
+      rcu = prepare_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, blocksize);
+    });
+    started = true;
+  }
+  int join() {
+    if (tl.joinable()) tl.join();
+    if (tu.joinable()) tu.join();
+    if (started) ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    started = false;
+    return rcl ? rcl : rcu;
+  }
+  ~OutPrep() { join(); }
+};
+
 // the values (nval FP64 on the device) into a prepared container; enqueued
 int finish_csr_out(data_d_matrix *B, const void *dval, size_t nval, cudaStream_t s) {
   return cudaMemcpyAsync(B->val, dval, 8 * nval, cudaMemcpyDeviceToHost, s) == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
@@ -169,7 +200,23 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   PhaseClock pc(c->verbose, "parilu");
   const bool bcsr = A->storage_type == Magma_BCSR;
   const int n = A->num_rows;
-  if (bcsr) {
+  OutPrep prep;
+  // The common case, the pattern the context already holds: checked first
+  // (on the GPU), so that the output containers can be prepared from the
+  // start, while A's values go up and the GPU sweeps.
+  bool known = false;
+  if (!bcsr && is_csr(A->storage_type) && c->bs == 0 && c->n_blk == n && c->nnzA == A->row[n] &&
+      (int)c->hArow.size() == n + 1 && (int)c->hL.ptr.size() == n + 1 && c->hL.idx.size() == (size_t)c->nnzL) {
+    const int *h[2] = {A->row, A->col};
+    const int *d[2] = {(const int *)c->Arow.p, (const int *)c->Acol.p};
+    const size_t cnt[2] = {(size_t)n + 1, (size_t)A->row[n]};
+    rc = c->same_on_device(2, h, d, cnt, &known);
+    if (rc) return fail(rc);
+  }
+  if (known) {
+    prep.start(L, U, c, false, n, 0);
+    rc = c->upload_values_same_pattern(A->val);
+  } else if (bcsr) {
     const int bs = A->blocksize;
     const int nblk = A->numblocks > 0 ? A->numblocks : A->row[n];
     rc = lace_gpu_upload_bcsr_host(c, n, bs, nblk, A->row, A->col, A->val);
@@ -210,23 +257,15 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   const int min_sweeps = (mode == 0 && !bcsr && depth + 1 <= 64) ? std::min(depth + 1, maxs) : 0;
   std::vector<double> steps;
   double step = 0.0, nonlin = 0.0;
-  // the output containers' host part is prepared while the GPU sweeps
-  L->diagorder_type = Magma_UNITY;
-  U->diagorder_type = Magma_VALUE;
-  int prep_rc = 0;
-  std::thread prep([&] {
-    prep_rc = prepare_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx,
-                              bcsr ? A->blocksize : 0);
-    if (!prep_rc)
-      prep_rc = prepare_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx,
-                                bcsr ? A->blocksize : 0);
-  });
+  // a new pattern: the output containers are prepared while the GPU sweeps
+  if (!known) prep.start(L, U, c, bcsr, n, bcsr ? A->blocksize : 0);
   auto t0 = std::chrono::steady_clock::now();
   rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol, min_sweeps);
   const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  prep.join();
+  const int prep_rc = prep.join();
   if (rc) return fail(rc);
   if (prep_rc) return fail(prep_rc);
+  if (c->verbose) printf("%% parilu (output containers prepared in %.2f ms)\n", prep.ms);
   pc.mark("residuals + sweeps");
   // L values (CSRL order) and U values (CSCU order) as FP64, copied straight
   // into the output containers

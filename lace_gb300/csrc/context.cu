@@ -681,9 +681,8 @@ int lace_gpu_ctx::device_anorm() {
   const size_t ld = bs ? (size_t)bs * bs : 1;
   const size_t count = (size_t)nnzA * ld;
   double *partials = (double *)part_ensure();
-  const void *z = zeros(count);
-  if (!partials || !z) return DEV_ERR_DEVICE_ALLOC;
-  launch_sqdiff(stream, (int)count, Aval.p, z, 0, partials, (int *)cnt_buf.p + 8, (double *)scal_buf.p + 8);
+  if (!partials) return DEV_ERR_DEVICE_ALLOC;
+  launch_sumsq(stream, count, (const double *)Aval.p, partials, (int *)cnt_buf.p + 8, (double *)scal_buf.p + 8);
   if (cudaMemcpyAsync(h_scal + 8, (double *)scal_buf.p + 8, 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
       cudaStreamSynchronize(stream) != cudaSuccess)
     return DEV_ERR_UNKNOWN;
@@ -838,6 +837,18 @@ int lace_gpu_ctx::upload_common(int n_, int nnz_, const int *hrow, const int *hc
   return 0;
 }
 
+// new values for the resident CSR pattern (the caller has checked that the
+// pattern is the same): the analysis, plans and maps are kept
+int lace_gpu_ctx::upload_values_same_pattern(const double *val) {
+  ++aval_version;
+  if (Aval.upload(val, 8 * (size_t)nnzA, stream)) return DEV_ERR_DEVICE_ALLOC;
+  factors_ready = false;
+  const int rc = device_anorm();
+  if (rc) return rc;
+  AT_ready = false;
+  return autotune_spmv();
+}
+
 extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const int *row,
                                         const int *col, const double *val) {
   if (!c || !row || (nnz > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
@@ -852,12 +863,14 @@ extern "C" int lace_gpu_upload_csr_host(lace_gpu_ctx *c, int n, int nnz, const i
     const int rc = c->same_on_device(2, h, d, cnt, &same);
     if (rc) return set_err(rc);
   }
-  int rc = same ? 0 : validate_csr(n, nnz, row, col);
+  if (same) {
+    const int rc = c->upload_values_same_pattern(val);
+    return rc ? set_err(rc) : DEV_SUCCESS;
+  }
+  int rc = validate_csr(n, nnz, row, col);
   if (rc) return set_err(rc);
   ++c->aval_version;
-  if (same) {
-    if (c->Aval.upload(val, 8 * (size_t)nnz, c->stream)) return set_err(DEV_ERR_DEVICE_ALLOC);
-  } else {
+  {
     c->sell_valid = false;
     if (c->Arow.upload(row, 4 * (size_t)(n + 1), c->stream) ||
         c->Acol.upload(col, 4 * (size_t)nnz, c->stream) || c->Aval.upload(val, 8 * (size_t)nnz, c->stream))
@@ -924,13 +937,8 @@ extern "C" int lace_gpu_update_values_device(lace_gpu_ctx *c, const double *val)
   LCHK(cudaMemcpyAsync(c->Aval.p, val, 8 * (size_t)c->nnzA * ld, cudaMemcpyDeviceToDevice, c->stream));
   ++c->aval_version;
   // ||A||_F on the device
-  double *partials = (double *)c->part_ensure();
-  if (!partials) return set_err(DEV_ERR_DEVICE_ALLOC);
-  launch_sqdiff(c->stream, (int)(c->nnzA * ld), c->Aval.p, c->zeros(c->nnzA * ld), 0, partials,
-                (int *)c->cnt_buf.p + 8, (double *)c->scal_buf.p + 8);
-  LCHK(cudaMemcpyAsync(c->h_scal + 8, (double *)c->scal_buf.p + 8, 8, cudaMemcpyDeviceToHost, c->stream));
-  LCHK(cudaStreamSynchronize(c->stream));
-  c->anorm = std::sqrt(c->h_scal[8]);
+  const int rc = c->device_anorm();
+  if (rc) return set_err(rc);
   c->factors_ready = false;
   c->AT_ready = false;
   return DEV_SUCCESS;
@@ -940,14 +948,6 @@ void *lace_gpu_ctx::part_ensure() {
   const size_t need = sizeof(double) * (size_t)(num_sms() * 16 + 8) * kLdT;
   if (part_buf.ensure(need)) return nullptr;
   return part_buf.p;
-}
-
-const void *lace_gpu_ctx::zeros(size_t count) {
-  if (zero_buf.bytes < count * 8) {
-    if (zero_buf.ensure(count * 8)) return nullptr;
-    cudaMemsetAsync(zero_buf.p, 0, count * 8, stream);
-  }
-  return zero_buf.p;
 }
 
 int lace_gpu_ctx::autotune_spmv() {
@@ -1129,12 +1129,12 @@ int lace_gpu_ctx::ilu_residuals(double *res, double *nonlin) {
   if (bs || !factors_ready) return DEV_ERR_NOT_SUPPORTED;
   IluArgs a = ilu_args();
   const VType t = vtype();
-  double *d = (double *)scal_buf.p + 40;
-  launch_ilu_residual(stream, a, t, Lv[cur].p, Ucv[cur].p, d);
-  launch_lu_fro(stream, a, t, (const int *)Urow.p, (const int *)Ucol.p, Lv[cur].p, Urv.p, Ucv[cur].p, d + 2);
-  LCHK(cudaMemcpyAsync(h_scal + 40, d, 4 * 8, cudaMemcpyDeviceToHost, stream));
+  // one kernel: ||LU||^2, sum over S(A) of (LU)_ij^2 and of (LU - A)_ij^2
+  double *d = (double *)scal_buf.p + 42;
+  launch_lu_fro(stream, a, t, (const int *)Urow.p, (const int *)Ucol.p, Lv[cur].p, Urv.p, Ucv[cur].p, d);
+  LCHK(cudaMemcpyAsync(h_scal + 42, d, 3 * 8, cudaMemcpyDeviceToHost, stream));
   LCHK(cudaStreamSynchronize(stream));
-  const double nl2 = h_scal[40], fro = h_scal[42], onS = h_scal[43];
+  const double fro = h_scal[42], onS = h_scal[43], nl2 = h_scal[44];
   if (nonlin) *nonlin = std::sqrt(nl2);
   if (res) *res = std::sqrt(std::max(0.0, nl2 + fro - onS));
   return 0;

@@ -118,7 +118,7 @@ struct lace_gpu_ctx {
   bool ws_zf32 = false;
   size_t ldv = 0;
   DBuf Vb, Vfb, Zb, Qmon, vec_w, vec_q, vec_t, vec_t2, vec_r;
-  DBuf part_buf, zero_buf;
+  DBuf part_buf;
   DBuf ctrl_buf, cycle_buf, scal_buf, cnt_buf;
   DBuf stage64;           // FP64 factor values on their way to FP32/BF16
   DBuf dropin_b, dropin_x;  // right-hand side and solution of the drop-in FGMRES
@@ -146,11 +146,11 @@ struct lace_gpu_ctx {
   int same_on_device(int parts, const int *const *h, const int *const *dev, const size_t *count, bool *same);
   std::vector<int> uc2ur_h;  // CSC position of U -> CSR position
   int upload_common(int n_, int nnz_, const int *row, const int *col, int bs_);
+  int upload_values_same_pattern(const double *val);
   void set_rows_per_lane(int R);
   lace::TriDev tri(int which) const;
   lace::VType vtype() const;
   void *part_ensure();
-  const void *zeros(size_t count);
   int autotune_spmv();
   int autotune_trsv();
   int alloc_factor_values();

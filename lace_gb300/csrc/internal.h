@@ -135,7 +135,7 @@ void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *
 // out2 = {||LU||_F^2, sum over S(A) of (LU)_ij^2}; Urow/Ucol/Ur: U in CSR,
 // a.Ucp/a.Uri + Uc: U in CSC (same values)
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
-                   const void *L, const void *Ur, const void *Uc, double *out2);
+                   const void *L, const void *Ur, const void *Uc, double *out3);
 // the sliced-ELL values of the operator: dst[q] = map[q] >= 0 ? src[map[q]] : 0
 void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst);
 // gather: dst[p] = src[perm[p]] with type conversion
@@ -212,6 +212,8 @@ void launch_bcsr_sptrsv(cudaStream_t s, const TriDev &t, int bs, VType vt, const
                         int grid_hint, bool honor_done);
 
 // *out = sum (a_i - b_i)^2 (typed by f32), deterministic grid reduction
+// sum of squares of count FP64 values into *out (partials: grid-sized scratch)
+void launch_sumsq(cudaStream_t s, size_t count, const double *a, double *partials, int *counter, double *out);
 void launch_sqdiff(cudaStream_t s, int n, const void *a, const void *b, int f32, double *partials,
                    int *counter, double *out);
 

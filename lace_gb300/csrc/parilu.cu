@@ -139,12 +139,12 @@ __global__ void __launch_bounds__(kPTPB) k_ilu_residual(
 // 389-398) without forming LU:  res^2 = sum_S (LU-A)^2 + ||LU||^2 - sum_S LU^2.
 template <typename FT, typename CT>
 __global__ void __launch_bounds__(kPTPB) k_lu_fro(
-    int n, const int *__restrict__ Arow, const int *__restrict__ Acol, const int *__restrict__ Lrow,
-    const int *__restrict__ Lcol, const FT *__restrict__ L, const int *__restrict__ Urow,
-    const int *__restrict__ Ucol, const FT *__restrict__ Ur, const int *__restrict__ Ucp,
-    const int *__restrict__ Uri, const FT *__restrict__ Uc, double *partials, int *counter,
-    double *out2) {
-  double fro = 0.0, onS = 0.0;
+    int n, const int *__restrict__ Arow, const int *__restrict__ Acol, const double *__restrict__ Aval,
+    const int *__restrict__ Lrow, const int *__restrict__ Lcol, const FT *__restrict__ L,
+    const int *__restrict__ Urow, const int *__restrict__ Ucol, const FT *__restrict__ Ur,
+    const int *__restrict__ Ucp, const int *__restrict__ Uri, const FT *__restrict__ Uc, double *partials,
+    int *counter, double *out3) {
+  double fro = 0.0, onS = 0.0, nl = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int lb = Lrow[i], le = Lrow[i + 1];
     for (int a = lb; a < le; ++a) {
@@ -189,42 +189,48 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
         }
       }
       onS = fma(t, t, onS);
+      const double d = t - Aval[p];  // the nonlinear residual's entry, from the same product
+      nl = fma(d, d, nl);
     }
   }
-  // two sums: fold each through the deterministic last-block protocol
+  // three sums: fold each through the deterministic last-block protocol
   double t1 = block_sum_p(fro);
   double t2 = block_sum_p(onS);
+  double t3 = block_sum_p(nl);
   if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = t1;
-    partials[2 * blockIdx.x + 1] = t2;
+    partials[3 * blockIdx.x] = t1;
+    partials[3 * blockIdx.x + 1] = t2;
+    partials[3 * blockIdx.x + 2] = t3;
   }
   if (!arrive_last(counter)) return;
   if (threadIdx.x == 0) {
-    double s1 = 0.0, s2 = 0.0;
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
     for (int b = 0; b < (int)gridDim.x; ++b) {
-      s1 += partials[2 * b];
-      s2 += partials[2 * b + 1];
+      s1 += partials[3 * b];
+      s2 += partials[3 * b + 1];
+      s3 += partials[3 * b + 2];
     }
-    out2[0] = s1;
-    out2[1] = s2;
+    out3[0] = s1;
+    out3[1] = s2;
+    out3[2] = s3;
   }
 }
 
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
-                   const void *L, const void *Ur, const void *Uc, double *out2) {
+                   const void *L, const void *Ur, const void *Uc, double *out3) {
   const int grid = sweep_grid_pub(a.n);
   if (t == VType::F64)
-    k_lu_fro<double, double><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const double *)L, Urow,
-                                                    Ucol, (const double *)Ur, a.Ucp, a.Uri, (const double *)Uc,
-                                                    a.partials, a.counter, out2);
+    k_lu_fro<double, double><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const double *)L,
+                                                    Urow, Ucol, (const double *)Ur, a.Ucp, a.Uri,
+                                                    (const double *)Uc, a.partials, a.counter, out3);
   else if (t == VType::F32)
-    k_lu_fro<float, float><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const float *)L, Urow,
-                                                  Ucol, (const float *)Ur, a.Ucp, a.Uri, (const float *)Uc,
-                                                  a.partials, a.counter, out2);
+    k_lu_fro<float, float><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const float *)L,
+                                                  Urow, Ucol, (const float *)Ur, a.Ucp, a.Uri, (const float *)Uc,
+                                                  a.partials, a.counter, out3);
   else
     k_lu_fro<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
-        a.n, a.Arow, a.Acol, a.Lrow, a.Lcol, (const __nv_bfloat16 *)L, Urow, Ucol, (const __nv_bfloat16 *)Ur,
-        a.Ucp, a.Uri, (const __nv_bfloat16 *)Uc, a.partials, a.counter, out2);
+        a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const __nv_bfloat16 *)L, Urow, Ucol,
+        (const __nv_bfloat16 *)Ur, a.Ucp, a.Uri, (const __nv_bfloat16 *)Uc, a.partials, a.counter, out3);
 }
 
 // ---------------------------------------------------------------- BCSR

@@ -313,6 +313,42 @@ __global__ void k_sqdiff(int n, const void *a, const void *b, int f32, double *p
   }
 }
 
+// sum of squares of count FP64 values (||A||_F^2 of the resident values):
+// 16-byte loads, one FMA per value, two accumulators; the last block folds
+// the blocks' partial sums in a fixed order
+__global__ void __launch_bounds__(kSTPB) k_sumsq(size_t count, const double *__restrict__ a, double *partials,
+                                                 int *counter, double *out) {
+  double acc0 = 0.0, acc1 = 0.0;
+  const size_t npair = count / 2;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += stride) {
+    const double2 v = __ldcs(reinterpret_cast<const double2 *>(a) + p);
+    acc0 = fma(v.x, v.x, acc0);
+    acc1 = fma(v.y, v.y, acc1);
+  }
+  if ((count & 1) && blockIdx.x == 0 && threadIdx.x == 0) acc0 = fma(a[count - 1], a[count - 1], acc0);
+  __shared__ double scratch[kSTPB / 32];
+  const double acc = warp_sum(acc0 + acc1);
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kSTPB / 32; ++w) t += scratch[w];
+    partials[blockIdx.x] = t;
+  }
+  if (!arrive_last(counter)) return;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b2 = 0; b2 < (int)gridDim.x; ++b2) s += partials[b2];
+    *out = s;
+  }
+}
+
+void launch_sumsq(cudaStream_t s, size_t count, const double *a, double *partials, int *counter, double *out) {
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms() * 4, (count / 2 + kSTPB - 1) / kSTPB));
+  k_sumsq<<<grid, kSTPB, 0, s>>>(count, a, partials, counter, out);
+}
+
 void launch_sqdiff(cudaStream_t s, int n, const void *a, const void *b, int f32, double *partials,
                    int *counter, double *out) {
   int grid = min((n + kSTPB - 1) / kSTPB, num_sms() * 4);
