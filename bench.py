@@ -280,10 +280,11 @@ def run_ours(args):
 
     # launches per solve: ParILU (4 initial-guess copies, the sweeps, 2 gathers,
     # the residual), 2 solve-plan value gathers, and per cycle the residual,
-    # the first vector, m steps of [fill, L solve, fill, U solve, passes A/B/C]
-    # and the x update (steps after convergence launch and exit at once)
+    # the first vector, m steps of [L solve, U solve, passes A/B/C] (pass C
+    # marks the next step's solve outputs, so the solves launch no fills) and
+    # the x update (steps after convergence launch and exit at once)
     cycles = r_mixed.restarts + 1
-    launches_per_solve = (4 + SWEEPS + 2 + 1) + 2 + cycles * (3 + M * 7)
+    launches_per_solve = (4 + SWEEPS + 2 + 1) + 2 + cycles * (3 + M * 5)
     med = statistics.median(t_mixed)
     if world > 1:
         tt = torch.tensor([med], device="cuda", dtype=torch.float64)
