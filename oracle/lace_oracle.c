@@ -887,3 +887,154 @@ int orc_fgmres_householder(const orc_operator *A, const orc_precond *M,
   free(g); free(gc); free(gs); free(bins); free(fa); free(fb);
   return info;
 }
+
+/* ========================================================= FGMRES-MGS */
+
+#define H(i, j) h[(size_t)(i) + (size_t)(j) * (size_t)(m + 1)]
+
+int orc_fgmres_mgs(const orc_operator *A, const orc_precond *M, const double *b,
+                   double *x0, const orc_gmres_par *par, int restarted,
+                   orc_gmres_log *log, double *resid_hist, double *orth_hist) {
+  const int n = A->n;
+  const int m = par->search_max;
+  const int restart_max = restarted ? par->restart_max : 1;
+  int info = -205; /* DEV_NOTCONVERGED */
+  double rtol = par->rtol;
+  memset(log, 0, sizeof(*log));
+
+  double *x = (double *)malloc(sizeof(double) * (size_t)n);
+  memcpy(x, x0, sizeof(double) * (size_t)n);
+  double *r = (double *)calloc((size_t)n, sizeof(double));
+  double *u = (double *)calloc((size_t)n, sizeof(double));
+  double *tmp = (double *)calloc((size_t)n, sizeof(double));
+  double *z = (double *)calloc((size_t)n, sizeof(double));
+  double *krylov = (double *)calloc((size_t)n * (size_t)(m + 1), sizeof(double));
+  double *Minvvj = (double *)calloc((size_t)n * (size_t)m, sizeof(double));
+  double *h = (double *)calloc((size_t)(m + 1) * (size_t)m, sizeof(double));
+  double *g = (double *)calloc((size_t)(m + 1), sizeof(double));
+  double *gc = (double *)calloc((size_t)m, sizeof(double));
+  double *gs = (double *)calloc((size_t)m, sizeof(double));
+  double *alpha = (double *)calloc((size_t)m, sizeof(double));
+  float *fa = (float *)malloc(sizeof(float) * (size_t)n);
+  float *fb = (float *)malloc(sizeof(float) * (size_t)n);
+  /* the Brown/Hindmarsh test's threshold (fgmres_restart.cpp:150) and the
+   * happy-breakdown threshold (:363; fgmres.cpp:341 uses DBL_EPSILON) */
+  const double eps = nextafter(0.0, 1.0);
+  const double brk = restarted ? 0.0 : DBL_EPSILON;
+  int total = 0;
+  int early_return = 0;
+
+  for (int restart = 0; restart < restart_max; ++restart) {
+    if (restart > 0) { /* fgmres_restart.cpp:181-189 (h and alpha are kept) */
+      memset(r, 0, sizeof(double) * (size_t)n);
+      memset(u, 0, sizeof(double) * (size_t)n);
+      memset(krylov, 0, sizeof(double) * (size_t)n * (size_t)(m + 1));
+      memset(Minvvj, 0, sizeof(double) * (size_t)n * (size_t)m);
+      memset(g, 0, sizeof(double) * (size_t)(m + 1));
+      memset(gc, 0, sizeof(double) * (size_t)m);
+      memset(gs, 0, sizeof(double) * (size_t)m);
+    }
+    op_residual(A, x, b, r); /* :192-194 */
+    const double rnorm2 = seq_nrm2(n, r);
+    if (restart == 0 && par->tol_type == 1) rtol = rtol * rnorm2; /* :195-201 */
+    if (rnorm2 < rtol) { /* :205-208: returns without copying x back */
+      info = 0;
+      log->converged = 1;
+      log->lost_update = (restart > 0);
+      early_return = 1;
+      break;
+    }
+    for (int i = 0; i < n; ++i) K(i, 0) = r[i] / rnorm2; /* :211-218 */
+    g[0] = rnorm2;
+    log->search_directions = 0; /* :221-223, every cycle */
+    log->initial_residual = rnorm2;
+
+    for (int search = 0; search < m; ++search) { /* :227 */
+      const int search1 = search + 1;
+      memset(u, 0, sizeof(double) * (size_t)n);
+      memset(tmp, 0, sizeof(double) * (size_t)n);
+      prec_apply(M, n, A->bs, &K(0, search), tmp, &Z(0, search), fa, fb); /* :239-270 */
+      op_apply(A, &Z(0, search), u);                                        /* :284-290 */
+      const double normav = seq_nrm2(n, u);                                 /* :291 */
+      for (int j = 0; j <= search; ++j) { /* :302-328, modified Gram-Schmidt */
+        double t = 0.0;
+        for (int i = 0; i < n; ++i) t = t + K(i, j) * u[i];
+        H(j, search) = t;
+#pragma omp parallel for schedule(static) if (n > 65536)
+        for (int i = 0; i < n; ++i) u[i] = u[i] - H(j, search) * K(i, j);
+      }
+      H(search1, search) = seq_nrm2(n, u); /* :329-330 */
+      const double normav2 = H(search1, search);
+      double hr = (normav + 0.001 * normav2) - normav; /* :336-360 */
+      if ((par->reorth == 0 && hr <= eps) || par->reorth == 2) {
+        for (int j = 0; j <= search; ++j) {
+          hr = 0.0;
+          for (int i = 0; i < n; ++i) hr = hr + K(i, j) * u[i];
+          H(j, search) = H(j, search) + hr;
+#pragma omp parallel for schedule(static) if (n > 65536)
+          for (int i = 0; i < n; ++i) u[i] = u[i] - hr * K(i, j);
+        }
+        H(search1, search) = seq_nrm2(n, u);
+      }
+      if (fabs(H(search1, search)) > brk) /* :362-378 */
+        for (int i = 0; i < n; ++i) K(i, search1) = u[i] / H(search1, search);
+      if (par->monitor_orthog) { /* :380-387 */
+        double oe = orc_orthogonality_error(n, n, krylov, search1);
+        if (orth_hist) orth_hist[total] = oe;
+      }
+      for (int j = 0; j < search; ++j) { /* :406-415 */
+        const double delta = H(j, search);
+        H(j, search) = gc[j] * delta - gs[j] * H(j + 1, search);
+        H(j + 1, search) = gs[j] * delta + gc[j] * H(j + 1, search);
+      }
+      const double gamma = sqrt(H(search, search) * H(search, search) +
+                                H(search1, search) * H(search1, search)); /* :417-420 */
+      if (gamma > 0.0) { /* :421-432 */
+        gc[search] = H(search, search) / gamma;
+        gs[search] = -H(search1, search) / gamma;
+        H(search, search) = gc[search] * H(search, search) - gs[search] * H(search1, search);
+        H(search1, search) = 0.0;
+        const double delta = g[search];
+        g[search] = gc[search] * delta - gs[search] * g[search1];
+        g[search1] = gs[search] * delta + gc[search] * g[search1];
+      }
+      if (resid_hist) resid_hist[total] = fabs(g[search1]);
+      total++;
+      /* :459 (fgmres.cpp:440 also stops on a non-finite residual) */
+      if (fabs(g[search1]) < rtol || search == m - 1 || (!restarted && !isfinite(g[search1]))) {
+        for (int i = 0; i <= search; ++i) alpha[i] = g[i] / H(i, i); /* :461-469 */
+        for (int j = search; j > 0; --j)
+          for (int i = j - 1; i > -1; --i) alpha[i] = alpha[i] - H(i, j) * alpha[j] / H(i, i);
+        if (restarted) { /* :472-481, column by column */
+          for (int j = 0; j <= search; ++j) {
+#pragma omp parallel for schedule(static) if (n > 65536)
+            for (int i = 0; i < n; ++i) x[i] = x[i] + Z(i, j) * alpha[j];
+          }
+        } else { /* fgmres.cpp:453-474: z = sum_j Z_j alpha_j, then x += z */
+#pragma omp parallel for schedule(static) if (n > 65536)
+          for (int i = 0; i < n; ++i) {
+            for (int j = 0; j <= search; ++j) z[i] = z[i] + Z(i, j) * alpha[j];
+            x[i] = x[i] + z[i];
+          }
+        }
+        if (restarted) log->restarts = restart;
+        log->search_directions = search1;
+        log->final_residual = fabs(g[search1]);
+        if (fabs(g[search1]) < rtol) {
+          log->converged = 1;
+          restart = restart_max;
+        }
+        break;
+      }
+    }
+  }
+  log->total_iterations = total;
+  if (!early_return) {
+    memcpy(x0, x, sizeof(double) * (size_t)n); /* :506-507 */
+    if (log->final_residual > rtol) info = 0;   /* :510-512, as written */
+  }
+  log->info = info;
+  free(x); free(r); free(u); free(tmp); free(z); free(krylov); free(Minvvj);
+  free(h); free(g); free(gc); free(gs); free(alpha); free(fa); free(fb);
+  return info;
+}

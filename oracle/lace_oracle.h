@@ -190,6 +190,7 @@ typedef struct {
   int search_max, restart_max, tol_type;  /* sparse_types.h:158-176 */
   double rtol;
   int monitor_orthog;
+  int reorth;  /* MGS only: 0 Brown/Hindmarsh test, 1 never, 2 always */
 } orc_gmres_par;
 
 typedef struct {
@@ -211,6 +212,17 @@ int orc_fgmres_householder(const orc_operator *A, const orc_precond *M,
                            const double *b, double *x, const orc_gmres_par *par,
                            orc_gmres_log *log, double *resid_hist,
                            double *orth_hist);
+
+/* Right-preconditioned FGMRES with modified Gram-Schmidt Arnoldi, a
+ * statement-by-statement mirror of src/fgmres_restart.cpp:63-532
+ * (restarted != 0) or src/fgmres.cpp:64-517 (restarted == 0: one cycle,
+ * breakdown threshold DBL_EPSILON, a non-finite residual stops, the update
+ * summed into z before x += z).  Same in/out conventions as
+ * orc_fgmres_householder; orth_hist holds the orthogonality error of the
+ * Krylov basis v_0..v_j. */
+int orc_fgmres_mgs(const orc_operator *A, const orc_precond *M, const double *b,
+                   double *x, const orc_gmres_par *par, int restarted,
+                   orc_gmres_log *log, double *resid_hist, double *orth_hist);
 
 #ifdef __cplusplus
 }

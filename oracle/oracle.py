@@ -60,7 +60,7 @@ class OrcPrecond(C.Structure):
 
 class OrcGmresPar(C.Structure):
     _fields_ = [("search_max", C.c_int), ("restart_max", C.c_int), ("tol_type", C.c_int),
-                ("rtol", C.c_double), ("monitor_orthog", C.c_int)]
+                ("rtol", C.c_double), ("monitor_orthog", C.c_int), ("reorth", C.c_int)]
 
 
 class OrcGmresLog(C.Structure):
@@ -103,6 +103,10 @@ def _setup(L: C.CDLL) -> None:
     L.orc_fgmres_householder.argtypes = [C.POINTER(OrcOperator), C.POINTER(OrcPrecond), _dp, _dp,
                                          C.POINTER(OrcGmresPar), C.POINTER(OrcGmresLog), C.c_void_p,
                                          C.c_void_p]
+    L.orc_fgmres_mgs.restype = C.c_int
+    L.orc_fgmres_mgs.argtypes = [C.POINTER(OrcOperator), C.POINTER(OrcPrecond), _dp, _dp,
+                                 C.POINTER(OrcGmresPar), C.c_int, C.POINTER(OrcGmresLog), C.c_void_p,
+                                 C.c_void_p]
 
 
 def set_threads(n: int) -> None:
@@ -437,14 +441,9 @@ class GmresResult:
 PREC = {"trsv": 0, "partrsv": 1, "none": 2, "trsv_f32": 3, "jacobi": 4, "bcsr": 5, "bcsr_f32": 6}
 
 
-def fgmres(op: dict, prec: dict, b, x0=None, search_max=30, restart_max=20, rtol=1e-10,
-           tol_type=1, monitor_orthog=False) -> GmresResult:
-    """FGMRES-Householder mirror (src/fgmres_householder_restart.cpp:63-788).
-
-    op: {'kind': 'csr', 'row','col','val'} or {'kind': 'bcsr', 'bs', 'row','col','val'}.
-    prec: {'kind': one of PREC, 't1': Tri, 't1_lower', 't1_unit', 't2': Tri, ...,
-           'bdinv': array, 'tol', 'max_sweeps'}."""
-    keep = []
+def _gmres_inputs(op: dict, prec: dict, keep: list):
+    """The operator and preconditioner structs of the C oracle (arrays kept
+    alive in `keep`)."""
 
     def ptr(a, dt):
         if a is None:
@@ -487,17 +486,52 @@ def fgmres(op: dict, prec: dict, b, x0=None, search_max=30, restart_max=20, rtol
             p.bdinv = ptr(bd, np.float64)
     p.tol = float(prec.get("tol", 1.0))
     p.max_sweeps = int(prec.get("max_sweeps", 100))
-    par = OrcGmresPar(search_max, restart_max, tol_type, rtol, int(monitor_orthog))
+    return o, p, n
+
+
+def _gmres_result(x, info, log, rh, oh) -> GmresResult:
+    t = log.total_iterations
+    return GmresResult(x, info, log.restarts, log.search_directions, t, log.initial_residual,
+                       log.final_residual, bool(log.converged), bool(log.lost_update), rh[:t].copy(),
+                       oh[:t].copy() if oh is not None else None)
+
+
+def fgmres(op: dict, prec: dict, b, x0=None, search_max=30, restart_max=20, rtol=1e-10,
+           tol_type=1, monitor_orthog=False) -> GmresResult:
+    """FGMRES-Householder mirror (src/fgmres_householder_restart.cpp:63-788).
+
+    op: {'kind': 'csr', 'row','col','val'} or {'kind': 'bcsr', 'bs', 'row','col','val'}.
+    prec: {'kind': one of PREC, 't1': Tri, 't1_lower', 't1_unit', 't2': Tri, ...,
+           'bdinv': array, 'tol', 'max_sweeps'}."""
+    keep = []
+    o, p, n = _gmres_inputs(op, prec, keep)
+    par = OrcGmresPar(search_max, restart_max, tol_type, rtol, int(monitor_orthog), 0)
     log = OrcGmresLog()
     x = np.zeros(n) if x0 is None else _d(x0).copy()
     rh = np.zeros(search_max * restart_max)
     oh = np.zeros(search_max * restart_max) if monitor_orthog else None
     info = lib().orc_fgmres_householder(C.byref(o), C.byref(p), _d(b), x, C.byref(par), C.byref(log),
                                          rh.ctypes.data, oh.ctypes.data if oh is not None else None)
-    t = log.total_iterations
-    return GmresResult(x, info, log.restarts, log.search_directions, t, log.initial_residual,
-                       log.final_residual, bool(log.converged), bool(log.lost_update), rh[:t].copy(),
-                       oh[:t].copy() if oh is not None else None)
+    return _gmres_result(x, info, log, rh, oh)
+
+
+def fgmres_mgs(op: dict, prec: dict, b, x0=None, search_max=30, restart_max=20, rtol=1e-10,
+               tol_type=1, monitor_orthog=False, reorth=0, restarted=True) -> GmresResult:
+    """FGMRES with modified Gram-Schmidt Arnoldi: src/fgmres_restart.cpp:63-532
+    (restarted) or src/fgmres.cpp:64-517 (one cycle).  Arguments as fgmres();
+    reorth: 0 Brown/Hindmarsh test, 1 never, 2 always (sparse_types.h:164-166)."""
+    keep = []
+    o, p, n = _gmres_inputs(op, prec, keep)
+    par = OrcGmresPar(search_max, restart_max if restarted else 1, tol_type, rtol, int(monitor_orthog),
+                      int(reorth))
+    log = OrcGmresLog()
+    x = np.zeros(n) if x0 is None else _d(x0).copy()
+    nc = restart_max if restarted else 1
+    rh = np.zeros(search_max * nc)
+    oh = np.zeros(search_max * nc) if monitor_orthog else None
+    info = lib().orc_fgmres_mgs(C.byref(o), C.byref(p), _d(b), x, C.byref(par), int(bool(restarted)),
+                                C.byref(log), rh.ctypes.data, oh.ctypes.data if oh is not None else None)
+    return _gmres_result(x, info, log, rh, oh)
 
 
 def ilu_precond(F: Factors, kind: str = "trsv", **kw) -> dict:

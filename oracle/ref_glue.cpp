@@ -77,9 +77,13 @@ int ref_parcsrtrsv(int uplo, int storage, int diag, int n, const double *val,
  * user_csrtrsv_choice, monitorOrthog, restart_max, precondition, reorth};
  * log7 = {restarts, search_directions, solve_time, initial_residual,
  * final_residual, scaled_residual, original_residual}.  x is in/out. */
-int ref_fgmres_householder_restart(data_d_matrix *A, const double *b, double *x,
-                                   data_d_matrix *L, data_d_matrix *U,
-                                   const double *par8, double *log7) {
+typedef int (*ref_solver_fn)(data_d_matrix *, data_d_matrix *, data_d_matrix *,
+                             data_d_matrix *, data_d_matrix *, data_d_gmres_param *,
+                             data_d_gmres_log *);
+
+static int ref_run_solver(ref_solver_fn solve, data_d_matrix *A, const double *b,
+                          double *x, data_d_matrix *L, data_d_matrix *U,
+                          const double *par8, double *log7) {
   data_d_matrix *bv = ref_vec_new(A->num_rows, b);
   data_d_matrix *xv = ref_vec_new(A->num_rows, x);
   data_d_gmres_param p;
@@ -94,7 +98,7 @@ int ref_fgmres_householder_restart(data_d_matrix *A, const double *b, double *x,
   p.reorth = (int)par8[7];
   data_d_gmres_log lg;
   memset(&lg, 0, sizeof(lg));
-  int info = data_fgmres_householder_restart(A, bv, xv, L, U, &p, &lg);
+  int info = solve(A, bv, xv, L, U, &p, &lg);
   memcpy(x, xv->val, sizeof(double) * (size_t)A->num_rows);
   log7[0] = lg.restarts;
   log7[1] = lg.search_directions;
@@ -106,6 +110,20 @@ int ref_fgmres_householder_restart(data_d_matrix *A, const double *b, double *x,
   ref_mat_free(bv);
   ref_mat_free(xv);
   return info;
+}
+
+int ref_fgmres_householder_restart(data_d_matrix *A, const double *b, double *x,
+                                   data_d_matrix *L, data_d_matrix *U,
+                                   const double *par8, double *log7) {
+  return ref_run_solver(data_fgmres_householder_restart, A, b, x, L, U, par8, log7);
+}
+
+/* FGMRES with modified Gram-Schmidt: data_fgmres_restart (restarted != 0)
+ * or data_fgmres (one cycle); par8 and log7 as above. */
+int ref_fgmres_mgs(data_d_matrix *A, const double *b, double *x, data_d_matrix *L,
+                   data_d_matrix *U, const double *par8, double *log7, int restarted) {
+  return ref_run_solver(restarted ? data_fgmres_restart : data_fgmres, A, b, x, L, U, par8,
+                        log7);
 }
 
 void ref_givens(double a, double b, double tol, double *c, double *s) {

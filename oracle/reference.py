@@ -62,6 +62,7 @@ def _load(path: str) -> C.CDLL:
             L.ref_parcsrtrsv.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                          C.c_double, C.POINTER(C.c_int)]
             L.ref_fgmres_householder_restart.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+            L.ref_fgmres_mgs.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int]
             L.ref_givens.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]
             L.ref_orthogonality_error.restype = C.c_double
@@ -195,6 +196,20 @@ def fgmres_householder_restart(A: Mat, b, x0, Lm: Mat, Um: Mat, search_max=20, r
                    dtype=np.float64)
     log = np.zeros(7)
     info = lib().ref_fgmres_householder_restart(A.h, _p(b), _p(x), Lm.h, Um.h, _p(par), _p(log))
+    keys = ["restarts", "search_directions", "solve_time", "initial_residual", "final_residual",
+            "scaled_residual", "original_residual"]
+    return x, info, dict(zip(keys, log.tolist()))
+
+
+def fgmres_mgs(A: Mat, b, x0, Lm: Mat, Um: Mat, search_max=20, restart_max=20, rtol=1e-3,
+               tol_type=0, choice=0, monitor_orthog=0, reorth=0, restarted=True):
+    """data_fgmres_restart (restarted) or data_fgmres, LACE's own code."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.ascontiguousarray(x0, dtype=np.float64).copy()
+    par = np.array([search_max, tol_type, rtol, choice, monitor_orthog, restart_max, 1, reorth],
+                   dtype=np.float64)
+    log = np.zeros(7)
+    info = lib().ref_fgmres_mgs(A.h, _p(b), _p(x), Lm.h, Um.h, _p(par), _p(log), int(bool(restarted)))
     keys = ["restarts", "search_directions", "solve_time", "initial_residual", "final_residual",
             "scaled_residual", "original_residual"]
     return x, info, dict(zip(keys, log.tolist()))

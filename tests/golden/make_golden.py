@@ -54,13 +54,15 @@ class CaptureStdout:
         self.tmp.close()
 
 
-def hist_from(text: str, tag: str = "mkltrsv") -> np.ndarray:
-    vals = re.findall(rf"FGMRES_Householders_{tag}_search\((\d+)\) = ([-+0-9.eE]+);", text)
+def hist_from(text: str, tag: str = "mkltrsv", solver: str = "FGMRES_Householders_") -> np.ndarray:
+    """|g_{j+1}| per search direction as LACE prints it (solver: the printed
+    prefix, "FGMRES_" for the Gram-Schmidt FGMRES)."""
+    vals = re.findall(rf"{solver}{tag}_search\((\d+)\) = ([-+0-9.eE]+);", text)
     return np.array([float(v) for _, v in vals])
 
 
-def orth_from(text: str, tag: str = "mkltrsv") -> np.ndarray:
-    vals = re.findall(rf"FGMRES_Householders_{tag}_ortherr\((\d+)\) = ([-+0-9.eE]+);", text)
+def orth_from(text: str, tag: str = "mkltrsv", solver: str = "FGMRES_Householders_") -> np.ndarray:
+    vals = re.findall(rf"{solver}{tag}_ortherr\((\d+)\) = ([-+0-9.eE]+);", text)
     return np.array([float(v) for _, v in vals])
 
 
@@ -110,6 +112,7 @@ def main():
     g["tref_mkl_zilures"] = np.array(ref.zilures(Tm, Lk, Uk))
     Ucsr = ref.convert(Um, ref.Magma_CSC, ref.Magma_CSR)
     ref.set_storage(Ucsr, ref.Magma_CSRU)  # as testing/test_linearSolver.cpp:671 does
+    Lt, Ut = Lm, Ucsr  # Trefethen_20's factors, for the Gram-Schmidt FGMRES below
     for choice in (0, 1):
         with CaptureStdout() as cap:
             x, info, glog = ref.fgmres_householder_restart(Tm, np.ones(T.n), np.zeros(T.n), Lm, Ucsr,
@@ -143,6 +146,16 @@ def main():
         g[f"{name}_fgmres_log"] = np.array([info, glog["restarts"], glog["search_directions"],
                                             glog["initial_residual"], glog["final_residual"], m])
         g[f"{name}_fgmres_hist"] = hist_from(cap.text)
+        # the same system through LACE's FGMRES with modified Gram-Schmidt
+        # (src/fgmres_restart.cpp); cd8 with reorthogonalisation always on
+        reorth = 2 if name == "cd8" else 0
+        with CaptureStdout() as cap:
+            x, info, glog = ref.fgmres_mgs(Sm, b, np.zeros(S.n), Lm, Ucsr, search_max=m, restart_max=50,
+                                           rtol=1e-10, tol_type=1, choice=0, reorth=reorth)
+        g[f"{name}_mgs_x"] = x
+        g[f"{name}_mgs_log"] = np.array([info, glog["restarts"], glog["search_directions"],
+                                         glog["initial_residual"], glog["final_residual"], m, reorth])
+        g[f"{name}_mgs_hist"] = hist_from(cap.text, solver="FGMRES_")
         # LACE's ParCSRTRSV on these factors (tol 1.0 as FGMRES uses it)
         rng = np.random.default_rng(5)
         rhs = rng.standard_normal(S.n)
@@ -162,6 +175,48 @@ def main():
         y, _ = ref.spmv(Sm, xs, alpha=1.25, beta=-0.75, y=ys)
         g[f"{name}_spmv_in"] = np.stack([xs, ys])
         g[f"{name}_spmv_out"] = y
+
+    # ------------------------- FGMRES with modified Gram-Schmidt (LACE)
+    # Trefethen_20 as in the Householder case above: data_fgmres_restart
+    # (restarted 1) and data_fgmres (restarted 0), exact solves and ParCSRTRSV
+    for restarted in (1, 0):
+        for choice in (0, 1):
+            with CaptureStdout() as cap:
+                x, info, glog = ref.fgmres_mgs(Tm, np.ones(T.n), np.zeros(T.n), Lt, Ut, search_max=20,
+                                               restart_max=20, rtol=1e-3, tol_type=0, choice=choice,
+                                               monitor_orthog=1, restarted=bool(restarted))
+            tag = "mkltrsv" if choice == 0 else "partrsv"
+            k = f"tref_mgs{restarted}{choice}"
+            g[f"{k}_x"] = x
+            g[f"{k}_log"] = np.array([info, glog["restarts"], glog["search_directions"],
+                                      glog["initial_residual"], glog["final_residual"]])
+            g[f"{k}_hist"] = hist_from(cap.text, tag, "FGMRES_")
+            g[f"{k}_orth"] = orth_from(cap.text, tag, "FGMRES_")
+    # Brown/Hindmarsh reorthogonalisation and happy breakdown: 20 decoupled
+    # [[2,1],[1,2]] blocks have two eigenvalues, so the second direction is
+    # already in the Krylov space (LACE prints "Reorthogonalize")
+    nb2 = 40
+    r2 = np.repeat(np.arange(nb2, dtype=np.int32), 2)
+    c2 = np.array([[i - i % 2, i - i % 2 + 1] for i in range(nb2)], dtype=np.int32).ravel()
+    v2 = np.array([[2.0, 1.0] if i % 2 == 0 else [1.0, 2.0] for i in range(nb2)]).ravel()
+    B2 = P.CSR(nb2, np.concatenate([[0], np.cumsum(np.bincount(r2, minlength=nb2))]).astype(np.int32), c2, v2)
+    g["blk2_row"], g["blk2_col"], g["blk2_val"] = B2.row, B2.col, B2.val
+    g["blk2_b"] = b2 = np.random.default_rng(3).standard_normal(nb2)
+    B2m = csr_of(B2)
+    with CaptureStdout():
+        L2, U2, _ = ref.parilu(B2m, 1e-15)
+    U2c = ref.convert(U2, ref.Magma_CSC, ref.Magma_CSR)
+    for restarted in (1, 0):
+        for choice in (0, 2):
+            with CaptureStdout() as cap:
+                x, info, glog = ref.fgmres_mgs(B2m, b2, np.zeros(nb2), L2, U2c, search_max=10, restart_max=3,
+                                               rtol=1e-12, tol_type=1, choice=choice, restarted=bool(restarted))
+            k = f"blk2_mgs{restarted}{choice}"
+            g[f"{k}_x"] = x
+            g[f"{k}_log"] = np.array([info, glog["restarts"], glog["search_directions"],
+                                      glog["initial_residual"], glog["final_residual"],
+                                      cap.text.count("Reorthogonalize"), cap.text.count("happy breakdown")])
+            g[f"{k}_hist"] = hist_from(cap.text, "mkltrsv" if choice == 0 else "partrsv", "FGMRES_")
 
     # --------------------------------------------------- BCSR ParILU (LACE)
     B = P.bcsr3d(3, seed=11)

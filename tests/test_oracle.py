@@ -135,6 +135,71 @@ def test_fgmres_equals_lace_synthetic(name):
     assert np.array_equal(r.resid_hist, G[f"{name}_fgmres_hist"])
 
 
+@pytest.mark.parametrize("restarted", [1, 0])
+def test_fgmres_mgs_equals_lace_trefethen(restarted):
+    """data_fgmres_restart (src/fgmres_restart.cpp) and data_fgmres
+    (src/fgmres.cpp) on Trefethen_20 with LACE's factors: x, log, residual
+    and orthogonality history reproduced exactly."""
+    T = P.trefethen(19)
+    F = orc.Factors(orc.Tri(G["tref_L_row"], G["tref_L_col"], G["tref_L_val"]),
+                    orc.Tri(G["tref_U_ptr"], G["tref_U_idx"], G["tref_U_val"]), [])
+    for choice, kind in ((0, "trsv"), (1, "partrsv")):
+        r = orc.fgmres_mgs({"kind": "csr", "row": T.row, "col": T.col, "val": T.val},
+                           orc.ilu_precond(F, kind, tol=1.0), np.ones(T.n), search_max=20, restart_max=20,
+                           rtol=1e-3, tol_type=0, monitor_orthog=True, restarted=bool(restarted))
+        k = f"tref_mgs{restarted}{choice}"
+        lg = G[f"{k}_log"]
+        assert r.info == int(lg[0])
+        assert r.restarts == int(lg[1]) and r.search_directions == int(lg[2])
+        assert r.initial_residual == lg[3] and r.final_residual == lg[4]
+        assert np.array_equal(r.x, G[f"{k}_x"])
+        assert np.array_equal(r.resid_hist, G[f"{k}_hist"])
+        assert np.allclose(r.orth_hist, G[f"{k}_orth"], rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("name", ["lap32", "cd8", "cd12"])
+def test_fgmres_mgs_equals_lace_synthetic(name):
+    """LACE's Gram-Schmidt FGMRES with restarts (lap32 restarts once; cd8
+    reorthogonalises every direction, reorth = 2)."""
+    S = {"lap32": P.laplace2d(32), "cd8": P.convdiff3d(8), "cd12": P.convdiff3d(12)}[name]
+    F = orc.initial_factors(S.row, S.col, S.val)
+    F.L.val = G[f"{name}_L_val"]
+    F.U.val = G[f"{name}_U_val"]
+    lg = G[f"{name}_mgs_log"]
+    r = orc.fgmres_mgs({"kind": "csr", "row": S.row, "col": S.col, "val": S.val}, orc.ilu_precond(F),
+                       G[f"{name}_b"], search_max=int(lg[5]), restart_max=50, rtol=1e-10, tol_type=1,
+                       reorth=int(lg[6]))
+    assert r.info == int(lg[0])
+    assert r.restarts == int(lg[1]) and r.search_directions == int(lg[2])
+    assert r.initial_residual == lg[3] and r.final_residual == lg[4]
+    assert np.array_equal(r.x, G[f"{name}_mgs_x"])
+    assert np.array_equal(r.resid_hist, G[f"{name}_mgs_hist"])
+
+
+def blk2_system():
+    """20 decoupled [[2,1],[1,2]] blocks (two eigenvalues): the second Krylov
+    direction is already in the space, so LACE's Brown/Hindmarsh test
+    reorthogonalises and (one cycle, DBL_EPSILON threshold) breaks down."""
+    return P.CSR(40, G["blk2_row"], G["blk2_col"], G["blk2_val"])
+
+
+@pytest.mark.parametrize("restarted", [1, 0])
+@pytest.mark.parametrize("choice", [0, 2])
+def test_fgmres_mgs_reorthogonalisation_equals_lace(restarted, choice):
+    S = blk2_system()
+    F = orc.parilu(S.row, S.col, S.val, 1, mode="async")
+    k = f"blk2_mgs{restarted}{choice}"
+    lg = G[f"{k}_log"]
+    assert lg[5] == 1  # LACE reorthogonalised once
+    r = orc.fgmres_mgs({"kind": "csr", "row": S.row, "col": S.col, "val": S.val},
+                       orc.ilu_precond(F, "trsv" if choice == 0 else "none"), G["blk2_b"], search_max=10,
+                       restart_max=3, rtol=1e-12, tol_type=1, restarted=bool(restarted))
+    assert r.info == int(lg[0]) and r.search_directions == int(lg[2])
+    assert r.initial_residual == lg[3] and r.final_residual == lg[4]
+    assert np.array_equal(r.x, G[f"{k}_x"])
+    assert np.array_equal(r.resid_hist, G[f"{k}_hist"])
+
+
 @pytest.mark.parametrize("name", ["lap32", "cd8", "cd12"])
 def test_parcsrtrsv_and_spmv_equal_lace(name):
     S = {"lap32": P.laplace2d(32), "cd8": P.convdiff3d(8), "cd12": P.convdiff3d(12)}[name]
@@ -228,6 +293,25 @@ def test_live_reference_random_convdiff(seed):
     assert np.array_equal(x, r.x)
     assert r.search_directions == glog["search_directions"] and r.restarts == glog["restarts"]
     del contextlib, io
+
+
+@needs_ref
+@pytest.mark.parametrize("restarted", [True, False])
+def test_live_reference_fgmres_mgs(restarted):
+    """Fresh inputs through LACE's Gram-Schmidt FGMRES and the restatement."""
+    rng = np.random.default_rng(7)
+    S = P.convdiff3d(7, 6, 5, pe=float(rng.uniform(0.5, 20)))
+    Sm = ref.Mat.from_arrays(ref.Magma_CSR, S.n, S.n, S.row, S.col, S.val)
+    Lm, Um, log = ref.parilu(Sm, 1e-15, max_sweeps=3)
+    F = orc.parilu(S.row, S.col, S.val, int(log["sweeps"]), mode="async")
+    b = rng.standard_normal(S.n)
+    Ucsr = ref.convert(Um, ref.Magma_CSC, ref.Magma_CSR)
+    x, info, glog = ref.fgmres_mgs(Sm, b, np.zeros(S.n), Lm, Ucsr, search_max=6, restart_max=30, rtol=1e-10,
+                                   tol_type=1, restarted=restarted)
+    r = orc.fgmres_mgs({"kind": "csr", "row": S.row, "col": S.col, "val": S.val}, orc.ilu_precond(F), b,
+                       search_max=6, restart_max=30, rtol=1e-10, tol_type=1, restarted=restarted)
+    assert np.array_equal(x, r.x) and info == r.info
+    assert r.search_directions == glog["search_directions"] and r.restarts == glog["restarts"]
 
 
 @needs_ref
