@@ -223,6 +223,24 @@ int data_fgmres_householder(data_d_matrix *A, data_d_matrix *b,
                             data_d_matrix *U, data_d_gmres_param *gmres_par,
                             data_d_gmres_log *gmres_log);
 
+/* Replaces src/fgmres_restart.cpp:63 (declared include/sparse.h:1034).
+ * Right-preconditioned restarted FGMRES with modified Gram-Schmidt Arnoldi;
+ * arguments, preconditioner choices and x0 handling as
+ * data_fgmres_householder_restart.  gmres_par->reorth: 0 reorthogonalise
+ * when the Brown/Hindmarsh test asks (:336), 2 always, other values never.
+ * Returns DEV_SUCCESS when the residual target was reached, DEV_NOTCONVERGED
+ * otherwise (LACE's own value is inverted, :510-512). */
+int data_fgmres_restart(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
+                        data_d_matrix *L, data_d_matrix *U,
+                        data_d_gmres_param *gmres_par, data_d_gmres_log *gmres_log);
+
+/* Replaces src/fgmres.cpp:64 (declared include/sparse.h:1027): one cycle of
+ * the same (happy breakdown below DBL_EPSILON, a non-finite residual stops,
+ * x += sum_j z_j y_j). */
+int data_fgmres(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
+                data_d_matrix *L, data_d_matrix *U, data_d_gmres_param *gmres_par,
+                data_d_gmres_log *gmres_log);
+
 /* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
  * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives
  * the same value (the fill-in part of LACE's res is not formed) and LU is
@@ -359,6 +377,20 @@ int lace_gpu_sptrsv(lace_gpu_ctx *ctx, int which, const double *b, double *x);
 int lace_gpu_fgmres_householder(lace_gpu_ctx *ctx, const double *b, double *x,
                                 const data_d_gmres_param *par,
                                 data_d_gmres_log *log, int *total_iters);
+
+/* FGMRES with modified Gram-Schmidt Arnoldi on device vectors (LACE's
+ * data_fgmres_restart when restarted != 0, else data_fgmres); par and log
+ * as lace_gpu_fgmres_householder, par->reorth as LACE's. */
+int lace_gpu_fgmres_mgs(lace_gpu_ctx *ctx, const double *b, double *x,
+                        const data_d_gmres_param *par, int restarted,
+                        data_d_gmres_log *log, int *total_iters);
+
+/* Facts about the last FGMRES solve of this context: out[0] = directions
+ * that the Gram-Schmidt FGMRES reorthogonalised (LACE prints
+ * "Reorthogonalize" for each), out[1] = 1 when its second pass runs as a
+ * conditional CUDA graph node (0: launched always, its kernels return at
+ * once unless needed). */
+int lace_gpu_get_solve_stats(lace_gpu_ctx *ctx, int *out);
 
 /* Adjoint of the solve x = A^{-1} b for a loss L(x): given dL/dx (device),
  * solves A^T lambda = dL/dx with FGMRES-Householder preconditioned by the

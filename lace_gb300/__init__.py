@@ -154,6 +154,8 @@ SIGNATURES = {
     "data_fgmres_householder_restart": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam),
                                              C.POINTER(GmresLog)]),
     "data_fgmres_householder": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
+    "data_fgmres_restart": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
+    "data_fgmres": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_zilures": (_i, [DataMatrix, DataMatrix, DataMatrix, _DM, C.POINTER(_d), C.POINTER(_d)]),
     "lace_gpu_default_options": (None, [C.POINTER(GpuOptions)]),
     "lace_gpu_dropin_set_options": (_i, [C.POINTER(GpuOptions)]),
@@ -174,6 +176,8 @@ SIGNATURES = {
     "lace_gpu_sptrsv": (_i, [_p, _i, _p, _p]),
     "lace_gpu_fgmres_householder": (_i, [_p, _p, _p, C.POINTER(GmresParam), C.POINTER(GmresLog),
                                          C.POINTER(_i)]),
+    "lace_gpu_fgmres_mgs": (_i, [_p, _p, _p, C.POINTER(GmresParam), _i, C.POINTER(GmresLog), C.POINTER(_i)]),
+    "lace_gpu_get_solve_stats": (_i, [_p, _p]),
     "lace_gpu_solve_backward": (_i, [_p, _p, _p, C.POINTER(GmresParam), _p, _p, C.POINTER(_i)]),
     "lace_gpu_last_error": (_i, []),
     "lace_gpu_error_string": (C.c_char_p, [_i]),

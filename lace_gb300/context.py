@@ -146,20 +146,42 @@ class Context:
         _chk(self._lib.lace_gpu_precond_enqueue(self.h, _ptr(q), _ptr(z)), "precond_enqueue")
 
     def fgmres(self, b, x, search_max: int = 30, restart_max: int = 20, rtol: float = 1e-10,
-               tol_type: int = 1) -> GmresResult:
+               tol_type: int = 1, orthogonalization: str = "householder", reorth: int = 0,
+               restarted: bool = True) -> GmresResult:
+        """FGMRES on device vectors b, x (x: initial guess in, solution out).
+        orthogonalization "householder" (LACE's data_fgmres_householder_restart)
+        or "mgs" (modified Gram-Schmidt: data_fgmres_restart, or data_fgmres
+        when restarted is False; reorth as LACE's gmres_par->reorth)."""
         par = GmresParam()
         par.search_max = search_max
         par.restart_max = restart_max
         par.rtol = rtol
         par.tol_type = tol_type
+        par.reorth = reorth
         log = GmresLog()
         tot = C.c_int()
-        rc = self._lib.lace_gpu_fgmres_householder(self.h, _ptr(b), _ptr(x), C.byref(par), C.byref(log),
-                                                   C.byref(tot))
+        if orthogonalization == "mgs":
+            rc = self._lib.lace_gpu_fgmres_mgs(self.h, _ptr(b), _ptr(x), C.byref(par), int(bool(restarted)),
+                                               C.byref(log), C.byref(tot))
+        elif orthogonalization == "householder":
+            rc = self._lib.lace_gpu_fgmres_householder(self.h, _ptr(b), _ptr(x), C.byref(par), C.byref(log),
+                                                       C.byref(tot))
+        else:
+            raise ValueError(f"orthogonalization {orthogonalization!r}: 'householder' or 'mgs'")
         if rc not in (DEV_SUCCESS, DEV_NOTCONVERGED):
-            raise LaceError(rc, "fgmres_householder")
+            raise LaceError(rc, "fgmres_" + orthogonalization)
         return GmresResult(rc == DEV_SUCCESS, log.restarts, log.search_directions, tot.value,
                            log.initial_residual, log.final_residual, log.solve_time, rc)
+
+    def solve_stats(self) -> dict:
+        """The last FGMRES solve: directions the Gram-Schmidt variant
+        reorthogonalised, and whether its second pass is a conditional graph
+        node."""
+        out = (C.c_int * 2)()
+        rc = self._lib.lace_gpu_get_solve_stats(self.h, out)
+        if rc != DEV_SUCCESS:
+            raise LaceError(rc, "get_solve_stats")
+        return {"reorthogonalised": out[0], "conditional_nodes": bool(out[1])}
 
     def backward(self, x, dLdx, dLdb=None, dLdA=None, search_max: int = 30, restart_max: int = 20,
                  rtol: float = 1e-10, tol_type: int = 1) -> int:

@@ -438,8 +438,11 @@ void u_as_csr(const data_d_matrix *U, std::vector<int> &ptr, std::vector<int> &i
   }
 }
 
+// method 0: FGMRES-Householder; 1: FGMRES with modified Gram-Schmidt
+// (restarted: data_fgmres_restart, else data_fgmres)
 int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_matrix *L,
-                  data_d_matrix *U, data_d_gmres_param *par, data_d_gmres_log *log, int restart_max) {
+                  data_d_matrix *U, data_d_gmres_param *par, data_d_gmres_log *log, int restart_max,
+                  int method, int restarted) {
   if (!A || !b || !x0 || !par || !log) return set_err(DEV_ERR_INVALID_PTR);
   if (!is_csr(A->storage_type)) return set_err(DEV_ERR_NOT_SUPPORTED);
   std::lock_guard<std::mutex> lk(g_mu);
@@ -481,7 +484,7 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
     return set_err(DEV_ERR_DEVICE_ALLOC);
   int total = 0;
   rc = c->fgmres((const double *)c->dropin_b.p, (double *)c->dropin_x.p, par->search_max, restart_max,
-                 par->tol_type, par->rtol, false, log, &total, nullptr);
+                 par->tol_type, par->rtol, false, log, &total, nullptr, method, restarted, par->reorth);
   if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
   pc.mark("b, x0 + solve");
   if (cudaMemcpy(x0->val, c->dropin_x.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -499,13 +502,23 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
 extern "C" int data_fgmres_householder_restart(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
                                                data_d_matrix *L, data_d_matrix *U,
                                                data_d_gmres_param *gmres_par, data_d_gmres_log *gmres_log) {
-  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, gmres_par ? gmres_par->restart_max : 0);
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, gmres_par ? gmres_par->restart_max : 0, 0, 1);
 }
 
 extern "C" int data_fgmres_householder(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
                                        data_d_matrix *L, data_d_matrix *U, data_d_gmres_param *gmres_par,
                                        data_d_gmres_log *gmres_log) {
-  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, 1);
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, 1, 0, 1);
+}
+
+extern "C" int data_fgmres_restart(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_matrix *L,
+                                   data_d_matrix *U, data_d_gmres_param *gmres_par, data_d_gmres_log *gmres_log) {
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, gmres_par ? gmres_par->restart_max : 0, 1, 1);
+}
+
+extern "C" int data_fgmres(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_matrix *L,
+                           data_d_matrix *U, data_d_gmres_param *gmres_par, data_d_gmres_log *gmres_log) {
+  return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, 1, 1, 0);
 }
 
 extern "C" int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U, data_d_matrix *LU,

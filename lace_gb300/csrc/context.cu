@@ -32,6 +32,12 @@
 
 namespace lace {
 
+// pinned host scalars: the residual history of a cycle (up to kLdT), then
+// single values at fixed slots
+constexpr int kScalHost = 256;
+constexpr int kScalCycleRnorm = 200;  // ||r|| at the start of the latest cycle
+constexpr int kScalReorth = 201;      // the cycle's reorthogonalised steps (an int)
+
 thread_local int g_last_error = 0;
 
 int set_err(int code) {
@@ -474,7 +480,7 @@ extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream)
   cudaMemsetAsync(c->cycle_buf.p, 0, sizeof(Cycle), c->stream);
   cudaMemsetAsync(c->cnt_buf.p, 0, 64 * sizeof(int), c->stream);
   if (cudaMallocHost(&c->h_ctrl, sizeof(Control)) != cudaSuccess ||
-      cudaMallocHost(&c->h_scal, 64 * sizeof(double)) != cudaSuccess) {
+      cudaMallocHost(&c->h_scal, kScalHost * sizeof(double)) != cudaSuccess) {
     delete c;
     return set_err(DEV_ERR_HOST_ALLOC);
   }
@@ -492,6 +498,7 @@ lace_gpu_ctx::~lace_gpu_ctx() {
   if (h_ctrl) cudaFreeHost(h_ctrl);
   if (h_scal) cudaFreeHost(h_scal);
   if (own_stream && stream) cudaStreamDestroy(stream);
+  if (side) cudaStreamDestroy(side);
 }
 
 extern "C" int lace_gpu_ctx_destroy(lace_gpu_ctx *c) {
@@ -1602,10 +1609,74 @@ int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) 
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 
+// the modified Gram-Schmidt search-direction loop of one cycle
+// (src/fgmres_restart.cpp:227-494), all on the device
+int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) {
+  const int tf32 = vtype() != VType::F64;
+  // LACE's test reorthogonalises for reorth 0 (when needed) and 2 (always)
+  const bool second = a.mgs_reorth == 0 || a.mgs_reorth == 2;
+  for (int j = 0; j < m; ++j) {
+    void *zj = (char *)a.Z + (size_t)j * a.ldz * (a.z_f32 ? 4 : 8);
+    const double *vj = a.V + (size_t)j * a.ldv;
+    // z_j = U^{-1} L^{-1} v_j (:239-270); outputs marked unsolved before
+    int rc = solve_tri(0, vj, 0, vec_t.p, tf32, true, vec_t2.p, a.prefill != 0);
+    if (!rc) rc = solve_tri(1, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p, a.prefill != 0);
+    if (rc) return rc;
+    launch_mgs_operator(stream, a, j);
+    for (int k = 1; k <= j; ++k) launch_mgs_sweep(stream, a, j, k, 0);
+    if (second && capturing && cond_nodes) {
+      // the second pass in a conditional node that the norm kernel sets
+      cudaStreamCaptureStatus st;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamGetCaptureInfo(stream, &st, nullptr, &g) != cudaSuccess || st != cudaStreamCaptureStatusActive)
+        return DEV_ERR_UNKNOWN;
+      cudaGraphConditionalHandle h;
+      if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+        return DEV_ERR_NOT_SUPPORTED;
+      launch_mgs_norm(stream, a, j, 0, (unsigned long long)h);
+      const cudaGraphNode_t *deps = nullptr;
+      size_t ndeps = 0;
+      if (cudaStreamGetCaptureInfo(stream, &st, nullptr, &g, &deps, nullptr, &ndeps) != cudaSuccess)
+        return DEV_ERR_UNKNOWN;
+      cudaGraphNodeParams p = {};
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = h;
+      p.conditional.type = cudaGraphCondTypeIf;
+      p.conditional.size = 1;
+      cudaGraphNode_t node;
+      if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) != cudaSuccess) return DEV_ERR_NOT_SUPPORTED;
+      cudaGraph_t body = p.conditional.phGraph_out[0];
+      if (cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+          cudaSuccess)
+        return DEV_ERR_NOT_SUPPORTED;
+      for (int k = 0; k <= j; ++k) launch_mgs_sweep(side, a, j, k, 1);
+      launch_mgs_norm(side, a, j, 1, 0);
+      cudaGraph_t captured = body;
+      const cudaError_t ce = cudaStreamEndCapture(side, &captured);
+      if (ce != cudaSuccess || cudaGetLastError() != cudaSuccess) return DEV_ERR_NOT_SUPPORTED;
+      if (cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+          cudaSuccess)
+        return DEV_ERR_UNKNOWN;
+    } else {
+      launch_mgs_norm(stream, a, j, 0, 0);
+      if (second) {  // launched always; returns at once unless the test asked for it
+        for (int k = 0; k <= j; ++k) launch_mgs_sweep(stream, a, j, k, 1);
+        launch_mgs_norm(stream, a, j, 1, 0);
+      }
+    }
+    launch_mgs_next(stream, a, j);
+    if (opt.monitor_orthog) launch_orthog_monitor(stream, a, j, a.V, a.ldv);  // v_0..v_j (:380-387)
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
+}
+
 int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int tol_type,
                          double rtol, bool adjoint, data_d_gmres_log *log, int *total_iters,
-                         std::vector<double> *hist) {
+                         std::vector<double> *hist, int method, int restarted, int reorth) {
   if (m < 1 || m > kMaxM) return DEV_ERR_NOT_SUPPORTED;
+  const bool mgs = method == 1;
+  if (mgs && adjoint) return DEV_ERR_NOT_SUPPORTED;
+  if (mgs && !restarted) restart_max = std::min(restart_max, 1);
   if (!factors_ready && opt.trsv_mode != LACE_TRSV_NONE) return DEV_ERR_NOT_INITIALIZED;
   SetupClock sc(verbose);
   int rc = ensure_krylov(m, opt.monitor_orthog != 0);
@@ -1622,7 +1693,11 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   }
   if (!rc && cudaStreamSynchronize(stream) != cudaSuccess) rc = DEV_ERR_UNKNOWN;
   if (rc) return rc;
+  if (mgs && !side && cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess)
+    return DEV_ERR_UNKNOWN;
   ArnoldiArgs a = arnoldi_args(m, adjoint);
+  a.mgs_restarted = restarted ? 1 : 0;
+  a.mgs_reorth = reorth;
   Cycle *cy = a.cy;
   // tolerance set-up scalars
   {
@@ -1637,48 +1712,80 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     LCHK(cudaMemcpyAsync(&a.ctrl->status, &zero, 4, cudaMemcpyHostToDevice, stream));
   }
   const auto key = std::make_tuple(m, adjoint ? 1 : 0, opt.trsv_mode, rows_per_lane,
-                                   opt.jacobi_sweeps, (int)vtype(), opt.monitor_orthog, lanes);
+                                   opt.jacobi_sweeps, (int)vtype(), opt.monitor_orthog, lanes, method,
+                                   mgs ? (restarted ? 1 : 0) : 0, mgs ? reorth : 0);
   int total = 0;
   bool converged = false;
   int last_cycle = 0, last_steps = 0;
+  last_reorth = 0;
   double rnorm0 = 0.0, final_res = 0.0;
   for (int restart = 0; restart < restart_max; ++restart) {
-    launch_cycle_residual(stream, a, b, x);
-    launch_cycle_init(stream, a);
-    if (opt.monitor_orthog && Qmon.p)
-      launch_convert(stream, n, a.q_f32 ? VType::F32 : VType::F64, a.q, VType::F64, Qmon.p);
+    launch_cycle_residual(stream, a, b, x, mgs);
+    if (mgs) {
+      launch_mgs_cycle_init(stream, a);
+    } else {
+      launch_cycle_init(stream, a);
+      if (opt.monitor_orthog && Qmon.p)
+        launch_convert(stream, n, a.q_f32 ? VType::F32 : VType::F64, a.q, VType::F64, Qmon.p);
+    }
     if (opt.use_graph) {
       auto it = graphs.find(key);
       if (it == graphs.end()) {
         SetupClock gc(verbose);
-        cudaGraph_t g;
-        LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        rc = enqueue_cycle_body(a, m, adjoint);
-        cudaError_t ce = cudaStreamEndCapture(stream, &g);
-        if (rc) {
-          if (ce == cudaSuccess) cudaGraphDestroy(g);
-          return rc;
+        cudaGraphExec_t ge = nullptr;
+        for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
+          cudaGraph_t g;
+          LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+          rc = mgs ? enqueue_mgs_body(a, m, true) : enqueue_cycle_body(a, m, adjoint);
+          cudaError_t ce = cudaStreamEndCapture(stream, &g);
+          if (rc == DEV_ERR_NOT_SUPPORTED && mgs && cond_nodes) {
+            // no conditional nodes here: capture again with the second
+            // pass launched always (its kernels check the test's flag)
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (verbose) printf("%% conditional graph nodes unavailable: the second Gram-Schmidt pass launches always\n");
+            cond_nodes = false;
+            rc = 0;
+            continue;
+          }
+          if (rc) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return rc;
+          }
+          LCHK(ce);
+          gc.mark("cycle graph capture");
+          ce = cudaGraphInstantiate(&ge, g, 0);
+          cudaGraphDestroy(g);
+          LCHK(ce);
+          gc.mark("cycle graph instantiation");
         }
-        LCHK(ce);
-        gc.mark("cycle graph capture");
-        cudaGraphExec_t ge;
-        ce = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
-        LCHK(ce);
-        gc.mark("cycle graph instantiation");
+        if (!ge) return DEV_ERR_UNKNOWN;
         it = graphs.emplace(key, ge).first;
       }
       LCHK(cudaGraphLaunch(it->second, stream));
     } else {
-      rc = enqueue_cycle_body(a, m, adjoint);
+      rc = mgs ? enqueue_mgs_body(a, m, false) : enqueue_cycle_body(a, m, adjoint);
       if (rc) return rc;
     }
-    launch_xupdate(stream, a, x);
+    if (mgs) launch_mgs_xupdate(stream, a, x);
+    else launch_xupdate(stream, a, x);
     LCHK(cudaMemcpyAsync(h_ctrl, a.ctrl, sizeof(Control), cudaMemcpyDeviceToHost, stream));
     LCHK(cudaMemcpyAsync(h_scal, cy->hist, 8 * (size_t)m, cudaMemcpyDeviceToHost, stream));
+    if (mgs) {
+      LCHK(cudaMemcpyAsync(h_scal + kScalCycleRnorm, &cy->rnorm, 8, cudaMemcpyDeviceToHost, stream));
+      LCHK(cudaMemcpyAsync(h_scal + kScalReorth, &cy->nreorth, 4, cudaMemcpyDeviceToHost, stream));
+    }
     LCHK(cudaStreamSynchronize(stream));
     const Control &hc = *h_ctrl;
     if (restart == 0) rnorm0 = hc.rnorm0;
+    // LACE's Gram-Schmidt FGMRES logs the residual at the start of every
+    // cycle (src/fgmres_restart.cpp:221-223), the Householder one the first
+    if (mgs && !(hc.converged && hc.nsteps == 0)) {
+      rnorm0 = h_scal[kScalCycleRnorm];
+      int nr = 0;
+      memcpy(&nr, h_scal + kScalReorth, 4);
+      last_reorth += nr;
+    }
     if (hc.status & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
     const int ns = hc.nsteps;
     if (hist)
@@ -1687,7 +1794,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
       std::vector<double> oh(ns);
       cudaMemcpy(oh.data(), cy->orth, 8 * (size_t)ns, cudaMemcpyDeviceToHost);
       for (int k = 0; k < ns; ++k)
-        printf("FGMRES_Householders_gpu_ortherr(%d) = %.16e;\n", total + k + 1, oh[k]);
+        printf("%s_gpu_ortherr(%d) = %.16e;\n", mgs ? "FGMRES" : "FGMRES_Householders", total + k + 1, oh[k]);
     }
     total += ns;
     if (ns > 0) {
@@ -1727,6 +1834,26 @@ extern "C" int lace_gpu_fgmres_householder(lace_gpu_ctx *c, const double *b, dou
     log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
   return rc;
+}
+
+extern "C" int lace_gpu_fgmres_mgs(lace_gpu_ctx *c, const double *b, double *x, const data_d_gmres_param *par,
+                                   int restarted, data_d_gmres_log *log, int *total_iters) {
+  if (!c || !b || !x || !par) return set_err(DEV_ERR_INVALID_PTR);
+  cudaSetDevice(c->device);
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = c->fgmres(b, x, par->search_max, restarted ? par->restart_max : 1, par->tol_type, par->rtol, false,
+                     log, total_iters, &c->last_hist, 1, restarted ? 1 : 0, par->reorth);
+  if (log)
+    log->solve_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (rc != DEV_SUCCESS && rc != DEV_NOTCONVERGED) return set_err(rc);
+  return rc;
+}
+
+extern "C" int lace_gpu_get_solve_stats(lace_gpu_ctx *c, int *out) {
+  if (!c || !out) return set_err(DEV_ERR_INVALID_PTR);
+  out[0] = c->last_reorth;
+  out[1] = c->cond_nodes ? 1 : 0;
+  return DEV_SUCCESS;
 }
 
 extern "C" int lace_gpu_solve_backward(lace_gpu_ctx *c, const double *x, const double *dLdx,

@@ -124,7 +124,12 @@ struct lace_gpu_ctx {
   DBuf dropin_b, dropin_x;  // right-hand side and solution of the drop-in FGMRES
   lace::Control *h_ctrl = nullptr;
   double *h_scal = nullptr;
-  std::map<std::tuple<int, int, int, int, int, int, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, int, int, int, int, int, int, int, int, int, int>, cudaGraphExec_t> graphs;
+  // second stream: the body of the conditional Gram-Schmidt second pass is
+  // captured on it
+  cudaStream_t side = nullptr;
+  bool cond_nodes = true;  // conditional graph nodes available (else the second pass launches always)
+  int last_reorth = 0;     // directions of the last Gram-Schmidt solve that reorthogonalised
   std::vector<double> last_hist;
 
   ~lace_gpu_ctx();
@@ -172,6 +177,13 @@ struct lace_gpu_ctx {
   int ensure_AT();
   lace::ArnoldiArgs arnoldi_args(int m, bool adjoint);
   int enqueue_cycle_body(const lace::ArnoldiArgs &a, int m, bool adjoint);
+  // the modified Gram-Schmidt cycle; capturing: inside a stream capture (the
+  // second pass goes into conditional nodes when cond_nodes)
+  int enqueue_mgs_body(const lace::ArnoldiArgs &a, int m, bool capturing);
+  // method 0: Householder (fgmres_householder_restart.cpp); 1: modified
+  // Gram-Schmidt, restarted (fgmres_restart.cpp) or one cycle (fgmres.cpp)
+  // with reorth as LACE's gmres_par->reorth
   int fgmres(const double *b, double *x, int m, int restart_max, int tol_type, double rtol,
-             bool adjoint, data_d_gmres_log *log, int *total_iters, std::vector<double> *hist);
+             bool adjoint, data_d_gmres_log *log, int *total_iters, std::vector<double> *hist,
+             int method = 0, int restarted = 1, int reorth = 0);
 };

@@ -34,6 +34,16 @@ struct Cycle {
   int tol_type;
   int first_cycle;
   double rtol;
+  // modified Gram-Schmidt Arnoldi (data_fgmres_restart / data_fgmres):
+  // column j of the Hessenberg matrix before the rotations, the second
+  // pass's coefficients, ||A z_j||, 1/h_{j+1,j} (0 after a breakdown) and
+  // whether this step reorthogonalises
+  double h[kLdT];
+  double hr[kLdT];
+  double normav;
+  double hinv;
+  int reorth;
+  int nreorth;  // steps of the cycle that reorthogonalised
 };
 
 // Handles for the two triangles of one solve direction.
@@ -104,15 +114,44 @@ struct ArnoldiArgs {
   int prefill = 0;
   void *fill_t = nullptr;
   int fill_t_f32 = 0;
+  // modified Gram-Schmidt variant: restarted (data_fgmres_restart: happy
+  // breakdown below 0, the x update column by column) or one cycle
+  // (data_fgmres: breakdown below DBL_EPSILON, x += sum_j z_j y_j);
+  // reorth 0 Brown/Hindmarsh test, 1 never, 2 always
+  int mgs_restarted = 1;
+  int mgs_reorth = 0;
 };
 
-void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x);
+// mgs: set up the Gram-Schmidt cycle (g = ||r|| e_0, rotations cleared)
+// instead of the first reflector
+void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x,
+                           bool mgs = false);
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a);
 void launch_passA(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_orthog_monitor(cudaStream_t s, const ArnoldiArgs &a, int j, double *Q, size_t ldq);
 void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
+
+// ------------------------------------ FGMRES, modified Gram-Schmidt Arnoldi
+// (src/fgmres_restart.cpp, src/fgmres.cpp).  Basis v_j in a.V, the
+// preconditioned vectors z_j in a.Z, u in a.w.  Step j: the two solves
+// z_j = M^{-1} v_j, then
+//   operator : u = A z_j, ||u||, h_0 = v_0 . u
+//   sweep k  : u -= c_{k-1} v_{k-1}, then v_k . u          (k = 1..j)
+//   norm     : u -= c_j v_j, h_{j+1} = ||u||; the Brown/Hindmarsh test, and
+//              (no second pass) the rotations and the convergence test
+//   [second pass when the test asks: sweep k = 0..j and norm again]
+//   next     : v_{j+1} = u / h_{j+1}
+// c_k is h_k in the first pass, the second pass's own coefficient in it.
+// cond: a conditional-node handle set to 1 when the step reorthogonalises
+// (0: none; the second-pass kernels also check Cycle::reorth).
+void launch_mgs_cycle_init(cudaStream_t s, const ArnoldiArgs &a);
+void launch_mgs_operator(cudaStream_t s, const ArnoldiArgs &a, int j);
+void launch_mgs_sweep(cudaStream_t s, const ArnoldiArgs &a, int j, int k, int pass);
+void launch_mgs_norm(cudaStream_t s, const ArnoldiArgs &a, int j, int pass, unsigned long long cond);
+void launch_mgs_next(cudaStream_t s, const ArnoldiArgs &a, int j);
+void launch_mgs_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
 
 // ------------------------------------------------------------ ParILU
 struct IluArgs {

@@ -18,11 +18,9 @@
 
 #include <algorithm>
 
-#include "internal.h"
+#include "krylov_tile.cuh"
 
 namespace lace {
-
-constexpr int kTPB = 256;   // threads per block of the row-tile kernels
 constexpr int kSlots = (kMaxM + 2 + 7) / 8;  // k-slots per warp (8 warps)
 
 // ------------------------------------------------------------------ SpMV
@@ -112,100 +110,6 @@ void launch_bcsr_spmv(cudaStream_t s, int nb, int bs, const int *row, const int 
 
 // --------------------------------------------------- row-tile machinery
 
-// FP32 -> FP64 exactly, with integer operations (conversions run on the FP64
-// unit, the scarce one on this part)
-__device__ __forceinline__ double to_f64(double v) { return v; }
-__device__ __forceinline__ double to_f64(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  unsigned m = b & 0x7fffffu;
-  unsigned long long ef;
-  if (e == 0) {
-    if (m == 0) {
-      ef = 0;
-    } else {  // subnormal: normalise
-      const int sh = __clz((int)m) - 8;
-      m = (m << sh) & 0x7fffffu;
-      ef = (unsigned long long)(897 - sh) << 52;
-    }
-  } else {
-    ef = (unsigned long long)(e == 255 ? 2047u : e + 896u) << 52;
-  }
-  return __longlong_as_double(
-      (long long)(((unsigned long long)(b & 0x80000000u) << 32) | ef | ((unsigned long long)m << 29)));
-}
-
-// operator row i of the tile: CSR (LPR lanes per row) or BCSR (thread/row)
-struct OpView {
-  int bs;
-  const int *row, *col;
-  const double *val;
-  const int *sell_ptr, *sell_col;  // sliced ELL (CSR row pointers give the row lengths)
-  const double *sell_val;
-};
-
-template <int LPR, typename ZT>
-__device__ __forceinline__ void tile_apply(const OpView &op, int n, int base, int tr,
-                                           const ZT *__restrict__ z, double *sw) {
-  if (op.bs == 0 && op.sell_ptr != nullptr) {
-    // sliced ELL: warp w takes the 32-row slices w, w+8, ... of the tile; entry
-    // t of the slice's rows is one coalesced load, four entries in flight
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t0 = wid * 32; t0 < tr; t0 += kTPB) {
-      const int i = base + t0 + lane;
-      double s = 0.0;
-      if (i < n) {
-        const int len = op.row[i + 1] - op.row[i];
-        const int *cp = op.sell_col + op.sell_ptr[(base + t0) >> 5] + lane;
-        const double *vp = op.sell_val + (cp - op.sell_col);
-        for (int t = 0; t < len; t += 4) {
-          int c[4];
-          double v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (t + u < len) {
-              c[u] = cp[32 * (t + u)];
-              v[u] = vp[32 * (t + u)];
-            }
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (t + u < len) s = fma(v[u], to_f64(z[c[u]]), s);
-        }
-      }
-      sw[t0 + lane] = s;
-    }
-  } else if (op.bs == 0) {
-    const int sub = threadIdx.x & (LPR - 1);
-    const int grp = threadIdx.x / LPR;
-    constexpr int G = kTPB / LPR;
-    for (int t = grp; t < tr; t += G) {
-      const int i = base + t;
-      double s = 0.0;
-      if (i < n) {
-        const int e = op.row[i + 1];
-        for (int p = op.row[i] + sub; p < e; p += LPR) s = fma(op.val[p], to_f64(z[op.col[p]]), s);
-      }
-#pragma unroll
-      for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
-      if (sub == 0) sw[t] = s;
-    }
-  } else {
-    const int bs = op.bs, ld = bs * bs;
-    for (int t = threadIdx.x; t < tr; t += kTPB) {
-      const int i = base + t;
-      double s = 0.0;
-      if (i < n) {
-        const int I = i / bs, r = i - I * bs;
-        for (int p = op.row[I]; p < op.row[I + 1]; ++p) {
-          const double *blk = op.val + (size_t)p * ld + r * bs;
-          const ZT *zj = z + (size_t)op.col[p] * bs;
-          for (int c = 0; c < bs; ++c) s = fma(blk[c], to_f64(zj[c]), s);
-        }
-      }
-      sw[t] = s;
-    }
-  }
-}
 
 // acc[slot] += sum over tile rows (masked by lo) of V[k][i] * sw[t]  with
 // k = slot*8 + warp.  Lanes walk rows, warps walk columns: every V load is a
@@ -257,40 +161,19 @@ __device__ __forceinline__ void block_reduce_slots(double (&acc)[NS], int ncols,
   }
 }
 
-__device__ __forceinline__ double block_sum(double v, double *scratch) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  v = warp_sum(v);
-  __syncthreads();
-  if (lane == 0) scratch[wid] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kTPB / 32; ++w) t += scratch[w];
-  return t;  // valid in thread 0
-}
 
-// last block: sred[k] = sum over blocks of partials[b*kLdT + k], k < count;
-// warp w takes k = w, w+8, ..., its lanes stride over the blocks (fixed
-// order, so the result is deterministic)
-__device__ __forceinline__ void fold_partials(const double *partials, int count, double *sred) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int k = wid; k < count; k += kTPB / 32) {
-    double s = 0.0;
-    for (int bb = lane; bb < (int)gridDim.x; bb += 32) s += partials[(size_t)bb * kLdT + k];
-    s = warp_sum(s);
-    if (lane == 0) sred[k] = s;
-  }
-}
 
 // ------------------------------------------------------- cycle start
 
 // r = b - A x (into a.w) and ||r||; last block sets up the first reflector
 // scalars (LACE :209-236, :239-308) and the convergence test at cycle start.
+// mgs: the Gram-Schmidt cycle instead (src/fgmres_restart.cpp:181-219):
+// g = ||r|| e_0 and the rotations cleared, 1/||r|| for v_0.
 template <int LPR>
 __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const double *__restrict__ b,
                                                          const double *__restrict__ x,
                                                          double *__restrict__ r, double *partials,
-                                                         Cycle *cy, Control *ctrl) {
+                                                         Cycle *cy, Control *ctrl, int mgs, int m) {
   __shared__ double sw[kTPB];
   __shared__ double scratch[kTPB / 32];
   const int tr = (op.bs == 0) ? kTPB : (kTPB / op.bs) * op.bs;
@@ -326,6 +209,14 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
       ctrl->done = 1;
       ctrl->converged = (rnorm < ctrl->rtol_abs) ? 1 : 0;
       if (!(rnorm == rnorm)) ctrl->status |= kStatusBreakdown;
+    } else if (mgs) {
+      for (int k = 0; k <= m; ++k) cy->g[k] = 0.0;
+      for (int k = 0; k < m; ++k) cy->cs[k] = cy->sn[k] = 0.0;
+      cy->g[0] = rnorm;
+      cy->hinv = 1.0 / rnorm;
+      cy->nreorth = 0;
+      ctrl->done = 0;
+      ctrl->converged = 0;
     } else {
       const double r0 = r[0];
       const double dd = mysgn(r0) * rnorm;
@@ -341,36 +232,6 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
 }
 
 // V[:,0] = (r + dd e_0)/alpha,  q = -r/dd
-// FP64 -> FP32 with integer operations, rounding toward zero (the FP64 unit,
-// which also converts, is the scarce one).  Finite values only: below the
-// FP32 normal range they become 0, above it NaN.
-__device__ __forceinline__ float dtof_rz(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
-  const unsigned m = ((hi & 0xfffffu) << 3) | ((unsigned)b >> 29);
-  const unsigned mag = e <= 0 ? 0u : (e >= 255 ? 0x7fc00000u : (((unsigned)e << 23) | m));
-  return __uint_as_float((hi & 0x80000000u) | mag);
-}
-
-// the unsolved pattern (all ones) into row i of an FP32 or FP64 vector: the
-// sync-free solve that writes the vector polls it until the pattern is gone
-__device__ __forceinline__ void mark_unsolved(void *x, int f32, size_t i) {
-  if (f32) reinterpret_cast<unsigned *>(x)[i] = ~0u;
-  else reinterpret_cast<unsigned long long *>(x)[i] = ~0ull;
-}
-
-// the vectors the next step's two solves write, marked unsolved (null: none)
-struct Prefill {
-  void *t, *z;
-  int t_f32, z_f32;
-};
-
-__device__ __forceinline__ void prefill_row(const Prefill &f, size_t i) {
-  if (f.t) mark_unsolved(f.t, f.t_f32, i);
-  if (f.z) mark_unsolved(f.z, f.z_f32, i);
-}
-
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
                                                      double *__restrict__ V, float *__restrict__ Vf,
@@ -784,9 +645,6 @@ __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ 
 
 // ------------------------------------------------------------ launchers
 
-static OpView opview(const ArnoldiArgs &a) {
-  return OpView{a.bs, a.row, a.col, a.val, a.sell_ptr, a.sell_col, a.sell_val};
-}
 
 __global__ void k_sell_values(size_t count, const int *__restrict__ map, const double *__restrict__ src,
                               double *__restrict__ dst) {
@@ -802,28 +660,19 @@ void launch_sell_values(cudaStream_t s, size_t count, const int *map, const doub
   k_sell_values<<<grid, 256, 0, s>>>(count, map, src, dst);
 }
 
-static int rowgrid(int n) {
-  int g = (n + kTPB - 1) / kTPB;
-  return min(g, num_sms() * 8);
-}
 
-void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x) {
+void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b, const double *x, bool mgs) {
   OpView op = opview(a);
+  const int g = mgs ? 1 : 0;
   switch (a.bs ? 8 : (a.lanes <= 8 ? 1 : a.lanes)) {
-    case 1: k_cycle_residual<1><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
-    case 4: k_cycle_residual<4><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
-    case 16: k_cycle_residual<16><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
-    case 32: k_cycle_residual<32><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
-    default: k_cycle_residual<8><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl); break;
+    case 1: k_cycle_residual<1><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl, g, a.m); break;
+    case 4: k_cycle_residual<4><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl, g, a.m); break;
+    case 16: k_cycle_residual<16><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl, g, a.m); break;
+    case 32: k_cycle_residual<32><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl, g, a.m); break;
+    default: k_cycle_residual<8><<<a.grid, kTPB, 0, s>>>(a.n, op, b, x, a.w, a.partials, a.cy, a.ctrl, g, a.m); break;
   }
 }
 
-// the outputs of step j's two solves (the L solve's vector and column j of Z)
-static Prefill prefill_for(const ArnoldiArgs &a, int j) {
-  if (!a.prefill || j >= a.m) return Prefill{nullptr, nullptr, 0, 0};
-  void *zj = (char *)a.Z + (size_t)j * a.ldz * (a.z_f32 ? 4 : 8);
-  return Prefill{a.fill_t, zj, a.fill_t_f32, a.z_f32};
-}
 
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
   const Prefill pf = prefill_for(a, 0);
@@ -833,19 +682,6 @@ void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
     k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, nullptr, (double *)a.q, a.cy, a.ctrl, pf);
 }
 
-// One wave: as many blocks as are resident at once (the passes loop over
-// their row tiles), so no partly filled last wave, and the last block folds
-// few partial sums.  Never more than the ArnoldiArgs grid the partial-sum
-// buffer is sized for.
-template <typename K>
-static int wave_grid(K kernel, int cap) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTPB, 0) != cudaSuccess || per_sm <= 0) {
-    cudaGetLastError();
-    return cap;
-  }
-  return std::max(1, std::min(cap, per_sm * num_sms()));
-}
 
 // dot-product slots per warp for j+1 basis columns
 static int slots_for(int jp1) {

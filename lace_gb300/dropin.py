@@ -204,6 +204,24 @@ def parilu_mats(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None)
 
 def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
                                rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, single_cycle=False):
+    """data_fgmres_householder_restart (or data_fgmres_householder)."""
+    f = lib()
+    fn = f.data_fgmres_householder if single_cycle else f.data_fgmres_householder_restart
+    return _fgmres_call(fn, A, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog, 0)
+
+
+def fgmres_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
+                   rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, reorth=0, single_cycle=False):
+    """data_fgmres_restart, FGMRES with modified Gram-Schmidt (or data_fgmres:
+    one cycle)."""
+    f = lib()
+    fn = f.data_fgmres if single_cycle else f.data_fgmres_restart
+    return _fgmres_call(fn, A, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog,
+                        reorth)
+
+
+def _fgmres_call(fn, A: Mat, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog,
+                 reorth):
     bv = dense(b, copy=False)
     xv = dense(x0)
     par = GmresParam()
@@ -214,11 +232,10 @@ def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, sear
     par.user_csrtrsv_choice = choice
     par.monitorOrthog = monitor_orthog
     par.precondition = 1
+    par.reorth = reorth
     log = GmresLog()
-    f = lib()
     Lr = L.ref if L is not None else None
     Ur = U.ref if U is not None else None
-    fn = f.data_fgmres_householder if single_cycle else f.data_fgmres_householder_restart
     rc = fn(A.ref, bv.ref, xv.ref, Lr, Ur, C.byref(par), C.byref(log))
     # the solution is written into x0's array in place: hand that array back
     own = xv.keep[-1]

@@ -282,6 +282,158 @@ def test_fgmres_mixed_precision(lg, torch_cuda, prec, mode):
         assert abs(res.total_iterations - r.total_iterations) <= 2
 
 
+@pytest.mark.parametrize("name,sweeps,m", [("lap64", 5, 30), ("cd16", 3, 50), ("cd_20x9x7", 3, 12)])
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("reorth", [0, 2])
+def test_fgmres_mgs_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, reorth):
+    """Same factors, FP64: GPU FGMRES with modified Gram-Schmidt (one kernel
+    per Gram-Schmidt sum, the second pass in a conditional graph node)
+    against the oracle's mirror of LACE's data_fgmres_restart: 1e-10
+    relative residual within +-2 directions, x within 1e-7, the initial
+    residual to 1e-12 relative."""
+    A = MATS[name]()
+    b = A.matvec(np.ones(A.n)) if name == "lap64" else P.rhs_normal(A.n, 0)
+    F = orc.parilu(A.row, A.col, A.val, sweeps, mode="sync")
+    r = orc.fgmres_mgs({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                       search_max=m, restart_max=50, rtol=1e-10, reorth=reorth)
+    with lg.Context(0) as ctx:
+        ctx.set_options(use_graph=graph)
+        ctx.upload(A)
+        ctx.parilu0(sweeps)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=m, restart_max=50, rtol=1e-10,
+                         orthogonalization="mgs", reorth=reorth)
+        x = xd.cpu().numpy()
+    assert res.converged and r.converged
+    assert abs(res.total_iterations - r.total_iterations) <= 2, (res.total_iterations, r.total_iterations)
+    if res.restarts == r.restarts:
+        # LACE logs the residual at the start of the final cycle
+        assert abs(res.initial_residual - r.initial_residual) <= 1e-6 * r.initial_residual
+    assert _true_rel(A, x, b) <= 2e-10
+    assert np.linalg.norm(x - r.x) <= 1e-7 * np.linalg.norm(r.x)
+
+
+@pytest.mark.parametrize("restarted", [True, False])
+def test_fgmres_mgs_one_cycle_and_restarted(lg, torch_cuda, restarted):
+    """data_fgmres (one cycle: stops at search_max) and data_fgmres_restart
+    on a system that needs more than one cycle: log and x as the oracle's."""
+    A = MATS["cd16"]()
+    b = P.rhs_normal(A.n, 1)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync")
+    r = orc.fgmres_mgs({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                       search_max=8, restart_max=50, rtol=1e-10, restarted=restarted)
+    with lg.Context(0) as ctx:
+        ctx.upload(A)
+        ctx.parilu0(3)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=8, restart_max=50, rtol=1e-10,
+                         orthogonalization="mgs", restarted=restarted)
+        x = xd.cpu().numpy()
+    assert res.converged == r.converged
+    assert res.search_directions == r.search_directions
+    if restarted:
+        assert abs(res.restarts - r.restarts) <= 1
+        assert _true_rel(A, x, b) <= 2e-10
+    else:
+        assert res.restarts == 0 and res.total_iterations == 8
+        assert abs(res.final_residual - r.final_residual) <= 1e-6 * r.final_residual
+    assert np.linalg.norm(x - r.x) <= 1e-6 * np.linalg.norm(r.x)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16"])
+@pytest.mark.parametrize("mode", ["syncfree", "levels", "jacobi"])
+def test_fgmres_mgs_mixed_precision(lg, torch_cuda, prec, mode):
+    """FP32/BF16 factors inside the FP64 Gram-Schmidt FGMRES: the same 1e-10
+    relative residual."""
+    A = MATS["cd16"]()
+    b = P.rhs_normal(A.n, 0)
+    F = orc.parilu(A.row, A.col, A.val, 3, mode="sync")
+    r = orc.fgmres_mgs({"kind": "csr", "row": A.row, "col": A.col, "val": A.val}, orc.ilu_precond(F), b,
+                       search_max=50, restart_max=50, rtol=1e-10)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec, trsv=mode, jacobi_sweeps=12)
+        ctx.upload(A)
+        ctx.parilu0(3)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=50, rtol=1e-10,
+                         orthogonalization="mgs")
+        x = xd.cpu().numpy()
+    assert res.converged
+    assert _true_rel(A, x, b) <= 2e-10
+    if mode != "jacobi" and prec == "fp32":
+        assert abs(res.total_iterations - r.total_iterations) <= 2
+
+
+@pytest.mark.parametrize("restarted", [1, 0])
+@pytest.mark.parametrize("choice", [0, 2])
+def test_dropin_fgmres_mgs_reorthogonalisation(lg, restarted, choice):
+    """LACE's Brown/Hindmarsh reorthogonalisation and happy breakdown
+    (golden case: 20 decoupled 2x2 blocks, two eigenvalues) through
+    data_fgmres_restart / data_fgmres: LACE's direction count, x to 1e-12."""
+    import os
+    from lace_gb300 import dropin
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "lace_golden.npz"))
+    S = P.CSR(40, G["blk2_row"], G["blk2_col"], G["blk2_val"])
+    Sm = dropin.csr(S.row, S.col, S.val, S.n)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(Sm, reduction=1e-15)
+    L = dropin.csr(lp, li, lv, S.n, dropin.Magma_CSRL)
+    U = dropin.csr(up, ui, uv, S.n, dropin.Magma_CSCU)
+    k = f"blk2_mgs{restarted}{choice}"
+    x, rc, log = dropin.fgmres_restart(Sm, G["blk2_b"], np.zeros(S.n), L, U, search_max=10, restart_max=3,
+                                       rtol=1e-12, tol_type=1, choice=choice, single_cycle=not restarted)
+    assert rc == 0
+    assert log["search_directions"] == int(G[f"{k}_log"][2])
+    assert np.linalg.norm(x - G[f"{k}_x"]) <= 1e-12 * np.linalg.norm(G[f"{k}_x"])
+
+
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("reorth", [0, 2])
+def test_fgmres_mgs_second_pass_runs(lg, torch_cuda, graph, reorth):
+    """The reorthogonalising pass runs exactly where LACE's runs: once on the
+    2x2-block golden case (reorth 0: the Brown/Hindmarsh test), at every
+    direction with reorth 2; from the conditional graph node when graphs are
+    on."""
+    import os
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "lace_golden.npz"))
+    S = P.CSR(40, G["blk2_row"], G["blk2_col"], G["blk2_val"])
+    b = G["blk2_b"]
+    with lg.Context(0) as ctx:
+        ctx.set_options(use_graph=graph, trsv="none")
+        ctx.upload(S)
+        xd = torch_cuda.zeros(S.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=10, restart_max=3, rtol=1e-12,
+                         orthogonalization="mgs", reorth=reorth)
+        st = ctx.solve_stats()
+        x = xd.cpu().numpy()
+    lg_ = G["blk2_mgs12_log"]
+    assert res.search_directions == int(lg_[2])
+    assert st["reorthogonalised"] == (int(lg_[5]) if reorth == 0 else res.total_iterations)
+    if graph:
+        assert st["conditional_nodes"]
+    assert np.linalg.norm(x - G["blk2_mgs12_x"]) <= 1e-12 * np.linalg.norm(G["blk2_mgs12_x"])
+
+
+def test_dropin_fgmres_mgs_trefethen(lg):
+    """LACE's FGMRESPreconditionedRestart test (testing/test_linearSolver.cpp:
+    407-505) through data_fgmres_restart: Trefethen_20, b = ones, x0 = 0, abs
+    tol 1e-3, search 20, restart 100, monitorOrthog on; exact solves, then
+    ParCSRTRSV and no preconditioner; data_fgmres (one cycle) too."""
+    from lace_gb300 import dropin
+    A = P.trefethen(19)
+    Am = dropin.csr(A.row, A.col, A.val, A.n)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(Am, reduction=1e-15)
+    L = dropin.csr(lp, li, lv, A.n, dropin.Magma_CSRL)
+    U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
+    b = np.ones(A.n)
+    for choice in (0, 1, 2):
+        for single in (False, True):
+            x, rc, log = dropin.fgmres_restart(Am, b, np.zeros(A.n), L, U, search_max=20, restart_max=100,
+                                               rtol=1e-3, tol_type=0, choice=choice, monitor_orthog=1,
+                                               single_cycle=single)
+            assert rc == 0, (choice, single)
+            assert np.linalg.norm(b - A.matvec(x)) <= 1e-3
+
+
 def test_dropin_trefethen_linear_solver(lg):
     """LACE's FGMRESHouseholderPreconditionedRestart test
     (testing/test_linearSolver.cpp:621-726) through the drop-in entry points:
