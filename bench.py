@@ -162,16 +162,16 @@ def run_ours(args):
         R, cpb, w, cl = (int(v) for v in args.trsv_schedule.split(","))
         pin = {"rows_per_lane": R, "schedule": (cpb, w, cl)}
 
-    def solve(prec):
+    def solve(prec, orth="householder"):
         ctx.set_options(precision=prec, **pin)
         with torch.cuda.stream(stream):
             xd.zero_()
         ctx.parilu0(SWEEPS)
-        return ctx.fgmres(bd, xd, search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+        return ctx.fgmres(bd, xd, search_max=M, restart_max=RESTART_MAX, rtol=RTOL, orthogonalization=orth)
 
-    def timed(prec, k, w):
+    def timed(prec, k, w, orth="householder"):
         for _ in range(w):
-            solve(prec)
+            solve(prec, orth)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -182,7 +182,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(k):
             ev0.record(stream)
-            res = solve(prec)
+            res = solve(prec, orth)
             ev1.record(stream)
             ev1.synchronize()
             times.append(ev0.elapsed_time(ev1) / 1e3)
@@ -192,12 +192,25 @@ def run_ours(args):
             torch.distributed.barrier()
         return times, wall, res
 
+    if args.only_mgs:
+        # profiling aid: the Gram-Schmidt solve alone (no contract line)
+        t_mgs, _, r_mgs = timed("fp32", args.steps, args.warmup, "mgs")
+        if rank == 0:
+            print(json.dumps({"mgs": {"value": statistics.median(t_mgs), "unit": "s",
+                                      "iterations": r_mgs.total_iterations}}))
+        ctx.close()
+        return
+
     with ClockSampler(local) as clk:
         t_mixed, wall_mixed, r_mixed = timed("fp32", args.steps, args.warmup)
     clocks = clk.summary()
     x_mixed = xd.cpu().numpy()
     t_fp64, wall_fp64, r_fp64 = timed("fp64", max(2, args.steps // 2), 1)
     x_fp64 = xd.cpu().numpy()
+    # the same solve with LACE's other Krylov solver, FGMRES with modified
+    # Gram-Schmidt (data_fgmres_restart), mixed precision
+    t_mgs, wall_mgs, r_mgs = timed("fp32", max(2, args.steps // 2), 1, "mgs")
+    x_mgs = xd.cpu().numpy()
 
     def true_rel(x):
         return float(np.linalg.norm(b - A.matvec(x)) / np.linalg.norm(b))
@@ -308,6 +321,9 @@ def run_ours(args):
         "iterations": {"mixed": r_mixed.total_iterations, "fp64": r_fp64.total_iterations},
         "true_rel_resid": {"mixed": true_rel(x_mixed), "fp64": true_rel(x_fp64)},
         "fp64": {"value": statistics.median(t_fp64), "unit": "s"},
+        "mgs": {"value": statistics.median(t_mgs), "unit": "s", "iterations": r_mgs.total_iterations,
+                "true_rel_resid": true_rel(x_mgs),
+                "path": "lace_gpu_fgmres_mgs (data_fgmres_restart semantics), fp32 factors"},
         "speedup_mixed_vs_fp64": statistics.median(t_fp64) / med,
         "kernels": {"sptrsv_pair_s": trsv_s, "sptrsv_pair_gbs": trsv_gbs, "spmv_s": spmv_s,
                     "spmv_gbs": spmv_gbs},
@@ -386,6 +402,8 @@ def main():
                     help="R,chunks,warps,cluster: pin the sync-free solve schedule (the autotune's choice is "
                          "reported as roofline.schedule) - for profiling the same kernels under ncu, whose "
                          "launch overhead would change the autotune's choice")
+    ap.add_argument("--only-mgs", action="store_true",
+                    help="time only the FGMRES with modified Gram-Schmidt (for profiling its kernels)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":

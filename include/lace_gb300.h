@@ -387,9 +387,11 @@ int lace_gpu_fgmres_mgs(lace_gpu_ctx *ctx, const double *b, double *x,
 
 /* Facts about the last FGMRES solve of this context: out[0] = directions
  * that the Gram-Schmidt FGMRES reorthogonalised (LACE prints
- * "Reorthogonalize" for each), out[1] = 1 when its second pass runs as a
- * conditional CUDA graph node (0: launched always, its kernels return at
- * once unless needed). */
+ * "Reorthogonalize" for each); out[1] = 1 when conditional CUDA graph nodes
+ * are available (the separate-kernel step puts its second pass in one);
+ * out[2] = 1 when each Arnoldi step after the solves runs as one cooperative
+ * kernel (environment LACE_GB300_MGS_STEP=0 at context creation selects the
+ * separate kernels). */
 int lace_gpu_get_solve_stats(lace_gpu_ctx *ctx, int *out);
 
 /* Adjoint of the solve x = A^{-1} b for a loss L(x): given dL/dx (device),

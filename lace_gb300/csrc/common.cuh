@@ -87,6 +87,41 @@ __device__ __forceinline__ bool arrive_last(int *counter) {
   return s_last != 0;
 }
 
+// sum of p[b * step] over b = first, first + stride, ... < end, added in
+// that order with eight loads in flight (a serial walk over a grid's
+// partial sums costs one L2 round trip per block).  L2 loads: the partials
+// were written by other blocks of the same grid.
+__device__ __forceinline__ double strided_sum(const double *p, size_t step, int first, int stride, int end) {
+  double s = 0.0;
+  int b = first;
+  for (; b + 7 * stride < end; b += 8 * stride) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldcg(p + (size_t)(b + u * stride) * step);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
+  for (; b < end; b += stride) s += __ldcg(p + (size_t)b * step);
+  return s;
+}
+
+// the last block's fold of count partial sums p[b * step], by all of its
+// threads: thread t adds b = t, t + blockDim.x, ..., then the warps and the
+// warp sums in a fixed order (deterministic for a given grid).  Every thread
+// of the block calls it; the sum is valid in thread 0.
+__device__ __forceinline__ double block_fold(const double *p, size_t step, int count) {
+  __shared__ double s_fold[32];
+  double s = strided_sum(p, step, threadIdx.x, blockDim.x, count);
+  s = warp_sum(s);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s_fold[threadIdx.x >> 5] = s;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_fold[w];
+  return t;
+}
+
 // mysgn of LACE (include/sparse.h:1129-1133): +1 for v >= 0, -1 otherwise
 __device__ __forceinline__ double mysgn(double v) { return v >= 0.0 ? 1.0 : -1.0; }
 

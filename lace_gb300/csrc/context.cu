@@ -460,6 +460,8 @@ extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream)
   lace_gpu_ctx *c = new lace_gpu_ctx();
   c->device = device;
   c->verbose = getenv("LACE_GB300_VERBOSE") != nullptr;
+  // LACE_GB300_MGS_STEP=0: the Gram-Schmidt step as separate kernels
+  if (const char *e = getenv("LACE_GB300_MGS_STEP")) c->mgs_persistent = atoi(e) != 0;
   lace_gpu_default_options(&c->opt);
   if (stream) {
     c->stream = (cudaStream_t)stream;
@@ -1622,6 +1624,18 @@ int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) 
     int rc = solve_tri(0, vj, 0, vec_t.p, tf32, true, vec_t2.p, a.prefill != 0);
     if (!rc) rc = solve_tri(1, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p, a.prefill != 0);
     if (rc) return rc;
+    // the whole step as one cooperative kernel where it applies
+    const int st = mgs_persistent ? launch_mgs_step(stream, a, j) : 1;
+    if (st == 2) {
+      // the cooperative launch was refused: inside a capture that ends the
+      // capture, so start it again without; otherwise carry on without
+      mgs_persistent = false;
+      if (verbose) printf("%% cooperative launch refused: the Gram-Schmidt step runs as separate kernels\n");
+      if (capturing) return DEV_ERR_NOT_SUPPORTED;
+    } else if (st == 0) {
+      if (opt.monitor_orthog) launch_orthog_monitor(stream, a, j, a.V, a.ldv);
+      continue;
+    }
     launch_mgs_operator(stream, a, j);
     for (int k = 1; k <= j; ++k) launch_mgs_sweep(stream, a, j, k, 0);
     if (second && capturing && cond_nodes) {
@@ -1631,8 +1645,10 @@ int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) 
       if (cudaStreamGetCaptureInfo(stream, &st, nullptr, &g) != cudaSuccess || st != cudaStreamCaptureStatusActive)
         return DEV_ERR_UNKNOWN;
       cudaGraphConditionalHandle h;
-      if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+      if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+        cond_nodes = false;
         return DEV_ERR_NOT_SUPPORTED;
+      }
       launch_mgs_norm(stream, a, j, 0, (unsigned long long)h);
       const cudaGraphNode_t *deps = nullptr;
       size_t ndeps = 0;
@@ -1644,6 +1660,7 @@ int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) 
       p.conditional.type = cudaGraphCondTypeIf;
       p.conditional.size = 1;
       cudaGraphNode_t node;
+      cond_nodes = false;  // until the node is in place
       if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) != cudaSuccess) return DEV_ERR_NOT_SUPPORTED;
       cudaGraph_t body = p.conditional.phGraph_out[0];
       if (cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
@@ -1654,6 +1671,7 @@ int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) 
       cudaGraph_t captured = body;
       const cudaError_t ce = cudaStreamEndCapture(side, &captured);
       if (ce != cudaSuccess || cudaGetLastError() != cudaSuccess) return DEV_ERR_NOT_SUPPORTED;
+      cond_nodes = true;
       if (cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
           cudaSuccess)
         return DEV_ERR_UNKNOWN;
@@ -1710,6 +1728,9 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     LCHK(cudaMemcpyAsync(&cy->rtol, &hs.rtol, 8, cudaMemcpyHostToDevice, stream));
     int zero = 0;
     LCHK(cudaMemcpyAsync(&a.ctrl->status, &zero, 4, cudaMemcpyHostToDevice, stream));
+    // grid-barrier arrivals of the one-kernel Gram-Schmidt step (left
+    // non-zero only by a step that gave up a wait)
+    LCHK(cudaMemsetAsync(&a.ctrl->block_count[3], 0, 4, stream));
   }
   const auto key = std::make_tuple(m, adjoint ? 1 : 0, opt.trsv_mode, rows_per_lane,
                                    opt.jacobi_sweeps, (int)vtype(), opt.monitor_orthog, lanes, method,
@@ -1733,18 +1754,17 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
       if (it == graphs.end()) {
         SetupClock gc(verbose);
         cudaGraphExec_t ge = nullptr;
-        for (int attempt = 0; attempt < 2 && !ge; ++attempt) {
+        for (int attempt = 0; attempt < 3 && !ge; ++attempt) {
           cudaGraph_t g;
           LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
           rc = mgs ? enqueue_mgs_body(a, m, true) : enqueue_cycle_body(a, m, adjoint);
           cudaError_t ce = cudaStreamEndCapture(stream, &g);
-          if (rc == DEV_ERR_NOT_SUPPORTED && mgs && cond_nodes) {
-            // no conditional nodes here: capture again with the second
-            // pass launched always (its kernels check the test's flag)
+          if (rc == DEV_ERR_NOT_SUPPORTED && mgs && attempt < 2) {
+            // a refused cooperative launch or conditional node (the flag
+            // that chose it is cleared): capture again without it
             if (ce == cudaSuccess) cudaGraphDestroy(g);
             cudaGetLastError();
-            if (verbose) printf("%% conditional graph nodes unavailable: the second Gram-Schmidt pass launches always\n");
-            cond_nodes = false;
+            if (verbose && !cond_nodes) printf("%% conditional graph nodes unavailable: the second Gram-Schmidt pass launches always\n");
             rc = 0;
             continue;
           }
@@ -1853,6 +1873,7 @@ extern "C" int lace_gpu_get_solve_stats(lace_gpu_ctx *c, int *out) {
   if (!c || !out) return set_err(DEV_ERR_INVALID_PTR);
   out[0] = c->last_reorth;
   out[1] = c->cond_nodes ? 1 : 0;
+  out[2] = c->mgs_persistent ? 1 : 0;
   return DEV_SUCCESS;
 }
 

@@ -129,6 +129,7 @@ struct lace_gpu_ctx {
   // captured on it
   cudaStream_t side = nullptr;
   bool cond_nodes = true;  // conditional graph nodes available (else the second pass launches always)
+  bool mgs_persistent = true;  // the one-kernel Gram-Schmidt step (cooperative launch) available
   int last_reorth = 0;     // directions of the last Gram-Schmidt solve that reorthogonalised
   std::vector<double> last_hist;
 

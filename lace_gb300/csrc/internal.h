@@ -152,6 +152,11 @@ void launch_mgs_sweep(cudaStream_t s, const ArnoldiArgs &a, int j, int k, int pa
 void launch_mgs_norm(cudaStream_t s, const ArnoldiArgs &a, int j, int pass, unsigned long long cond);
 void launch_mgs_next(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_mgs_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
+// the whole step after the solves (operator, both passes, rotations, next
+// vector) as one cooperative kernel with u in shared memory; returns 1 when
+// it does not apply (BCSR, no sliced ELL, u too large for shared memory),
+// 2 when the cooperative launch failed, 0 on success
+int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j);
 
 // ------------------------------------------------------------ ParILU
 struct IluArgs {

@@ -194,9 +194,8 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
   double tot = block_sum(nrm, scratch);
   if (threadIdx.x == 0) partials[blockIdx.x] = tot;
   if (!arrive_last(&ctrl->block_count[0])) return;
+  const double s = block_fold(partials, 1, (int)gridDim.x);
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < (int)gridDim.x; ++k) s += partials[k];
     const double rnorm = sqrt(s);
     cy->rnorm = rnorm;
     if (cy->first_cycle) {

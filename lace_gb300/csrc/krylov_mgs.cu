@@ -43,14 +43,9 @@ __device__ __forceinline__ void block_sum2(double &a, double &b, double *scratch
 }
 
 // the last block's sum of partials[b * kLdT + k] over the blocks, in fixed
-// order (valid in every thread of warp 0)
+// order (valid in thread 0; every thread calls it)
 __device__ __forceinline__ double fold_one(const double *partials, int k) {
-  double s = 0.0;
-  if (threadIdx.x < 32) {
-    for (int bb = threadIdx.x; bb < (int)gridDim.x; bb += 32) s += partials[(size_t)bb * kLdT + k];
-    s = warp_sum(s);
-  }
-  return s;
+  return block_fold(partials + k, kLdT, (int)gridDim.x);
 }
 
 // ------------------------------------------------------------ cycle start
@@ -124,6 +119,8 @@ __global__ void __launch_bounds__(kTPB) k_mgs_sweep(int n, const double *__restr
   const double *vk = V + (size_t)k * ldv;
   double dot = 0.0;
   const int npair = n / 2;
+  // a few row pairs per thread: unrolled so that their loads are in flight together
+#pragma unroll 4
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += gridDim.x * blockDim.x) {
     const int i = 2 * p;
     double2 uu = *reinterpret_cast<const double2 *>(u + i);
@@ -218,6 +215,7 @@ __global__ void __launch_bounds__(kTPB) k_mgs_norm(int n, const double *__restri
   const double *vj = V + (size_t)j * ldv;
   double nrm = 0.0;
   const int npair = n / 2;
+#pragma unroll 4
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += gridDim.x * blockDim.x) {
     const int i = 2 * p;
     double2 uu = *reinterpret_cast<const double2 *>(u + i);
@@ -312,7 +310,312 @@ __global__ void __launch_bounds__(kTPB) k_mgs_xupdate(int n, const ZT *__restric
   }
 }
 
+// ------------------------------------------ one persistent kernel per step
+
+// The whole Arnoldi step after the solves (operator, both Gram-Schmidt
+// passes, rotations, the next basis vector) in one cooperative launch of
+// one block per SM: block b keeps rows [b*RB, (b+1)*RB) of u in shared
+// memory, and each Gram-Schmidt sum is a block sum, a grid barrier and a
+// fold of the blocks' partial sums that every block performs in the same
+// order, so every block holds the same coefficient.  u never leaves the SM;
+// a sum costs one barrier instead of a kernel boundary.
+constexpr int kStepTPB = 1024;
+constexpr int kStepSmemMax = 200 * 1024;  // rows of u per block: at most 25,600 (plus 16 KB static)
+
+// Grid barrier over a cooperatively launched grid (Control::block_count[3]
+// arrivals, [4] generation).  Bounded: a wait that gives up sets
+// kStatusSpinTimeout, and every block leaves at its next barrier.
+__device__ __forceinline__ bool grid_barrier(Control *ctrl) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int *count = &ctrl->block_count[3];
+    int *gen = &ctrl->block_count[4];
+    const int g = ld_acquire(gen);
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(count, 1) == (int)gridDim.x - 1) {
+      *count = 0;
+      st_release(gen, g + 1);
+    } else {
+      for (int spins = 0;; ++spins) {
+        if (ld_acquire(gen) != g) break;
+        if (spins > kMaxSpins || ((spins & 1023) == 1023 && (ld_relaxed(&ctrl->status) & kStatusSpinTimeout))) {
+          atomicOr(&ctrl->status, kStatusSpinTimeout);
+          ok = 0;
+          break;
+        }
+        if (spins > 32) __nanosleep(32);
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// v[q] summed over the grid, the same value in every block.  FP64 adds are
+// this part's scarce resource, so both reductions stage the values in
+// shared memory and let few warps add them (a butterfly in every warp would
+// cost five FP64 adds per warp): the block's threads' values are summed by
+// four warps (one per SM sub-partition) and the four results in order; after
+// the barrier one warp folds the grid's partial sums.  Fixed orders: every
+// block computes the same value.  partials: 4 x gridDim.x doubles, two
+// phases so that a block may run ahead into the next sum while others still
+// fold this one.  sbuf: NV x blockDim.x doubles; sred: 8 * NV + NV doubles.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *partials, int &phase, Control *ctrl,
+                                         double *sbuf, double *sred) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int T = blockDim.x, G = gridDim.x;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) sbuf[q * T + threadIdx.x] = v[q];
+  __syncthreads();
+  if (wid < 4) {
+    const int quarter = T >> 2;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double t = 0.0;
+      for (int k = wid * quarter + lane; k < (wid + 1) * quarter; k += 32) t += sbuf[q * T + k];
+      t = warp_sum(t);
+      if (lane == 0) sred[q * 8 + wid] = t;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < NV)
+    partials[(size_t)(phase * 2 + threadIdx.x) * G + blockIdx.x] =
+        ((sred[threadIdx.x * 8] + sred[threadIdx.x * 8 + 1]) + sred[threadIdx.x * 8 + 2]) + sred[threadIdx.x * 8 + 3];
+  if (!grid_barrier(ctrl)) return false;
+  if (wid == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double t = 0.0;
+      for (int b = lane; b < G; b += 32) t += __ldcg(partials + (size_t)(phase * 2 + q) * G + b);
+      t = warp_sum(t);
+      if (lane == 0) sred[8 * NV + q] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) v[q] = sred[8 * NV + q];
+  __syncthreads();
+  phase ^= 1;
+  return true;
+}
+
+struct MgsStep {
+  int n, rb;  // rows; rows of u per block (a multiple of 32)
+  OpView op;  // sliced ELL
+  const void *z;
+  double *V;
+  size_t ldv;
+  double *partials;
+  Cycle *cy;
+  Control *ctrl;
+  int m, restarted, reorth;
+  Prefill pf;
+};
+
+template <typename ZT>
+__global__ void __launch_bounds__(kStepTPB, 1) k_mgs_step(MgsStep a, int j) {
+  if (a.ctrl->done) return;
+  extern __shared__ double su[];
+  __shared__ double sbuf[2 * kStepTPB];
+  __shared__ double sred[8 * 2 + 2];
+  __shared__ double sh[kLdT + 1];
+  const int r0 = blockIdx.x * a.rb, r1 = min(a.n, r0 + a.rb);
+  const int T = blockDim.x;
+  const ZT *z = (const ZT *)a.z;
+  int phase = 0;
+  // u = A z_j for this block's rows (a warp per 32-row slice), ||u||^2, v_0 . u
+  double acc[2] = {0.0, 0.0};
+  {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = T >> 5;
+    for (int sl = (r0 >> 5) + wid; 32 * sl < r1; sl += nw) {
+      const int i = 32 * sl + lane;
+      double s = 0.0;
+      if (i < r1) {
+        const int len = a.op.row[i + 1] - a.op.row[i];
+        const int *cp = a.op.sell_col + a.op.sell_ptr[sl] + lane;
+        const double *vp = a.op.sell_val + (cp - a.op.sell_col);
+        for (int t = 0; t < len; t += 4) {
+          int c[4];
+          double v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (t + u < len) {
+              c[u] = cp[32 * (t + u)];
+              v[u] = vp[32 * (t + u)];
+            }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (t + u < len) s = fma(v[u], to_f64(z[c[u]]), s);
+        }
+        su[i - r0] = s;
+        acc[0] = fma(s, s, acc[0]);
+        acc[1] = fma(a.V[i], s, acc[1]);
+      }
+    }
+  }
+  if (!grid_sum<2>(acc, a.partials, phase, a.ctrl, sbuf, sred)) return;
+  const double normav = sqrt(acc[0]);
+  if (threadIdx.x == 0) sh[0] = acc[1];
+  __syncthreads();
+  // Gram-Schmidt passes: sums k = 1..j+1 (the last one the norm); pass 1
+  // (the second pass) only when the Brown/Hindmarsh test asks
+  double hn = 0.0;
+  int again = 0;
+  // the vector loops walk row pairs (16-byte loads, four pairs per thread in
+  // flight: one 8-byte load per thread would keep too few bytes in flight to
+  // stream from HBM); an odd last row is thread 0's
+  const int p0 = r0 >> 1, p1 = r1 >> 1;
+  const bool tail = (r1 & 1) && r1 > r0 && threadIdx.x == 0;
+  double2 *su2 = reinterpret_cast<double2 *>(su);
+  for (int pass = 0; pass < 2; ++pass) {
+    double c = sh[0];
+    if (pass) {
+      // hr_0 = v_0 . u before any subtraction of the second pass
+      double d[1] = {0.0};
+      const double2 *v2 = reinterpret_cast<const double2 *>(a.V);
+#pragma unroll 4
+      for (int p = p0 + threadIdx.x; p < p1; p += T) {
+        const double2 v = __ldg(v2 + p), u = su2[p - p0];
+        d[0] = fma(v.x, u.x, d[0]);
+        d[0] = fma(v.y, u.y, d[0]);
+      }
+      if (tail) d[0] = fma(a.V[r1 - 1], su[r1 - 1 - r0], d[0]);
+      if (!grid_sum<1>(d, a.partials, phase, a.ctrl, sbuf, sred)) return;
+      c = d[0];
+      if (threadIdx.x == 0) sh[0] += c;
+    }
+    for (int k = 1; k <= j + 1; ++k) {
+      const double *vp = a.V + (size_t)(k - 1) * a.ldv;
+      const double *vk = a.V + (size_t)k * a.ldv;
+      const double2 *vp2 = reinterpret_cast<const double2 *>(vp);
+      const double2 *vk2 = reinterpret_cast<const double2 *>(vk);
+      double d[1] = {0.0};
+      if (k <= j) {
+#pragma unroll 4
+        for (int p = p0 + threadIdx.x; p < p1; p += T) {
+          const double2 v = __ldg(vp2 + p), w = __ldg(vk2 + p);
+          double2 u = su2[p - p0];
+          u.x = fma(-c, v.x, u.x);
+          u.y = fma(-c, v.y, u.y);
+          su2[p - p0] = u;
+          d[0] = fma(w.x, u.x, d[0]);
+          d[0] = fma(w.y, u.y, d[0]);
+        }
+        if (tail) {
+          const double ui = fma(-c, vp[r1 - 1], su[r1 - 1 - r0]);
+          su[r1 - 1 - r0] = ui;
+          d[0] = fma(vk[r1 - 1], ui, d[0]);
+        }
+      } else {
+#pragma unroll 4
+        for (int p = p0 + threadIdx.x; p < p1; p += T) {
+          const double2 v = __ldg(vp2 + p);
+          double2 u = su2[p - p0];
+          u.x = fma(-c, v.x, u.x);
+          u.y = fma(-c, v.y, u.y);
+          su2[p - p0] = u;
+          d[0] = fma(u.x, u.x, d[0]);
+          d[0] = fma(u.y, u.y, d[0]);
+        }
+        if (tail) {
+          const double ui = fma(-c, vp[r1 - 1], su[r1 - 1 - r0]);
+          su[r1 - 1 - r0] = ui;
+          d[0] = fma(ui, ui, d[0]);
+        }
+      }
+      if (!grid_sum<1>(d, a.partials, phase, a.ctrl, sbuf, sred)) return;
+      if (k <= j) {
+        c = d[0];
+        if (threadIdx.x == 0) sh[k] = pass ? sh[k] + c : c;
+      } else {
+        hn = sqrt(d[0]);
+      }
+      __syncthreads();
+    }
+    if (pass) break;
+    const double hr = (normav + 0.001 * hn) - normav;  // :336-338
+    again = ((a.reorth == 0 && hr <= 4.9406564584124654e-324) || a.reorth == 2) ? 1 : 0;
+    if (!again) break;
+  }
+  // block 0: the column, the rotations and the convergence test
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Cycle *cy = a.cy;
+    for (int k = 0; k <= j; ++k) cy->h[k] = sh[k];
+    cy->h[j + 1] = hn;
+    cy->normav = normav;
+    cy->reorth = again;
+    cy->nreorth += again;
+    mgs_finish(j, a.m, a.restarted, cy, a.ctrl);
+  }
+  // v_{j+1} = u / h_{j+1} (zero after a breakdown), the next solves' outputs marked
+  const double brk = a.restarted ? 0.0 : DBL_EPSILON;
+  const double inv = fabs(hn) > brk ? 1.0 / hn : 0.0;
+  double *vn = a.V + (size_t)(j + 1) * a.ldv;
+  double2 *vn2 = reinterpret_cast<double2 *>(vn);
+#pragma unroll 4
+  for (int p = p0 + threadIdx.x; p < p1; p += T) {
+    const double2 u = su2[p - p0];
+    vn2[p] = inv == 0.0 ? make_double2(0.0, 0.0) : make_double2(u.x * inv, u.y * inv);
+    prefill_row(a.pf, 2 * p);
+    prefill_row(a.pf, 2 * p + 1);
+  }
+  if (tail) {
+    vn[r1 - 1] = inv == 0.0 ? 0.0 : su[r1 - 1 - r0] * inv;
+    prefill_row(a.pf, r1 - 1);
+  }
+}
+
 // -------------------------------------------------------------- launchers
+
+template <typename ZT>
+static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  static int G = -1;
+  if (G < 0) {
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(k_mgs_step<ZT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStepSmemMax) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mgs_step<ZT>, kStepTPB, kStepSmemMax) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      G = 0;
+    } else {
+      G = num_sms();
+    }
+  }
+  if (G == 0) return 1;
+  MgsStep p;
+  p.n = a.n;
+  p.rb = ((a.n + G - 1) / G + 31) / 32 * 32;
+  if ((size_t)p.rb * 8 > (size_t)kStepSmemMax) return 1;
+  p.op = opview(a);
+  p.z = (const char *)a.Z + (size_t)j * a.ldz * sizeof(ZT);
+  p.V = a.V;
+  p.ldv = a.ldv;
+  p.partials = a.partials;
+  p.cy = a.cy;
+  p.ctrl = a.ctrl;
+  p.m = a.m;
+  p.restarted = a.mgs_restarted;
+  p.reorth = a.mgs_reorth;
+  p.pf = prefill_for(a, j + 1);
+  void *args[] = {&p, &j};
+  if (cudaLaunchCooperativeKernel((const void *)k_mgs_step<ZT>, dim3(G), dim3(kStepTPB), args,
+                                  (size_t)p.rb * 8, s) != cudaSuccess) {
+    cudaGetLastError();
+    return 2;
+  }
+  return 0;
+}
+
+int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  if (a.bs || !a.sell_ptr) return 1;
+  return a.z_f32 ? mgs_step_t<float>(s, a, j) : mgs_step_t<double>(s, a, j);
+}
 
 void launch_mgs_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
   k_mgs_cycle_init<<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.cy, a.ctrl, prefill_for(a, 0));

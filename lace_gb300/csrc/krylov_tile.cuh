@@ -126,8 +126,7 @@ __device__ __forceinline__ double block_sum(double v, double *scratch) {
 __device__ __forceinline__ void fold_partials(const double *partials, int count, double *sred) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int k = wid; k < count; k += kTPB / 32) {
-    double s = 0.0;
-    for (int bb = lane; bb < (int)gridDim.x; bb += 32) s += partials[(size_t)bb * kLdT + k];
+    double s = strided_sum(partials + k, kLdT, lane, 32, (int)gridDim.x);
     s = warp_sum(s);
     if (lane == 0) sred[k] = s;
   }

@@ -43,11 +43,8 @@ __device__ __forceinline__ void finish_sum(double local, double *partials, int *
   double t = block_sum_p(local);
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
   if (!arrive_last(counter)) return;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) s += partials[b];
-    *out = s;
-  }
+  const double s = block_fold(partials, 1, (int)gridDim.x);
+  if (threadIdx.x == 0) *out = s;
 }
 
 template <typename FT, typename CT>
@@ -203,13 +200,10 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
     partials[3 * blockIdx.x + 2] = t3;
   }
   if (!arrive_last(counter)) return;
+  const double s1 = block_fold(partials, 3, (int)gridDim.x);
+  const double s2 = block_fold(partials + 1, 3, (int)gridDim.x);
+  const double s3 = block_fold(partials + 2, 3, (int)gridDim.x);
   if (threadIdx.x == 0) {
-    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) {
-      s1 += partials[3 * b];
-      s2 += partials[3 * b + 1];
-      s3 += partials[3 * b + 2];
-    }
     out3[0] = s1;
     out3[1] = s2;
     out3[2] = s3;

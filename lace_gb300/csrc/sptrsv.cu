@@ -306,11 +306,8 @@ __global__ void k_sqdiff(int n, const void *a, const void *b, int f32, double *p
     partials[blockIdx.x] = t;
   }
   if (!arrive_last(counter)) return;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b2 = 0; b2 < (int)gridDim.x; ++b2) s += partials[b2];
-    *out = s;
-  }
+  const double s = block_fold(partials, 1, (int)gridDim.x);
+  if (threadIdx.x == 0) *out = s;
 }
 
 // sum of squares of count FP64 values (||A||_F^2 of the resident values):
@@ -337,11 +334,8 @@ __global__ void __launch_bounds__(kSTPB) k_sumsq(size_t count, const double *__r
     partials[blockIdx.x] = t;
   }
   if (!arrive_last(counter)) return;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int b2 = 0; b2 < (int)gridDim.x; ++b2) s += partials[b2];
-    *out = s;
-  }
+  const double s = block_fold(partials, 1, (int)gridDim.x);
+  if (threadIdx.x == 0) *out = s;
 }
 
 void launch_sumsq(cudaStream_t s, size_t count, const double *a, double *partials, int *counter, double *out) {

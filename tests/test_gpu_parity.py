@@ -282,15 +282,21 @@ def test_fgmres_mixed_precision(lg, torch_cuda, prec, mode):
         assert abs(res.total_iterations - r.total_iterations) <= 2
 
 
+@pytest.fixture(params=["one_kernel", "separate"])
+def mgs_step(request, monkeypatch):
+    """The Gram-Schmidt step as one cooperative kernel, or as one kernel per
+    Gram-Schmidt sum with the second pass in a conditional graph node."""
+    monkeypatch.setenv("LACE_GB300_MGS_STEP", "1" if request.param == "one_kernel" else "0")
+    return request.param
+
+
 @pytest.mark.parametrize("name,sweeps,m", [("lap64", 5, 30), ("cd16", 3, 50), ("cd_20x9x7", 3, 12)])
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("reorth", [0, 2])
-def test_fgmres_mgs_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, reorth):
-    """Same factors, FP64: GPU FGMRES with modified Gram-Schmidt (one kernel
-    per Gram-Schmidt sum, the second pass in a conditional graph node)
-    against the oracle's mirror of LACE's data_fgmres_restart: 1e-10
-    relative residual within +-2 directions, x within 1e-7, the initial
-    residual to 1e-12 relative."""
+def test_fgmres_mgs_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, reorth, mgs_step):
+    """Same factors, FP64: GPU FGMRES with modified Gram-Schmidt against the
+    oracle's mirror of LACE's data_fgmres_restart: 1e-10 relative residual
+    within +-2 directions, x within 1e-7."""
     A = MATS[name]()
     b = A.matvec(np.ones(A.n)) if name == "lap64" else P.rhs_normal(A.n, 0)
     F = orc.parilu(A.row, A.col, A.val, sweeps, mode="sync")
@@ -303,6 +309,7 @@ def test_fgmres_mgs_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, 
         xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
         res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=m, restart_max=50, rtol=1e-10,
                          orthogonalization="mgs", reorth=reorth)
+        assert ctx.solve_stats()["one_kernel_step"] == (mgs_step == "one_kernel")
         x = xd.cpu().numpy()
     assert res.converged and r.converged
     assert abs(res.total_iterations - r.total_iterations) <= 2, (res.total_iterations, r.total_iterations)
@@ -314,7 +321,7 @@ def test_fgmres_mgs_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, 
 
 
 @pytest.mark.parametrize("restarted", [True, False])
-def test_fgmres_mgs_one_cycle_and_restarted(lg, torch_cuda, restarted):
+def test_fgmres_mgs_one_cycle_and_restarted(lg, torch_cuda, restarted, mgs_step):
     """data_fgmres (one cycle: stops at search_max) and data_fgmres_restart
     on a system that needs more than one cycle: log and x as the oracle's."""
     A = MATS["cd16"]()
@@ -388,11 +395,11 @@ def test_dropin_fgmres_mgs_reorthogonalisation(lg, restarted, choice):
 
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("reorth", [0, 2])
-def test_fgmres_mgs_second_pass_runs(lg, torch_cuda, graph, reorth):
+def test_fgmres_mgs_second_pass_runs(lg, torch_cuda, graph, reorth, mgs_step):
     """The reorthogonalising pass runs exactly where LACE's runs: once on the
     2x2-block golden case (reorth 0: the Brown/Hindmarsh test), at every
-    direction with reorth 2; from the conditional graph node when graphs are
-    on."""
+    direction with reorth 2; inside the one-kernel step, or from the
+    conditional graph node of the separate-kernel step."""
     import os
     G = np.load(os.path.join(os.path.dirname(__file__), "golden", "lace_golden.npz"))
     S = P.CSR(40, G["blk2_row"], G["blk2_col"], G["blk2_val"])
@@ -408,7 +415,8 @@ def test_fgmres_mgs_second_pass_runs(lg, torch_cuda, graph, reorth):
     lg_ = G["blk2_mgs12_log"]
     assert res.search_directions == int(lg_[2])
     assert st["reorthogonalised"] == (int(lg_[5]) if reorth == 0 else res.total_iterations)
-    if graph:
+    assert st["one_kernel_step"] == (mgs_step == "one_kernel")
+    if graph and mgs_step == "separate":
         assert st["conditional_nodes"]
     assert np.linalg.norm(x - G["blk2_mgs12_x"]) <= 1e-12 * np.linalg.norm(G["blk2_mgs12_x"])
 
