@@ -217,7 +217,10 @@ int data_fgmres_householder_restart(data_d_matrix *A, data_d_matrix *b,
                                     data_d_gmres_param *gmres_par,
                                     data_d_gmres_log *gmres_log);
 
-/* Replaces src/fgmres_householder_opt4.cpp:63 (one cycle, no restarts). */
+/* Replaces src/fgmres_householder_opt4.cpp:63 (one cycle, no restarts).
+ * The FGMRES entry points hold at most 128 search directions per cycle on
+ * the device: a larger search_max (LACE's tests pass 2000) runs cycles of
+ * 128 and returns DEV_ERR_NOT_SUPPORTED if a cycle needs more. */
 int data_fgmres_householder(data_d_matrix *A, data_d_matrix *b,
                             data_d_matrix *x0, data_d_matrix *L,
                             data_d_matrix *U, data_d_gmres_param *gmres_par,

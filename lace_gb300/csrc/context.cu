@@ -1691,7 +1691,12 @@ int lace_gpu_ctx::enqueue_mgs_body(const ArnoldiArgs &a, int m, bool capturing) 
 int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int tol_type,
                          double rtol, bool adjoint, data_d_gmres_log *log, int *total_iters,
                          std::vector<double> *hist, int method, int restarted, int reorth) {
-  if (m < 1 || m > kMaxM) return DEV_ERR_NOT_SUPPORTED;
+  if (m < 1) return DEV_ERR_NOT_SUPPORTED;
+  // LACE's own tests ask for up to 2000 directions per cycle where a handful
+  // converge: the device cycle holds kMaxM, and a longer one runs its first
+  // kMaxM directions and reports DEV_ERR_NOT_SUPPORTED only if it needs more
+  const bool capped = m > kMaxM;
+  if (capped) m = kMaxM;
   const bool mgs = method == 1;
   if (mgs && adjoint) return DEV_ERR_NOT_SUPPORTED;
   if (mgs && !restarted) restart_max = std::min(restart_max, 1);
@@ -1808,6 +1813,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     }
     if (hc.status & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
     const int ns = hc.nsteps;
+    if (capped && ns == m && !hc.converged && !(hc.status & kStatusBreakdown)) return DEV_ERR_NOT_SUPPORTED;
     if (hist)
       for (int k = 0; k < ns; ++k) hist->push_back(h_scal[k]);
     if (opt.monitor_orthog && verbose) {

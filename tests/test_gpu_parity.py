@@ -442,6 +442,27 @@ def test_dropin_fgmres_mgs_trefethen(lg):
             assert np.linalg.norm(b - A.matvec(x)) <= 1e-3
 
 
+def test_dropin_lace_tests_with_search_2000(lg):
+    """LACE's FGMRESPreconditioned (testing/test_linearSolver.cpp:300-398:
+    data_fgmres, search 2000, restart 2000) and FGMRESHouseholderPreconditioned
+    (:514-611: data_fgmres_householder, search 2000) on Trefethen_20: the
+    device cycle holds 128 directions, these converge well within them."""
+    from lace_gb300 import dropin
+    A = P.trefethen(19)
+    Am = dropin.csr(A.row, A.col, A.val, A.n)
+    (lp, li, lv), (up, ui, uv), info = dropin.parilu(Am, reduction=1e-15)
+    L = dropin.csr(lp, li, lv, A.n, dropin.Magma_CSRL)
+    U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
+    b = np.ones(A.n)
+    x, rc, log = dropin.fgmres_restart(Am, b, np.zeros(A.n), L, U, search_max=2000, restart_max=2000, rtol=1e-3,
+                                       tol_type=0, choice=0, monitor_orthog=1, single_cycle=True)
+    assert rc == 0 and np.linalg.norm(b - A.matvec(x)) <= 1e-3
+    x, rc, log = dropin.fgmres_householder_restart(Am, b, np.zeros(A.n), L, U, search_max=2000, restart_max=0,
+                                                   rtol=1e-3, tol_type=0, choice=0, monitor_orthog=1,
+                                                   single_cycle=True)
+    assert rc == 0 and np.linalg.norm(b - A.matvec(x)) <= 1e-3
+
+
 def test_dropin_trefethen_linear_solver(lg):
     """LACE's FGMRESHouseholderPreconditionedRestart test
     (testing/test_linearSolver.cpp:621-726) through the drop-in entry points:
