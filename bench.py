@@ -100,9 +100,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
-def build_problem():
+def build_problem(grid: int = GRID):
     from lace_gb300 import problems as P
-    A = P.convdiff3d(GRID)
+    A = P.convdiff3d(grid)
     b = P.rhs_normal(A.n, 0)
     return A, b
 
@@ -150,7 +150,7 @@ def run_ours(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    A, b = build_problem()
+    A, b = build_problem(args.grid if args.only_mgs else GRID)
     stream = torch.cuda.Stream()
     ctx = lg.Context(local, stream=stream)
     ctx.upload(A)
@@ -404,6 +404,8 @@ def main():
                          "launch overhead would change the autotune's choice")
     ap.add_argument("--only-mgs", action="store_true",
                     help="time only the FGMRES with modified Gram-Schmidt (for profiling its kernels)")
+    ap.add_argument("--grid", type=int, default=GRID,
+                    help="with --only-mgs: the convection-diffusion grid side (a smaller case for ncu)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":
