@@ -392,9 +392,10 @@ int lace_gpu_fgmres_mgs(lace_gpu_ctx *ctx, const double *b, double *x,
  * that the Gram-Schmidt FGMRES reorthogonalised (LACE prints
  * "Reorthogonalize" for each); out[1] = 1 when conditional CUDA graph nodes
  * are available (the separate-kernel step puts its second pass in one);
- * out[2] = 1 when each Arnoldi step after the solves runs as one cooperative
- * kernel (environment LACE_GB300_MGS_STEP=0 at context creation selects the
- * separate kernels). */
+ * out[2] = 1 when each Gram-Schmidt Arnoldi step after the solves runs as
+ * one cooperative kernel (environment LACE_GB300_MGS_STEP=0 at context
+ * creation selects the separate kernels); out[3] = the same for the
+ * Householder step (LACE_GB300_HH_STEP=0: passes A, B, C).  out: 4 ints. */
 int lace_gpu_get_solve_stats(lace_gpu_ctx *ctx, int *out);
 
 /* Adjoint of the solve x = A^{-1} b for a loss L(x): given dL/dx (device),

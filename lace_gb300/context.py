@@ -177,11 +177,12 @@ class Context:
         """The last FGMRES solve: directions the Gram-Schmidt variant
         reorthogonalised, and whether its second pass is a conditional graph
         node."""
-        out = (C.c_int * 3)()
+        out = (C.c_int * 4)()
         rc = self._lib.lace_gpu_get_solve_stats(self.h, out)
         if rc != DEV_SUCCESS:
             raise LaceError(rc, "get_solve_stats")
-        return {"reorthogonalised": out[0], "conditional_nodes": bool(out[1]), "one_kernel_step": bool(out[2])}
+        return {"reorthogonalised": out[0], "conditional_nodes": bool(out[1]), "one_kernel_step": bool(out[2]),
+                "one_kernel_householder_step": bool(out[3])}
 
     def backward(self, x, dLdx, dLdb=None, dLdA=None, search_max: int = 30, restart_max: int = 20,
                  rtol: float = 1e-10, tol_type: int = 1) -> int:

@@ -462,6 +462,8 @@ extern "C" int lace_gpu_ctx_create(lace_gpu_ctx **out, int device, void *stream)
   c->verbose = getenv("LACE_GB300_VERBOSE") != nullptr;
   // LACE_GB300_MGS_STEP=0: the Gram-Schmidt step as separate kernels
   if (const char *e = getenv("LACE_GB300_MGS_STEP")) c->mgs_persistent = atoi(e) != 0;
+  // LACE_GB300_HH_STEP=0: the Householder step as passes A, B, C
+  if (const char *e = getenv("LACE_GB300_HH_STEP")) c->hh_persistent = atoi(e) != 0;
   lace_gpu_default_options(&c->opt);
   if (stream) {
     c->stream = (cudaStream_t)stream;
@@ -1589,7 +1591,7 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
 }
 
 // the search-direction loop of one cycle (LACE :311-759), all on the device
-int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) {
+int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint, bool capturing) {
   const int t1 = adjoint ? 2 : 0, t2 = adjoint ? 3 : 1;
   const int tf32 = vtype() != VType::F64;  // the intermediate vector of the two solves
   for (int j = 0; j < m; ++j) {
@@ -1598,9 +1600,18 @@ int lace_gpu_ctx::enqueue_cycle_body(const ArnoldiArgs &a, int m, bool adjoint) 
     int rc = solve_tri(t1, a.q, a.q_f32, vec_t.p, tf32, true, vec_t2.p, a.prefill != 0);
     if (!rc) rc = solve_tri(t2, vec_t.p, tf32, zj, a.z_f32, true, vec_t2.p, a.prefill != 0);
     if (rc) return rc;
-    launch_passA(stream, a, j);
-    launch_passB(stream, a, j);
-    launch_passC(stream, a, j);
+    // passes A, B and C as one cooperative kernel where it applies
+    const int st = hh_persistent ? launch_hh_step(stream, a, j) : 1;
+    if (st == 2) {
+      hh_persistent = false;
+      if (verbose) printf("%% cooperative launch refused: the Householder step runs as three passes\n");
+      if (capturing) return DEV_ERR_NOT_SUPPORTED;
+    }
+    if (st != 0) {
+      launch_passA(stream, a, j);
+      launch_passB(stream, a, j);
+      launch_passC(stream, a, j);
+    }
     if (opt.monitor_orthog && Qmon.p) {
       // q_{j+1} into the monitor basis, then ||I - Q^T Q|| over q_0..q_j
       launch_convert(stream, n, a.q_f32 ? VType::F32 : VType::F64, a.q, VType::F64,
@@ -1762,9 +1773,9 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
         for (int attempt = 0; attempt < 3 && !ge; ++attempt) {
           cudaGraph_t g;
           LCHK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-          rc = mgs ? enqueue_mgs_body(a, m, true) : enqueue_cycle_body(a, m, adjoint);
+          rc = mgs ? enqueue_mgs_body(a, m, true) : enqueue_cycle_body(a, m, adjoint, true);
           cudaError_t ce = cudaStreamEndCapture(stream, &g);
-          if (rc == DEV_ERR_NOT_SUPPORTED && mgs && attempt < 2) {
+          if (rc == DEV_ERR_NOT_SUPPORTED && attempt < 2) {
             // a refused cooperative launch or conditional node (the flag
             // that chose it is cleared): capture again without it
             if (ce == cudaSuccess) cudaGraphDestroy(g);
@@ -1789,7 +1800,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
       }
       LCHK(cudaGraphLaunch(it->second, stream));
     } else {
-      rc = mgs ? enqueue_mgs_body(a, m, false) : enqueue_cycle_body(a, m, adjoint);
+      rc = mgs ? enqueue_mgs_body(a, m, false) : enqueue_cycle_body(a, m, adjoint, false);
       if (rc) return rc;
     }
     if (mgs) launch_mgs_xupdate(stream, a, x);
@@ -1880,6 +1891,7 @@ extern "C" int lace_gpu_get_solve_stats(lace_gpu_ctx *c, int *out) {
   out[0] = c->last_reorth;
   out[1] = c->cond_nodes ? 1 : 0;
   out[2] = c->mgs_persistent ? 1 : 0;
+  out[3] = c->hh_persistent ? 1 : 0;
   return DEV_SUCCESS;
 }
 

@@ -130,6 +130,7 @@ struct lace_gpu_ctx {
   cudaStream_t side = nullptr;
   bool cond_nodes = true;  // conditional graph nodes available (else the second pass launches always)
   bool mgs_persistent = true;  // the one-kernel Gram-Schmidt step (cooperative launch) available
+  bool hh_persistent = true;   // the one-kernel Householder step (cooperative launch) available
   int last_reorth = 0;     // directions of the last Gram-Schmidt solve that reorthogonalised
   std::vector<double> last_hist;
 
@@ -177,7 +178,7 @@ struct lace_gpu_ctx {
   int ensure_krylov(int m, bool monitor);
   int ensure_AT();
   lace::ArnoldiArgs arnoldi_args(int m, bool adjoint);
-  int enqueue_cycle_body(const lace::ArnoldiArgs &a, int m, bool adjoint);
+  int enqueue_cycle_body(const lace::ArnoldiArgs &a, int m, bool adjoint, bool capturing);
   // the modified Gram-Schmidt cycle; capturing: inside a stream capture (the
   // second pass goes into conditional nodes when cond_nodes)
   int enqueue_mgs_body(const lace::ArnoldiArgs &a, int m, bool capturing);

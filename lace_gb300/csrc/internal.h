@@ -44,6 +44,9 @@ struct Cycle {
   double hinv;
   int reorth;
   int nreorth;  // steps of the cycle that reorthogonalised
+  // rows 0..j+1 of w after the step's update, published by the blocks that
+  // own them (the one-kernel Householder step)
+  double wtop[kLdT];
 };
 
 // Handles for the two triangles of one solve direction.
@@ -132,6 +135,10 @@ void launch_passB(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j);
 void launch_orthog_monitor(cudaStream_t s, const ArnoldiArgs &a, int j, double *Q, size_t ldq);
 void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
+// passes A, B and C of step j as one cooperative kernel with w in shared
+// memory; returns 1 when it does not apply (BCSR, no sliced ELL, w too large
+// for shared memory), 2 when the cooperative launch failed, 0 on success
+int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j);
 
 // ------------------------------------ FGMRES, modified Gram-Schmidt Arnoldi
 // (src/fgmres_restart.cpp, src/fgmres.cpp).  Basis v_j in a.V, the

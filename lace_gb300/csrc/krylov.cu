@@ -560,6 +560,339 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, f
   }
 }
 
+// ------------------------------------------- one persistent kernel per step
+
+// Passes A, B and C of step j in one cooperative launch of one block per SM:
+// block b keeps rows [b*RB, (b+1)*RB) of w in shared memory through the step,
+// the two sets of dot products (V^T w, then V^T w over rows > j with ||w||^2)
+// are grid reductions (block partials, grid barrier, a fold every block
+// performs in the same order), and the small-matrix work of pass B's last
+// block (new reflector, T column, c = T rho) is done by every block
+// identically, so pass C's combination follows without another barrier.
+// The formulas and summation orders are the passes' own.
+constexpr int kHHTPB = 1024;
+constexpr int kHHSmemMax = 200 * 1024;  // rows of w per block: at most 25,600
+
+struct HHStep {
+  int n, rb;
+  OpView op;  // sliced ELL
+  const void *z;
+  double *V;
+  float *Vf;
+  size_t ldv;
+  void *q;
+  double *partials;  // 2 phases x kLdT x gridDim.x
+  Cycle *cy;
+  Control *ctrl;
+  int m;
+  Prefill pf;
+};
+
+// block partial sums sacc[k] = sum over this block's rows i > lo of
+// V[k][i] w[i], k < jp1: up to 32 columns as (column, row group) pairs over
+// the 32 warps, more as up to five columns per warp; lanes walk rows
+__device__ __forceinline__ void hh_block_dots(const double *__restrict__ V, size_t ldv, int jp1, int r0, int r1,
+                                              int lo, const double *sw, double *swarp, double *sacc) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nsl = r1 > r0 ? (r1 - r0 + 31) >> 5 : 0;
+  if (jp1 <= 32) {
+    const int G = 32 / jp1;
+    double acc = 0.0;
+    if (wid < G * jp1) {
+      // a warp streams its column over 1/G of the rows: eight rows per lane
+      // in flight (one block per SM has few warps to hide the latency)
+      const int k = wid % jp1, g = wid / jp1;
+      const double *Vk = V + (size_t)k * ldv + r0;
+      for (int sl0 = g; sl0 < nsl; sl0 += 8 * G) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int t = 32 * (sl0 + u * G) + lane;
+          v[u] = (sl0 + u * G < nsl && r0 + t < r1) ? Vk[t] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int t = 32 * (sl0 + u * G) + lane;
+          const int i = r0 + t;
+          acc = fma(v[u], (sl0 + u * G < nsl && i < r1 && i > lo) ? sw[t] : 0.0, acc);
+        }
+      }
+      acc = warp_sum(acc);
+    }
+    if (lane == 0) swarp[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x < jp1) {
+      double t = 0.0;
+      for (int g = 0; g < G; ++g) t += swarp[g * jp1 + threadIdx.x];
+      sacc[threadIdx.x] = t;
+    }
+  } else {
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int sl0 = 0; sl0 < nsl; sl0 += 4) {
+      // four rows per lane for each of the warp's columns in flight
+      double wv[4];
+      int ii[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = 32 * (sl0 + u) + lane;
+        const int i = r0 + t;
+        const bool ok = sl0 + u < nsl && i < r1 && i > lo;
+        wv[u] = ok ? sw[t] : 0.0;
+        ii[u] = ok ? i : r0;
+      }
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        const int k = wid + 32 * c;
+        if (32 * c < jp1 && k < jp1) {
+          double v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = V[(size_t)k * ldv + ii[u]];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[c] = fma(v[u], wv[u], acc[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int k = wid + 32 * c;
+      if (32 * c < jp1) {  // warp-uniform
+        const double v = warp_sum(acc[c]);
+        if (lane == 0 && k < jp1) swarp[k] = v;
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < jp1; k += blockDim.x) sacc[k] = swarp[k];
+  }
+  __syncthreads();
+}
+
+// sres[k] = sum over the grid of the blocks' sacc[k], k < nv, the same in
+// every block (warp w folds k = w, w+32, ...; lanes stride over the blocks)
+__device__ __forceinline__ bool hh_grid_fold(const double *sacc, int nv, double *partials, int &phase,
+                                             Control *ctrl, double *sres) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int G = gridDim.x;
+  double *P = partials + (size_t)phase * kLdT * G;
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) P[(size_t)k * G + blockIdx.x] = sacc[k];
+  if (!grid_barrier(ctrl)) return false;
+  for (int k = wid; k < nv; k += (int)(blockDim.x >> 5)) {
+    double t = strided_sum(P + (size_t)k * G, 1, lane, 32, G);
+    t = warp_sum(t);
+    if (lane == 0) sres[k] = t;
+  }
+  __syncthreads();
+  phase ^= 1;
+  return true;
+}
+
+template <typename ZT, typename QT>
+__global__ void __launch_bounds__(kHHTPB, 1) k_hh_step(HHStep a, int j) {
+  if (a.ctrl->done) return;
+  constexpr bool kF32 = sizeof(QT) == 4;
+  extern __shared__ double sw[];
+  __shared__ double swarp[5 * 32];
+  __shared__ double sacc[kLdT + 1], sres[kLdT + 1];
+  __shared__ double sy[kLdT], sd[kLdT], srho[kLdT], sc[kLdT];
+  __shared__ float scf[kLdT];
+  __shared__ double sbuf[kHHTPB];
+  __shared__ double s_dd, s_ia, s_vjj;
+  const int n = a.n, jp1 = j + 1, T = blockDim.x;
+  const int r0 = blockIdx.x * a.rb, r1 = min(n, r0 + a.rb);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const size_t ldv = a.ldv;
+  const double *__restrict__ V = a.V;
+  Cycle *cy = a.cy;
+  int phase = 0;
+  // ---- pass A: w = A z_j (a warp per 32-row slice), s = V^T w
+  {
+    const ZT *z = (const ZT *)a.z;
+    for (int sl = (r0 >> 5) + wid; 32 * sl < r1; sl += (T >> 5)) {
+      const int i = 32 * sl + lane;
+      if (i < r1) {
+        const int len = a.op.row[i + 1] - a.op.row[i];
+        const int *cp = a.op.sell_col + a.op.sell_ptr[sl] + lane;
+        const double *vp = a.op.sell_val + (cp - a.op.sell_col);
+        double s = 0.0;
+        for (int t = 0; t < len; t += 8) {  // a 7-point row in one round of loads
+          int c[8];
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) {
+              c[u] = cp[32 * (t + u)];
+              v[u] = vp[32 * (t + u)];
+            }
+          ZT zv[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) zv[u] = z[c[u]];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) s = fma(v[u], to_f64(zv[u]), s);
+        }
+        sw[i - r0] = s;
+      }
+    }
+  }
+  __syncthreads();
+  hh_block_dots(V, ldv, jp1, r0, r1, -1, sw, swarp, sacc);
+  if (!hh_grid_fold(sacc, jp1, a.partials, phase, a.ctrl, sres)) return;
+  // y = T^T s
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    double y = 0.0;
+    for (int l = 0; l <= k; ++l) y = fma(cy->T[l + k * kLdT], sres[l], y);
+    sy[k] = y;
+  }
+  __syncthreads();
+  // ---- pass B: w -= V y (a row pair per thread), then V^T w over rows > j
+  // and ||w_{j+1:}||^2; rows 0..j+1 of w published for every block
+  double nrm = 0.0;
+  {
+    const int p0 = r0 >> 1, p1 = r1 >> 1;
+    for (int p = p0 + threadIdx.x; p < p1; p += T) {
+      const int i = 2 * p;
+      const double2 c = vcomb8x2(V, ldv, i, jp1, sy);
+      const double s0 = sw[i - r0] - c.x, s1 = sw[i + 1 - r0] - c.y;
+      sw[i - r0] = s0;
+      sw[i + 1 - r0] = s1;
+      if (i > j) nrm = fma(s0, s0, nrm);
+      if (i + 1 > j) nrm = fma(s1, s1, nrm);
+      if (i <= jp1) cy->wtop[i] = s0;
+      if (i + 1 <= jp1) cy->wtop[i + 1] = s1;
+    }
+    if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {  // the last row of an odd n
+      const int i = r1 - 1;
+      const double s0 = sw[i - r0] - vcomb8(V, ldv, i, jp1, sy);
+      sw[i - r0] = s0;
+      if (i > j) nrm = fma(s0, s0, nrm);
+      if (i <= jp1) cy->wtop[i] = s0;
+    }
+  }
+  sbuf[threadIdx.x] = nrm;
+  __syncthreads();  // w and the norm terms in place
+  hh_block_dots(V, ldv, jp1, r0, r1, j, sw, swarp, sacc);
+  if (wid < 4) {  // the norm: four warps add a quarter each (few FP64 adds)
+    const int quarter = T >> 2;
+    double t = 0.0;
+    for (int k = wid * quarter + lane; k < (wid + 1) * quarter; k += 32) t += sbuf[k];
+    t = warp_sum(t);
+    if (lane == 0) swarp[wid] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sacc[jp1] = ((swarp[0] + swarp[1]) + swarp[2]) + swarp[3];
+  __syncthreads();
+  if (!hh_grid_fold(sacc, jp1 + 1, a.partials, phase, a.ctrl, sres)) return;
+  // ---- pass B's last-block work, in every block: new reflector, T column,
+  // c = T_{j+1} rho (LACE :476-511)
+  if (threadIdx.x == 0) {
+    const double nrm2 = jp1 < n ? sres[jp1] : 0.0;
+    const double wn = sqrt(nrm2);
+    const double wj1 = jp1 < n ? __ldcg(&cy->wtop[jp1]) : 0.0;
+    const double dd = mysgn(wj1) * wn;
+    const double alpha = sqrt(2.0 * (nrm2 + fabs(wj1) * wn));
+    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    s_dd = dd;
+    s_ia = ia;
+    s_vjj = (wj1 + dd) * ia;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    const double vk = jp1 < n ? V[(size_t)k * ldv + jp1] : 0.0;
+    sd[k] = (sres[k] + s_dd * vk) * s_ia;
+    srho[k] = vk;
+  }
+  if (threadIdx.x == 0) srho[jp1] = s_vjj;
+  __syncthreads();
+  // the new column of T (kept in sacc) and c
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    double t = 0.0;
+    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], sd[l], t);
+    sacc[k] = -2.0 * t;
+  }
+  if (threadIdx.x == 0) sacc[jp1] = 2.0;
+  __syncthreads();
+  for (int k = threadIdx.x; k <= jp1; k += T) {
+    double t = 0.0;
+    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], srho[l], t);
+    t = fma(sacc[k], srho[jp1], t);
+    sc[k] = t;
+    scf[k] = (float)t;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    // the record: T column, reflector scalars, c; rotations and the test
+    double *Tg = cy->T;
+    for (int k = threadIdx.x; k < kLdT; k += T) Tg[k + jp1 * kLdT] = k <= jp1 ? sacc[k] : 0.0;
+    for (int k = threadIdx.x; k <= jp1; k += T) cy->c[k] = sc[k];
+    if (threadIdx.x == 0) {
+      cy->dd = s_dd;
+      cy->inv_alpha = s_ia;
+      // Hessenberg column j: h_k = w_k (k <= j), h_{j+1} = -dd (LACE :658-701)
+      double *sh = sbuf;
+      for (int k = 0; k <= j; ++k) sh[k] = __ldcg(&cy->wtop[k]);
+      for (int k = 0; k < j; ++k) {
+        const double t0 = sh[k], t1 = sh[k + 1];
+        sh[k + 1] = -cy->sn[k] * t0 + cy->cs[k] * t1;
+        sh[k] = cy->cs[k] * t0 + cy->sn[k] * t1;
+      }
+      const double dd = s_dd;
+      double c, sn;
+      givens_rot(sh[j], -dd, 4.9406564584124654e-324, &c, &sn);
+      cy->cs[j] = c;
+      cy->sn[j] = sn;
+      sh[j] = c * sh[j] - sn * dd;
+      const double gj = cy->g[j];
+      cy->g[jp1] = -sn * gj;
+      cy->g[j] = c * gj;
+      const double resid = fabs(-sn * gj);
+      cy->hist[j] = resid;
+      a.ctrl->resid = resid;
+      const bool conv = resid < a.ctrl->rtol_abs;
+      double *R = cy->R + (size_t)j * kLdT;
+      for (int k = 0; k <= j; ++k) R[k] = sh[k];
+      if (conv || j == a.m - 1 || !(resid == resid)) {  // LACE :714 (+ opt4's non-finite stop)
+        a.ctrl->nsteps = jp1;
+        a.ctrl->converged = conv ? 1 : 0;
+        if (!(resid == resid)) a.ctrl->status |= kStatusBreakdown;
+        a.ctrl->done = 1;
+      }
+    }
+  }
+  // ---- pass C: v_{j+1} and q = e_{j+1} - V_{j+1} c for this block's rows
+  const double dd = s_dd, ia = s_ia;
+  double *vn = a.V + (size_t)jp1 * ldv;
+  QT *q = (QT *)a.q;
+  const int p0 = r0 >> 1, p1 = r1 >> 1;
+  for (int p = p0 + threadIdx.x; p < p1; p += T) {
+    const int i = 2 * p;
+    const double w0 = sw[i - r0], w1 = sw[i + 1 - r0];
+    const double v0 = (i > j) ? (i == jp1 ? w0 + dd : w0) * ia : 0.0;
+    const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? w1 + dd : w1) * ia : 0.0;
+    *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
+    if constexpr (kF32) {
+      const float2 vf = make_float2(dtof_rz(v0), dtof_rz(v1));
+      *reinterpret_cast<float2 *>(a.Vf + (size_t)jp1 * ldv + i) = vf;
+      const float2 sm = vcomb8x2f(a.Vf, ldv, i, jp1, scf);
+      *reinterpret_cast<float2 *>(q + i) = make_float2(((i == jp1 ? 1.f : 0.f) - vf.x * scf[jp1]) - sm.x,
+                                                       ((i + 1 == jp1 ? 1.f : 0.f) - vf.y * scf[jp1]) - sm.y);
+    } else {
+      const double2 sm = vcomb8x2(V, ldv, i, jp1, sc);
+      *reinterpret_cast<double2 *>(q + i) = make_double2(((i == jp1 ? 1.0 : 0.0) - v0 * sc[jp1]) - sm.x,
+                                                         ((i + 1 == jp1 ? 1.0 : 0.0) - v1 * sc[jp1]) - sm.y);
+    }
+    prefill_row(a.pf, i);
+    prefill_row(a.pf, i + 1);
+  }
+  if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {
+    const int i = r1 - 1;
+    const double v = (i > j) ? (i == jp1 ? sw[i - r0] + dd : sw[i - r0]) * ia : 0.0;
+    vn[i] = v;
+    if (kF32) a.Vf[(size_t)jp1 * ldv + i] = dtof_rz(v);
+    q[i] = (QT)(((i == jp1 ? 1.0 : 0.0) - v * sc[jp1]) - vcomb8(V, ldv, i, jp1, sc));
+    prefill_row(a.pf, i);
+  }
+}
+
 // ----------------------------------------------- orthogonality monitor
 // orth[j+1] = ||I - Q^T Q||_inf over q_0..q_{j} (LACE :628-656 evaluates it on
 // the first search+1 stored vectors); Q columns stored by the host driver.
@@ -745,6 +1078,54 @@ void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
     k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, nullptr, a.ldv, j, a.w, (double *)a.q,
                                                                   a.cy, a.ctrl, pf);
   }
+}
+
+template <typename ZT, typename QT>
+static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  static int G = -1;
+  if (G < 0) {
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(k_hh_step<ZT, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHHSmemMax) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hh_step<ZT, QT>, kHHTPB, kHHSmemMax) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      G = 0;
+    } else {
+      G = num_sms();
+    }
+  }
+  if (G == 0) return 1;
+  HHStep p;
+  p.n = a.n;
+  p.rb = ((a.n + G - 1) / G + 31) / 32 * 32;
+  if ((size_t)p.rb * 8 > (size_t)kHHSmemMax || (size_t)G * kLdT * 2 > (size_t)a.grid * kLdT) return 1;
+  p.op = opview(a);
+  p.z = (const char *)a.Z + (size_t)j * a.ldz * sizeof(ZT);
+  p.V = a.V;
+  p.Vf = a.Vf;
+  p.ldv = a.ldv;
+  p.q = a.q;
+  p.partials = a.partials;
+  p.cy = a.cy;
+  p.ctrl = a.ctrl;
+  p.m = a.m;
+  p.pf = prefill_for(a, j + 1);
+  void *args[] = {&p, &j};
+  if (cudaLaunchCooperativeKernel((const void *)k_hh_step<ZT, QT>, dim3(G), dim3(kHHTPB), args,
+                                  (size_t)p.rb * 8, s) != cudaSuccess) {
+    cudaGetLastError();
+    return 2;
+  }
+  return 0;
+}
+
+int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j) {
+  if (a.bs || !a.sell_ptr) return 1;
+  if (a.z_f32 && a.q_f32 && a.Vf) return hh_step_t<float, float>(s, a, j);
+  if (!a.z_f32 && !a.q_f32) return hh_step_t<double, double>(s, a, j);
+  return 1;
 }
 
 void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x) {

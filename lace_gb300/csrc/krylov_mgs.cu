@@ -322,38 +322,6 @@ __global__ void __launch_bounds__(kTPB) k_mgs_xupdate(int n, const ZT *__restric
 constexpr int kStepTPB = 1024;
 constexpr int kStepSmemMax = 200 * 1024;  // rows of u per block: at most 25,600 (plus 16 KB static)
 
-// Grid barrier over a cooperatively launched grid (Control::block_count[3]
-// arrivals, [4] generation).  Bounded: a wait that gives up sets
-// kStatusSpinTimeout, and every block leaves at its next barrier.
-__device__ __forceinline__ bool grid_barrier(Control *ctrl) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int *count = &ctrl->block_count[3];
-    int *gen = &ctrl->block_count[4];
-    const int g = ld_acquire(gen);
-    __threadfence();
-    int ok = 1;
-    if (atomicAdd(count, 1) == (int)gridDim.x - 1) {
-      *count = 0;
-      st_release(gen, g + 1);
-    } else {
-      for (int spins = 0;; ++spins) {
-        if (ld_acquire(gen) != g) break;
-        if (spins > kMaxSpins || ((spins & 1023) == 1023 && (ld_relaxed(&ctrl->status) & kStatusSpinTimeout))) {
-          atomicOr(&ctrl->status, kStatusSpinTimeout);
-          ok = 0;
-          break;
-        }
-        if (spins > 32) __nanosleep(32);
-      }
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
 // v[q] summed over the grid, the same value in every block.  FP64 adds are
 // this part's scarce resource, so both reductions stage the values in
 // shared memory and let few warps add them (a butterfly in every warp would
@@ -438,18 +406,22 @@ __global__ void __launch_bounds__(kStepTPB, 1) k_mgs_step(MgsStep a, int j) {
         const int len = a.op.row[i + 1] - a.op.row[i];
         const int *cp = a.op.sell_col + a.op.sell_ptr[sl] + lane;
         const double *vp = a.op.sell_val + (cp - a.op.sell_col);
-        for (int t = 0; t < len; t += 4) {
-          int c[4];
-          double v[4];
+        for (int t = 0; t < len; t += 8) {  // a 7-point row in one round of loads
+          int c[8];
+          double v[8];
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
+          for (int u = 0; u < 8; ++u)
             if (t + u < len) {
               c[u] = cp[32 * (t + u)];
               v[u] = vp[32 * (t + u)];
             }
+          ZT zv[8];
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (t + u < len) s = fma(v[u], to_f64(z[c[u]]), s);
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) zv[u] = z[c[u]];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) s = fma(v[u], to_f64(zv[u]), s);
         }
         su[i - r0] = s;
         acc[0] = fma(s, s, acc[0]);

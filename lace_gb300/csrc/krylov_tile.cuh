@@ -162,6 +162,41 @@ __device__ __forceinline__ void prefill_row(const Prefill &f, size_t i) {
   if (f.z) mark_unsolved(f.z, f.z_f32, i);
 }
 
+// ------------------------------------- persistent (cooperative) kernels
+
+// Grid barrier over a cooperatively launched grid (Control::block_count[3]
+// arrivals, [4] generation).  Bounded: a wait that gives up sets
+// kStatusSpinTimeout, and every block leaves at its next barrier.
+__device__ __forceinline__ bool grid_barrier(Control *ctrl) {
+  __shared__ int s_ok;
+  __threadfence();  // every thread's writes before the arrival (partial sums)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int *count = &ctrl->block_count[3];
+    int *gen = &ctrl->block_count[4];
+    const int g = ld_acquire(gen);
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(count, 1) == (int)gridDim.x - 1) {
+      *count = 0;
+      st_release(gen, g + 1);
+    } else {
+      for (int spins = 0;; ++spins) {
+        if (ld_acquire(gen) != g) break;
+        if (spins > kMaxSpins || ((spins & 1023) == 1023 && (ld_relaxed(&ctrl->status) & kStatusSpinTimeout))) {
+          atomicOr(&ctrl->status, kStatusSpinTimeout);
+          ok = 0;
+          break;
+        }
+        if (spins > 32) __nanosleep(32);
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // ------------------------------------------------------------ host side
 
 static inline OpView opview(const ArnoldiArgs &a) {

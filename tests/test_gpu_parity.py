@@ -233,9 +233,16 @@ def _true_rel(A, x, b):
     return np.linalg.norm(b - A.matvec(x)) / np.linalg.norm(b)
 
 
+@pytest.fixture(params=["one_kernel", "passes"])
+def hh_step(request, monkeypatch):
+    """The Householder step as one cooperative kernel, or as passes A, B, C."""
+    monkeypatch.setenv("LACE_GB300_HH_STEP", "1" if request.param == "one_kernel" else "0")
+    return request.param
+
+
 @pytest.mark.parametrize("name,sweeps,m", [("lap64", 5, 30), ("cd16", 3, 50), ("cd_20x9x7", 3, 20)])
 @pytest.mark.parametrize("graph", [True, False])
-def test_fgmres_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph):
+def test_fgmres_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph, hh_step):
     """Same factors, FP64: GPU FGMRES-Householder (compact-WY reflectors,
     sync-free solves) reaches 1e-10 relative residual within +-2 directions
     of the oracle, which mirrors LACE's FGMRES-Householder."""
@@ -250,6 +257,7 @@ def test_fgmres_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph):
         ctx.parilu0(sweeps)
         xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
         res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=m, restart_max=50, rtol=1e-10)
+        assert ctx.solve_stats()["one_kernel_householder_step"] == (hh_step == "one_kernel")
         x = xd.cpu().numpy()
     assert res.converged and r.converged
     assert abs(res.total_iterations - r.total_iterations) <= 2, (res.total_iterations, r.total_iterations)
@@ -260,7 +268,7 @@ def test_fgmres_fp64_matches_oracle(lg, torch_cuda, name, sweeps, m, graph):
 
 @pytest.mark.parametrize("prec", ["fp32", "bf16"])
 @pytest.mark.parametrize("mode", ["syncfree", "levels", "jacobi"])
-def test_fgmres_mixed_precision(lg, torch_cuda, prec, mode):
+def test_fgmres_mixed_precision(lg, torch_cuda, prec, mode, hh_step):
     """FP32 (or BF16-stored) factors and solves inside the FP64 FGMRES reach
     the same 1e-10 relative residual (the flexible basis absorbs the inexact
     preconditioner)."""
