@@ -398,6 +398,14 @@ int lace_gpu_fgmres_mgs(lace_gpu_ctx *ctx, const double *b, double *x,
  * Householder step (LACE_GB300_HH_STEP=0: passes A, B, C).  out: 4 ints. */
 int lace_gpu_get_solve_stats(lace_gpu_ctx *ctx, int *out);
 
+/* Measurement: the mean device time of one launch of the one-kernel Arnoldi
+ * step j (method 0 Householder, 1 Gram-Schmidt), replayed reps times on the
+ * basis the last FGMRES solve of this context left (j + 2 <= its
+ * search_max), timed with CUDA events on the context's stream.  The replays
+ * overwrite that solve's cycle state; the next solve starts afresh.
+ * DEV_ERR_NOT_SUPPORTED when that step runs as separate kernels. */
+int lace_gpu_time_arnoldi_step(lace_gpu_ctx *ctx, int method, int j, int reps, double *seconds);
+
 /* Adjoint of the solve x = A^{-1} b for a loss L(x): given dL/dx (device),
  * solves A^T lambda = dL/dx with FGMRES-Householder preconditioned by the
  * transposed factors (U^T then L^T), and returns dL/db = lambda and

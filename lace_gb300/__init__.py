@@ -178,6 +178,7 @@ SIGNATURES = {
                                          C.POINTER(_i)]),
     "lace_gpu_fgmres_mgs": (_i, [_p, _p, _p, C.POINTER(GmresParam), _i, C.POINTER(GmresLog), C.POINTER(_i)]),
     "lace_gpu_get_solve_stats": (_i, [_p, _p]),
+    "lace_gpu_time_arnoldi_step": (_i, [_p, _i, _i, _i, C.POINTER(_d)]),
     "lace_gpu_solve_backward": (_i, [_p, _p, _p, C.POINTER(GmresParam), _p, _p, C.POINTER(_i)]),
     "lace_gpu_last_error": (_i, []),
     "lace_gpu_error_string": (C.c_char_p, [_i]),

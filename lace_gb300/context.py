@@ -184,6 +184,16 @@ class Context:
         return {"reorthogonalised": out[0], "conditional_nodes": bool(out[1]), "one_kernel_step": bool(out[2]),
                 "one_kernel_householder_step": bool(out[3])}
 
+    def time_arnoldi_step(self, orthogonalization: str = "householder", j: int = 15, reps: int = 20) -> float:
+        """Seconds per launch of the one-kernel Arnoldi step j, replayed on the
+        basis of the last solve (overwrites that solve's cycle state)."""
+        t = C.c_double()
+        rc = self._lib.lace_gpu_time_arnoldi_step(self.h, 1 if orthogonalization == "mgs" else 0, int(j),
+                                                  int(reps), C.byref(t))
+        if rc != DEV_SUCCESS:
+            raise LaceError(rc, "time_arnoldi_step")
+        return t.value
+
     def backward(self, x, dLdx, dLdb=None, dLdA=None, search_max: int = 30, restart_max: int = 20,
                  rtol: float = 1e-10, tol_type: int = 1) -> int:
         par = GmresParam()

@@ -1708,6 +1708,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   // kMaxM directions and reports DEV_ERR_NOT_SUPPORTED only if it needs more
   const bool capped = m > kMaxM;
   if (capped) m = kMaxM;
+  last_m = m;
   const bool mgs = method == 1;
   if (mgs && adjoint) return DEV_ERR_NOT_SUPPORTED;
   if (mgs && !restarted) restart_max = std::min(restart_max, 1);
@@ -1892,6 +1893,39 @@ extern "C" int lace_gpu_get_solve_stats(lace_gpu_ctx *c, int *out) {
   out[1] = c->cond_nodes ? 1 : 0;
   out[2] = c->mgs_persistent ? 1 : 0;
   out[3] = c->hh_persistent ? 1 : 0;
+  return DEV_SUCCESS;
+}
+
+extern "C" int lace_gpu_time_arnoldi_step(lace_gpu_ctx *c, int method, int j, int reps, double *seconds) {
+  if (!c || !seconds) return set_err(DEV_ERR_INVALID_PTR);
+  if (reps < 1 || j < 0 || j + 2 > c->last_m || !c->Vb.p) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  cudaSetDevice(c->device);
+  ArnoldiArgs a = c->arnoldi_args(c->last_m, false);
+  a.mgs_restarted = 1;
+  a.mgs_reorth = 0;
+  // the replays must neither stop nor skip: no convergence (tolerance 0),
+  // not done, barrier arrivals cleared
+  const double zero = 0.0;
+  LCHK(cudaMemcpyAsync(&a.ctrl->rtol_abs, &zero, 8, cudaMemcpyHostToDevice, c->stream));
+  LCHK(cudaMemsetAsync(&a.ctrl->done, 0, 4, c->stream));
+  LCHK(cudaMemsetAsync(&a.ctrl->status, 0, 4, c->stream));
+  LCHK(cudaMemsetAsync(&a.ctrl->block_count[3], 0, 4, c->stream));
+  auto launch = [&]() { return method == 1 ? launch_mgs_step(c->stream, a, j) : launch_hh_step(c->stream, a, j); };
+  if (launch() != 0) return set_err(DEV_ERR_NOT_SUPPORTED);
+  cudaEvent_t e0, e1;
+  LCHK(cudaEventCreate(&e0));
+  LCHK(cudaEventCreate(&e1));
+  cudaEventRecord(e0, c->stream);
+  for (int r = 0; r < reps; ++r) launch();
+  cudaEventRecord(e1, c->stream);
+  const cudaError_t ce = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  LCHK(ce);
+  if (c->h_status() & kStatusSpinTimeout) return set_err(DEV_ERR_INTERNAL_LIMIT);
+  *seconds = ms * 1e-3 / reps;
   return DEV_SUCCESS;
 }
 

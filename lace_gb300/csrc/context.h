@@ -132,6 +132,7 @@ struct lace_gpu_ctx {
   bool mgs_persistent = true;  // the one-kernel Gram-Schmidt step (cooperative launch) available
   bool hh_persistent = true;   // the one-kernel Householder step (cooperative launch) available
   int last_reorth = 0;     // directions of the last Gram-Schmidt solve that reorthogonalised
+  int last_m = 0;          // search directions per cycle of the last FGMRES solve
   std::vector<double> last_hist;
 
   ~lace_gpu_ctx();
