@@ -279,8 +279,8 @@ typedef struct lace_gpu_options {
   int monitor_orthog;   /* ||I - Q^T Q||_inf after every step (slow)     */
   /* Sync-free solve schedule.  0 = autotune; trsv_chunks_per_block > 0 pins
    * it (with trsv_rows_per_lane, 0 meaning 1): chunks per block (<= 1024),
-   * warps per CTA (1-16, 0 = 16) and CTAs per thread-block cluster (1, 2, 4
-   * or 8; 0 = 1; a cluster the device or the shared memory cannot hold runs
+   * warps per CTA (1-16, 0 = 16) and CTAs per thread-block cluster (1, 2, 4,
+   * 8 or 16; 0 = 1; a cluster the device or the shared memory cannot hold runs
    * as 1). */
   int trsv_chunks_per_block;
   int trsv_warps;

@@ -527,7 +527,7 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
   if (o->trsv_chunks_per_block < 0 || o->trsv_chunks_per_block > kBlkMaxUnits || o->trsv_warps < 0 ||
       o->trsv_warps > 16 ||
       !(o->trsv_cluster == 0 || o->trsv_cluster == 1 || o->trsv_cluster == 2 || o->trsv_cluster == 4 ||
-        o->trsv_cluster == 8))
+        o->trsv_cluster == 8 || o->trsv_cluster == 16))
     return set_err(DEV_ERR_ILLEGAL_VALUE);
   const bool prec_changed = o->precision != c->opt.precision;
   // a new schedule choice: tuned again before the next solve

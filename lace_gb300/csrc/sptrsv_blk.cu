@@ -609,6 +609,9 @@ static cudaError_t cl_launch(cudaStream_t s, const BlkPlanDev &P, int warps, int
   auto fn = k_sptrsv_cl<CT, VT, R, LOWER>;
   const size_t sm = (2 * (size_t)P.win + 1) * sizeof(CT);
   if (sm > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  // clusters of 16 (one 128x128 plane per CTA: 8 clusters cover 128 planes) are
+  // beyond the portable size of 8
+  if (a.cl > 8) cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid, a.nrhs);
   cfg.blockDim = dim3(32 * warps);

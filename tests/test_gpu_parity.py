@@ -200,7 +200,7 @@ SCHED_MATS = {
 
 # (rows per lane, chunks per block, warps, CTAs per cluster)
 SCHEDULES = [(1, 8, 4, 1), (1, 8, 4, 2), (1, 8, 4, 4), (1, 16, 8, 8), (1, 3, 2, 4), (1, 5, 16, 8), (2, 4, 4, 4),
-             (4, 4, 4, 2), (4, 2, 2, 1), (8, 2, 4, 2)]
+             (4, 4, 4, 2), (4, 2, 2, 1), (8, 2, 4, 2), (1, 4, 4, 16), (1, 7, 8, 16)]
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-4)])
