@@ -256,11 +256,13 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   const int depth = c->nlevels[0] + c->nlevels[1];
   const int min_sweeps = (mode == 0 && !bcsr && depth + 1 <= 64) ? std::min(depth + 1, maxs) : 0;
   std::vector<double> steps;
-  double step = 0.0, nonlin = 0.0;
+  double step = 0.0;
   // a new pattern: the output containers are prepared while the GPU sweeps
   if (!known) prep.start(L, U, c, bcsr, n, bcsr ? A->blocksize : 0);
   auto t0 = std::chrono::steady_clock::now();
-  rc = c->parilu(maxs, &step, bcsr ? nullptr : &nonlin, true, &steps, tol, min_sweeps);
+  // the sweeps start from the initial guess the residuals above were taken
+  // of (no second initialisation); like LACE, no residual after them
+  rc = c->parilu(maxs, &step, nullptr, true, &steps, tol, min_sweeps, !bcsr);
   const double gen = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   const int prep_rc = prep.join();
   if (rc) return fail(rc);
@@ -296,7 +298,6 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   log->precond_generation_time = gen;
   log->initial_residual = ares;
   log->initial_nonlinear_residual = nonlin0;
-  log->nonlinear_residual = bcsr ? 0.0 : nonlin * c->anorm;
   log->omp_num_threads = num_sms();
   set_err(0);
 }

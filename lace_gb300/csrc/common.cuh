@@ -122,6 +122,37 @@ __device__ __forceinline__ double block_fold(const double *p, size_t step, int c
   return t;
 }
 
+// FP32 -> FP64 exactly, with integer operations (conversions run on the FP64
+// unit, the scarce one on this part)
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  unsigned m = b & 0x7fffffu;
+  unsigned long long ef;
+  if (e == 0) {
+    if (m == 0) {
+      ef = 0;
+    } else {  // subnormal: normalise
+      const int sh = __clz((int)m) - 8;
+      m = (m << sh) & 0x7fffffu;
+      ef = (unsigned long long)(897 - sh) << 52;
+    }
+  } else {
+    ef = (unsigned long long)(e == 255 ? 2047u : e + 896u) << 52;
+  }
+  return __longlong_as_double(
+      (long long)(((unsigned long long)(b & 0x80000000u) << 32) | ef | ((unsigned long long)m << 29)));
+}
+
+// a stored factor value in FP64, exactly, without an FP64-pipe conversion
+template <typename T> __device__ __forceinline__ double fval(T v);
+template <> __device__ __forceinline__ double fval<double>(double v) { return v; }
+template <> __device__ __forceinline__ double fval<float>(float v) { return to_f64(v); }
+template <> __device__ __forceinline__ double fval<__nv_bfloat16>(__nv_bfloat16 v) {
+  return to_f64(__bfloat162float(v));
+}
+
 // mysgn of LACE (include/sparse.h:1129-1133): +1 for v >= 0, -1 otherwise
 __device__ __forceinline__ double mysgn(double v) { return v >= 0.0 ? 1.0 : -1.0; }
 

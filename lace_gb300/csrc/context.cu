@@ -1093,9 +1093,9 @@ int lace_gpu_ctx::init_factors() {
 }
 
 int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
-                         std::vector<double> *steps, double stop_below, int min_sweeps) {
+                         std::vector<double> *steps, double stop_below, int min_sweeps, bool reuse_init) {
   if (!n_blk) return DEV_ERR_NOT_INITIALIZED;
-  int rc = init_factors();
+  int rc = reuse_init && factors_ready ? 0 : init_factors();
   if (rc) return rc;
   IluArgs a = ilu_args();
   if (!a.partials) return DEV_ERR_DEVICE_ALLOC;

@@ -167,8 +167,10 @@ struct lace_gpu_ctx {
   int finish_factors();
   // up to `sweeps` sweeps; with sync_each, stops once the normalised step is
   // <= stop_below (LACE's stopping tests); steps receives every sweep's step
+  // reuse_init: the factors already hold the initial guess (no re-initialisation)
   int parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
-             std::vector<double> *steps, double stop_below = -1.0, int min_sweeps = 0);
+             std::vector<double> *steps, double stop_below = -1.0, int min_sweeps = 0,
+             bool reuse_init = false);
   int h_status();
   int ilu_residuals(double *res, double *nonlin);
   // prefilled: x already holds the unsolved pattern (sync-free block solves)

@@ -13,29 +13,6 @@ namespace lace {
 
 constexpr int kTPB = 256;   // threads per block of the row-tile kernels
 
-// FP32 -> FP64 exactly, with integer operations (conversions run on the FP64
-// unit, the scarce one on this part)
-__device__ __forceinline__ double to_f64(double v) { return v; }
-__device__ __forceinline__ double to_f64(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  unsigned m = b & 0x7fffffu;
-  unsigned long long ef;
-  if (e == 0) {
-    if (m == 0) {
-      ef = 0;
-    } else {  // subnormal: normalise
-      const int sh = __clz((int)m) - 8;
-      m = (m << sh) & 0x7fffffu;
-      ef = (unsigned long long)(897 - sh) << 52;
-    }
-  } else {
-    ef = (unsigned long long)(e == 255 ? 2047u : e + 896u) << 52;
-  }
-  return __longlong_as_double(
-      (long long)(((unsigned long long)(b & 0x80000000u) << 32) | ef | ((unsigned long long)m << 29)));
-}
-
 // operator row i of the tile: CSR (LPR lanes per row) or BCSR (thread/row)
 struct OpView {
   int bs;

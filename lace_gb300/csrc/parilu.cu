@@ -80,13 +80,13 @@ __global__ void __launch_bounds__(kPTPB) k_parilu_sweep(
       if (i > j) {
         const CT nv = s / cvt<CT>(Uold[ue - 1]);
         while (Lcol[lpos] != j) ++lpos;
-        const double d = (double)nv - (double)cvt<CT>(Lold[lpos]);
+        const double d = to_f64(nv) - fval(Lold[lpos]);  // exact conversions on the integer pipes
         acc = fma(d, d, acc);
         Lnew[lpos] = cvt<FT>(nv);
         ++lpos;
       } else {
         while (Uri[iu] != i) ++iu;
-        const double d = (double)s - (double)cvt<CT>(Uold[iu]);
+        const double d = to_f64(s) - fval(Uold[iu]);
         acc = fma(d, d, acc);
         Unew[iu] = cvt<FT>(s);
       }
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kPTPB) k_ilu_residual(
       while (il < le && iu < ue) {
         const int jl = Lcol[il], ju = Uri[iu];
         if (jl == ju) {
-          t = fma((double)cvt<CT>(L[il]), (double)cvt<CT>(U[iu]), t);
+          t = fma(fval(L[il]), fval(U[iu]), t);
           ++il;
           ++iu;
         } else if (jl < ju) {
@@ -146,17 +146,17 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
     const int lb = Lrow[i], le = Lrow[i + 1];
     for (int a = lb; a < le; ++a) {
       const int k = Lcol[a];
-      const double lk = (k == i) ? 1.0 : (double)cvt<CT>(L[a]);
+      const double lk = (k == i) ? 1.0 : fval(L[a]);
       for (int b = a; b < le; ++b) {
         const int k2 = Lcol[b];
-        const double lk2 = (k2 == i) ? 1.0 : (double)cvt<CT>(L[b]);
+        const double lk2 = (k2 == i) ? 1.0 : fval(L[b]);
         double dot = 0.0;
         int p = Urow[k], q = Urow[k2];
         const int pe = Urow[k + 1], qe = Urow[k2 + 1];
         while (p < pe && q < qe) {
           const int cp = Ucol[p], cq = Ucol[q];
           if (cp == cq) {
-            dot = fma((double)cvt<CT>(Ur[p]), (double)cvt<CT>(Ur[q]), dot);
+            dot = fma(fval(Ur[p]), fval(Ur[q]), dot);
             ++p;
             ++q;
           } else if (cp < cq) {
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
       while (il < le && iu < ue) {
         const int jl = Lcol[il], ju = Uri[iu];
         if (jl == ju) {
-          t = fma(jl == i ? 1.0 : (double)cvt<CT>(L[il]), (double)cvt<CT>(Uc[iu]), t);
+          t = fma(jl == i ? 1.0 : fval(L[il]), fval(Uc[iu]), t);
           ++il;
           ++iu;
         } else if (jl < ju) {
