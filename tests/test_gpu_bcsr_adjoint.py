@@ -60,6 +60,30 @@ def test_bcsr_dropin_parilu_matches_oracle(lg):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_bcsr_fgmres_mgs(lg, torch_cuda, prec):
+    """The Gram-Schmidt FGMRES on a BCSR operator (the separate-kernel step:
+    the one-kernel step takes CSR operators) against the oracle's mirror of
+    data_fgmres_restart with block factors."""
+    B = P.bcsr3d(8, seed=4)
+    b = P.rhs_normal(B.n, 0)
+    F = orc.bcsr_parilu(B, 3, mode="sync")
+    op = {"kind": "bcsr", "bs": B.bs, "row": B.row, "col": B.col, "val": B.val}
+    r = orc.fgmres_mgs(op, orc.bcsr_precond(F), b, search_max=50, restart_max=20, rtol=1e-10)
+    with lg.Context(0) as ctx:
+        ctx.set_options(precision=prec)
+        ctx.upload(B)
+        ctx.parilu0(3)
+        xd = torch_cuda.zeros(B.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=20, rtol=1e-10,
+                         orthogonalization="mgs")
+        x = xd.cpu().numpy()
+    assert res.converged and r.converged
+    if prec == "fp64":
+        assert abs(res.total_iterations - r.total_iterations) <= 2
+    assert np.linalg.norm(b - B.to_csr().matvec(x)) <= 2e-10 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
 def test_bcsr_fgmres(lg, torch_cuda, prec):
     B = P.bcsr3d(8, seed=4)
     b = P.rhs_normal(B.n, 0)
