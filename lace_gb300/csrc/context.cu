@@ -1095,6 +1095,9 @@ int lace_gpu_ctx::init_factors() {
 int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
                          std::vector<double> *steps, double stop_below, int min_sweeps, bool reuse_init) {
   if (!n_blk) return DEV_ERR_NOT_INITIALIZED;
+  // the status bits describe this factorisation only (an earlier solve may
+  // have left its own)
+  if (cudaMemsetAsync(&ctrl()->status, 0, 4, stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
   int rc = reuse_init && factors_ready ? 0 : init_factors();
   if (rc) return rc;
   IluArgs a = ilu_args();
@@ -1910,7 +1913,12 @@ extern "C" int lace_gpu_time_arnoldi_step(lace_gpu_ctx *c, int method, int j, in
   LCHK(cudaMemsetAsync(&a.ctrl->done, 0, 4, c->stream));
   LCHK(cudaMemsetAsync(&a.ctrl->status, 0, 4, c->stream));
   LCHK(cudaMemsetAsync(&a.ctrl->block_count[3], 0, 4, c->stream));
-  auto launch = [&]() { return method == 1 ? launch_mgs_step(c->stream, a, j) : launch_hh_step(c->stream, a, j); };
+  // the unsolved marks go to two scratch vectors (same element types, same
+  // traffic), so that the basis and Z stay as the solve left them
+  void *mt = c->vec_t2.p, *mz = c->vec_r.p;
+  auto launch = [&]() {
+    return method == 1 ? launch_mgs_step(c->stream, a, j, mt, mz) : launch_hh_step(c->stream, a, j, mt, mz);
+  };
   if (launch() != 0) return set_err(DEV_ERR_NOT_SUPPORTED);
   cudaEvent_t e0, e1;
   LCHK(cudaEventCreate(&e0));
@@ -1924,7 +1932,12 @@ extern "C" int lace_gpu_time_arnoldi_step(lace_gpu_ctx *c, int method, int j, in
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   LCHK(ce);
-  if (c->h_status() & kStatusSpinTimeout) return set_err(DEV_ERR_INTERNAL_LIMIT);
+  const int st = c->h_status();
+  // the replays' own status (their drifting rotations may even report a
+  // breakdown) must not reach the next operation
+  LCHK(cudaMemsetAsync(&a.ctrl->status, 0, 4, c->stream));
+  LCHK(cudaMemsetAsync(&a.ctrl->done, 0, 4, c->stream));
+  if (st & kStatusSpinTimeout) return set_err(DEV_ERR_INTERNAL_LIMIT);
   *seconds = ms * 1e-3 / reps;
   return DEV_SUCCESS;
 }

@@ -138,7 +138,9 @@ void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
 // passes A, B and C of step j as one cooperative kernel with w in shared
 // memory; returns 1 when it does not apply (BCSR, no sliced ELL, w too large
 // for shared memory), 2 when the cooperative launch failed, 0 on success
-int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j);
+// mark_t/mark_z (both or neither): where the unsolved marks go instead of
+// the next step's solve outputs (a measurement's replays must keep Z intact)
+int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t = nullptr, void *mark_z = nullptr);
 
 // ------------------------------------ FGMRES, modified Gram-Schmidt Arnoldi
 // (src/fgmres_restart.cpp, src/fgmres.cpp).  Basis v_j in a.V, the
@@ -163,7 +165,7 @@ void launch_mgs_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x);
 // vector) as one cooperative kernel with u in shared memory; returns 1 when
 // it does not apply (BCSR, no sliced ELL, u too large for shared memory),
 // 2 when the cooperative launch failed, 0 on success
-int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j);
+int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t = nullptr, void *mark_z = nullptr);
 
 // ------------------------------------------------------------ ParILU
 struct IluArgs {

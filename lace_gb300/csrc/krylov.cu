@@ -1081,7 +1081,7 @@ void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
 }
 
 template <typename ZT, typename QT>
-static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
+static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   static int G = -1;
   if (G < 0) {
     int per_sm = 0;
@@ -1112,6 +1112,10 @@ static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
   p.ctrl = a.ctrl;
   p.m = a.m;
   p.pf = prefill_for(a, j + 1);
+  if (mark_t && p.pf.t) {
+    p.pf.t = mark_t;
+    p.pf.z = mark_z;
+  }
   void *args[] = {&p, &j};
   if (cudaLaunchCooperativeKernel((const void *)k_hh_step<ZT, QT>, dim3(G), dim3(kHHTPB), args,
                                   (size_t)p.rb * 8, s) != cudaSuccess) {
@@ -1121,10 +1125,10 @@ static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
   return 0;
 }
 
-int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j) {
+int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   if (a.bs || !a.sell_ptr) return 1;
-  if (a.z_f32 && a.q_f32 && a.Vf) return hh_step_t<float, float>(s, a, j);
-  if (!a.z_f32 && !a.q_f32) return hh_step_t<double, double>(s, a, j);
+  if (a.z_f32 && a.q_f32 && a.Vf) return hh_step_t<float, float>(s, a, j, mark_t, mark_z);
+  if (!a.z_f32 && !a.q_f32) return hh_step_t<double, double>(s, a, j, mark_t, mark_z);
   return 1;
 }
 

@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(kStepTPB, 1) k_mgs_step(MgsStep a, int j) {
 // -------------------------------------------------------------- launchers
 
 template <typename ZT>
-static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
+static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   static int G = -1;
   if (G < 0) {
     int per_sm = 0;
@@ -575,6 +575,10 @@ static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
   p.restarted = a.mgs_restarted;
   p.reorth = a.mgs_reorth;
   p.pf = prefill_for(a, j + 1);
+  if (mark_t && p.pf.t) {
+    p.pf.t = mark_t;
+    p.pf.z = mark_z;
+  }
   void *args[] = {&p, &j};
   if (cudaLaunchCooperativeKernel((const void *)k_mgs_step<ZT>, dim3(G), dim3(kStepTPB), args,
                                   (size_t)p.rb * 8, s) != cudaSuccess) {
@@ -584,9 +588,9 @@ static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j) {
   return 0;
 }
 
-int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j) {
+int launch_mgs_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   if (a.bs || !a.sell_ptr) return 1;
-  return a.z_f32 ? mgs_step_t<float>(s, a, j) : mgs_step_t<double>(s, a, j);
+  return a.z_f32 ? mgs_step_t<float>(s, a, j, mark_t, mark_z) : mgs_step_t<double>(s, a, j, mark_t, mark_z);
 }
 
 void launch_mgs_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {

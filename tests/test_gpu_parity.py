@@ -456,6 +456,21 @@ def test_dropin_fgmres_mgs_trefethen(lg):
             assert np.linalg.norm(b - A.matvec(x)) <= 1e-3
 
 
+def test_parilu_after_a_breakdown(lg, torch_cuda):
+    """A factorisation reports only its own breakdown: the status an earlier
+    operation left (here a solve with a non-finite right-hand side) does not
+    make the next ParILU fail."""
+    A = MATS["cd16"]()
+    with lg.Context(0) as ctx:
+        ctx.upload(A)
+        ctx.parilu0(3)
+        b = np.full(A.n, np.nan)
+        xd = torch_cuda.zeros(A.n, dtype=torch_cuda.float64, device="cuda")
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=10, restart_max=2, rtol=1e-10)
+        assert not res.converged
+        ctx.parilu0(3)  # must not raise
+
+
 def test_dropin_lace_tests_with_search_2000(lg):
     """LACE's FGMRESPreconditioned (testing/test_linearSolver.cpp:300-398:
     data_fgmres, search 2000, restart 2000) and FGMRESHouseholderPreconditioned
