@@ -244,6 +244,23 @@ int data_fgmres(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0,
                 data_d_matrix *L, data_d_matrix *U, data_d_gmres_param *gmres_par,
                 data_d_gmres_log *gmres_log);
 
+/* Matrix Market files (replace control/magma_zmio.cpp:92, 941 and 587;
+ * declared in include/sparse.h).  Same results as LACE's: entries in file
+ * order, symmetric and hermitian files expanded entry by entry, each row
+ * sorted by column; output lines "%d %d %.16g" in row order (or, for
+ * MagmaColMajor from a row-major matrix, column order), byte for byte.
+ * Parsed and formatted on host threads.  Arrays allocated like LACE_CALLOC
+ * (data_zmfree releases them).  Returns DEV_ERR_NOT_FOUND for a missing
+ * file, DEV_ERR_NOT_SUPPORTED for a banner LACE rejects (only coordinate
+ * real, integer, pattern or complex matrices), DEV_ERR_UNKNOWN for a
+ * malformed size line or missing entries, DEV_ERR_ILLEGAL_VALUE for an index
+ * outside the declared size (LACE writes out of bounds there); -1 when the
+ * output file cannot be opened, as LACE. */
+int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz,
+                        dataType **val, int **row, int **col, const char *filename);
+int data_z_csr_mtx(data_d_matrix *A, const char *filename);
+int data_zwrite_csr_mtx(data_d_matrix A, data_order_t MajorType, const char *filename);
+
 /* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
  * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives
  * the same value (the fill-in part of LACE's res is not formed) and LU is

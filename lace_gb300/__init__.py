@@ -157,6 +157,10 @@ SIGNATURES = {
     "data_fgmres_restart": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_fgmres": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_zilures": (_i, [DataMatrix, DataMatrix, DataMatrix, _DM, C.POINTER(_d), C.POINTER(_d)]),
+    "read_z_csr_from_mtx": (_i, [C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_p),
+                                 C.POINTER(_p), C.POINTER(_p), C.c_char_p]),
+    "data_z_csr_mtx": (_i, [_DM, C.c_char_p]),
+    "data_zwrite_csr_mtx": (_i, [DataMatrix, _i, C.c_char_p]),
     "lace_gpu_default_options": (None, [C.POINTER(GpuOptions)]),
     "lace_gpu_dropin_set_options": (_i, [C.POINTER(GpuOptions)]),
     "lace_gpu_ctx_create": (_i, [C.POINTER(_p), _i, _p]),

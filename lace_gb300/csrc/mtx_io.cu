@@ -1,0 +1,399 @@
+// Matrix Market files for LACE's data_d_matrix, on host threads:
+// read_z_csr_from_mtx / data_z_csr_mtx (control/magma_zmio.cpp:92-351,
+// 941-955) and data_zwrite_csr_mtx (:587-774).
+//
+// LACE reads one entry per fscanf call and writes one per fprintf call, which
+// makes the generate_iLU -> solver file exchange (factors written, read back)
+// take seconds for a million-row system.  Here the file is read whole, split
+// into line-aligned chunks that host threads parse with correctly rounded
+// conversions (std::from_chars, as scanf's %lf rounds), and written from
+// per-thread buffers formatted like %.16g (std::to_chars with precision 16 is
+// specified as printf's %g).  The results are LACE's: the same entries in the
+// same order (symmetric files expanded entry by entry; rows filled in file
+// order, then each row sorted by column with the same std::sort), and the
+// same bytes on output.
+#include <algorithm>
+#include <atomic>
+#include <cctype>
+#include <charconv>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/lace_gb300.h"
+#include "hostpar.h"
+
+namespace {
+
+using lace::par_for;
+
+// LACE_CALLOC's allocation (include/dense_types.h:430-449): posix_memalign(64)
+// and zeroed, so that data_zmfree releases it
+template <typename T>
+T *calloc64(size_t count) {
+  void *p = nullptr;
+  const size_t padded = (count * sizeof(T) / 64 + 1) * 64;
+  if (posix_memalign(&p, 64, padded) != 0) return nullptr;
+  memset(p, 0, padded);
+  return (T *)p;
+}
+
+bool is_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+
+// one token of [p, e) after whitespace; false at the end
+bool next_token(const char *&p, const char *e, const char *&t0, const char *&t1) {
+  while (p < e && is_space(*p)) ++p;
+  if (p >= e) return false;
+  t0 = p;
+  while (p < e && !is_space(*p)) ++p;
+  t1 = p;
+  return true;
+}
+
+// %d: optional sign, decimal digits
+bool parse_int(const char *t0, const char *t1, int &v) {
+  if (t0 < t1 && *t0 == '+') ++t0;
+  auto r = std::from_chars(t0, t1, v);
+  return r.ec == std::errc() && r.ptr == t1;
+}
+
+// %lf: from_chars where it reads the whole token (decimal, inf, nan), else
+// strtod (hexadecimal floats, a leading '+')
+bool parse_double(const char *t0, const char *t1, double &v) {
+  auto r = std::from_chars(t0, t1, v);
+  if (r.ec == std::errc() && r.ptr == t1) return true;
+  std::string s(t0, t1);
+  char *end = nullptr;
+  v = strtod(s.c_str(), &end);
+  return end == s.c_str() + s.size() && !s.empty();
+}
+
+struct Banner {
+  bool ok = false, coordinate = false, real = false, integer = false, pattern = false, complex = false;
+  bool symmetric = false, hermitian = false, skew = false;
+};
+
+// mm_read_banner + mm_is_valid (control/mmio.cpp:100-210): five tokens, the
+// banner prefix, fields compared in lower case
+Banner read_banner(const char *line, const char *e) {
+  Banner b;
+  const char *p = line, *t0, *t1;
+  std::string tok[5];
+  for (int k = 0; k < 5; ++k) {
+    if (!next_token(p, e, t0, t1)) return b;
+    tok[k].assign(t0, t1);
+    if (k > 0)
+      for (auto &c : tok[k]) c = (char)tolower((unsigned char)c);
+  }
+  if (tok[0].compare(0, 14, "%%MatrixMarket") != 0 || tok[1] != "matrix") return b;
+  if (tok[2] == "coordinate") b.coordinate = true;
+  else if (tok[2] != "array") return b;
+  if (tok[3] == "real") b.real = true;
+  else if (tok[3] == "integer") b.integer = true;
+  else if (tok[3] == "pattern") b.pattern = true;
+  else if (tok[3] == "complex") b.complex = true;
+  else return b;
+  if (tok[4] == "symmetric") b.symmetric = true;
+  else if (tok[4] == "hermitian") b.hermitian = true;
+  else if (tok[4] == "skew-symmetric") b.skew = true;
+  else if (tok[4] != "general") return b;
+  if (!b.coordinate && b.pattern) return b;  // mm_is_valid
+  if (b.real && b.hermitian) return b;
+  if (b.pattern && (b.hermitian || b.skew)) return b;
+  b.ok = true;
+  return b;
+}
+
+// the data entries of [p, e) as LACE's loop reads them: `fields` numbers per
+// entry separated by any whitespace (fscanf), nnz entries.  In parallel over
+// line-aligned chunks when every line holds one whole entry; else token by
+// token.
+bool parse_entries(const char *p, const char *e, int nnz, int fields, bool pattern, std::vector<int> &r,
+                   std::vector<int> &c, std::vector<double> &v) {
+  r.assign(nnz, 0);
+  c.assign(nnz, 0);
+  v.assign(nnz, pattern ? 1.0 : 0.0);
+  auto parse_one = [&](const char *&q, const char *end, int k) -> bool {
+    const char *t0, *t1;
+    int row, col;
+    if (!next_token(q, end, t0, t1) || !parse_int(t0, t1, row)) return false;
+    if (!next_token(q, end, t0, t1) || !parse_int(t0, t1, col)) return false;
+    double val = 1.0;
+    if (!pattern) {
+      if (!next_token(q, end, t0, t1) || !parse_double(t0, t1, val)) return false;
+      for (int f = 3; f < fields; ++f)  // the imaginary part of a complex entry: read, dropped
+        if (!next_token(q, end, t0, t1)) return false;
+    }
+    r[k] = row - 1;
+    c[k] = col - 1;
+    v[k] = val;
+    return true;
+  };
+  // line-aligned chunks, their entry counts, then the entries
+  const size_t bytes = (size_t)(e - p);
+  const int nt = std::max(1, std::min(16, (int)(bytes / (1 << 20))));
+  std::vector<const char *> cut(nt + 1);
+  cut[0] = p;
+  cut[nt] = e;
+  for (int t = 1; t < nt; ++t) {
+    const char *q = p + bytes * t / nt;
+    while (q < e && *q != '\n') ++q;
+    cut[t] = q < e ? q + 1 : e;
+  }
+  std::vector<long long> lines(nt, 0);
+  std::vector<char> regular(nt, 1);
+  par_for((size_t)nt, 1, [&](size_t b, size_t en) {
+    for (size_t t = b; t < en; ++t) {
+      long long cnt = 0;
+      const char *q = cut[t], *end = cut[t + 1];
+      while (q < end) {
+        const char *le = (const char *)memchr(q, '\n', (size_t)(end - q));
+        if (!le) le = end;
+        int toks = 0;
+        const char *s = q, *t0, *t1;
+        while (next_token(s, le, t0, t1)) ++toks;
+        if (toks == fields) ++cnt;
+        else if (toks != 0) regular[t] = 0;
+        q = le + 1;
+      }
+      lines[t] = cnt;
+    }
+  });
+  long long total = 0;
+  bool reg = true;
+  std::vector<long long> first(nt, 0);
+  for (int t = 0; t < nt; ++t) {
+    first[t] = total;
+    total += lines[t];
+    reg = reg && regular[t];
+  }
+  if (reg && total >= nnz) {
+    std::atomic<int> bad(0);
+    par_for((size_t)nt, 1, [&](size_t b, size_t en) {
+      for (size_t t = b; t < en; ++t) {
+        long long k = first[t];
+        const char *q = cut[t], *end = cut[t + 1];
+        while (k < nnz && q < end) {
+          const char *le = (const char *)memchr(q, '\n', (size_t)(end - q));
+          if (!le) le = end;
+          const char *s = q, *t0, *t1;
+          const char *probe = s;
+          if (next_token(probe, le, t0, t1)) {  // a line with an entry
+            if (!parse_one(s, le, (int)k)) bad = 1;
+            ++k;
+          }
+          q = le + 1;
+        }
+      }
+    });
+    return bad == 0;
+  }
+  // irregular layout: one token stream, as fscanf reads it
+  const char *q = p;
+  for (int k = 0; k < nnz; ++k)
+    if (!parse_one(q, e, k)) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz, dataType **val,
+                                   int **row, int **col, const char *filename) {
+  if (!type || !n_row || !n_col || !nnz || !val || !row || !col || !filename) return DEV_ERR_INVALID_PTR;
+  FILE *f = fopen(filename, "rb");
+  if (!f) return DEV_ERR_NOT_FOUND;
+  std::vector<char> buf;
+  if (fseek(f, 0, SEEK_END) == 0) {
+    const long size = ftell(f);
+    if (size > 0) {
+      buf.resize((size_t)size);
+      fseek(f, 0, SEEK_SET);
+      if (fread(buf.data(), 1, buf.size(), f) != buf.size()) buf.clear();
+    }
+  }
+  fclose(f);
+  const char *p = buf.data(), *e = buf.data() + buf.size();
+  // the banner line (at most 1024 characters, as mmio's fgets reads it)
+  const char *le = (const char *)memchr(p, '\n', buf.size());
+  if (!le) le = e;
+  const Banner b = read_banner(p, std::min(le, p + 1024));
+  if (!b.ok || !b.coordinate || !(b.real || b.integer || b.pattern || b.complex)) return DEV_ERR_NOT_SUPPORTED;
+  p = le < e ? le + 1 : e;
+  // comment lines, then the size line (mm_read_mtx_crd_size, mmio.cpp:219-258)
+  while (p < e && *p == '%') {
+    le = (const char *)memchr(p, '\n', (size_t)(e - p));
+    p = le ? le + 1 : e;
+  }
+  int M = 0, N = 0, NZ = 0;
+  {
+    const char *t0, *t1;
+    if (!next_token(p, e, t0, t1) || !parse_int(t0, t1, M) || !next_token(p, e, t0, t1) || !parse_int(t0, t1, N) ||
+        !next_token(p, e, t0, t1) || !parse_int(t0, t1, NZ) || M < 0 || N < 0 || NZ < 0)
+      return DEV_ERR_UNKNOWN;
+  }
+  std::vector<int> cr, cc;
+  std::vector<double> cv;
+  const int fields = b.pattern ? 2 : (b.complex ? 4 : 3);
+  if (!parse_entries(p, e, NZ, fields, b.pattern, cr, cc, cv)) return DEV_ERR_UNKNOWN;
+  for (int k = 0; k < NZ; ++k)
+    if (cr[k] < 0 || cr[k] >= M || cc[k] < 0 || cc[k] >= N) return DEV_ERR_ILLEGAL_VALUE;
+  // symmetric and hermitian files: each off-diagonal entry followed by its
+  // mirror (:215-269); skew-symmetric ones are read as they are
+  long long total = NZ;
+  if (b.symmetric || b.hermitian) {
+    std::vector<int> off(NZ + 1, 0);
+    for (int k = 0; k < NZ; ++k) off[k + 1] = off[k] + (cr[k] != cc[k] ? 2 : 1);
+    total = off[NZ];
+    if (total > 0x7fffffff) return DEV_ERR_NOT_SUPPORTED;
+    std::vector<int> nr((size_t)total), nc((size_t)total);
+    std::vector<double> nv((size_t)total);
+    par_for((size_t)NZ, 1 << 16, [&](size_t b0, size_t b1) {
+      for (size_t k = b0; k < b1; ++k) {
+        const int o = off[k];
+        nr[o] = cr[k];
+        nc[o] = cc[k];
+        nv[o] = cv[k];
+        if (cr[k] != cc[k]) {
+          nr[o + 1] = cc[k];
+          nc[o + 1] = cr[k];
+          nv[o + 1] = cv[k];
+        }
+      }
+    });
+    cr.swap(nr);
+    cc.swap(nc);
+    cv.swap(nv);
+  }
+  const int nz = (int)total;
+  // CSR: rows in file order (the stable scatter of :276-313), then each row
+  // sorted by column with std::sort on (column, value) pairs (:315-329)
+  int *R = calloc64<int>((size_t)M + 1);
+  int *C = calloc64<int>((size_t)nz);
+  double *V = calloc64<double>((size_t)nz);
+  if (!R || !C || !V) {
+    free(R);
+    free(C);
+    free(V);
+    return DEV_ERR_HOST_ALLOC;
+  }
+  for (int k = 0; k < nz; ++k) ++R[cr[k] + 1];
+  for (int i = 0; i < M; ++i) R[i + 1] += R[i];
+  {
+    std::vector<int> next(R, R + M);
+    for (int k = 0; k < nz; ++k) {
+      const int d = next[cr[k]]++;
+      C[d] = cc[k];
+      V[d] = cv[k];
+    }
+  }
+  par_for((size_t)M, 4096, [&](size_t i0, size_t i1) {
+    std::vector<std::pair<int, double>> rv;
+    for (size_t i = i0; i < i1; ++i) {
+      const int kk = R[i], len = R[i + 1] - R[i];
+      rv.resize(len);
+      for (int q = 0; q < len; ++q) rv[q] = std::make_pair(C[kk + q], V[kk + q]);
+      std::sort(rv.begin(), rv.end(),
+                [](const std::pair<int, double> &a, const std::pair<int, double> &b) { return a.first < b.first; });
+      for (int q = 0; q < len; ++q) {
+        C[kk + q] = rv[q].first;
+        V[kk + q] = rv[q].second;
+      }
+    }
+  });
+  *type = Magma_CSR;
+  *n_row = M;
+  *n_col = N;
+  *nnz = nz;
+  *row = R;
+  *col = C;
+  *val = V;
+  return DEV_SUCCESS;
+}
+
+extern "C" int data_z_csr_mtx(data_d_matrix *A, const char *filename) {
+  if (!A) return DEV_ERR_INVALID_PTR;
+  data_storage_t st = Magma_CSR;
+  const int rc = read_z_csr_from_mtx(&st, &A->num_rows, &A->num_cols, &A->nnz, &A->val, &A->row, &A->col, filename);
+  if (rc) return rc;
+  A->true_nnz = A->nnz;
+  A->major = MagmaRowMajor;
+  return DEV_SUCCESS;
+}
+
+namespace {
+
+// "%d %d %.16g\n" for entries [k0, k1) of rows [i0, i1) of (R, C, V), the
+// first number from rows (row-major output) or from columns (column-major)
+void format_rows(const int *R, const int *C, const double *V, int i0, int i1, bool col_first, std::string &out) {
+  char num[64];
+  for (int i = i0; i < i1; ++i)
+    for (int k = R[i]; k < R[i + 1]; ++k) {
+      const int a = col_first ? C[k] + 1 : i + 1, b = col_first ? i + 1 : C[k] + 1;
+      auto r = std::to_chars(num, num + sizeof num, a);
+      out.append(num, r.ptr);
+      out.push_back(' ');
+      r = std::to_chars(num, num + sizeof num, b);
+      out.append(num, r.ptr);
+      out.push_back(' ');
+      r = std::to_chars(num, num + sizeof num, V[k], std::chars_format::general, 16);
+      out.append(num, r.ptr);
+      out.push_back('\n');
+    }
+}
+
+}  // namespace
+
+extern "C" int data_zwrite_csr_mtx(data_d_matrix A, data_order_t MajorType, const char *filename) {
+  if (!filename) return DEV_ERR_INVALID_PTR;
+  if (A.storage_type == Magma_DENSE || A.storage_type == Magma_BCSR) return DEV_ERR_NOT_SUPPORTED;
+  const int nr = A.num_rows, nc = A.num_cols, nz = A.nnz;
+  if (nr < 0 || (nr > 0 && !A.row) || (nz > 0 && (!A.col || !A.val))) return DEV_ERR_INVALID_PTR;
+  // column-major output of a row-major matrix: its transpose, rows of the
+  // transpose in ascending order of the original rows (:597-651)
+  const bool transpose = MajorType == MagmaColMajor && A.major != MagmaColMajor;
+  std::vector<int> tr, tc;
+  std::vector<double> tv;
+  const int *R = A.row, *C = A.col;
+  const double *V = A.val;
+  int rows = nr;
+  if (transpose) {
+    tr.assign((size_t)nc + 1, 0);
+    tc.resize((size_t)nz);
+    tv.resize((size_t)nz);
+    for (int k = 0; k < A.row[nr]; ++k) ++tr[A.col[k] + 1];
+    for (int j = 0; j < nc; ++j) tr[j + 1] += tr[j];
+    std::vector<int> next(tr.begin(), tr.end() - 1);
+    for (int i = 0; i < nr; ++i)
+      for (int k = A.row[i]; k < A.row[i + 1]; ++k) {
+        const int d = next[A.col[k]]++;
+        tc[d] = i;
+        tv[d] = A.val[k];
+      }
+    R = tr.data();
+    C = tc.data();
+    V = tv.data();
+    rows = nc;
+  }
+  FILE *fp = fopen(filename, "w");
+  if (!fp) return -1;  // :606-610
+  fprintf(fp, "%%%%MatrixMarket matrix coordinate real general\n");
+  // (rows, columns) of A either way: LACE prints the transpose's (columns, rows)
+  fprintf(fp, "%d %d %d\n", nr, nc, nz);
+  // per-thread buffers of whole rows, written in order
+  const int nt = std::max(1, std::min(16, (int)(((size_t)(R[rows] - R[0]) * 32) >> 20)));
+  std::vector<std::string> part(nt);
+  par_for((size_t)nt, 1, [&](size_t b0, size_t b1) {
+    for (size_t t = b0; t < b1; ++t) {
+      const int i0 = (int)((long long)rows * t / nt), i1 = (int)((long long)rows * (t + 1) / nt);
+      part[t].reserve((size_t)(R[i1] - R[i0]) * 32);
+      format_rows(R, C, V, i0, i1, transpose, part[t]);
+    }
+  });
+  bool ok = true;
+  for (auto &s : part) ok = ok && fwrite(s.data(), 1, s.size(), fp) == s.size();
+  if (fclose(fp) != 0) ok = false;
+  return ok ? DEV_SUCCESS : DEV_ERR_UNKNOWN;
+}

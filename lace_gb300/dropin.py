@@ -244,6 +244,30 @@ def _fgmres_call(fn, A: Mat, b, x0, L, U, search_max, restart_max, rtol, tol_typ
                                                  "initial_residual", "final_residual")}
 
 
+def read_mtx(path: str):
+    """read_z_csr_from_mtx: (rc, n_rows, n_cols, row, col, val) as numpy
+    arrays (copies; the library's arrays are released)."""
+    st, nr, nc, nz = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    val, row, col = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    rc = lib().read_z_csr_from_mtx(C.byref(st), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(val),
+                                   C.byref(row), C.byref(col), path.encode())
+    if rc != 0:
+        return rc, 0, 0, None, None, None
+    n, z = nr.value, nz.value
+    r = np.ctypeslib.as_array(C.cast(row, C.POINTER(C.c_int)), shape=(n + 1,)).copy()
+    c = np.ctypeslib.as_array(C.cast(col, C.POINTER(C.c_int)), shape=(max(z, 1),))[:z].copy()
+    v = np.ctypeslib.as_array(C.cast(val, C.POINTER(C.c_double)), shape=(max(z, 1),))[:z].copy()
+    libc = C.CDLL(None)
+    for p in (val, row, col):
+        libc.free(p)
+    return rc, n, nc.value, r, c, v
+
+
+def write_mtx(A: "Mat", path: str, major: int = 101) -> int:
+    """data_zwrite_csr_mtx (major 101 row-major, 102 column-major)."""
+    return lib().data_zwrite_csr_mtx(A.m, int(major), path.encode())
+
+
 def spmv(alpha: float, A: Mat, x, beta: float = 0.0, y=None):
     nout = A.m.num_rows * (A.m.blocksize if A.m.storage_type == Magma_BCSR else 1)
     xv = dense(x)

@@ -143,6 +143,23 @@ double ref_orthogonality_error(int n, int ncols, const double *Q, int search) {
   return err;
 }
 
+/* LACE's own Matrix Market reader (control/magma_zmio.cpp:92) into a new
+ * CSR handle, and its writer (:587) */
+data_d_matrix *ref_read_csr_mtx(const char *filename, int *info) {
+  data_d_matrix *A = (data_d_matrix *)calloc(1, sizeof(data_d_matrix));
+  A->storage_type = Magma_CSR;
+  data_storage_t st = Magma_CSR;
+  *info = read_z_csr_from_mtx(&st, &A->num_rows, &A->num_cols, &A->nnz, &A->val, &A->row, &A->col,
+                              filename);
+  A->true_nnz = A->nnz;
+  A->major = MagmaRowMajor;
+  return A;
+}
+
+int ref_write_csr_mtx(data_d_matrix *A, int major, const char *filename) {
+  return data_zwrite_csr_mtx(*A, (data_order_t)major, filename);
+}
+
 /* MKL-semantics ILU(0) baseline (blas/zcsrilu0.cpp), in place on A's values */
 int ref_csrilu0(data_d_matrix *A) { return data_dcsrilu0_mkl(A); }
 

@@ -68,6 +68,9 @@ def _load(path: str) -> C.CDLL:
             L.ref_orthogonality_error.restype = C.c_double
             L.ref_orthogonality_error.argtypes = [C.c_int, C.c_int, vp, C.c_int]
             L.ref_csrilu0.argtypes = [vp]
+            L.ref_read_csr_mtx.restype = vp
+            L.ref_read_csr_mtx.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+            L.ref_write_csr_mtx.argtypes = [vp, C.c_int, C.c_char_p]
         else:
             L.ref_bcsr_parilu.argtypes = [vp, C.c_double, C.POINTER(vp), C.POINTER(vp), vp]
             L.ref_dense_inverse.argtypes = [C.c_int, vp, vp]
@@ -247,6 +250,23 @@ def dense_inverse(a: np.ndarray) -> np.ndarray:
     out = np.zeros((bs, bs))
     lib_bcsr().ref_dense_inverse(bs, _p(a), _p(out))
     return out
+
+
+def read_csr_mtx(path: str):
+    """LACE's own read_z_csr_from_mtx: (info, n_rows, n_cols, row, col, val)."""
+    info = C.c_int()
+    h = lib().ref_read_csr_mtx(path.encode(), C.byref(info))
+    M = Mat(h, lib())
+    if info.value != 0:
+        return info.value, 0, 0, None, None, None
+    d = M.info()
+    r, c, v = M.arrays()
+    return info.value, d["nrows"], d["ncols"], r.copy(), c.copy(), v.copy()
+
+
+def write_csr_mtx(A: Mat, path: str, major: int = 101) -> int:
+    """LACE's own data_zwrite_csr_mtx (major 101 row-major, 102 column-major)."""
+    return lib().ref_write_csr_mtx(A.h, int(major), path.encode())
 
 
 def read_mtx(path: str):

@@ -240,6 +240,38 @@ def main():
     g["orth_Q"] = Q
     g["orth_err"] = np.array([ref.orthogonality_error(Q, s) for s in range(1, 13)])
 
+    # ---------------------------------------- Matrix Market files (LACE's IO)
+    # LACE's own reader and writer on generated files: SHA-256 digests of the
+    # arrays read and of the files written (row- and column-major)
+    sys.path.insert(0, os.path.dirname(HERE))
+    import mtx_cases as MC
+    tmp = tempfile.mkdtemp()
+    texts = dict(MC.cases())
+    texts["large"] = MC.large_text()
+    for name, text in texts.items():
+        fn = os.path.join(tmp, name + ".mtx")
+        with open(fn, "w", newline="") as f:
+            f.write(text)
+        with CaptureStdout():
+            info, nr, nc, r, c, v = ref.read_csr_mtx(fn)
+        g[f"mtx_{name}_info"] = np.array([info])
+        if info != 0:
+            continue
+        g[f"mtx_{name}_read"] = np.array([MC.digest_arrays(nr, nc, r, c, v)])
+        Am = ref.Mat.from_arrays(ref.Magma_CSR, nr, nc, r, c, v)
+        for major in ((101, 102) if nr == nc else (101,)):  # LACE's transpose asserts on non-square input
+            out = fn + ".%d" % major
+            with CaptureStdout():
+                ref.write_csr_mtx(Am, out, major)
+            g[f"mtx_{name}_write{major}"] = np.array([MC.digest_file(out)])
+    n, r, c, v = MC.write_values_matrix()
+    Am = ref.Mat.from_arrays(ref.Magma_CSR, n, n, r, c, v)
+    for major in (101, 102):
+        out = os.path.join(tmp, "values.%d" % major)
+        with CaptureStdout():
+            ref.write_csr_mtx(Am, out, major)
+        g[f"mtx_values_write{major}"] = np.array([MC.digest_file(out)])
+
     np.savez_compressed(OUT, **{k: np.asarray(v) for k, v in g.items() if not isinstance(v, tuple)},
                         **{f"{k}_{i}": np.asarray(a) for k, v in g.items() if isinstance(v, tuple)
                            for i, a in enumerate(v)})

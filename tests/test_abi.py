@@ -22,7 +22,7 @@ def declared_functions():
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", txt,
                        flags=re.M)
-    return sorted(set(n for n in names if n.startswith(("data_", "lace_gpu_"))))
+    return sorted(set(n for n in names if n.startswith(("data_", "lace_gpu_", "read_z_"))))
 
 
 def test_library_exports_every_declared_symbol():
