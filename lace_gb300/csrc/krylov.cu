@@ -11,6 +11,9 @@
 //            (LACE :658-714)
 //   pass C : v_{j+1} and q = P_0...P_{j+1} e_{j+1} (LACE :519-617) in one read
 //   x update (end of cycle): small least-squares solve + x += Z y (:721-744)
+// k_hh_step runs passes A, B and C of a step as one cooperative kernel (w in
+// shared memory, two grid reductions) where the operator is CSR and w fits;
+// the separate passes serve the rest (BCSR, the adjoint, large n).
 // Every kernel returns at once when Control::done is set, so a whole cycle can
 // be launched (or replayed from a CUDA graph) without host round trips.
 #include <math.h>

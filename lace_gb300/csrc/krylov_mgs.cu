@@ -3,16 +3,19 @@
 //
 // Modified Gram-Schmidt is sequential in the basis index: the coefficient of
 // v_k is taken from u after v_0..v_{k-1} were removed, so step j needs j+2
-// grid-wide sums one after another.  One kernel per sum, each fusing the
-// previous subtraction with the next dot product in a single pass over u
-// (one wave of blocks, deterministic fold in the last block), keeps u and
-// the two basis vectors it touches streaming from L2; the scalars
-// (coefficients, Brown/Hindmarsh test, Givens rotations, convergence) stay
-// in device memory, so a cycle runs from a CUDA graph without host round
-// trips.  The reorthogonalising second pass (LACE :336-360) sits in a
-// conditional graph node that the first pass's norm kernel switches on, so
-// steps that do not need it launch nothing.  Every kernel returns at once
-// once Control::done is set.
+// grid-wide sums one after another.  Two forms of the step after the solves:
+//   k_mgs_step (default): one cooperative kernel, one block per SM keeping
+//     its rows of u in shared memory; each sum is a block sum, a grid barrier
+//     and a fold every block performs in the same order; the second pass
+//     (LACE :336-360) and the rotations run in the same kernel;
+//   one kernel per sum (BCSR operators, u too large for shared memory), each
+//     fusing the previous subtraction with the next dot product in one pass
+//     over u, the second pass in a conditional graph node that the first
+//     pass's norm kernel switches on.
+// The scalars (coefficients, Brown/Hindmarsh test, Givens rotations,
+// convergence) stay in device memory, so a cycle runs from a CUDA graph
+// without host round trips, and every kernel returns at once once
+// Control::done is set.
 #include <float.h>
 #include <math.h>
 
@@ -620,7 +623,7 @@ void launch_mgs_operator(cudaStream_t s, const ArnoldiArgs &a, int j) {
 }
 
 void launch_mgs_sweep(cudaStream_t s, const ArnoldiArgs &a, int j, int k, int pass) {
-  (void)j;
+  (void)j;  // the sweep depends on k only
   static const int g = wave_grid(k_mgs_sweep, a.grid);
   k_mgs_sweep<<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.ldv, k, a.w, pass, a.partials, a.cy,
                                                           a.ctrl);
