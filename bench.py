@@ -50,6 +50,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float) -> float:
+    """The slowest rank's value (each rank times its own replica); the
+    reduction tensor lives where the process group's backend works (the GPU
+    for NCCL, the host for gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -324,9 +338,7 @@ def run_ours(args):
     launches_per_solve = (4 + SWEEPS + 2 + 1) + 2 + cycles * (3 + M * 3)
     med = statistics.median(t_mixed)
     if world > 1:
-        tt = torch.tensor([med], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        med = float(tt.item())
+        med = max_over_ranks(med)
     out = {
         "metric": METRIC,
         "value": med,
