@@ -23,12 +23,26 @@
 #include <utility>
 #include <vector>
 
+#include <chrono>
+
 #include "../../include/lace_gb300.h"
 #include "hostpar.h"
 
 namespace {
 
 using lace::par_for;
+
+// LACE_GB300_VERBOSE: the reader's phases
+struct IoClock {
+  bool on = getenv("LACE_GB300_VERBOSE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char *what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    printf("%% mtx %-24s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
 
 // LACE_CALLOC's allocation (include/dense_types.h:430-449): posix_memalign(64)
 // and zeroed, so that data_zmfree releases it
@@ -107,34 +121,31 @@ Banner read_banner(const char *line, const char *e) {
   return b;
 }
 
+// one line of [q, le): 1 and the entry when it holds exactly `fields`
+// numbers, 0 when it is blank, -1 otherwise
+int parse_line(const char *q, const char *le, int fields, bool pattern, int &row, int &col, double &val) {
+  const char *t0, *t1;
+  if (!next_token(q, le, t0, t1)) return 0;
+  if (!parse_int(t0, t1, row)) return -1;
+  if (!next_token(q, le, t0, t1) || !parse_int(t0, t1, col)) return -1;
+  val = 1.0;
+  if (!pattern) {
+    if (!next_token(q, le, t0, t1) || !parse_double(t0, t1, val)) return -1;
+    for (int f = 3; f < fields; ++f)  // the imaginary part of a complex entry: read, dropped
+      if (!next_token(q, le, t0, t1)) return -1;
+  }
+  return next_token(q, le, t0, t1) ? -1 : 1;
+}
+
 // the data entries of [p, e) as LACE's loop reads them: `fields` numbers per
-// entry separated by any whitespace (fscanf), nnz entries.  In parallel over
-// line-aligned chunks when every line holds one whole entry; else token by
+// entry separated by any whitespace (fscanf), nnz entries.  In one parallel
+// pass over line-aligned chunks when every line holds one whole entry (each
+// chunk into its own arrays, then concatenated in chunk order); else token by
 // token.
 bool parse_entries(const char *p, const char *e, int nnz, int fields, bool pattern, std::vector<int> &r,
                    std::vector<int> &c, std::vector<double> &v) {
-  r.assign(nnz, 0);
-  c.assign(nnz, 0);
-  v.assign(nnz, pattern ? 1.0 : 0.0);
-  auto parse_one = [&](const char *&q, const char *end, int k) -> bool {
-    const char *t0, *t1;
-    int row, col;
-    if (!next_token(q, end, t0, t1) || !parse_int(t0, t1, row)) return false;
-    if (!next_token(q, end, t0, t1) || !parse_int(t0, t1, col)) return false;
-    double val = 1.0;
-    if (!pattern) {
-      if (!next_token(q, end, t0, t1) || !parse_double(t0, t1, val)) return false;
-      for (int f = 3; f < fields; ++f)  // the imaginary part of a complex entry: read, dropped
-        if (!next_token(q, end, t0, t1)) return false;
-    }
-    r[k] = row - 1;
-    c[k] = col - 1;
-    v[k] = val;
-    return true;
-  };
-  // line-aligned chunks, their entry counts, then the entries
   const size_t bytes = (size_t)(e - p);
-  const int nt = std::max(1, std::min(16, (int)(bytes / (1 << 20))));
+  const int nt = std::max(1, std::min(64, (int)(bytes / (1 << 20))));
   std::vector<const char *> cut(nt + 1);
   cut[0] = p;
   cut[nt] = e;
@@ -143,23 +154,37 @@ bool parse_entries(const char *p, const char *e, int nnz, int fields, bool patte
     while (q < e && *q != '\n') ++q;
     cut[t] = q < e ? q + 1 : e;
   }
-  std::vector<long long> lines(nt, 0);
-  std::vector<char> regular(nt, 1);
-  par_for((size_t)nt, 1, [&](size_t b, size_t en) {
-    for (size_t t = b; t < en; ++t) {
-      long long cnt = 0;
+  struct Part {
+    std::vector<int> r, c;
+    std::vector<double> v;
+    bool regular = true;
+  };
+  std::vector<Part> part(nt);
+  par_for((size_t)nt, 1, [&](size_t b0, size_t b1) {
+    for (size_t t = b0; t < b1; ++t) {
+      Part &P = part[t];
+      const size_t guess = (size_t)(cut[t + 1] - cut[t]) / 16 + 16;
+      P.r.reserve(guess);
+      P.c.reserve(guess);
+      P.v.reserve(guess);
       const char *q = cut[t], *end = cut[t + 1];
       while (q < end) {
         const char *le = (const char *)memchr(q, '\n', (size_t)(end - q));
         if (!le) le = end;
-        int toks = 0;
-        const char *s = q, *t0, *t1;
-        while (next_token(s, le, t0, t1)) ++toks;
-        if (toks == fields) ++cnt;
-        else if (toks != 0) regular[t] = 0;
+        int row, col;
+        double val;
+        const int got = parse_line(q, le, fields, pattern, row, col, val);
+        if (got < 0) {
+          P.regular = false;
+          break;
+        }
+        if (got > 0) {
+          P.r.push_back(row - 1);
+          P.c.push_back(col - 1);
+          P.v.push_back(val);
+        }
         q = le + 1;
       }
-      lines[t] = cnt;
     }
   });
   long long total = 0;
@@ -167,34 +192,41 @@ bool parse_entries(const char *p, const char *e, int nnz, int fields, bool patte
   std::vector<long long> first(nt, 0);
   for (int t = 0; t < nt; ++t) {
     first[t] = total;
-    total += lines[t];
-    reg = reg && regular[t];
+    total += (long long)part[t].r.size();
+    reg = reg && part[t].regular;
   }
+  r.assign(nnz, 0);
+  c.assign(nnz, 0);
+  v.assign(nnz, pattern ? 1.0 : 0.0);
   if (reg && total >= nnz) {
-    std::atomic<int> bad(0);
-    par_for((size_t)nt, 1, [&](size_t b, size_t en) {
-      for (size_t t = b; t < en; ++t) {
-        long long k = first[t];
-        const char *q = cut[t], *end = cut[t + 1];
-        while (k < nnz && q < end) {
-          const char *le = (const char *)memchr(q, '\n', (size_t)(end - q));
-          if (!le) le = end;
-          const char *s = q, *t0, *t1;
-          const char *probe = s;
-          if (next_token(probe, le, t0, t1)) {  // a line with an entry
-            if (!parse_one(s, le, (int)k)) bad = 1;
-            ++k;
-          }
-          q = le + 1;
-        }
+    par_for((size_t)nt, 1, [&](size_t b0, size_t b1) {
+      for (size_t t = b0; t < b1; ++t) {
+        const long long k0 = first[t];
+        const long long cnt = std::min<long long>((long long)part[t].r.size(), (long long)nnz - k0);
+        if (cnt <= 0) continue;
+        memcpy(r.data() + k0, part[t].r.data(), 4 * (size_t)cnt);
+        memcpy(c.data() + k0, part[t].c.data(), 4 * (size_t)cnt);
+        memcpy(v.data() + k0, part[t].v.data(), 8 * (size_t)cnt);
       }
     });
-    return bad == 0;
+    return true;
   }
   // irregular layout: one token stream, as fscanf reads it
-  const char *q = p;
-  for (int k = 0; k < nnz; ++k)
-    if (!parse_one(q, e, k)) return false;
+  const char *q = p, *t0, *t1;
+  for (int k = 0; k < nnz; ++k) {
+    int row, col;
+    double val = 1.0;
+    if (!next_token(q, e, t0, t1) || !parse_int(t0, t1, row)) return false;
+    if (!next_token(q, e, t0, t1) || !parse_int(t0, t1, col)) return false;
+    if (!pattern) {
+      if (!next_token(q, e, t0, t1) || !parse_double(t0, t1, val)) return false;
+      for (int f = 3; f < fields; ++f)
+        if (!next_token(q, e, t0, t1)) return false;
+    }
+    r[k] = row - 1;
+    c[k] = col - 1;
+    v[k] = val;
+  }
   return true;
 }
 
@@ -203,6 +235,7 @@ bool parse_entries(const char *p, const char *e, int nnz, int fields, bool patte
 extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz, dataType **val,
                                    int **row, int **col, const char *filename) {
   if (!type || !n_row || !n_col || !nnz || !val || !row || !col || !filename) return DEV_ERR_INVALID_PTR;
+  IoClock clk;
   FILE *f = fopen(filename, "rb");
   if (!f) return DEV_ERR_NOT_FOUND;
   std::vector<char> buf;
@@ -215,6 +248,7 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
     }
   }
   fclose(f);
+  clk.mark("file read");
   const char *p = buf.data(), *e = buf.data() + buf.size();
   // the banner line (at most 1024 characters, as mmio's fgets reads it)
   const char *le = (const char *)memchr(p, '\n', buf.size());
@@ -238,6 +272,7 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
   std::vector<double> cv;
   const int fields = b.pattern ? 2 : (b.complex ? 4 : 3);
   if (!parse_entries(p, e, NZ, fields, b.pattern, cr, cc, cv)) return DEV_ERR_UNKNOWN;
+  clk.mark("entries parsed");
   for (int k = 0; k < NZ; ++k)
     if (cr[k] < 0 || cr[k] >= M || cc[k] < 0 || cc[k] >= N) return DEV_ERR_ILLEGAL_VALUE;
   // symmetric and hermitian files: each off-diagonal entry followed by its
@@ -268,6 +303,7 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
     cv.swap(nv);
   }
   const int nz = (int)total;
+  clk.mark("checked, expanded");
   // CSR: rows in file order (the stable scatter of :276-313), then each row
   // sorted by column with std::sort on (column, value) pairs (:315-329)
   int *R = calloc64<int>((size_t)M + 1);
@@ -289,6 +325,7 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
       V[d] = cv[k];
     }
   }
+  clk.mark("rows filled");
   par_for((size_t)M, 4096, [&](size_t i0, size_t i1) {
     std::vector<std::pair<int, double>> rv;
     for (size_t i = i0; i < i1; ++i) {
@@ -303,6 +340,7 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
       }
     }
   });
+  clk.mark("rows sorted");
   *type = Magma_CSR;
   *n_row = M;
   *n_col = N;
