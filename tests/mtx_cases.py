@@ -131,7 +131,9 @@ def large_text() -> str:
             if ok:
                 ents.append((i, j))
     order = rng.permutation(len(ents))
-    vals = rng.standard_normal(len(ents)) * np.exp(rng.uniform(-20, 20, len(ents)))
+    # exact power-of-two scales: the file text must not depend on the
+    # platform's exp (numpy's differs in the last bit between x86 and Arm)
+    vals = np.ldexp(rng.standard_normal(len(ents)), rng.integers(-30, 30, len(ents)))
     lines = ["%%MatrixMarket matrix coordinate real general", "%d %d %d" % (n, n, len(ents))]
     lines += ["%d %d %r" % (ents[k][0] + 1, ents[k][1] + 1, float(vals[k])) for k in order]
     return "\n".join(lines) + "\n"
