@@ -111,6 +111,22 @@ def test_dropin_argument_checks_match_lace():
     assert rc == -1
 
 
+def test_new_entry_points_reject_null_arguments():
+    """The Gram-Schmidt FGMRES, the solve facts and the step timing answer
+    DEV_ERR_INVALID_PTR for missing arguments before any GPU work."""
+    L = lg.lib()
+    par = lg.GmresParam()
+    log = lg.GmresLog()
+    assert L.lace_gpu_fgmres_mgs(None, None, None, C.byref(par), 1, C.byref(log), None) == lg.DEV_ERR_INVALID_PTR
+    assert L.lace_gpu_get_solve_stats(None, None) == lg.DEV_ERR_INVALID_PTR
+    t = C.c_double()
+    assert L.lace_gpu_time_arnoldi_step(None, 0, 1, 1, C.byref(t)) == lg.DEV_ERR_INVALID_PTR
+    assert L.data_fgmres(None, None, None, None, None, None, None) == lg.DEV_ERR_INVALID_PTR
+    assert L.data_fgmres_restart(None, None, None, None, None, None, None) == lg.DEV_ERR_INVALID_PTR
+    assert L.read_z_csr_from_mtx(None, None, None, None, None, None, None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
+    assert L.data_z_csr_mtx(None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
+
+
 def test_error_strings():
     L = lg.lib()
     for code in (0, -101, -103, -104, -107, -113, -115, -116, -204, -205):
