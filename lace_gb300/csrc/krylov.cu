@@ -1085,8 +1085,9 @@ void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
 
 template <typename ZT, typename QT>
 static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
-  static int G = -1;
-  if (G < 0) {
+  // one block per SM when the kernel fits there with the largest shared
+  // memory (0: it does not); set once, thread-safely
+  static const int G = [] {
     int per_sm = 0;
     if (cudaFuncSetAttribute(k_hh_step<ZT, QT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHHSmemMax) !=
             cudaSuccess ||
@@ -1094,11 +1095,10 @@ static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, 
             cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
-      G = 0;
-    } else {
-      G = num_sms();
+      return 0;
     }
-  }
+    return num_sms();
+  }();
   if (G == 0) return 1;
   HHStep p;
   p.n = a.n;
@@ -1143,13 +1143,13 @@ void launch_xupdate(cudaStream_t s, const ArnoldiArgs &a, double *x) {
 }
 
 int num_sms() {
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
+  // the first device's count, set once (thread-safe static initialisation)
+  static const int sms = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 132;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 132;
+  }();
   return sms;
 }
 

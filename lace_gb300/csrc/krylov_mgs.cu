@@ -548,8 +548,9 @@ __global__ void __launch_bounds__(kStepTPB, 1) k_mgs_step(MgsStep a, int j) {
 
 template <typename ZT>
 static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
-  static int G = -1;
-  if (G < 0) {
+  // one block per SM when the kernel fits there with the largest shared
+  // memory (0: it does not); set once, thread-safely
+  static const int G = [] {
     int per_sm = 0;
     if (cudaFuncSetAttribute(k_mgs_step<ZT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStepSmemMax) !=
             cudaSuccess ||
@@ -557,11 +558,10 @@ static int mgs_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t,
             cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
-      G = 0;
-    } else {
-      G = num_sms();
+      return 0;
     }
-  }
+    return num_sms();
+  }();
   if (G == 0) return 1;
   MgsStep p;
   p.n = a.n;
