@@ -81,6 +81,18 @@ int main() {
     assert vals == lg.abi_layout()
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(ref.REF_SRC, "include")), reason="LACE tree not present")
+def test_header_compiles_next_to_lace_headers(tmp_path):
+    """A LACE caller includes both headers: every function both declare
+    (the drop-ins, the Matrix Market files) must be declared alike."""
+    src = tmp_path / "both.cpp"
+    src.write_text('#include "sparse.h"\n#include "lace_gb300.h"\nint main() { return 0; }\n')
+    r = subprocess.run(["g++", "-fsyntax-only", "-Werror", "-I", os.path.join(ref.REF_SRC, "include"), "-I",
+                        os.path.join(ROOT, "oracle", "mkl_shim"), "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
 def test_context_without_gpu_fails_loudly():
     import torch
     if torch.cuda.is_available():
