@@ -260,6 +260,12 @@ int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz,
                         dataType **val, int **row, int **col, const char *filename);
 int data_z_csr_mtx(data_d_matrix *A, const char *filename);
 int data_zwrite_csr_mtx(data_d_matrix A, data_order_t MajorType, const char *filename);
+/* Replace control/magma_zmio.cpp:353-557 and 957-967: the entries in file order
+ * (symmetric and hermitian files expanded; LACE returns freed arrays for
+ * those), *type set to Magma_CSR as LACE sets it. */
+int read_z_coo_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz,
+                        dataType **coo_val, int **coo_row, int **coo_col, const char *filename);
+int data_z_coo_mtx(data_d_matrix *A, const char *filename);
 
 /* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
  * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives

@@ -230,12 +230,10 @@ bool parse_entries(const char *p, const char *e, int nnz, int fields, bool patte
   return true;
 }
 
-}  // namespace
-
-extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz, dataType **val,
-                                   int **row, int **col, const char *filename) {
-  if (!type || !n_row || !n_col || !nnz || !val || !row || !col || !filename) return DEV_ERR_INVALID_PTR;
-  IoClock clk;
+// the file's entries in file order, symmetric and hermitian files expanded
+// entry by entry (the part both of LACE's readers share)
+int read_coo(const char *filename, int &M, int &N, std::vector<int> &cr, std::vector<int> &cc,
+             std::vector<double> &cv, IoClock &clk) {
   FILE *f = fopen(filename, "rb");
   if (!f) return DEV_ERR_NOT_FOUND;
   std::vector<char> buf;
@@ -261,15 +259,14 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
     le = (const char *)memchr(p, '\n', (size_t)(e - p));
     p = le ? le + 1 : e;
   }
-  int M = 0, N = 0, NZ = 0;
+  int NZ = 0;
+  M = N = 0;
   {
     const char *t0, *t1;
     if (!next_token(p, e, t0, t1) || !parse_int(t0, t1, M) || !next_token(p, e, t0, t1) || !parse_int(t0, t1, N) ||
         !next_token(p, e, t0, t1) || !parse_int(t0, t1, NZ) || M < 0 || N < 0 || NZ < 0)
       return DEV_ERR_UNKNOWN;
   }
-  std::vector<int> cr, cc;
-  std::vector<double> cv;
   const int fields = b.pattern ? 2 : (b.complex ? 4 : 3);
   if (!parse_entries(p, e, NZ, fields, b.pattern, cr, cc, cv)) return DEV_ERR_UNKNOWN;
   clk.mark("entries parsed");
@@ -302,8 +299,22 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
     cc.swap(nc);
     cv.swap(nv);
   }
-  const int nz = (int)total;
   clk.mark("checked, expanded");
+  return DEV_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz, dataType **val,
+                                   int **row, int **col, const char *filename) {
+  if (!type || !n_row || !n_col || !nnz || !val || !row || !col || !filename) return DEV_ERR_INVALID_PTR;
+  IoClock clk;
+  int M = 0, N = 0;
+  std::vector<int> cr, cc;
+  std::vector<double> cv;
+  const int rc = read_coo(filename, M, N, cr, cc, cv, clk);
+  if (rc) return rc;
+  const int nz = (int)cr.size();
   // CSR: rows in file order (the stable scatter of :276-313), then each row
   // sorted by column with std::sort on (column, value) pairs (:315-329)
   int *R = calloc64<int>((size_t)M + 1);
@@ -349,6 +360,47 @@ extern "C" int read_z_csr_from_mtx(data_storage_t *type, int *n_row, int *n_col,
   *col = C;
   *val = V;
   return DEV_SUCCESS;
+}
+
+// LACE's COO reader (control/magma_zmio.cpp:353-557): the entries in file
+// order.  LACE labels them Magma_CSR (:409) and, for symmetric files, hands
+// back arrays it has just freed (:527-533); here the expanded arrays are
+// returned, allocated like LACE_CALLOC.
+extern "C" int read_z_coo_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz, dataType **coo_val,
+                                   int **coo_row, int **coo_col, const char *filename) {
+  if (!type || !n_row || !n_col || !nnz || !coo_val || !coo_row || !coo_col || !filename) return DEV_ERR_INVALID_PTR;
+  IoClock clk;
+  int M = 0, N = 0;
+  std::vector<int> cr, cc;
+  std::vector<double> cv;
+  const int rc = read_coo(filename, M, N, cr, cc, cv, clk);
+  if (rc) return rc;
+  const size_t nz = cr.size();
+  int *R = calloc64<int>(nz), *C = calloc64<int>(nz);
+  double *V = calloc64<double>(nz);
+  if (!R || !C || !V) {
+    free(R);
+    free(C);
+    free(V);
+    return DEV_ERR_HOST_ALLOC;
+  }
+  memcpy(R, cr.data(), 4 * nz);
+  memcpy(C, cc.data(), 4 * nz);
+  memcpy(V, cv.data(), 8 * nz);
+  *type = Magma_CSR;
+  *n_row = M;
+  *n_col = N;
+  *nnz = (int)nz;
+  *coo_row = R;
+  *coo_col = C;
+  *coo_val = V;
+  return DEV_SUCCESS;
+}
+
+extern "C" int data_z_coo_mtx(data_d_matrix *A, const char *filename) {
+  if (!A) return DEV_ERR_INVALID_PTR;
+  data_storage_t st = Magma_COO;
+  return read_z_coo_from_mtx(&st, &A->num_rows, &A->num_cols, &A->nnz, &A->val, &A->row, &A->col, filename);
 }
 
 extern "C" int data_z_csr_mtx(data_d_matrix *A, const char *filename) {

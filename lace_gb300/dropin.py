@@ -244,17 +244,20 @@ def _fgmres_call(fn, A: Mat, b, x0, L, U, search_max, restart_max, rtol, tol_typ
                                                  "initial_residual", "final_residual")}
 
 
-def read_mtx(path: str):
-    """read_z_csr_from_mtx: (rc, n_rows, n_cols, row, col, val) as numpy
-    arrays (copies; the library's arrays are released)."""
+def read_mtx(path: str, coo: bool = False):
+    """read_z_csr_from_mtx (or read_z_coo_from_mtx): (rc, n_rows, n_cols,
+    row (pointers, or indices), col, val) as numpy arrays (copies; the
+    library's arrays are released)."""
     st, nr, nc, nz = C.c_int(), C.c_int(), C.c_int(), C.c_int()
     val, row, col = C.c_void_p(), C.c_void_p(), C.c_void_p()
-    rc = lib().read_z_csr_from_mtx(C.byref(st), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(val),
-                                   C.byref(row), C.byref(col), path.encode())
+    fn = lib().read_z_coo_from_mtx if coo else lib().read_z_csr_from_mtx
+    rc = fn(C.byref(st), C.byref(nr), C.byref(nc), C.byref(nz), C.byref(val), C.byref(row), C.byref(col),
+            path.encode())
     if rc != 0:
         return rc, 0, 0, None, None, None
     n, z = nr.value, nz.value
-    r = np.ctypeslib.as_array(C.cast(row, C.POINTER(C.c_int)), shape=(n + 1,)).copy()
+    nrow = max(z, 1) if coo else n + 1
+    r = np.ctypeslib.as_array(C.cast(row, C.POINTER(C.c_int)), shape=(nrow,))[:(z if coo else n + 1)].copy()
     c = np.ctypeslib.as_array(C.cast(col, C.POINTER(C.c_int)), shape=(max(z, 1),))[:z].copy()
     v = np.ctypeslib.as_array(C.cast(val, C.POINTER(C.c_double)), shape=(max(z, 1),))[:z].copy()
     libc = C.CDLL(None)

@@ -156,6 +156,24 @@ data_d_matrix *ref_read_csr_mtx(const char *filename, int *info) {
   return A;
 }
 
+/* LACE's COO reader (:353) for non-symmetric files (it returns freed arrays
+ * for symmetric ones): copies into caller-sized buffers, then releases */
+int ref_read_coo_mtx(const char *filename, int *dims3, int cap, int *row, int *col, double *val) {
+  data_storage_t st = Magma_COO;
+  int *r = NULL, *c = NULL;
+  double *v = NULL;
+  int info = read_z_coo_from_mtx(&st, &dims3[0], &dims3[1], &dims3[2], &v, &r, &c, filename);
+  if (info == 0 && dims3[2] <= cap) {
+    memcpy(row, r, sizeof(int) * (size_t)dims3[2]);
+    memcpy(col, c, sizeof(int) * (size_t)dims3[2]);
+    memcpy(val, v, sizeof(double) * (size_t)dims3[2]);
+  }
+  free(r);
+  free(c);
+  free(v);
+  return info;
+}
+
 int ref_write_csr_mtx(data_d_matrix *A, int major, const char *filename) {
   return data_zwrite_csr_mtx(*A, (data_order_t)major, filename);
 }

@@ -71,6 +71,7 @@ def _load(path: str) -> C.CDLL:
             L.ref_read_csr_mtx.restype = vp
             L.ref_read_csr_mtx.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
             L.ref_write_csr_mtx.argtypes = [vp, C.c_int, C.c_char_p]
+            L.ref_read_coo_mtx.argtypes = [C.c_char_p, vp, C.c_int, vp, vp, vp]
         else:
             L.ref_bcsr_parilu.argtypes = [vp, C.c_double, C.POINTER(vp), C.POINTER(vp), vp]
             L.ref_dense_inverse.argtypes = [C.c_int, vp, vp]
@@ -262,6 +263,18 @@ def read_csr_mtx(path: str):
     d = M.info()
     r, c, v = M.arrays()
     return info.value, d["nrows"], d["ncols"], r.copy(), c.copy(), v.copy()
+
+
+def read_coo_mtx(path: str, cap: int = 1 << 22):
+    """LACE's own read_z_coo_from_mtx (non-symmetric files):
+    (info, n_rows, n_cols, row, col, val)."""
+    dims = np.zeros(3, dtype=np.int32)
+    r = np.zeros(cap, dtype=np.int32)
+    c = np.zeros(cap, dtype=np.int32)
+    v = np.zeros(cap)
+    info = lib().ref_read_coo_mtx(path.encode(), _p(dims), cap, _p(r), _p(c), _p(v))
+    z = int(dims[2])
+    return info, int(dims[0]), int(dims[1]), r[:z].copy(), c[:z].copy(), v[:z].copy()
 
 
 def write_csr_mtx(A: Mat, path: str, major: int = 101) -> int:

@@ -258,6 +258,10 @@ def main():
         if info != 0:
             continue
         g[f"mtx_{name}_read"] = np.array([MC.digest_arrays(nr, nc, r, c, v)])
+        if "symmetric" not in text.split("\n", 1)[0].lower() and "hermitian" not in text.split("\n", 1)[0].lower():
+            with CaptureStdout():
+                ci, cnr, cnc, crr, ccc, cvv = ref.read_coo_mtx(fn)
+            g[f"mtx_{name}_coo"] = np.array([MC.digest_arrays(cnr, cnc, crr, ccc, cvv)])
         Am = ref.Mat.from_arrays(ref.Magma_CSR, nr, nc, r, c, v)
         for major in ((101, 102) if nr == nc else (101,)):  # LACE's transpose asserts on non-square input
             out = fn + ".%d" % major

@@ -137,6 +137,8 @@ def test_new_entry_points_reject_null_arguments():
     assert L.data_fgmres_restart(None, None, None, None, None, None, None) == lg.DEV_ERR_INVALID_PTR
     assert L.read_z_csr_from_mtx(None, None, None, None, None, None, None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
     assert L.data_z_csr_mtx(None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
+    assert L.read_z_coo_from_mtx(None, None, None, None, None, None, None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
+    assert L.data_z_coo_mtx(None, b"x.mtx") == lg.DEV_ERR_INVALID_PTR
 
 
 def test_error_strings():

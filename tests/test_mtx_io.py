@@ -40,6 +40,26 @@ def test_read_equals_lace(tmp_path, name):
 
 
 @pytest.mark.parametrize("name", sorted(set(CASES) - MC.REJECTED))
+def test_coo_read_equals_lace(tmp_path, name):
+    """read_z_coo_from_mtx: the entries in file order as LACE reads them
+    (symmetric files: LACE returns freed arrays; here the expansion, which
+    must equal the CSR reader's entries before the row fill)."""
+    fn = _file(tmp_path, name, CASES[name])
+    rc, nr, nc, r, c, v = dropin.read_mtx(fn, coo=True)
+    assert rc == 0
+    key = f"mtx_{name}_coo"
+    if key in G.files:
+        assert MC.digest_arrays(nr, nc, r, c, v) == str(G[key][0])
+    # the CSR reader's arrays are these entries stably bucketed by row, each
+    # row then sorted by column
+    rc2, nr2, nc2, rp, ci, cv = dropin.read_mtx(fn)
+    order = np.argsort(r, kind="stable")
+    assert np.array_equal(np.diff(rp), np.bincount(r, minlength=nr))
+    assert sorted(zip(r[order].tolist(), c[order].tolist())) == sorted(
+        zip(np.repeat(np.arange(nr), np.diff(rp)).tolist(), ci.tolist()))
+
+
+@pytest.mark.parametrize("name", sorted(set(CASES) - MC.REJECTED))
 @pytest.mark.parametrize("major", [101, 102])
 def test_write_equals_lace(tmp_path, name, major):
     """data_zwrite_csr_mtx writes LACE's bytes, row- and column-major."""
@@ -68,6 +88,8 @@ def test_large_file_parallel_paths(tmp_path):
     buffers, still LACE's arrays and bytes; then read back what was written."""
     fn = _file(tmp_path, "large", MC.large_text())
     rc, nr, nc, r, c, v = _read_and_check(fn, "large")
+    rcc, cnr, cnc, cr, cc, cv = dropin.read_mtx(fn, coo=True)
+    assert rcc == 0 and MC.digest_arrays(cnr, cnc, cr, cc, cv) == str(G["mtx_large_coo"][0])
     A = dropin.csr(r, c, v, nr)
     for major in (101, 102):
         out = str(tmp_path / ("w%d.mtx" % major))
@@ -81,6 +103,7 @@ def test_large_file_parallel_paths(tmp_path):
 
 def test_missing_file():
     assert dropin.read_mtx("/nonexistent/dir/none.mtx")[0] == DEV_ERR_NOT_FOUND
+    assert dropin.read_mtx("/nonexistent/dir/none.mtx", coo=True)[0] == DEV_ERR_NOT_FOUND
 
 
 needs_ref = pytest.mark.skipif(not ref.available(), reason="LACE source tree not present")
@@ -105,3 +128,8 @@ def test_live_lace_reader_on_random_files(tmp_path):
         assert ours[0] == theirs[0] == 0
         for a, b in zip(ours[3:], theirs[3:]):
             assert np.array_equal(a, b)
+        if k != 1:  # LACE's COO reader returns released arrays for symmetric files
+            ours, theirs = dropin.read_mtx(fn, coo=True), ref.read_coo_mtx(fn)
+            assert ours[0] == theirs[0] == 0 and ours[1:3] == theirs[1:3]
+            for a, b in zip(ours[3:], theirs[3:]):
+                assert np.array_equal(a, b)
