@@ -267,6 +267,19 @@ int read_z_coo_from_mtx(data_storage_t *type, int *n_row, int *n_col, int *nnz,
                         dataType **coo_val, int **coo_row, int **coo_col, const char *filename);
 int data_z_coo_mtx(data_d_matrix *A, const char *filename);
 
+/* The setup conversions, on host threads, with LACE's results:
+ * data_zmconvert (control/magma_zmconverter.cpp:199) for CSR, CSRL or CSRU
+ * sources to CSR, CUCSR, CSRL, CSRU, COO, CSRCOO, CSC, CSCL, CSCU, CSCCOO and
+ * BCSR (B->blocksize set), and BCSR to BCSRL, BCSRU, BCSCU; B->diagorder_type
+ * selects the diagonal of a split as in LACE.  Other pairs return
+ * DEV_ERR_NOT_SUPPORTED with B untouched.  data_zmtranspose
+ * (control/magma_zmtranspose.cpp:484) and data_rowindex
+ * (control/magma_zmconverter.cpp:145).  Output arrays are posix_memalign(64)
+ * and zeroed, so data_zmfree releases them. */
+int data_zmconvert(data_d_matrix A, data_d_matrix *B, data_storage_t old_format, data_storage_t new_format);
+int data_zmtranspose(data_d_matrix A, data_d_matrix *B);
+int data_rowindex(data_d_matrix *A, int **rowidx);
+
 /* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
  * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives
  * the same value (the fill-in part of LACE's res is not formed) and LU is

@@ -163,6 +163,9 @@ SIGNATURES = {
     "read_z_coo_from_mtx": (_i, [C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_p),
                                  C.POINTER(_p), C.POINTER(_p), C.c_char_p]),
     "data_z_coo_mtx": (_i, [_DM, C.c_char_p]),
+    "data_zmconvert": (_i, [DataMatrix, _DM, _i, _i]),
+    "data_zmtranspose": (_i, [DataMatrix, _DM]),
+    "data_rowindex": (_i, [_DM, C.POINTER(_p)]),
     "data_zwrite_csr_mtx": (_i, [DataMatrix, _i, C.c_char_p]),
     "lace_gpu_default_options": (None, [C.POINTER(GpuOptions)]),
     "lace_gpu_dropin_set_options": (_i, [C.POINTER(GpuOptions)]),

@@ -86,6 +86,16 @@ data_d_matrix *ref_convert(const data_d_matrix *A, int old_format,
   return B;
 }
 
+/* the same with B->blocksize preset (CSR -> BCSR reads it) */
+data_d_matrix *ref_convert_bs(const data_d_matrix *A, int old_format,
+                              int new_format, int diagorder, int blocksize) {
+  data_d_matrix *B = (data_d_matrix *)calloc(1, sizeof(data_d_matrix));
+  B->diagorder_type = (data_diagorder_t)diagorder;
+  B->blocksize = blocksize;
+  data_zmconvert(*A, B, (data_storage_t)old_format, (data_storage_t)new_format);
+  return B;
+}
+
 data_d_matrix *ref_transpose(const data_d_matrix *A) {
   data_d_matrix *B = (data_d_matrix *)calloc(1, sizeof(data_d_matrix));
   data_zmtranspose(*A, B);

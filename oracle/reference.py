@@ -53,6 +53,8 @@ def _load(path: str) -> C.CDLL:
         L.ref_mat_free.argtypes = [vp]
         L.ref_convert.restype = vp
         L.ref_convert.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.ref_convert_bs.restype = vp
+        L.ref_convert_bs.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.ref_transpose.restype = vp
         L.ref_transpose.argtypes = [vp]
         if path == LIB:
@@ -149,6 +151,11 @@ def set_storage(A: Mat, storage: int) -> None:
 
 def convert(A: Mat, old, new, diagorder=0) -> Mat:
     return Mat(A.L.ref_convert(A.h, old, new, diagorder), A.L)
+
+
+def transpose(A: Mat) -> Mat:
+    """LACE's data_zmtranspose into a fresh matrix."""
+    return Mat(A.L.ref_transpose(A.h), A.L)
 
 
 def parilu(A: Mat, reduction: float, max_sweeps: int = -1):

@@ -268,6 +268,13 @@ def main():
             with CaptureStdout():
                 ref.write_csr_mtx(Am, out, major)
             g[f"mtx_{name}_write{major}"] = np.array([MC.digest_file(out)])
+    # ------------------------ setup conversions (LACE's data_zmconvert etc.)
+    # digests of every field and array of LACE's output for each job
+    import convert_cases as CC
+    from test_convert import run_lace
+    for key, *_ in CC.jobs():
+        with CaptureStdout():
+            g[key] = np.array([CC.digest(run_lace(key))])
     n, r, c, v = MC.write_values_matrix()
     Am = ref.Mat.from_arrays(ref.Magma_CSR, n, n, r, c, v)
     for major in (101, 102):
