@@ -270,7 +270,7 @@ int data_z_coo_mtx(data_d_matrix *A, const char *filename);
 /* The setup conversions, on host threads, with LACE's results:
  * data_zmconvert (control/magma_zmconverter.cpp:199) for CSR, CSRL or CSRU
  * sources to CSR, CUCSR, CSRL, CSRU, COO, CSRCOO, CSC, CSCL, CSCU, CSCCOO and
- * BCSR (B->blocksize set), and BCSR to BCSRL, BCSRU, BCSCU; B->diagorder_type
+ * BCSR (B->blocksize set), COO to CSR, and BCSR to BCSRL, BCSRU, BCSCU; B->diagorder_type
  * selects the diagonal of a split as in LACE.  Other pairs return
  * DEV_ERR_NOT_SUPPORTED with B untouched.  data_zmtranspose
  * (control/magma_zmtranspose.cpp:484) and data_rowindex

@@ -1,6 +1,6 @@
 // The setup conversions a LACE caller runs before the solve, on host threads:
 // data_zmconvert (control/magma_zmconverter.cpp:199-1601) for the storage
-// changes the factorisation path uses, data_zmtranspose
+// changes the factorisation path uses and COO -> CSR, data_zmtranspose
 // (control/magma_zmtranspose.cpp:85-515) and data_rowindex
 // (control/magma_zmconverter.cpp:145-167).
 //
@@ -397,6 +397,52 @@ int to_bcsr(const data_d_matrix &A, data_d_matrix *B) {
   return DEV_SUCCESS;
 }
 
+// COO -> CSR (:853-926): entries scattered to their rows in input order,
+// then each row sorted by column with std::sort on (column, value) pairs
+// (LACE's compare_first, the same call); storage_type and fill_mode are left
+// as they were, as LACE leaves them
+int coo_to_csr(const data_d_matrix &A, data_d_matrix *B) {
+  const int R = row_limit(A);
+  const int nz = std::max(A.nnz, 0);
+  B->nnz = A.nnz;
+  B->true_nnz = A.true_nnz;
+  B->num_rows = A.num_rows;
+  B->num_cols = A.num_cols;
+  B->pad_rows = A.pad_rows;
+  B->pad_cols = A.pad_cols;
+  B->major = MagmaRowMajor;
+  B->val = calloc64<double>((size_t)nz);
+  B->row = calloc64<int>((size_t)R + 1);
+  B->col = calloc64<int>((size_t)nz);
+  if (!B->val || !B->row || !B->col) return DEV_ERR_HOST_ALLOC;
+  std::vector<int> cnt((size_t)R, 0);
+  for (int k = 0; k < nz; ++k) ++cnt[A.row[k]];
+  prefix(cnt, B->row, (size_t)R);
+  B->row[R] = A.nnz;
+  std::vector<int> next(B->row, B->row + R);
+  for (int k = 0; k < nz; ++k) {
+    const int o = next[A.row[k]]++;
+    B->col[o] = A.col[k];
+    B->val[o] = A.val[k];
+  }
+  par_for((size_t)R, 1 << 12, [&](size_t b, size_t e) {
+    std::vector<std::pair<int, double>> rv;
+    for (size_t i = b; i < e; ++i) {
+      const int k0 = B->row[i], len = B->row[i + 1] - k0;
+      if (len < 2) continue;
+      rv.resize((size_t)len);
+      for (int q = 0; q < len; ++q) rv[q] = std::make_pair(B->col[k0 + q], B->val[k0 + q]);
+      std::sort(rv.begin(), rv.end(),
+                [](const std::pair<int, double> &x, const std::pair<int, double> &y) { return x.first < y.first; });
+      for (int q = 0; q < len; ++q) {
+        B->col[k0 + q] = rv[q].first;
+        B->val[k0 + q] = rv[q].second;
+      }
+    }
+  });
+  return DEV_SUCCESS;
+}
+
 bool csr_family(data_storage_t s) {
   return s == Magma_CSR || s == Magma_CSRD || s == Magma_CSRL || s == Magma_CSRU || s == Magma_CSRCOO ||
          s == Magma_CSCD || s == Magma_CSCL || s == Magma_CSCU || s == Magma_CSCCOO;
@@ -436,7 +482,16 @@ extern "C" int data_zmconvert(data_d_matrix A, data_d_matrix *B, data_storage_t 
                           new_format == Magma_CSCCOO || new_format == Magma_BCSR;
   const bool from_bcsr = old_format == Magma_BCSR && (new_format == Magma_BCSRL || new_format == Magma_BCSRU ||
                                                       new_format == Magma_BCSCU);
-  if (!(from_csr && csr_target) && !from_bcsr) return DEV_ERR_NOT_SUPPORTED;
+  const bool from_coo = old_format == Magma_COO && new_format == Magma_CSR;
+  if (!(from_csr && csr_target) && !from_bcsr && !from_coo) return DEV_ERR_NOT_SUPPORTED;
+  if (from_coo) {
+    // an entry outside the rows: an error, not LACE's write out of bounds
+    const int Rc = row_limit(A);
+    for (int k = 0; k < A.nnz; ++k)
+      if (A.row[k] < 0 || A.row[k] >= Rc) return DEV_ERR_ILLEGAL_VALUE;
+    release(B);
+    return coo_to_csr(A, B);
+  }
   if (from_csr && new_format == Magma_BCSR && B->blocksize <= 0) return DEV_ERR_NOT_SUPPORTED;
   release(B);
   const int R = row_limit(A);

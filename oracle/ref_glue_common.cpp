@@ -44,6 +44,25 @@ data_d_matrix *ref_mat_new(int storage, int nrows, int ncols, int nnz,
   return A;
 }
 
+/* COO handle: row, col and val each nnz long */
+data_d_matrix *ref_coo_new(int nrows, int ncols, int nnz, const int *row,
+                           const int *col, const double *val) {
+  data_d_matrix *A = (data_d_matrix *)calloc(1, sizeof(data_d_matrix));
+  A->storage_type = Magma_COO;
+  A->num_rows = nrows;
+  A->num_cols = ncols;
+  A->fill_mode = MagmaFull;
+  A->major = MagmaRowMajor;
+  A->nnz = A->true_nnz = nnz;
+  LACE_CALLOC(A->row, (nnz > 0 ? nnz : 1));
+  LACE_CALLOC(A->col, (nnz > 0 ? nnz : 1));
+  LACE_CALLOC(A->val, (nnz > 0 ? nnz : 1));
+  memcpy(A->row, row, sizeof(int) * (size_t)nnz);
+  memcpy(A->col, col, sizeof(int) * (size_t)nnz);
+  memcpy(A->val, val, sizeof(double) * (size_t)nnz);
+  return A;
+}
+
 /* dense column vector handle (n x 1, Magma_DENSE) */
 data_d_matrix *ref_vec_new(int n, const double *v) {
   data_d_matrix *x = (data_d_matrix *)calloc(1, sizeof(data_d_matrix));

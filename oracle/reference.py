@@ -55,6 +55,8 @@ def _load(path: str) -> C.CDLL:
         L.ref_convert.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.ref_convert_bs.restype = vp
         L.ref_convert_bs.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.ref_coo_new.restype = vp
+        L.ref_coo_new.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
         L.ref_transpose.restype = vp
         L.ref_transpose.argtypes = [vp]
         if path == LIB:

@@ -81,6 +81,8 @@ def jobs():
             out.append((f"conv_blocks_{new}_{d}", "blocks", BCSR, new, d, 0))
     out.append(("conv_blocks_t", "blocks", BCSR, None, 0, 0))
     out.append(("conv_onebased_square_t", "onebased:square", CSR, None, 0, 0))
+    for name in ("square", "empty_rows", "large"):
+        out.append((f"conv_coo_{name}", "coo:" + name, COO, CSR, 0, 0))
     # LACE's CSRL with the default diagonal order, transposed again
     out.append(("conv_square_csrl0_t", "csrl0:square", CSRL, None, 0, 0))
     return out
@@ -95,6 +97,18 @@ def job_input(spec):
     if spec.startswith("onebased:"):
         n, m, r, c, v = matrices()[spec.split(":")[1]]
         return CSR, n, m, r + 1, c + 1, v, 0
+    if spec.startswith("coo:"):
+        # the entries in a shuffled order, a tenth of them repeated (equal
+        # columns in a row: the sort's own order decides between them)
+        n, m, r, c, v = matrices()[spec.split(":")[1]]
+        rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(r))
+        rng = np.random.default_rng(n)
+        dup = rng.choice(len(c), len(c) // 10, replace=False)
+        rows = np.concatenate([rows, rows[dup]])
+        cols = np.concatenate([c, c[dup]])
+        vals = np.concatenate([v, v[dup] + 0.5])
+        order = rng.permutation(len(cols))
+        return COO, n, m, rows[order], cols[order], vals[order], 0
     if spec.startswith("csrl0:"):
         # rows with their diagonal dropped and nnz counting it (LACE's CSRL
         # under diagorder 0): the tail holds zero entries in column 0

@@ -62,7 +62,12 @@ def run_ours(key):
 def run_lace(key):
     _, spec, old, new, d, bs = JOBS[key]
     st, n, m, r, c, v, bsi = CC.job_input(spec)
-    A = ref.Mat.from_arrays(st, n, m, r, c, v, blocksize=bsi)
+    if st == CC.COO:
+        L = ref.lib()
+        r, c, v = (np.ascontiguousarray(x, dtype=t) for x, t in ((r, np.int32), (c, np.int32), (v, np.float64)))
+        A = ref.Mat(L.ref_coo_new(n, m, len(c), r.ctypes.data, c.ctypes.data, v.ctypes.data), L)
+    else:
+        A = ref.Mat.from_arrays(st, n, m, r, c, v, blocksize=bsi)
     if spec.startswith("csrl0:"):
         C.cast(A.h, C.POINTER(lg.DataMatrix))[0].nnz = len(c)
     if new is None:
