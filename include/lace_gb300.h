@@ -185,11 +185,17 @@ void data_PariLU_v0_3_gpu_prescribedSweeps(data_d_matrix *A, data_d_matrix *L,
                                            data_d_matrix *U, dataType reduction,
                                            data_d_preconditioner_log *log);
 
-/* Replaces src/trisolve.cpp:256.  Triangular sweeps until
- * sum (y_new - y_old)^2 <= tol or a non-finite step (GPU: synchronous
- * Jacobi sweeps).  uplo MagmaLower needs storage Magma_CSRL (diagonal last),
- * MagmaUpper needs Magma_CSRU (diagonal first); otherwise returns -1 as
- * LACE does.  Host arrays. */
+/* Replaces src/trisolve.cpp:256.  LACE's in-place sweeps in LACE's order
+ * (L rows from the first, U rows from the last; each row's off-diagonal
+ * products summed in storage order, then divided by the stored diagonal)
+ * until sum (y_new - y_old)^2 <= tol or a non-finite step; the iterate and
+ * *iter equal LACE's one-thread run bit for bit.  uplo MagmaLower needs
+ * storage Magma_CSRL (diagonal last), MagmaUpper needs Magma_CSRU (diagonal
+ * first); otherwise returns -1 as LACE does.  A column outside the matrix or
+ * a diagonal position outside the arrays (where LACE would read outside
+ * them) returns DEV_ERR_ILLEGAL_VALUE.  LACE loops forever for a negative
+ * tol; here the loop also ends at a sweep that changes nothing.  Host
+ * arrays. */
 int data_parcsrtrsv(const data_uplo_t uplo, const data_storage_t storage,
                     const data_diagorder_t diag, const int num_rows,
                     const dataType *Aval, const int *row, const int *col,
@@ -205,7 +211,9 @@ int data_z_spmv(dataType alpha, data_d_matrix *A, data_d_matrix *x,
  * restarted FGMRES with Householder Arnoldi; preconditioner M = L*U given as
  * L (Magma_CSRL) and U (Magma_CSRU, or Magma_CSCU as ParILU returns it).
  * gmres_par->user_csrtrsv_choice: 0 exact triangular solves (sync-free
- * SpTRSV), 1 Jacobi ParCSRTRSV sweeps with tol 1.0, 2 no preconditioner.
+ * SpTRSV), 1 ParCSRTRSV with tol 1.0 (in LACE's sweep order the first sweep
+ * is the exact substitution and the second changes nothing, so the
+ * preconditioned vectors are the exact solves'), 2 no preconditioner.
  * x0 is overwritten with the solution (LACE frees and re-allocates
  * x0->val; this replacement writes into the existing array).  Returns
  * DEV_SUCCESS when the residual target was reached, DEV_NOTCONVERGED
@@ -300,7 +308,8 @@ enum { LACE_PREC_FP64 = 0, LACE_PREC_FP32 = 1, LACE_PREC_BF16_STORE = 2 };
 enum {
   LACE_TRSV_SYNCFREE = 0, /* exact, sync-free (ready flags per row chunk) */
   LACE_TRSV_LEVELS = 1,   /* exact, level-scheduled                       */
-  LACE_TRSV_JACOBI = 2,   /* ParCSRTRSV: synchronous Jacobi sweeps        */
+  LACE_TRSV_JACOBI = 2,   /* synchronous Jacobi sweeps (not LACE's order: */
+                          /* inexact; jacobi_sweeps / jacobi_tol)         */
   LACE_TRSV_NONE = 3      /* identity                                     */
 };
 
@@ -354,7 +363,9 @@ int lace_gpu_update_values_device(lace_gpu_ctx *ctx, const double *val);
 
 /* ParILU(0): `sweeps` synchronous sweeps from the A-initial guess.
  * step_out (may be NULL): step of the last sweep, normalised by ||A||_F.
- * nonlinres_out (may be NULL): ||(A-LU)|_S||_F / ||A||_F after the sweeps. */
+ * nonlinres_out (may be NULL): ||(A-LU)|_S||_F / ||A||_F after the sweeps.
+ * Returns DEV_ERR_BADPRECOND when the last step is not finite (a zero or
+ * non-finite pivot); the factors are then left as the sweeps made them. */
 int lace_gpu_parilu0(lace_gpu_ctx *ctx, int sweeps, double *step_out,
                      double *nonlinres_out);
 
@@ -387,21 +398,45 @@ int lace_gpu_precond_enqueue(lace_gpu_ctx *ctx, const void *q, void *z);
  * whose device memory belongs to its own pool or arena, which forbids further
  * allocations, and code in a latency-critical loop, where cudaMalloc/cudaFree
  * would synchronise the whole device.  Same arguments, rule for uplo /
- * storage / diag, sweeps and result as data_parcsrtrsv, but Aval, row, col,
- * rhsval and yval (start vector in, solution out) are device pointers, and
- * the sweeps run on `stream` (NULL: the default stream); the call returns
- * when the solve is done.  Its scratch is one fixed device array (about
- * 2 MB, held by every GPU that loads the library): num_rows above
- * LACE_GPU_NOALLOC_MAX_ROWS returns DEV_ERR_NOT_SUPPORTED.  The first call on
- * a device sets the scratch up (looks up its address and clears its counter)
- * and should come before any stream capture.  Every call uses the same
- * scratch: calls that overlap on the GPU (from several threads or streams)
- * race and give wrong results. */
+ * storage / diag, sweeps and result as data_parcsrtrsv (LACE's sweep order,
+ * bit for bit), but Aval, row, col, rhsval and yval (start vector in,
+ * solution out) are device pointers, and the sweeps run on `stream` (NULL:
+ * the default stream), which must belong to the current device
+ * (DEV_ERR_ILLEGAL_VALUE otherwise); the call returns when the solve is done,
+ * after one host synchronisation per two sweeps.  Its scratch is one fixed
+ * device array (about 2 MB, held by every GPU that loads the library):
+ * num_rows above LACE_GPU_NOALLOC_MAX_ROWS returns DEV_ERR_NOT_SUPPORTED.
+ * The first call on a device looks the scratch's address up and should come
+ * before any stream capture.  Every call clears the scratch's counters
+ * itself, but all calls use the same scratch: calls that overlap on the GPU
+ * (from several threads or streams) race and give wrong results. */
 int lace_gpu_parcsrtrsv_noalloc(const data_uplo_t uplo, const data_storage_t storage,
                                 const data_diagorder_t diag, const int num_rows,
                                 const dataType *Aval, const int *row, const int *col,
                                 const dataType *rhsval, dataType *yval, const dataType tol,
                                 int *iter, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Failure handling (no counterpart in LACE, which exits or returns codes)
+ * ---------------------------------------------------------------------- */
+
+/* Self-test of the bounded device waits.  Runs data_parcsrtrsv's sweep
+ * kernel on a built-in 4096-row bidiagonal triangle with its first row group
+ * withheld (its ticket is never handed out), so the rows after it wait for
+ * values nothing writes; each wait gives up after max_polls polls (<= 0: the
+ * library's limit, about a second), sets a status bit and returns, which the
+ * host reads into *status_out (may be NULL; bit 1 = a wait gave up).  Then
+ * the same sweep runs with every row group on the same device (with the
+ * library's own limit).  Returns
+ * DEV_SUCCESS when the first sweep reported the timeout and the second is
+ * the exact substitution with no status bit (the device stayed usable). */
+int lace_gpu_selftest_wait_limit(int max_polls, int *status_out);
+
+/* Fault injection for the host side: the next `after` device allocations of
+ * the library succeed and every one after them fails as if cudaMalloc had
+ * (the call that needed it returns DEV_ERR_DEVICE_ALLOC); after < 0 turns
+ * the injection off.  Process-wide. */
+void lace_gpu_inject_alloc_failure(int after);
 
 /* one triangle: which 0 = L (unit lower), 1 = U (upper), 2 = U^T (lower),
  * 3 = L^T (unit upper); device FP64 in/out (converted internally) */

@@ -116,10 +116,14 @@ class Context:
         _chk(self._lib.lace_gpu_update_values_device(self.h, _ptr(val)), "update_values")
 
     # ------------------------------------------------------------ kernels
-    def parilu0(self, sweeps: int) -> tuple[float, float]:
+    def parilu0(self, sweeps: int, residual: bool = True) -> tuple[float, float]:
+        """`sweeps` synchronous sweeps; returns (last normalised step,
+        ||(A-LU)|_S||_F/||A||_F), the residual only when asked for (it is one
+        more kernel over A's pattern; NaN otherwise)."""
         step = C.c_double()
-        nl = C.c_double()
-        _chk(self._lib.lace_gpu_parilu0(self.h, int(sweeps), C.byref(step), C.byref(nl)), "parilu0")
+        nl = C.c_double(float("nan"))
+        _chk(self._lib.lace_gpu_parilu0(self.h, int(sweeps), C.byref(step), C.byref(nl) if residual else None),
+             "parilu0")
         return step.value, nl.value
 
     def spmv(self, x, y, alpha: float = 1.0, beta: float = 0.0) -> None:

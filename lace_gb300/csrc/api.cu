@@ -339,42 +339,34 @@ extern "C" int data_parcsrtrsv(const data_uplo_t uplo, const data_storage_t stor
   else if (storage == Magma_CSRU && uplo == MagmaUpper && diag != Magma_NODIAG) lower = false;
   else if (storage == Magma_CSRU || uplo == MagmaUpper) return -1;
   else return 0;
+  if (!iter) return set_err(DEV_ERR_INVALID_PTR);
+  *iter = 0;
+  if (num_rows <= 0) return 0;
+  if (!Aval || !row || !col || !rhsval || !yval) return set_err(DEV_ERR_INVALID_PTR);
   std::lock_guard<std::mutex> lk(g_mu);
   lace_gpu_ctx *c = nullptr;
   int rc = default_ctx(&c);
   if (rc) return set_err(rc);
   const int n = num_rows;
   const int nnz = row[n];
-  DBuf drow, dcol, dval, drhs, y0, y1;
+  if (nnz < 0) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  DBuf drow, dcol, dval, drhs, dy, da;
   if (drow.upload(row, 4 * (size_t)(n + 1), c->stream) || dcol.upload(col, 4 * (size_t)nnz, c->stream) ||
       dval.upload(Aval, 8 * (size_t)nnz, c->stream) || upload_vec(drhs, rhsval, n, c->stream) ||
-      upload_vec(y0, yval, n, c->stream) || y1.ensure(8 * (size_t)n))
+      upload_vec(dy, yval, n, c->stream) || da.ensure(8 * (size_t)n))
     return set_err(DEV_ERR_DEVICE_ALLOC);
-  TriDev t;
-  t.n = n;
-  t.nnz = nnz;
-  t.row = (const int *)drow.p;
-  t.col = (const int *)dcol.p;
-  t.val = dval.p;
-  t.lower = lower ? 1 : 0;
-  t.unit = 0;  // LACE divides by the stored diagonal (last / first in the row)
-  double *partials = (double *)c->part_ensure();
-  if (!partials) return set_err(DEV_ERR_DEVICE_ALLOC);
-  void *cur = y0.p, *nxt = y1.p;
-  double step = 1.e8;
-  *iter = 0;
-  // Jacobi sweeps converge in at most (number of levels) sweeps; bound the loop
-  const int cap = n + 2;
-  while (step > tol && std::isfinite(step) && *iter < cap) {
-    launch_jacobi_sweep(c->stream, t, VType::F64, drhs.p, 0, cur, nxt, 0, nullptr, false);
-    launch_sqdiff(c->stream, n, nxt, cur, 0, partials, (int *)c->cnt_buf.p + 9, (double *)c->scal_buf.p + 9);
-    cudaMemcpyAsync(c->h_scal + 9, (double *)c->scal_buf.p + 9, 8, cudaMemcpyDeviceToHost, c->stream);
-    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
-    step = c->h_scal[9];
-    std::swap(cur, nxt);
-    *iter = *iter + 1;
-  }
-  if (cudaMemcpy(yval, cur, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
+  PartrsvScratch sc;
+  sc.a = (double *)da.p;
+  sc.partials = (double *)c->part_ensure();
+  if (!sc.partials) return set_err(DEV_ERR_DEVICE_ALLOC);
+  sc.counters = (int *)c->cnt_buf.p + 16;
+  sc.steps = (double *)c->scal_buf.p + 48;
+  sc.h_steps = c->h_scal + 48;
+  sc.h_status = (int *)(c->h_scal + 50);
+  rc = partrsv_solve(c->stream, lower, n, (const int *)drow.p, (const int *)dcol.p, (const double *)dval.p,
+                     (const double *)drhs.p, (double *)dy.p, tol, iter, sc);
+  if (rc) return set_err(rc);
+  if (cudaMemcpy(yval, dy.p, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
   return 0;
 }
 
@@ -453,9 +445,12 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
   if (rc) return set_err(rc);
   lace_gpu_options o = dropin_opts();
   o.monitor_orthog = par->monitorOrthog == 1;
+  // choice 1 (data_parcsrtrsv with tol 1.0, fgmres_householder_restart.cpp:
+  // 333-344) sweeps in LACE's order, where the first sweep is the exact
+  // substitution and the second changes nothing: its preconditioned vector is
+  // the exact solve's, which the sync-free solves give (choice 0)
   const int choice = par->user_csrtrsv_choice;
-  if (choice == 1) o.trsv_mode = LACE_TRSV_JACOBI;
-  else if (choice == 2) o.trsv_mode = LACE_TRSV_NONE;
+  if (choice == 2) o.trsv_mode = LACE_TRSV_NONE;
   else if (o.trsv_mode != LACE_TRSV_LEVELS) o.trsv_mode = LACE_TRSV_SYNCFREE;
   lace_gpu_set_options(c, &o);
   PhaseClock pc(c->verbose, "fgmres");

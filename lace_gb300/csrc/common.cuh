@@ -13,6 +13,9 @@ constexpr int kWarp = 32;
 constexpr int kStatusSpinTimeout = 1;
 // Bit set when a kernel met a non-finite value it must not divide by.
 constexpr int kStatusBreakdown = 2;
+// Bit set when a kernel met an index it must not follow (a column outside the
+// matrix, a diagonal entry outside the value array).
+constexpr int kStatusBadInput = 4;
 // Upper bound on polls of one ready flag before a wait gives up.  A poll is
 // one L2 round trip (~0.5 us), so this is ~1 s - far above any correct wait.
 constexpr int kMaxSpins = 1 << 21;

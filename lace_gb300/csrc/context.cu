@@ -14,6 +14,7 @@
 //          32 so that columns are not a power of two bytes apart),
 //          Z[ldv x m] f32 (mixed precision) or f64, w/q/t vectors
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -63,10 +64,19 @@ void DBuf::free() {
   p = nullptr;
   bytes = 0;
 }
+// Injected allocation failure (lace_gpu_inject_alloc_failure): the number of
+// device allocations still allowed to succeed; negative = no injection.
+std::atomic<long long> g_alloc_budget{-1};
+
 int DBuf::ensure(size_t b) {
   if (b <= bytes && p) return 0;
   free();
   if (b == 0) b = 16;
+  if (g_alloc_budget.load() >= 0 && g_alloc_budget.fetch_sub(1) <= 0) {
+    g_alloc_budget.store(0);
+    p = nullptr;
+    return DEV_ERR_DEVICE_ALLOC;
+  }
   cudaError_t e = cudaMalloc(&p, b);
   if (e != cudaSuccess) {
     p = nullptr;
@@ -346,6 +356,8 @@ int build_blk_plan_host(const Pattern &T, bool lower, bool unit, int R, int cpb,
 }
 
 int upload_blk_plan(const HostPlan &hp, PlanBufs &pb, cudaStream_t s) {
+  // a failed upload leaves no plan behind that points at freed buffers
+  pb.valid = false;
   const int S = blk_slots(hp.R);
   const size_t nu = hp.urec.size(), rs = nu * (size_t)hp.R * 32;
   int rc = 0;
@@ -617,7 +629,70 @@ int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
   rc |= map_l2a.upload(l2a.data(), 4 * l2a.size(), stream);
   rc |= map_uc2a.upload(uc2a.data(), 4 * uc2a.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
+  sweep_ao = false;
+  if (bs_ == 0) {
+    rc = build_sweep_records(row, col, L, Ur, l2a, ur2a, uc2a);
+    if (rc) return rc;
+    sc.mark("sweep records");
+  }
   AT_ready = false;
+  return 0;
+}
+
+// The A-order sweep's records (parilu.cu k_parilu_sweep_ao): for every entry
+// p = (i,j) of A, the pairs (position of l_ik, position of u_kj) in A with
+// k < min(i,j), ascending k (L row i merged with U column j), and for i > j
+// the position of u_jj.  Counted per row, offset by one prefix sum and
+// filled, over parallel row ranges.
+int lace_gpu_ctx::build_sweep_records(const int *row, const int *col, const Pattern &L, const Pattern &Ur,
+                                      const std::vector<int> &l2a, const std::vector<int> &ur2a,
+                                      const std::vector<int> &uc2a) {
+  const int nr = n_blk;
+  const int nz = row[nr];
+  std::vector<int> pptr((size_t)nz + 1, 0), dpos(std::max(1, nz), -1);
+  auto walk = [&](int i, int p, int2 *out) {
+    const int j = col[p];
+    const int kmax = std::min(i, j);
+    int il = L.ptr[i], ie = L.ptr[i + 1] - 1;  // strict lower part (the unit diagonal is last)
+    int iu = hUc.ptr[j], ue = hUc.ptr[j + 1];
+    int cnt = 0;
+    while (il < ie && iu < ue) {
+      const int kl = L.idx[il], ku = hUc.idx[iu];
+      if (kl >= kmax || ku >= kmax) break;
+      if (kl == ku) {
+        if (out) out[cnt] = make_int2(l2a[il], uc2a[iu]);
+        ++cnt;
+        ++il;
+        ++iu;
+      } else if (kl < ku) {
+        ++il;
+      } else {
+        ++iu;
+      }
+    }
+    return cnt;
+  };
+  par_for((size_t)nr, 16384, [&](size_t b, size_t e) {
+    for (int i = (int)b; i < (int)e; ++i)
+      for (int p = row[i]; p < row[i + 1]; ++p) {
+        pptr[p + 1] = walk(i, p, nullptr);
+        if (col[p] < i) dpos[p] = ur2a[Ur.ptr[col[p]]];  // u_jj: first entry of U's row j
+      }
+  });
+  for (int p = 0; p < nz; ++p) pptr[p + 1] += pptr[p];
+  std::vector<int2> pairs(std::max(1, pptr[nz]));
+  par_for((size_t)nr, 16384, [&](size_t b, size_t e) {
+    for (int i = (int)b; i < (int)e; ++i)
+      for (int p = row[i]; p < row[i + 1]; ++p) walk(i, p, pairs.data() + pptr[p]);
+  });
+  int rc = 0;
+  rc |= sw_pptr.upload(pptr.data(), 4 * pptr.size(), stream);
+  rc |= sw_pairs.upload(pairs.data(), sizeof(int2) * pairs.size(), stream);
+  rc |= sw_dpos.upload(dpos.data(), 4 * dpos.size(), stream);
+  if (rc) return DEV_ERR_DEVICE_ALLOC;
+  // the host arrays go when this returns
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  sweep_ao = true;
   return 0;
 }
 
@@ -1030,6 +1105,10 @@ int lace_gpu_ctx::alloc_factor_values() {
   rc |= Urv.ensure(s * nnzU * ld);
   rc |= Ltv.ensure(s * nnzL * ld);
   if (bs) rc |= dinv.ensure(s * (size_t)n_blk * ld);
+  if (sweep_ao) {
+    rc |= Fv[0].ensure(s * (size_t)nnzA);
+    rc |= Fv[1].ensure(s * (size_t)nnzA);
+  }
   return rc ? DEV_ERR_DEVICE_ALLOC : 0;
 }
 
@@ -1098,16 +1177,28 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
   // the status bits describe this factorisation only (an earlier solve may
   // have left its own)
   if (cudaMemsetAsync(&ctrl()->status, 0, 4, stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
-  int rc = reuse_init && factors_ready ? 0 : init_factors();
+  // CSR: the sweeps run on the A-order values F from A itself (the A-initial
+  // guess), and L and U are gathered from F after them
+  const bool ao = sweep_ao && bs == 0 && sweeps > 0;
+  int rc = ao ? alloc_factor_values() : (reuse_init && factors_ready ? 0 : init_factors());
   if (rc) return rc;
   IluArgs a = ilu_args();
   if (!a.partials) return DEV_ERR_DEVICE_ALLOC;
   const VType t = vtype();
+  int fc = 0;
+  if (ao) launch_convert(stream, nnzA, VType::F64, Aval.p, t, Fv[0].p);
   double *dstep = (double *)scal_buf.p;  // [0..] per sweep
   for (int s = 0; s < sweeps; ++s) {
-    launch_parilu_sweep(stream, a, t, Lv[cur].p, Lv[1 - cur].p, Ucv[cur].p, Ucv[1 - cur].p,
-                        dstep + (s % 32));
-    cur = 1 - cur;
+    if (ao) {
+      launch_parilu_sweep_ao(stream, nnzA, t, (const double *)Aval.p, (const int *)sw_dpos.p,
+                             (const int *)sw_pptr.p, (const int2 *)sw_pairs.p, Fv[fc].p, Fv[1 - fc].p, a.partials,
+                             a.counter, dstep + (s % 32));
+      fc = 1 - fc;
+    } else {
+      launch_parilu_sweep(stream, a, t, Lv[cur].p, Lv[1 - cur].p, Ucv[cur].p, Ucv[1 - cur].p,
+                          dstep + (s % 32));
+      cur = 1 - cur;
+    }
     if (sync_each || s % 32 == 31 || s == sweeps - 1) {
       // entries of this batch not yet read: one when reading every sweep
       const int first = sync_each ? s % 32 : (s / 32) * 32 % 32;
@@ -1119,6 +1210,11 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
       if (step_out) *step_out = h_scal[cnt - 1] / anorm;
       if (sync_each && s + 1 >= min_sweeps && !(h_scal[cnt - 1] / anorm > stop_below)) break;
     }
+  }
+  if (ao) {
+    cur = 0;
+    launch_factor_gather(stream, nnzL, (const int *)map_l2a.p, t, Fv[fc].p, Lv[0].p);
+    launch_factor_gather(stream, nnzU, (const int *)map_uc2a.p, t, Fv[fc].p, Ucv[0].p);
   }
   rc = finish_factors();
   if (rc) return rc;
@@ -1164,8 +1260,14 @@ extern "C" int lace_gpu_parilu0(lace_gpu_ctx *c, int sweeps, double *step_out, d
   if (!c) return set_err(DEV_ERR_INVALID_PTR);
   if (sweeps < 0) return set_err(DEV_ERR_ILLEGAL_VALUE);
   cudaSetDevice(c->device);
-  int rc = c->parilu(sweeps, step_out, nonlin_out, false, nullptr);
-  return rc ? set_err(rc) : DEV_SUCCESS;
+  double step = 0.0;
+  int rc = c->parilu(sweeps, &step, nonlin_out, false, nullptr);
+  if (step_out) *step_out = step;
+  if (rc) return set_err(rc);
+  // a zero or non-finite pivot makes the factors non-finite (LACE's drop-in
+  // only logs it as a non-finite step; this call reports it)
+  if (sweeps > 0 && !std::isfinite(step)) return set_err(DEV_ERR_BADPRECOND);
+  return DEV_SUCCESS;
 }
 
 // ======================================================================
@@ -1175,10 +1277,14 @@ extern "C" int lace_gpu_parilu0(lace_gpu_ctx *c, int sweeps, double *step_out, d
 extern "C" int lace_gpu_spmv(lace_gpu_ctx *c, double alpha, const double *x, double beta, double *y) {
   if (!c || !x || !y) return set_err(DEV_ERR_INVALID_PTR);
   if (!c->n_blk) return set_err(DEV_ERR_NOT_INITIALIZED);
-  if (c->bs)
+  if (c->bs) {
     launch_bcsr_spmv(c->stream, c->n_blk, c->bs, (const int *)c->Arow.p, (const int *)c->Acol.p,
                      (const double *)c->Aval.p, x, alpha, beta, y);
-  else
+  } else if (c->opt.spmv_lanes <= 0 && c->ensure_sell() == 0 && c->sell_valid) {
+    // the sliced-ELL copy the Arnoldi operator uses (built on the first call)
+    launch_sell_spmv(c->stream, c->n_blk, (const int *)c->Arow.p, (const int *)c->sell_ptr.p,
+                     (const int *)c->sell_col.p, (const double *)c->sell_val.p, x, alpha, beta, y);
+  } else
     launch_spmv_f64x(c->stream, c->lanes, c->n_blk, (const int *)c->Arow.p, (const int *)c->Acol.p,
                      (const double *)c->Aval.p, x, alpha, beta, y);
   LCHK(cudaGetLastError());
@@ -1972,6 +2078,10 @@ extern "C" int lace_gpu_solve_backward(lace_gpu_ctx *c, const double *x, const d
 }
 
 extern "C" int lace_gpu_last_error(void) { return g_last_error; }
+
+extern "C" void lace_gpu_inject_alloc_failure(int after) {
+  g_alloc_budget.store(after < 0 ? -1 : (long long)after);
+}
 
 extern "C" const char *lace_gpu_error_string(int code) {
   switch (code) {

@@ -96,6 +96,10 @@ struct lace_gpu_ctx {
   DBuf map_l2a, map_uc2a, map_ur2uc, map_lt2l, map_ur2uc_el;
   // factor values (value type from opt.precision)
   DBuf Lv[2], Ucv[2], Urv, Ltv, dinv;
+  // CSR sweeps: the factor values in A's order (ping-pong) and the sweep's
+  // per-entry records (pair ranges, pairs of A positions, u_jj position)
+  DBuf Fv[2], sw_pptr, sw_pairs, sw_dpos;
+  bool sweep_ao = false;
   int cur = 0;
   bool factors_ready = false;
   int fact_version = 0;  // bumped whenever the factor values change
@@ -140,6 +144,8 @@ struct lace_gpu_ctx {
   void drop_graphs();
   int analyse(int n_, const int *row, const int *col, int bs_);
   int analyse_factors(const lace::Pattern &L, const lace::Pattern &Ur);
+  int build_sweep_records(const int *row, const int *col, const lace::Pattern &L, const lace::Pattern &Ur,
+                          const std::vector<int> &l2a, const std::vector<int> &ur2a, const std::vector<int> &uc2a);
   int set_factors_host(int nrows, const int *lrow, const int *lcol, const double *lval,
                        const int *urow, const int *ucol, const double *uval);
   // the same from U in CSC order (diagonal last in each column), when L's and

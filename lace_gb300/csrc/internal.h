@@ -78,6 +78,9 @@ void launch_spmv_f32x(cudaStream_t s, int lanes, int n, const int *row, const in
                       const double *val, const float *x, double alpha, double beta, double *y);
 void launch_bcsr_spmv(cudaStream_t s, int nb, int bs, const int *row, const int *col,
                       const double *val, const double *x, double alpha, double beta, double *y);
+// the same on A's sliced-ELL copy (row: A's CSR row pointers, for the row lengths)
+void launch_sell_spmv(cudaStream_t s, int n, const int *row, const int *sell_ptr, const int *sell_col,
+                      const double *sell_val, const double *x, double alpha, double beta, double *y);
 
 // ---------------------------------------------------- FGMRES-Householder
 struct ArnoldiArgs {
@@ -182,6 +185,13 @@ struct IluArgs {
 // one synchronous sweep old -> new; writes sum (new-old)^2 to *step (device)
 void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *Lold, void *Lnew,
                          const void *Uold, void *Unew, double *step);
+// one synchronous sweep over A's entries in A's order on F (factor values in
+// A's order), from the host-built pair records (parilu.cu); *step as above
+void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos,
+                            const int *pptr, const int2 *pairs, const void *Fold, void *Fnew, double *partials,
+                            int *counter, double *step);
+// dst[q] = map[q] >= 0 ? src[map[q]] : 1, value type t
+void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, const void *src, void *dst);
 // ||(A - LU)|_S||_F^2 to *out (device)
 void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
                          double *out);
@@ -258,6 +268,29 @@ void launch_sptrsv_levels(cudaStream_t s, const TriDev &t, VType vt, const void 
 // one synchronous Jacobi sweep y_new = D^{-1}(b - (T - D) y_old); step partial sums
 void launch_jacobi_sweep(cudaStream_t s, const TriDev &t, VType vt, const void *b, int in_f32,
                          const void *yold, void *ynew, int y_f32, Control *ctrl, bool honor_done);
+// ParCSRTRSV in LACE's sweep order (partrsv.cu).  Scratch: a (n doubles),
+// partials (partrsv_partials_needed() doubles), counters (4 ints), steps (2
+// doubles) on the device; h_steps (2 doubles) and h_status (1 int) on the host
+struct PartrsvScratch {
+  double *a = nullptr;
+  double *partials = nullptr;
+  int *counters = nullptr;
+  double *steps = nullptr;
+  double *h_steps = nullptr;
+  int *h_status = nullptr;
+};
+int partrsv_partials_needed();
+// one sweep in LACE's order: rows before row i in the sweep are read from
+// ynew (waiting until written), the others from yold; ynew must hold the
+// unsolved pattern and *ticket 0; guard (may be null): run only while
+// *guard > tol and finite; a wait gives up after max_polls polls (0: kMaxSpins)
+void launch_partrsv_sweep(cudaStream_t s, bool lower, int n, const int *row, const int *col, const double *val,
+                          const double *rhs, const double *yold, double *ynew, int *ticket, int *status,
+                          const double *guard, double tol, int max_polls);
+// data_parcsrtrsv's loop on device arrays: y is the start vector in and the
+// iterate out; returns 0 or a DEV_ERR_* code
+int partrsv_solve(cudaStream_t s, bool lower, int n, const int *row, const int *col, const double *val,
+                  const double *rhs, double *y, double tol, int *iter, const PartrsvScratch &sc);
 // block (BCSR) triangular solves: lower with identity diagonal blocks, or
 // upper applying the inverted diagonal blocks dinv
 void launch_bcsr_sptrsv(cudaStream_t s, const TriDev &t, int bs, VType vt, const void *dinv,

@@ -82,6 +82,58 @@ void launch_spmv_f32x(cudaStream_t s, int lanes, int n, const int *row, const in
   spmv_dispatch<float>(s, lanes, n, row, col, val, x, alpha, beta, y);
 }
 
+// y = alpha*A*x + beta*y on the sliced-ELL copy of A (slices of 32 rows,
+// entry t of a slice's rows stored together): a warp per slice, a lane per
+// row, so every column and value load is one coalesced 128- or 256-byte
+// segment; a row's entries are loaded eight at a time (a 7-point row in one
+// round) before their x gathers, with the entries summed in CSR order.
+__global__ void __launch_bounds__(kTPB) k_sell_spmv(int n, const int *__restrict__ row,
+                                                    const int *__restrict__ sell_ptr,
+                                                    const int *__restrict__ sell_col,
+                                                    const double *__restrict__ sell_val,
+                                                    const double *__restrict__ x, double alpha, double beta,
+                                                    double *__restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int nsl = (n + 31) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sl < nsl; sl += nw) {
+    const int i = 32 * sl + lane;
+    if (i >= n) continue;
+    const int len = __ldg(row + i + 1) - __ldg(row + i);
+    const int *cp = sell_col + __ldg(sell_ptr + sl) + lane;
+    const double *vp = sell_val + (cp - sell_col);
+    double s = 0.0;
+    for (int t = 0; t < len; t += 8) {
+      int c[8];
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (t + u < len) {
+          c[u] = __ldcs(cp + 32 * (t + u));
+          v[u] = __ldcs(vp + 32 * (t + u));
+        }
+      double xv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (t + u < len) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (t + u < len) s = fma(v[u], xv[u], s);
+    }
+    y[i] = (beta == 0.0) ? alpha * s : fma(beta, y[i], alpha * s);
+  }
+}
+
+void launch_sell_spmv(cudaStream_t s, int n, const int *row, const int *sell_ptr, const int *sell_col,
+                      const double *sell_val, const double *x, double alpha, double beta, double *y) {
+  if (n <= 0) return;
+  const int nsl = (n + 31) / 32;
+  int grid = (nsl + kTPB / 32 - 1) / (kTPB / 32);
+  const int cap = num_sms() * (2048 / kTPB);
+  if (grid > cap) grid = cap;
+  k_sell_spmv<<<grid, kTPB, 0, s>>>(n, row, sell_ptr, sell_col, sell_val, x, alpha, beta, y);
+}
+
 // BCSR: one thread per scalar row, the bs threads of a block row read the
 // same blocks (row-major bs x bs)
 __global__ void __launch_bounds__(kTPB) k_bcsr_spmv(int nb, int bs, const int *__restrict__ row,

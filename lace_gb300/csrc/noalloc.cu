@@ -1,5 +1,4 @@
-// The Jacobi triangular solve of data_parcsrtrsv on device arrays, without
-// allocating any memory.
+// data_parcsrtrsv on device arrays, without allocating any memory.
 //
 // data_parcsrtrsv takes host arrays and copies them into device buffers it
 // allocates on every call.  Some callers cannot allocate device memory at
@@ -8,10 +7,10 @@
 // cudaMalloc or cudaFree would synchronise the whole device and stall work on
 // other streams.  lace_gpu_parcsrtrsv_noalloc serves them: the caller passes
 // device arrays, and the scratch of the sweeps - the second iterate, the
-// partial sums of the step reduction, its arrival counter and the step itself
-// - sits in one file-scope device array of fixed size, so a call allocates
-// nothing.  The sweeps are the same kernels, in the same order, as in
-// data_parcsrtrsv, so both return the same iterate.
+// partial sums of the step reduction, the counters and the steps - sits in
+// one file-scope device array of fixed size, so a call allocates nothing.
+// The sweeps are the same kernels, in the same order, as in data_parcsrtrsv
+// (LACE's sweep order, partrsv.cu), so both return the same iterate.
 #include <cmath>
 #include <mutex>
 #include <utility>
@@ -24,12 +23,13 @@ namespace {
 constexpr int kNaMaxRows = LACE_GPU_NOALLOC_MAX_ROWS;
 constexpr int kNaMaxPartials = 4096;  // blocks of the step reduction (4 per SM)
 constexpr int kNaMaxDevices = 64;
-// layout in doubles: the second iterate, the partial sums, the step, and the
-// arrival counter (an int in the last slot)
+// layout in doubles: the second iterate, the partial sums, the two steps of
+// a round and four int counters (two tickets, the reduction's arrival
+// counter, the status bits) in the last two slots
 constexpr size_t kNaPartials = kNaMaxRows;
-constexpr size_t kNaStep = kNaPartials + kNaMaxPartials;
-constexpr size_t kNaCounter = kNaStep + 1;
-constexpr size_t kNaWords = kNaCounter + 1;
+constexpr size_t kNaSteps = kNaPartials + kNaMaxPartials;
+constexpr size_t kNaCounters = kNaSteps + 2;
+constexpr size_t kNaWords = kNaCounters + 2;
 
 // About 2 MB, held by every GPU that loads the library until the process
 // exits.  In host code this name is a host-side stand-in, not a device
@@ -39,10 +39,11 @@ static __device__ __align__(256) double g_noalloc_scratch[kNaWords];
 std::mutex g_na_mu;
 double *g_na_addr[kNaMaxDevices] = {};
 
-// Device address of the scratch on the current device.  The first call on a
-// device looks it up (with that device current) and clears the counter on
-// stream s, then waits for that clear.
-int noalloc_scratch(cudaStream_t s, double **out) {
+// Device address of the scratch on the current device, looked up (with that
+// device current) by the first call on the device.  Every call clears the
+// counters itself on its own stream, so nothing depends on how an earlier
+// call ended.
+int noalloc_scratch(double **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
@@ -56,11 +57,6 @@ int noalloc_scratch(cudaStream_t s, double **out) {
       cudaGetLastError();
       return DEV_ERR_UNKNOWN;
     }
-    // the reduction's arrival counter must start at zero; its last block
-    // puts it back to zero after every reduction
-    if (cudaMemsetAsync(p + kNaCounter, 0, sizeof(double), s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return DEV_ERR_UNKNOWN;
     g_na_addr[dev] = p;
   }
   *out = g_na_addr[dev];
@@ -89,35 +85,28 @@ extern "C" int lace_gpu_parcsrtrsv_noalloc(const data_uplo_t uplo, const data_st
   if (num_rows < 0 || num_rows > kNaMaxRows) return set_err(DEV_ERR_NOT_SUPPORTED);
   if (num_rows == 0) return 0;
   if (!Aval || !row || !col || !rhsval || !yval) return set_err(DEV_ERR_INVALID_PTR);
-  if (num_sms() * 4 > kNaMaxPartials) return set_err(DEV_ERR_NOT_SUPPORTED);
+  if (partrsv_partials_needed() > kNaMaxPartials) return set_err(DEV_ERR_NOT_SUPPORTED);
   cudaStream_t s = (cudaStream_t)stream;
+  // the stream must belong to the current device, where the scratch address
+  // is looked up
+  int cur_dev = 0, stream_dev = 0;
+  if (cudaGetDevice(&cur_dev) != cudaSuccess || cudaStreamGetDevice(s, &stream_dev) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(DEV_ERR_ILLEGAL_VALUE);
+  }
+  if (cur_dev != stream_dev) return set_err(DEV_ERR_ILLEGAL_VALUE);
   double *scr = nullptr;
-  int rc = noalloc_scratch(s, &scr);
+  int rc = noalloc_scratch(&scr);
   if (rc) return set_err(rc);
-  TriDev t;
-  t.n = num_rows;
-  t.row = row;
-  t.col = col;
-  t.val = Aval;
-  t.lower = lower ? 1 : 0;
-  t.unit = 0;  // LACE divides by the stored diagonal
-  double *cur = yval, *nxt = scr;
-  double step = 1.e8;
-  // Jacobi sweeps converge in at most (number of levels) sweeps; bound the loop
-  const int cap = num_rows + 2;
-  while (step > tol && std::isfinite(step) && *iter < cap) {
-    launch_jacobi_sweep(s, t, VType::F64, rhsval, 0, cur, nxt, 0, nullptr, false);
-    launch_sqdiff(s, num_rows, nxt, cur, 0, scr + kNaPartials, (int *)(scr + kNaCounter), scr + kNaStep);
-    if (cudaMemcpyAsync(&step, scr + kNaStep, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return set_err(DEV_ERR_UNKNOWN);
-    std::swap(cur, nxt);
-    *iter = *iter + 1;
-  }
-  if (cur != yval) {
-    if (cudaMemcpyAsync(yval, cur, sizeof(double) * (size_t)num_rows, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return set_err(DEV_ERR_UNKNOWN);
-  }
-  return 0;
+  double h_steps[2] = {0.0, 0.0};
+  int h_status = 0;
+  PartrsvScratch sc;
+  sc.a = scr;
+  sc.partials = scr + kNaPartials;
+  sc.steps = scr + kNaSteps;
+  sc.counters = (int *)(scr + kNaCounters);
+  sc.h_steps = h_steps;
+  sc.h_status = &h_status;
+  rc = partrsv_solve(s, lower, num_rows, row, col, Aval, rhsval, yval, tol, iter, sc);
+  return rc ? set_err(rc) : 0;
 }

@@ -386,6 +386,85 @@ static int sweep_grid(int rows) {
   return g < 1 ? 1 : (g > cap ? cap : g);
 }
 
+// ---------------------------------------------------------------- A order
+// The synchronous sweep over A's entries in A's own order, on one array F of
+// factor values in A's order (F[p] = l_ij for i > j, u_ij for i <= j; L's
+// unit diagonal implicit).  The pattern's merges are done once on the host:
+// for entry p = (i,j) the positions in A of the pairs (l_ik, u_kj) with
+// k < min(i,j), in ascending k (pairs[pptr[p] .. pptr[p+1])), and for i > j
+// the position of u_jj (dpos[p], -1 for i <= j).  A sweep is then a stream
+// of A's values and the per-entry records, coalesced, thread per entry, with
+// the few pair operands gathered from the previous F (on a 7-point stencil
+// three pairs per row, all on the diagonal entry):
+//     s = a_ij - sum_k l_ik u_kj          (ascending k, as the merge walk)
+//     F_new[p] = i > j ? s / u_jj : s
+// The step sum (F_new - F_old)^2 is accumulated per thread in the compute
+// type and folded in FP64 across the grid.
+template <typename FT, typename CT>
+__global__ void __launch_bounds__(kPTPB) k_parilu_sweep_ao(int nnz, const double *__restrict__ Aval,
+                                                           const int *__restrict__ dpos,
+                                                           const int *__restrict__ pptr,
+                                                           const int2 *__restrict__ pairs,
+                                                           const FT *__restrict__ Fold, FT *__restrict__ Fnew,
+                                                           double *partials, int *counter, double *step) {
+  CT acc = (CT)0;
+  const int stride = gridDim.x * blockDim.x;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += stride) {
+    CT s = (CT)__ldcs(Aval + p);
+    const int b = __ldcs(pptr + p), e = __ldg(pptr + p + 1);
+    const int d = __ldcs(dpos + p);
+    for (int q = b; q < e; ++q) {
+      const int2 pr = __ldg(pairs + q);
+      s = fma(-cvt<CT>(Fold[pr.x]), cvt<CT>(Fold[pr.y]), s);
+    }
+    const CT nv = d >= 0 ? s / cvt<CT>(Fold[d]) : s;
+    const CT df = nv - cvt<CT>(Fold[p]);
+    acc = fma(df, df, acc);
+    Fnew[p] = cvt<FT>(nv);
+  }
+  finish_sum((double)acc, partials, counter, step);
+}
+
+// dst[q] = map[q] >= 0 ? src[map[q]] : 1 (L's unit diagonal), same value type
+template <typename T>
+__global__ void k_factor_gather(int count, const int *__restrict__ map, const T *__restrict__ src,
+                                T *__restrict__ dst) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x) {
+    const int m = map[q];
+    dst[q] = m >= 0 ? src[m] : cvt<T>(1.0f);
+  }
+}
+
+void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos,
+                            const int *pptr, const int2 *pairs, const void *Fold, void *Fnew, double *partials,
+                            int *counter, double *step) {
+  int grid = (nnz + kPTPB - 1) / kPTPB;
+  const int cap = num_sms() * (2048 / kPTPB);
+  grid = grid < 1 ? 1 : (grid > cap ? cap : grid);
+  if (t == VType::F64)
+    k_parilu_sweep_ao<double, double><<<grid, kPTPB, 0, s>>>(nnz, Aval, dpos, pptr, pairs, (const double *)Fold,
+                                                             (double *)Fnew, partials, counter, step);
+  else if (t == VType::F32)
+    k_parilu_sweep_ao<float, float><<<grid, kPTPB, 0, s>>>(nnz, Aval, dpos, pptr, pairs, (const float *)Fold,
+                                                           (float *)Fnew, partials, counter, step);
+  else
+    k_parilu_sweep_ao<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+        nnz, Aval, dpos, pptr, pairs, (const __nv_bfloat16 *)Fold, (__nv_bfloat16 *)Fnew, partials, counter, step);
+}
+
+void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, const void *src, void *dst) {
+  int grid = (count + 255) / 256;
+  const int cap = num_sms() * 8;
+  grid = grid < 1 ? 1 : (grid > cap ? cap : grid);
+  if (t == VType::F64)
+    k_factor_gather<double><<<grid, 256, 0, s>>>(count, map, (const double *)src, (double *)dst);
+  else if (t == VType::F32)
+    k_factor_gather<float><<<grid, 256, 0, s>>>(count, map, (const float *)src, (float *)dst);
+  else
+    k_factor_gather<__nv_bfloat16><<<grid, 256, 0, s>>>(count, map, (const __nv_bfloat16 *)src,
+                                                        (__nv_bfloat16 *)dst);
+}
+
 void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *Lold, void *Lnew,
                          const void *Uold, void *Unew, double *step) {
   if (a.bs > 0) {

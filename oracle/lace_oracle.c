@@ -70,6 +70,39 @@ double orc_parilu_sweep(int mode, int nnzA, const int *Arowidx, const int *Acol,
     }
     return step;
   }
+  if (mode == 2) {
+    /* src/parilu_v0_3.cpp:66-102 as LACE runs it: in place, entries split
+     * statically over the OpenMP threads (racy across the threads' ranges,
+     * as LACE's own loop) */
+    double *Lv = Lnew, *Uv = Unew;
+    (void)Lold;
+    (void)Uold;
+#pragma omp parallel for schedule(static) reduction(+ : step)
+    for (int k = 0; k < nnzA; k++) {
+      int i = Arowidx[k], j = Acol[k];
+      double s = Aval[k], sp = 0.0;
+      int il = Lrow[i], iu = Ucolptr[j];
+      while (il < Lrow[i + 1] && iu < Ucolptr[j + 1]) {
+        sp = 0.0;
+        int jl = Lcol[il], ju = Urowidx[iu];
+        sp = (jl == ju) ? Lv[il] * Uv[iu] : sp;
+        s = (jl == ju) ? s - sp : s;
+        il = (jl <= ju) ? il + 1 : il;
+        iu = (jl >= ju) ? iu + 1 : iu;
+      }
+      s += sp;
+      if (i > j) {
+        double tmp = s / Uv[Ucolptr[j + 1] - 1];
+        step += pow(Lv[il - 1] - tmp, 2);
+        Lv[il - 1] = tmp;
+      } else {
+        double tmp = s;
+        step += pow(Uv[iu - 1] - tmp, 2);
+        Uv[iu - 1] = tmp;
+      }
+    }
+    return step;
+  }
   /* synchronous sweep: same update formula (:70-101) evaluated from the
    * previous iterate, sum over k < min(i,j) only */
 #pragma omp parallel for schedule(static) reduction(+ : step)

@@ -214,6 +214,8 @@ def parilu(row, col, val, sweeps: int, mode: str = "sync", f32: bool = False,
            stop_eps: bool = False) -> Factors:
     """`sweeps` ParILU(0) sweeps from the A-initial guess.  mode 'async' is
     LACE's in-place sweep (src/parilu_v0_3.cpp:62-108, one-thread order);
+    'async_omp' the same loop split statically over the OpenMP threads, as
+    LACE runs it (racy across the threads' ranges, so not reproducible);
     'sync' the Jacobi form.  stop_eps mirrors the prescribed-sweeps stop
     (step <= 4*eps, src/parilu_v0_3_prescribedSweeps.cpp:62). Steps recorded
     are normalised by ||A||_F (:104)."""
@@ -241,9 +243,9 @@ def parilu(row, col, val, sweeps: int, mode: str = "sync", f32: bool = False,
             Uc, Un = Un, Uc
             Ln[:] = Lc
             Un[:] = Uc
-        elif mode == "async":
-            s = lb.orc_parilu_sweep(0, len(col), rid, col, val, F.L.ptr, F.L.idx, Lc, Lc,
-                                    F.U.ptr, F.U.idx, Uc, Uc)
+        elif mode in ("async", "async_omp"):
+            s = lb.orc_parilu_sweep(0 if mode == "async" else 2, len(col), rid, col, val, F.L.ptr, F.L.idx, Lc,
+                                    Lc, F.U.ptr, F.U.idx, Uc, Uc)
         else:
             s = lb.orc_parilu_sweep(1, len(col), rid, col, val, F.L.ptr, F.L.idx, Lc, Ln,
                                     F.U.ptr, F.U.idx, Uc, Un)

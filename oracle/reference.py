@@ -1,8 +1,9 @@
 """ctypes access to LACE's own implementation, compiled unmodified from the
 LACE sources by `make -C oracle ref` into oracle/_ref/ (TEST INFRASTRUCTURE).
 
-Only available where the LACE source tree is present (the recipe reads it
-from REF=/root/reference); callers must skip when `available()` is False.
+Only available where the LACE source tree is present (oracle/Makefile names
+where it reads it; LACE_REF_SRC overrides); callers must skip when
+`available()` is False.
 Used to pin the C restatement and to generate the golden fixtures in
 tests/golden/.
 """
@@ -15,7 +16,22 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("LACE_REF_SRC", "/root/reference")
+
+
+def _ref_src() -> str:
+    """The LACE source tree the oracle's Makefile reads (LACE_REF_SRC, else the
+    recipe's default)."""
+    env = os.environ.get("LACE_REF_SRC")
+    if env:
+        return env
+    try:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True, check=True)
+        return r.stdout.strip()
+    except (subprocess.CalledProcessError, OSError):
+        return ""
+
+
+REF_SRC = _ref_src()
 LIB = os.path.join(HERE, "_ref", "liblace_ref.so")
 LIB_BCSR = os.path.join(HERE, "_ref", "liblace_ref_bcsr.so")
 

@@ -1,7 +1,8 @@
 """Generate tests/golden/lace_golden.npz from LACE's own implementation.
 
 Runs LACE's unmodified sources, compiled by `make -C oracle ref` from the
-LACE source tree (REF, default /root/reference), on small inputs and stores
+LACE source tree (the tree oracle/Makefile reads; LACE_REF_SRC overrides),
+on small inputs and stores
 inputs and outputs as fixtures.  The inputs are this project's seeded
 synthetic systems plus two of LACE's own tiny test fixtures
 (testing/matrices/io_test.mtx, 4x4; the Trefethen_20 matrix, which is also

@@ -51,7 +51,12 @@ def test_io_test_known_answers():
 def test_trefethen_generator_matches_lace_fixture():
     T = P.trefethen(19)
     assert T.n == 19 and T.nnz == 147
-    assert np.array_equal(T.row, G["tref_L_row"][:0].astype(T.row.dtype)) or True
+    # the factor patterns LACE built from its own copy of the file (golden)
+    # are the generated matrix's: CSRL (unit diagonal last) and CSCU
+    Lg = orc.split_lower(T.row, T.col, T.val, "unity")
+    assert np.array_equal(Lg.ptr, G["tref_L_row"]) and np.array_equal(Lg.idx, G["tref_L_col"])
+    F0 = orc.initial_factors(T.row, T.col, T.val)
+    assert np.array_equal(F0.U.ptr, G["tref_U_ptr"]) and np.array_equal(F0.U.idx, G["tref_U_idx"])
     # the generated matrix is LACE's Trefethen_20 (checked against the file
     # itself when the LACE tree is present)
     if ref.available():
@@ -86,6 +91,24 @@ def test_parilu_prescribed_equals_lace(name):
     F = orc.parilu(S.row, S.col, S.val, int(log[0]), mode="async")
     assert np.array_equal(F.L.val, G[f"{name}_L_val"])
     assert np.array_equal(F.U.val, G[f"{name}_U_val"])
+
+
+def test_parilu_openmp_form_on_one_thread_equals_lace():
+    """The OpenMP form of LACE's in-place sweep (the loop split statically
+    over the threads, as LACE runs it; the CPU baseline) is LACE's one-thread
+    sweep when it runs on one thread, and on several threads its residual
+    stays at the same (rounding) level on these orderings."""
+    S = P.convdiff3d(12)
+    log = G["cd12_parilu_log"]
+    try:
+        orc.set_threads(1)
+        F = orc.parilu(S.row, S.col, S.val, int(log[0]), mode="async_omp")
+        assert np.array_equal(F.L.val, G["cd12_L_val"]) and np.array_equal(F.U.val, G["cd12_U_val"])
+        orc.set_threads(4)
+        F = orc.parilu(S.row, S.col, S.val, 3, mode="async_omp")
+        assert orc.ilu_nonlinres(S.row, S.col, S.val, F) <= 1e-12 * np.linalg.norm(S.val)
+    finally:
+        orc.set_threads(os.cpu_count() or 1)
 
 
 def test_sync_sweeps_converge_to_exact_ilu0():
