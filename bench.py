@@ -196,7 +196,7 @@ def run_ours(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    A, b = build_problem(args.grid if (args.only_mgs or args.only_householder) else GRID)
+    A, b = build_problem(args.grid if (args.only_mgs or args.only_householder or args.only_kernels) else GRID)
     stream = torch.cuda.Stream()
     ctx = lg.Context(local, stream=stream)
     ctx.upload(A)
@@ -237,6 +237,22 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
         return times, wall, res
+
+    if args.only_kernels:
+        # profiling aid (no contract line): the standalone kernels of the
+        # roofline table on the workload - ParILU sweeps, SpMV, the
+        # preconditioner pair - a few launches each
+        ctx.set_options(precision="fp32", **pin)
+        for _ in range(2):
+            ctx.parilu0(SWEEPS, residual=False)
+        q = torch.randn(A.n, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(q)
+        for _ in range(3):
+            ctx.spmv(q, y)
+        ctx.apply_precond(q, y)
+        torch.cuda.synchronize()
+        ctx.close()
+        return
 
     if args.only_mgs or args.only_householder:
         # profiling aid: one solve kind alone (no contract line)
@@ -634,8 +650,11 @@ def main():
                     help="time only the FGMRES with modified Gram-Schmidt (for profiling its kernels)")
     ap.add_argument("--only-householder", action="store_true",
                     help="time only the FGMRES-Householder solve (for profiling its kernels)")
+    ap.add_argument("--only-kernels", action="store_true",
+                    help="run only the standalone kernels (ParILU sweeps, SpMV, one preconditioner pair) a few "
+                         "times, for profiling them")
     ap.add_argument("--grid", type=int, default=GRID,
-                    help="with --only-mgs / --only-householder: the convection-diffusion grid side "
+                    help="with --only-mgs / --only-householder / --only-kernels: the convection-diffusion grid side "
                          "(a smaller case for ncu)")
     args = ap.parse_args()
     rank, world, local = dist_env()

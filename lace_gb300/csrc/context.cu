@@ -551,6 +551,7 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
   if (prec_changed) {
     c->factors_ready = false;
     c->trsv_tuned = false;  // the window and the best schedule depend on the value type
+    c->bcsr_tuned = false;
   }
   if (o->trsv_rows_per_lane > 0) c->set_rows_per_lane(o->trsv_rows_per_lane);
   if (o->spmv_lanes > 0) c->lanes = o->spmv_lanes;
@@ -630,7 +631,7 @@ int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
   rc |= map_uc2a.upload(uc2a.data(), 4 * uc2a.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
   sweep_ao = false;
-  if (bs_ == 0) {
+  if (bs_ <= 5) {  // scalar entries, or blocks whose values fit one warp's lanes
     rc = build_sweep_records(row, col, L, Ur, l2a, ur2a, uc2a);
     if (rc) return rc;
     sc.mark("sweep records");
@@ -685,10 +686,14 @@ int lace_gpu_ctx::build_sweep_records(const int *row, const int *col, const Patt
     for (int i = (int)b; i < (int)e; ++i)
       for (int p = row[i]; p < row[i + 1]; ++p) walk(i, p, pairs.data() + pptr[p]);
   });
+  // the position in A of every (block) row's diagonal entry
+  std::vector<int> diag(std::max(1, nr));
+  for (int i = 0; i < nr; ++i) diag[i] = ur2a[Ur.ptr[i]];
   int rc = 0;
   rc |= sw_pptr.upload(pptr.data(), 4 * pptr.size(), stream);
   rc |= sw_pairs.upload(pairs.data(), sizeof(int2) * pairs.size(), stream);
   rc |= sw_dpos.upload(dpos.data(), 4 * dpos.size(), stream);
+  rc |= sw_diag.upload(diag.data(), 4 * diag.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
   // the host arrays go when this returns
   if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
@@ -751,6 +756,36 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
     if (!rc) cudaMemsetAsync(ready[t].p, 0, 4 * (size_t)maxch, stream);
   }
   sc.mark("level sets");
+  if (bs > 0) {
+    // chunks of the BCSR solves: at most 64 block rows, in solve order, a
+    // new chunk wherever a block row does not depend on the one solved just
+    // before it (so a chunk is at most a grid line: the chain along the line
+    // stays in one warp's registers)
+    const int cap = 64;
+    for (int t = 0; t < 2; ++t) {
+      const Pattern &P = t == 0 ? hL : hU;
+      const int nb = P.n;
+      std::vector<int> first;
+      int in_chunk = 0;
+      for (int pos = 0; pos < nb; ++pos) {
+        const int I = t == 0 ? pos : nb - 1 - pos;
+        const int prev = t == 0 ? I - 1 : I + 1;
+        bool dep = false;
+        if (pos > 0)
+          for (int q = P.ptr[I]; q < P.ptr[I + 1] && !dep; ++q) dep = P.idx[q] == prev;
+        if (pos == 0 || !dep || in_chunk == cap) {
+          first.push_back(pos);
+          in_chunk = 0;
+        }
+        ++in_chunk;
+      }
+      first.push_back(nb);
+      bnch[t] = (int)first.size() - 1;
+      rc |= bch_first[t].upload(first.data(), 4 * first.size(), stream);
+    }
+    // the host vectors go when this returns
+    if (!rc && cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
+  }
   // the epochs of the new ready arrays restart with the zeroed flags
   Control zero;
   memset(&zero, 0, sizeof(zero));
@@ -758,6 +793,7 @@ int lace_gpu_ctx::analyse_factors(const Pattern &L, const Pattern &Ur) {
   if (rc) return DEV_ERR_DEVICE_ALLOC;
   factors_ready = false;
   trsv_tuned = false;
+  bcsr_tuned = false;
   ws_m = 0;
   drop_graphs();
   return 0;
@@ -905,6 +941,10 @@ TriDev lace_gpu_ctx::tri(int which) const {
   t.lvl_ptr = (const int *)lvl_ptr[which].p;
   t.lvl_rows = (const int *)lvl_rows[which].p;
   t.nlevels = nlevels[which];
+  if (which < 2) {
+    t.bchunk_first = (const int *)bch_first[which].p;
+    t.bnch = bnch[which];
+  }
   switch (which) {
     case 0: t.row = (const int *)Lrow.p; t.col = (const int *)Lcol.p; t.val = Lv[cur].p; t.lower = 1; t.unit = 1; t.nnz = nnzL; break;
     case 1: t.row = (const int *)Urow.p; t.col = (const int *)Ucol.p; t.val = Urv.p; t.lower = 0; t.unit = 0; t.nnz = nnzU; break;
@@ -1106,8 +1146,9 @@ int lace_gpu_ctx::alloc_factor_values() {
   rc |= Ltv.ensure(s * nnzL * ld);
   if (bs) rc |= dinv.ensure(s * (size_t)n_blk * ld);
   if (sweep_ao) {
-    rc |= Fv[0].ensure(s * (size_t)nnzA);
-    rc |= Fv[1].ensure(s * (size_t)nnzA);
+    rc |= Fv[0].ensure(s * (size_t)nnzA * ld);
+    rc |= Fv[1].ensure(s * (size_t)nnzA * ld);
+    if (bs) rc |= sw_dinv.ensure((t == VType::F64 ? 8 : 4) * (size_t)n_blk * ld);
   }
   return rc ? DEV_ERR_DEVICE_ALLOC : 0;
 }
@@ -1177,19 +1218,27 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
   // the status bits describe this factorisation only (an earlier solve may
   // have left its own)
   if (cudaMemsetAsync(&ctrl()->status, 0, 4, stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
-  // CSR: the sweeps run on the A-order values F from A itself (the A-initial
+  // the sweeps run on the A-order values F from A itself (the A-initial
   // guess), and L and U are gathered from F after them
-  const bool ao = sweep_ao && bs == 0 && sweeps > 0;
+  const bool ao = sweep_ao && sweeps > 0;
+  const int ldb = bs ? bs * bs : 1;
   int rc = ao ? alloc_factor_values() : (reuse_init && factors_ready ? 0 : init_factors());
   if (rc) return rc;
   IluArgs a = ilu_args();
   if (!a.partials) return DEV_ERR_DEVICE_ALLOC;
   const VType t = vtype();
   int fc = 0;
-  if (ao) launch_convert(stream, nnzA, VType::F64, Aval.p, t, Fv[0].p);
+  if (ao) launch_convert(stream, nnzA * ldb, VType::F64, Aval.p, t, Fv[0].p);
   double *dstep = (double *)scal_buf.p;  // [0..] per sweep
   for (int s = 0; s < sweeps; ++s) {
-    if (ao) {
+    if (ao && bs) {
+      launch_bcsr_diag_inverse_ao(stream, n_blk, bs, (const int *)sw_diag.p, t, Fv[fc].p, sw_dinv.p,
+                                  &ctrl()->status);
+      launch_bcsr_parilu_sweep_ao(stream, nnzA, bs, t, (const double *)Aval.p, (const int *)Acol.p,
+                                  (const int *)sw_dpos.p, (const int *)sw_pptr.p, (const int2 *)sw_pairs.p,
+                                  sw_dinv.p, Fv[fc].p, Fv[1 - fc].p, a.partials, a.counter, dstep + (s % 32));
+      fc = 1 - fc;
+    } else if (ao) {
       launch_parilu_sweep_ao(stream, nnzA, t, (const double *)Aval.p, (const int *)sw_dpos.p,
                              (const int *)sw_pptr.p, (const int2 *)sw_pairs.p, Fv[fc].p, Fv[1 - fc].p, a.partials,
                              a.counter, dstep + (s % 32));
@@ -1211,7 +1260,11 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
       if (sync_each && s + 1 >= min_sweeps && !(h_scal[cnt - 1] / anorm > stop_below)) break;
     }
   }
-  if (ao) {
+  if (ao && bs) {
+    cur = 0;
+    launch_factor_gather_blk(stream, nnzL, bs, (const int *)map_l2a.p, t, Fv[fc].p, Lv[0].p);
+    launch_factor_gather_blk(stream, nnzU, bs, (const int *)map_uc2a.p, t, Fv[fc].p, Ucv[0].p);
+  } else if (ao) {
     cur = 0;
     launch_factor_gather(stream, nnzL, (const int *)map_l2a.p, t, Fv[fc].p, Lv[0].p);
     launch_factor_gather(stream, nnzU, (const int *)map_uc2a.p, t, Fv[fc].p, Ucv[0].p);
@@ -1327,8 +1380,12 @@ int lace_gpu_ctx::solve_tri(int which, const void *b, int in_f32, void *x, int o
       break;
     default:
       if (bs) {
+        if (b == x) {  // the solve fills x before it reads b
+          cudaMemcpyAsync(tmp, b, (size_t)n * (in_f32 ? 4 : 8), cudaMemcpyDeviceToDevice, stream);
+          b = tmp;
+        }
         launch_bcsr_sptrsv(stream, t, bs, vt, which == 1 ? dinv.p : nullptr, b, in_f32, x, out_f32, cb,
-                           0, honor_done);
+                           bcsr_grid, honor_done);
       } else {
         int rc = ensure_plan(which);
         if (rc) return rc;
@@ -1354,7 +1411,50 @@ int lace_gpu_ctx::ensure_vectors() {
   return rc ? DEV_ERR_DEVICE_ALLOC : 0;
 }
 
+// BCSR solves: the grid (resident blocks per SM) that solves the pair
+// fastest, timed as the cycle runs it
+int lace_gpu_ctx::autotune_bcsr_trsv() {
+  if (bcsr_tuned) return 0;
+  int rc = ensure_vectors();
+  if (rc) return rc;
+  const int f32 = vtype() != VType::F64;
+  cudaMemsetAsync(vec_q.p, 0, 8 * (size_t)n, stream);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int best_grid = num_sms() * 8;
+  for (int per_sm : {2, 4, 8}) {
+    bcsr_grid = num_sms() * per_sm;
+    float ms = 0.f;
+    for (int rep = 0; rep < 3 && !rc; ++rep) {
+      cudaEventRecord(e0, stream);
+      rc = solve_tri(0, vec_q.p, 0, vec_t.p, f32, false, vec_t2.p);
+      if (!rc) rc = solve_tri(1, vec_t.p, f32, vec_r.p, f32, false, vec_t2.p);
+      cudaEventRecord(e1, stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = DEV_ERR_UNKNOWN;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0) ms += t;  // the first rep warms up
+    }
+    if (rc) break;
+    if (verbose) printf("%% bcsr trsv autotune: %d blocks/SM: %.3f ms per pair\n", per_sm, ms / 2);
+    if (ms < best) {
+      best = ms;
+      best_grid = bcsr_grid;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  bcsr_grid = best_grid;
+  if (rc) return rc;
+  if (h_status() & kStatusSpinTimeout) return DEV_ERR_INTERNAL_LIMIT;
+  bcsr_tuned = true;
+  return 0;
+}
+
 int lace_gpu_ctx::autotune_trsv() {
+  if (bs && opt.trsv_mode == LACE_TRSV_SYNCFREE) return autotune_bcsr_trsv();
   if (bs || opt.trsv_mode != LACE_TRSV_SYNCFREE) return 0;
   if (trsv_tuned) return 0;
   int rc = ensure_vectors();

@@ -98,7 +98,7 @@ struct lace_gpu_ctx {
   DBuf Lv[2], Ucv[2], Urv, Ltv, dinv;
   // CSR sweeps: the factor values in A's order (ping-pong) and the sweep's
   // per-entry records (pair ranges, pairs of A positions, u_jj position)
-  DBuf Fv[2], sw_pptr, sw_pairs, sw_dpos;
+  DBuf Fv[2], sw_pptr, sw_pairs, sw_dpos, sw_diag, sw_dinv;
   bool sweep_ao = false;
   int cur = 0;
   bool factors_ready = false;
@@ -106,6 +106,12 @@ struct lace_gpu_ctx {
 
   // SpTRSV per triangle (0 L, 1 U, 2 U^T, 3 L^T)
   DBuf ready[4];
+  // BCSR solves of L and U: chunk tables (see sptrsv.cu k_bcsr_sptrsv)
+  DBuf bch_first[2];
+  int bnch[2] = {0, 0};
+  int bcsr_grid = 0;  // blocks of the BCSR solves (autotuned; 0: the launcher's default)
+  bool bcsr_tuned = false;
+  int autotune_bcsr_trsv();
   DBuf lvl_ptr[4], lvl_rows[4];
   int nlevels[4] = {0, 0, 0, 0};
   int rows_per_lane = 4;

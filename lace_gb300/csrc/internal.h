@@ -66,6 +66,10 @@ struct TriDev {
   const int *lvl_ptr = nullptr;
   const int *lvl_rows = nullptr;
   int nlevels = 0;
+  // BCSR solves: chunks of block rows in solve order (first position of each
+  // chunk, bnch + 1 entries)
+  const int *bchunk_first = nullptr;
+  int bnch = 0;
 };
 
 enum class VType { F64 = 0, F32 = 1, BF16 = 2 };
@@ -192,6 +196,18 @@ void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval
                             int *counter, double *step);
 // dst[q] = map[q] >= 0 ? src[map[q]] : 1, value type t
 void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, const void *src, void *dst);
+// the block sweep in A's block order (bs <= 5), Dinv: the block inverses of
+// U's diagonal blocks of Fold in the compute type (float for FP32 / BF16)
+void launch_bcsr_parilu_sweep_ao(cudaStream_t s, int nnzb, int bs, VType t, const double *Aval, const int *Acol,
+                                 const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv,
+                                 const void *Fold, void *Fnew, double *partials, int *counter, double *step);
+// Dinv[I] = inv(F[diag[I]]) per block row (bs <= 5, compute type), breakdown
+// bit on a non-finite inverse
+void launch_bcsr_diag_inverse_ao(cudaStream_t s, int nb, int bs, const int *diag, VType t, const void *F,
+                                 void *Dinv, int *status);
+// block gather: dst block q = src block map[q], identity for map[q] < 0
+void launch_factor_gather_blk(cudaStream_t s, int count, int bs, const int *map, VType t, const void *src,
+                              void *dst);
 // ||(A - LU)|_S||_F^2 to *out (device)
 void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
                          double *out);

@@ -12,6 +12,8 @@
 // each column).  One thread per row of A: the row's L entries are reused for
 // all of its nonzeros, and the target position of an entry is found by the
 // same merge walk (no position map is stored).
+#include <algorithm>
+
 #include "internal.h"
 
 namespace lace {
@@ -400,6 +402,11 @@ static int sweep_grid(int rows) {
 //     F_new[p] = i > j ? s / u_jj : s
 // The step sum (F_new - F_old)^2 is accumulated per thread in the compute
 // type and folded in FP64 across the grid.
+constexpr int kAoU = 4;  // entries per thread in flight
+
+// Each thread takes kAoU entries a grid stride apart (coalesced across the
+// warp): their independent loads first, then the pair operands of all of
+// them round by round, then the arithmetic.
 template <typename FT, typename CT>
 __global__ void __launch_bounds__(kPTPB) k_parilu_sweep_ao(int nnz, const double *__restrict__ Aval,
                                                            const int *__restrict__ dpos,
@@ -409,18 +416,55 @@ __global__ void __launch_bounds__(kPTPB) k_parilu_sweep_ao(int nnz, const double
                                                            double *partials, int *counter, double *step) {
   CT acc = (CT)0;
   const int stride = gridDim.x * blockDim.x;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += stride) {
-    CT s = (CT)__ldcs(Aval + p);
-    const int b = __ldcs(pptr + p), e = __ldg(pptr + p + 1);
-    const int d = __ldcs(dpos + p);
-    for (int q = b; q < e; ++q) {
-      const int2 pr = __ldg(pairs + q);
-      s = fma(-cvt<CT>(Fold[pr.x]), cvt<CT>(Fold[pr.y]), s);
+  for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < nnz; base += kAoU * stride) {
+    CT sv[kAoU], dv[kAoU], fo[kAoU];
+    int b[kAoU], cnt[kAoU];
+    bool isl[kAoU];
+    int most = 0;
+#pragma unroll
+    for (int u = 0; u < kAoU; ++u) {
+      const int p = base + u * stride;
+      b[u] = 0;
+      cnt[u] = 0;
+      sv[u] = (CT)0;
+      dv[u] = (CT)1;
+      fo[u] = (CT)0;
+      isl[u] = false;
+      if (p < nnz) {
+        sv[u] = (CT)__ldcs(Aval + p);
+        b[u] = __ldcs(pptr + p);
+        cnt[u] = __ldg(pptr + p + 1) - b[u];
+        const int d = __ldcs(dpos + p);
+        isl[u] = d >= 0;
+        if (isl[u]) dv[u] = cvt<CT>(Fold[d]);
+        fo[u] = cvt<CT>(Fold[p]);
+      }
+      most = max(most, cnt[u]);
     }
-    const CT nv = d >= 0 ? s / cvt<CT>(Fold[d]) : s;
-    const CT df = nv - cvt<CT>(Fold[p]);
-    acc = fma(df, df, acc);
-    Fnew[p] = cvt<FT>(nv);
+    for (int k = 0; k < most; ++k) {
+      int2 pr[kAoU];
+#pragma unroll
+      for (int u = 0; u < kAoU; ++u) pr[u] = k < cnt[u] ? __ldg(pairs + b[u] + k) : make_int2(-1, -1);
+      CT lv[kAoU], uv[kAoU];
+#pragma unroll
+      for (int u = 0; u < kAoU; ++u) {
+        lv[u] = pr[u].x >= 0 ? cvt<CT>(Fold[pr[u].x]) : (CT)0;
+        uv[u] = pr[u].x >= 0 ? cvt<CT>(Fold[pr[u].y]) : (CT)0;
+      }
+#pragma unroll
+      for (int u = 0; u < kAoU; ++u)
+        if (k < cnt[u]) sv[u] = fma(-lv[u], uv[u], sv[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kAoU; ++u) {
+      const int p = base + u * stride;
+      if (p < nnz) {
+        const CT nv = isl[u] ? sv[u] / dv[u] : sv[u];
+        const CT df = nv - fo[u];
+        acc = fma(df, df, acc);
+        Fnew[p] = cvt<FT>(nv);
+      }
+    }
   }
   finish_sum((double)acc, partials, counter, step);
 }
@@ -463,6 +507,230 @@ void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, co
   else
     k_factor_gather<__nv_bfloat16><<<grid, 256, 0, s>>>(count, map, (const __nv_bfloat16 *)src,
                                                         (__nv_bfloat16 *)dst);
+}
+
+// ------------------------------------------------------ BCSR, A order
+// The block sweep in A's block order (block sizes up to 5: a block's BS*BS
+// values on one warp's lanes, lane r*BS + c holding entry (r, c)), on the
+// block analogue of F: F[p] = L_IJ (I > J) or U_IJ (I <= J) as a BS*BS
+// row-major block, L's identity diagonal blocks implicit.  Per block, from
+// the pair records of the scalar sweep (pattern-level):
+//     S = A_IJ - sum_K L_IK U_KJ      (each product an FMA chain over q, then
+//                                      subtracted, as the row-walking kernel)
+//     F_new[p] = I > J ? S inv(U_JJ) : S
+// inv(U_JJ) of the previous iterate comes from k_bcsr_diag_inverse_warp,
+// once per sweep and block row, not once per L block.  A warp keeps two
+// blocks in flight.
+template <typename FT, typename CT, int BS>
+__global__ void __launch_bounds__(kPTPB) k_bcsr_parilu_sweep_ao(int nnzb, const double *__restrict__ Aval,
+                                                                const int *__restrict__ Acol,
+                                                                const int *__restrict__ dpos,
+                                                                const int *__restrict__ pptr,
+                                                                const int2 *__restrict__ pairs,
+                                                                const CT *__restrict__ Dinv,
+                                                                const FT *__restrict__ Fold, FT *__restrict__ Fnew,
+                                                                double *partials, int *counter, double *step) {
+  constexpr int LD = BS * BS;
+  constexpr int U = 2;
+  const int lane = threadIdx.x & 31;
+  const bool on = lane < LD;
+  const int r = lane / BS, c = lane % BS;
+  const int e = on ? lane : 0;
+  CT acc = (CT)0;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int base = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; base < nnzb; base += U * nw) {
+    CT sv[U], fo[U], di[U];
+    int b[U], cnt[U];
+    bool isl[U];
+    int most = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int p = base + u * nw;
+      sv[u] = fo[u] = di[u] = (CT)0;
+      b[u] = cnt[u] = 0;
+      isl[u] = false;
+      if (p < nnzb) {
+        sv[u] = on ? (CT)__ldcs(Aval + (size_t)p * LD + e) : (CT)0;
+        fo[u] = on ? cvt<CT>(Fold[(size_t)p * LD + e]) : (CT)0;
+        b[u] = __ldg(pptr + p);
+        cnt[u] = __ldg(pptr + p + 1) - b[u];
+        isl[u] = __ldg(dpos + p) >= 0;
+        if (isl[u]) di[u] = on ? Dinv[(size_t)__ldg(Acol + p) * LD + e] : (CT)0;
+      }
+      most = max(most, cnt[u]);
+    }
+    for (int k = 0; k < most; ++k) {
+      CT lv[U], uv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        lv[u] = uv[u] = (CT)0;
+        if (k < cnt[u]) {
+          const int2 pr = __ldg(pairs + b[u] + k);
+          lv[u] = on ? cvt<CT>(Fold[(size_t)pr.x * LD + e]) : (CT)0;
+          uv[u] = on ? cvt<CT>(Fold[(size_t)pr.y * LD + e]) : (CT)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (k < cnt[u]) {  // warp-uniform: the whole warp works on block u
+          CT t = (CT)0;
+#pragma unroll
+          for (int q = 0; q < BS; ++q)
+            t = fma(__shfl_sync(0xffffffffu, lv[u], r * BS + q), __shfl_sync(0xffffffffu, uv[u], q * BS + c), t);
+          sv[u] -= t;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int p = base + u * nw;
+      if (p >= nnzb) continue;  // warp-uniform
+      CT nv = sv[u];
+      if (isl[u]) {
+        CT t = (CT)0;
+#pragma unroll
+        for (int q = 0; q < BS; ++q)
+          t = fma(__shfl_sync(0xffffffffu, sv[u], r * BS + q), __shfl_sync(0xffffffffu, di[u], q * BS + c), t);
+        nv = t;
+      }
+      if (on) {
+        const CT df = nv - fo[u];
+        acc = fma(df, df, acc);
+        Fnew[(size_t)p * LD + e] = cvt<FT>(nv);
+      }
+    }
+  }
+  finish_sum((double)acc, partials, counter, step);
+}
+
+// inv of each block row's diagonal block of F, one block per warp: lane
+// r*BS + c holds entry (r, c) of [D | I] in two registers, and each
+// Gauss-Jordan step shares the pivot row and column by shuffles - the
+// operations and their order are blk_inverse's.  A non-finite inverse sets
+// the breakdown bit.
+template <typename FT, typename CT, int BS>
+__global__ void __launch_bounds__(kPTPB) k_bcsr_diag_inverse_warp(int nb, const int *__restrict__ diag,
+                                                                  const FT *__restrict__ F, CT *__restrict__ Dinv,
+                                                                  int *status) {
+  constexpr int LD = BS * BS;
+  const int lane = threadIdx.x & 31;
+  const bool on = lane < LD;
+  const int r = lane / BS, c = lane % BS;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  bool bad = false;
+  for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < nb; I += nw) {
+    CT wl = on ? cvt<CT>(F[(size_t)__ldg(diag + I) * LD + lane]) : (CT)0;  // D
+    CT wr = (on && r == c) ? (CT)1 : (CT)0;                                 // I
+#pragma unroll
+    for (int p = 0; p < BS; ++p) {
+      const CT rp = (CT)1 / __shfl_sync(0xffffffffu, wl, p * BS + p);
+      if (r == p) {
+        wl *= rp;
+        wr *= rp;
+      }
+      const CT f = __shfl_sync(0xffffffffu, wl, (r * BS + p) & 31);  // w[r][p], untouched for r != p
+      const CT pl = __shfl_sync(0xffffffffu, wl, p * BS + c), pr = __shfl_sync(0xffffffffu, wr, p * BS + c);
+      if (r != p) {
+        wl -= f * pl;
+        wr -= f * pr;
+      }
+    }
+    if (on) {
+      if (!(wr == wr) || isinf((double)wr)) bad = true;
+      Dinv[(size_t)I * LD + lane] = wr;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(status, kStatusBreakdown);
+}
+
+// block values from F to BCSRL / BCSCU positions: dst block q = src block
+// map[q], or the identity (L's diagonal blocks) for map[q] < 0
+template <typename T>
+__global__ void k_factor_gather_blk(int count, int bs, const int *__restrict__ map, const T *__restrict__ src,
+                                    T *__restrict__ dst) {
+  const int ld = bs * bs;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)count * ld;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int blk = (int)(q / ld), e = (int)(q % ld);
+    const int m = map[blk];
+    dst[q] = m >= 0 ? src[(size_t)m * ld + e] : cvt<T>((e / bs == e % bs) ? 1.0f : 0.0f);
+  }
+}
+
+template <typename FT, typename CT>
+static void bcsr_sweep_ao_bs(cudaStream_t s, int grid, int bs, int nnzb, const double *Aval, const int *Acol,
+                             const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv, const void *Fold,
+                             void *Fnew, double *partials, int *counter, double *step) {
+#define LACE_BSW(BSV)                                                                                   \
+  k_bcsr_parilu_sweep_ao<FT, CT, BSV><<<grid, kPTPB, 0, s>>>(nnzb, Aval, Acol, dpos, pptr, pairs,       \
+                                                             (const CT *)Dinv, (const FT *)Fold,        \
+                                                             (FT *)Fnew, partials, counter, step)
+  switch (bs) {
+    case 1: LACE_BSW(1); break;
+    case 2: LACE_BSW(2); break;
+    case 3: LACE_BSW(3); break;
+    case 4: LACE_BSW(4); break;
+    default: LACE_BSW(5); break;
+  }
+#undef LACE_BSW
+}
+
+template <typename FT, typename CT>
+static void diag_inverse_warp_bs(cudaStream_t s, int grid, int nb, int bs, const int *diag, const void *F,
+                                 void *Dinv, int *status) {
+#define LACE_DIW(BSV) \
+  k_bcsr_diag_inverse_warp<FT, CT, BSV><<<grid, kPTPB, 0, s>>>(nb, diag, (const FT *)F, (CT *)Dinv, status)
+  switch (bs) {
+    case 1: LACE_DIW(1); break;
+    case 2: LACE_DIW(2); break;
+    case 3: LACE_DIW(3); break;
+    case 4: LACE_DIW(4); break;
+    default: LACE_DIW(5); break;
+  }
+#undef LACE_DIW
+}
+
+static int warp_grid(int items) {
+  int grid = (items + kPTPB / 32 - 1) / (kPTPB / 32);
+  const int cap = num_sms() * (2048 / kPTPB);
+  return grid < 1 ? 1 : (grid > cap ? cap : grid);
+}
+
+void launch_bcsr_parilu_sweep_ao(cudaStream_t s, int nnzb, int bs, VType t, const double *Aval, const int *Acol,
+                                 const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv,
+                                 const void *Fold, void *Fnew, double *partials, int *counter, double *step) {
+  const int grid = warp_grid(nnzb);
+  if (t == VType::F64)
+    bcsr_sweep_ao_bs<double, double>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials,
+                                     counter, step);
+  else if (t == VType::F32)
+    bcsr_sweep_ao_bs<float, float>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials,
+                                   counter, step);
+  else
+    bcsr_sweep_ao_bs<__nv_bfloat16, float>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew,
+                                           partials, counter, step);
+}
+
+void launch_bcsr_diag_inverse_ao(cudaStream_t s, int nb, int bs, const int *diag, VType t, const void *F,
+                                 void *Dinv, int *status) {
+  const int grid = warp_grid(nb);
+  if (t == VType::F64) diag_inverse_warp_bs<double, double>(s, grid, nb, bs, diag, F, Dinv, status);
+  else if (t == VType::F32) diag_inverse_warp_bs<float, float>(s, grid, nb, bs, diag, F, Dinv, status);
+  else diag_inverse_warp_bs<__nv_bfloat16, float>(s, grid, nb, bs, diag, F, Dinv, status);
+}
+
+void launch_factor_gather_blk(cudaStream_t s, int count, int bs, const int *map, VType t, const void *src,
+                              void *dst) {
+  const long long tot = (long long)count * bs * bs;
+  int grid = (int)std::min<long long>((tot + 255) / 256, (long long)num_sms() * 16);
+  if (grid < 1) return;
+  if (t == VType::F64)
+    k_factor_gather_blk<double><<<grid, 256, 0, s>>>(count, bs, map, (const double *)src, (double *)dst);
+  else if (t == VType::F32)
+    k_factor_gather_blk<float><<<grid, 256, 0, s>>>(count, bs, map, (const float *)src, (float *)dst);
+  else
+    k_factor_gather_blk<__nv_bfloat16><<<grid, 256, 0, s>>>(count, bs, map, (const __nv_bfloat16 *)src,
+                                                            (__nv_bfloat16 *)dst);
 }
 
 void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *Lold, void *Lnew,

@@ -1,15 +1,15 @@
 // Sparse triangular solves x = T^{-1} b on the GPU.
 //
 // Exact solves replace LACE's mkl_dcsrtrsv calls
-// (src/fgmres_householder_restart.cpp:320-332); the Jacobi sweep replaces
-// data_parcsrtrsv (src/trisolve.cpp:256-351) in synchronous form.
+// (src/fgmres_householder_restart.cpp:320-332).  The Jacobi sweeps are a
+// GPU-native inexact mode (LACE_TRSV_JACOBI), not LACE's data_parcsrtrsv,
+// whose in-place order partrsv.cu reproduces.
 //
 // Here: the level-scheduled solve, the Jacobi sweeps and the BCSR solve (the
 // default CSR solve, block-scheduled and sync-free, is in sptrsv_blk.cu).  The
-// BCSR solve takes block rows in dependency order from an atomic ticket, so a
-// warp only ever waits for block rows already held by running warps, and
-// waits for them through per-block-row ready flags (acquire/release, bounded
-// spin) that carry an epoch advancing every launch, so they are never reset.
+// BCSR solve takes chunks of block rows in solve order from an atomic ticket,
+// so a warp only ever waits for rows already held by running warps, and
+// waits for their values themselves (bounded spin).
 #include "internal.h"
 
 namespace lace {
@@ -172,117 +172,265 @@ void launch_jacobi_sweep(cudaStream_t s, const TriDev &t, VType vt, const void *
 }
 
 // ------------------------------------------------------------- BCSR
-// Block rows in chunks of 32 block rows per warp is not needed for the
-// block-stencil systems: one thread per scalar row of a block row, the bs
-// threads of a block row sit in one warp segment.  Block rows are taken by
-// ticket in dependency order; the block row's diagonal block is applied
-// through its precomputed inverse (upper) or is the identity (lower).
-template <typename CT, typename VT, bool LOWER>
-__global__ void __launch_bounds__(kSTPB) k_bcsr_sptrsv(int nb, int bs, const int *__restrict__ row,
+// One warp per chunk of consecutive block rows in solve order (rows upwards
+// for L, downwards for U), chunks taken by atomic ticket in solve order, so a
+// warp only ever waits for rows that earlier tickets hold.  A chunk holds at
+// most 64 block rows and never crosses a place where a block row does not
+// depend on the one solved before it (host-built chunk table), so chunks
+// follow the grid lines: a chunk that straddled the end of one line and the
+// start of the next would make every line wait for the whole previous one.
+// A solved value is its own ready flag: the output starts as an all-ones bit
+// pattern (a NaN arithmetic does not produce; a result with those bits is
+// stored as a quiet NaN), so no flags, fences or epochs.  Lanes sub*BS + r
+// work on scalar row r of a block: sub-group `sub` takes the row's
+// off-diagonal blocks sub, sub + 32/BS, ...; lane r of a sub-group waits for
+// entry r of the block's x segment and the sub-group shares the segment by
+// shuffles; the previous block row of the chunk (the chain along a grid
+// line) comes from registers.  While a row waits and computes, the warp
+// loads the next row's structure, block values and far dependencies.  The
+// diagonal block is the identity (lower) or applied through its precomputed
+// inverse (upper).
+template <typename XT> struct Unsolved;
+template <> struct Unsolved<float> {
+  __device__ static bool is(float v) { return __float_as_uint(v) == 0xffffffffu; }
+  __device__ static float fix(float v) { return is(v) ? __uint_as_float(0x7fc00000u) : v; }
+  __device__ static float load(const float *p) {
+    float v;
+    asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+  }
+  __device__ static void store(float *p, float v) {
+    asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+  }
+};
+template <> struct Unsolved<double> {
+  __device__ static bool is(double v) { return (unsigned long long)__double_as_longlong(v) == ~0ull; }
+  __device__ static double fix(double v) { return is(v) ? __longlong_as_double(0x7ff8000000000000ll) : v; }
+  __device__ static double load(const double *p) {
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+  }
+  __device__ static void store(double *p, double v) {
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+  }
+};
+
+// What a lane needs for one block row: its off-diagonal block (the k-th of
+// the row for k = k0 + sub), that block's row r, entry r of the block's x
+// segment if it is already there, the right-hand side and (upper) row r of
+// the diagonal block's inverse.
+template <typename CT, typename XT, int BS>
+struct BcsrRow {
+  int I, J, p;
+  bool more;  // more off-diagonal blocks than this round
+  CT a[BS];
+  XT xv;
+  bool have;  // xv holds a solved value (or is not needed)
+  CT bv;
+  CT d[BS];
+};
+
+template <typename CT, typename VT, typename XT, int BS, bool LOWER>
+__device__ __forceinline__ void bcsr_fetch(BcsrRow<CT, XT, BS> &w, int I, int prevI, int k0,
+                                           const int *__restrict__ row, const int *__restrict__ col,
+                                           const VT *__restrict__ val, const VT *__restrict__ dinv,
+                                           const void *b, int in_f32, const XT *x, int sub, int r,
+                                           bool active) {
+  constexpr int PER = 32 / BS;
+  constexpr int LD = BS * BS;
+  w.I = I;
+  const int rb = __ldg(row + I), re = __ldg(row + I + 1);
+  w.J = -1;
+  w.p = -1;
+  w.more = false;
+  int k = 0;
+  for (int e = rb; e < re; ++e) {
+    const int c = __ldg(col + e);
+    if (LOWER ? c >= I : c <= I) continue;
+    if (k == k0 + sub) {
+      w.J = c;
+      w.p = e;
+    }
+    if (k >= k0 + PER) w.more = true;
+    ++k;
+  }
+  const bool mine = active && w.J >= 0;
+#pragma unroll
+  for (int cc = 0; cc < BS; ++cc) w.a[cc] = mine ? cvt<CT>(__ldg(val + (size_t)w.p * LD + r * BS + cc)) : (CT)0;
+  w.have = !mine || w.J == prevI;  // the previous row comes from registers
+  w.xv = (XT)0;
+  if (mine && w.J != prevI) {
+    w.xv = Unsolved<XT>::load(x + (size_t)w.J * BS + r);
+    w.have = !Unsolved<XT>::is(w.xv);
+  }
+  w.bv = sub == 0 ? ldin<CT>(b, in_f32, I * BS + r) : (CT)0;
+  if (!LOWER) {
+#pragma unroll
+    for (int cc = 0; cc < BS; ++cc) w.d[cc] = cvt<CT>(__ldg(dinv + (size_t)I * LD + r * BS + cc));
+  }
+}
+
+template <typename CT, typename VT, typename XT, int BS, bool LOWER>
+__global__ void __launch_bounds__(kSTPB) k_bcsr_sptrsv(int nb, const int *__restrict__ row,
                                                        const int *__restrict__ col,
                                                        const VT *__restrict__ val,
-                                                       const VT *__restrict__ dinv, const void *b,
-                                                       int in_f32, void *x, int out_f32, int *ready,
-                                                       int *tickets, int *epoch_slot, const int *done_flag,
-                                                       int *status) {
+                                                       const VT *__restrict__ dinv,
+                                                       const int *__restrict__ chunk_first, int nch,
+                                                       const void *b, int in_f32, XT *x, int *tickets,
+                                                       const int *done_flag, int *status) {
   if (done_flag != nullptr && *(volatile const int *)done_flag) return;
+  constexpr int PER = 32 / BS;  // sub-groups
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const int epoch = *(volatile int *)epoch_slot + 1;
-  const int per = 32 / bs;          // block rows per warp pass
-  const int ld = bs * bs;
-  const int sub = lane / bs, r = lane % bs;
-  const int nch = (nb + per - 1) / per;  // chunks of `per` block rows
+  const int sub = lane / BS, r = lane % BS;
+  const bool active = sub < PER;
+  const int src0 = lane - r;  // lane 0 of this lane's sub-group
+  bool gave_up = false;
+  // bounded warp-uniform wait until every lane's x entry is solved
+  auto wait_x = [&](XT &xv, bool &have, int J) {
+    int spins = 0;
+    while (!__all_sync(0xffffffffu, have)) {
+      if (!have) {
+        xv = Unsolved<XT>::load(x + (size_t)J * BS + r);
+        have = !Unsolved<XT>::is(xv);
+      }
+      ++spins;
+      if ((spins & 1023) == 1023 && (ld_relaxed(status) & kStatusSpinTimeout)) gave_up = true;
+      if (spins > kMaxSpins) {
+        if (lane == 0) atomicOr(status, kStatusSpinTimeout);
+        gave_up = true;
+      }
+      if (gave_up) have = true;  // the solve is reported as failed
+      if (spins > 16) __nanosleep(32);
+    }
+  };
+  BcsrRow<CT, XT, BS> cur, nxt;
   while (true) {
     int t = 0;
     if (lane == 0) t = atomicAdd(&tickets[0], 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= nch) break;
-    const int c = LOWER ? t : nch - 1 - t;
-    // block rows of the chunk are processed one after the other (in solve
-    // order) by the whole warp; lanes sub*bs + r hold scalar row r
-    const int first = c * per;
-    const int cnt = min(per, nb - first);
+    const int first = __ldg(chunk_first + t), cnt = __ldg(chunk_first + t + 1) - first;
+    CT prev = (CT)0;  // lanes 0..BS-1: the previous block row of the chunk
+    int prevI = -1;
+    bcsr_fetch<CT, VT, XT, BS, LOWER>(nxt, LOWER ? first : nb - 1 - first, -1, 0, row, col, val, dinv, b, in_f32,
+                                      x, sub, r, active);
     for (int q = 0; q < cnt; ++q) {
-      const int I = LOWER ? first + q : first + cnt - 1 - q;
+      cur = nxt;
+      if (q + 1 < cnt)
+        bcsr_fetch<CT, VT, XT, BS, LOWER>(nxt, LOWER ? first + q + 1 : nb - 2 - (first + q), cur.I, 0, row, col,
+                                          val, dinv, b, in_f32, x, sub, r, active);
+      const CT fromprev = __shfl_sync(0xffffffffu, prev, r);
+      if (cur.J >= 0 && cur.J == prevI && active) cur.xv = (XT)fromprev;
+      wait_x(cur.xv, cur.have, cur.J);
       CT acc = (CT)0;
-      if (sub == 0) acc = ldin<CT>(b, in_f32, I * bs + r);
-      // lanes with sub > 0 help: each sub-group takes every per-th block
-      if (lane < per * bs) {
-        int k = 0;
-        for (int p = row[I]; p < row[I + 1]; ++p) {
-          const int J = col[p];
-          if (LOWER ? J >= I : J <= I) continue;
-          if ((k++ % per) != sub) continue;
-          const int cj = J / per;
-          if (cj != c) wait_flag(&ready[cj], epoch, status);
-          const VT *blk = val + (size_t)p * ld + r * bs;
-          CT s = (CT)0;
-          for (int cc = 0; cc < bs; ++cc) s += cvt<CT>(blk[cc]) * ldx<CT>(x, out_f32, J * bs + cc);
-          acc -= s;
-        }
+      {
+        CT s = (CT)0;
+#pragma unroll
+        for (int cc = 0; cc < BS; ++cc) s = fma(cur.a[cc], (CT)__shfl_sync(0xffffffffu, cur.xv, src0 + cc), s);
+        if (active && cur.J >= 0) acc -= s;
       }
-      // sum the sub-groups' partials onto sub 0
-      for (int g = 1; g < per; ++g) {
-        CT v = __shfl_sync(0xffffffffu, acc, (g * bs + r) & 31);
-        if (sub == 0 && g * bs + r < 32) acc += v;
+      // further rounds of off-diagonal blocks (none on a 7-point stencil)
+      for (int k0 = PER; __any_sync(0xffffffffu, cur.more); k0 += PER) {
+        BcsrRow<CT, XT, BS> extra;
+        bcsr_fetch<CT, VT, XT, BS, LOWER>(extra, cur.I, prevI, k0, row, col, val, dinv, b, in_f32, x, sub, r,
+                                          active);
+        if (extra.J >= 0 && extra.J == prevI && active) extra.xv = (XT)fromprev;
+        wait_x(extra.xv, extra.have, extra.J);
+        CT s = (CT)0;
+#pragma unroll
+        for (int cc = 0; cc < BS; ++cc) s = fma(extra.a[cc], (CT)__shfl_sync(0xffffffffu, extra.xv, src0 + cc), s);
+        if (active && extra.J >= 0) acc -= s;
+        cur.more = extra.more;
       }
-      // apply the diagonal: identity (lower) or dinv (upper); row r of dinv
+      // the sub-groups' partial sums onto sub-group 0
+#pragma unroll
+      for (int g = 1; g < PER; ++g) {
+        const CT v = __shfl_sync(0xffffffffu, acc, (g * BS + r) & 31);
+        if (sub == 0) acc += v;
+      }
+      acc += cur.bv;
       CT xr = acc;
       if (!LOWER) {
         CT t2 = (CT)0;
-        for (int cc = 0; cc < bs; ++cc) {
-          CT ac = __shfl_sync(0xffffffffu, acc, cc);
-          t2 += cvt<CT>(dinv[(size_t)I * ld + r * bs + cc]) * ac;
-        }
+#pragma unroll
+        for (int cc = 0; cc < BS; ++cc) t2 = fma(cur.d[cc], __shfl_sync(0xffffffffu, acc, cc), t2);
         xr = t2;
       }
-      if (sub == 0) stout<CT>(x, out_f32, I * bs + r, xr);
-      __threadfence();
-      __syncwarp();
+      if (lane < BS) {
+        const XT out = Unsolved<XT>::fix((XT)xr);
+        Unsolved<XT>::store(x + (size_t)cur.I * BS + r, out);
+        prev = (CT)out;
+      }
+      prevI = cur.I;
     }
-    if (lane == 0) st_release(&ready[c], epoch);
   }
   if (lane == 0) {
     const int e = atomicAdd(&tickets[1], 1);
     if (e == nwarps - 1) {
       tickets[0] = 0;
       tickets[1] = 0;
-      *epoch_slot = epoch;
       __threadfence();
     }
+  }
+}
+
+template <typename CT, typename VT, typename XT, int BS>
+static void bcsr_launch(cudaStream_t s, int grid, const TriDev &t, const void *dinv, const void *b, int in_f32,
+                        void *x, int *tickets, const int *dfl, int *status) {
+  const int nb = t.n / BS;
+  if (t.lower)
+    k_bcsr_sptrsv<CT, VT, XT, BS, true><<<grid, kSTPB, 0, s>>>(nb, t.row, t.col, (const VT *)t.val,
+                                                              (const VT *)dinv, t.bchunk_first, t.bnch, b,
+                                                              in_f32, (XT *)x, tickets, dfl, status);
+  else
+    k_bcsr_sptrsv<CT, VT, XT, BS, false><<<grid, kSTPB, 0, s>>>(nb, t.row, t.col, (const VT *)t.val,
+                                                               (const VT *)dinv, t.bchunk_first, t.bnch, b,
+                                                               in_f32, (XT *)x, tickets, dfl, status);
+}
+
+template <typename CT, typename VT, typename XT>
+static void bcsr_launch_bs(cudaStream_t s, int grid, int bs, const TriDev &t, const void *dinv, const void *b,
+                           int in_f32, void *x, int *tickets, const int *dfl, int *status) {
+  switch (bs) {
+    case 1: bcsr_launch<CT, VT, XT, 1>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 2: bcsr_launch<CT, VT, XT, 2>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 3: bcsr_launch<CT, VT, XT, 3>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 4: bcsr_launch<CT, VT, XT, 4>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 5: bcsr_launch<CT, VT, XT, 5>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 6: bcsr_launch<CT, VT, XT, 6>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    case 7: bcsr_launch<CT, VT, XT, 7>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    default: bcsr_launch<CT, VT, XT, 8>(s, grid, t, dinv, b, in_f32, x, tickets, dfl, status); break;
   }
 }
 
 void launch_bcsr_sptrsv(cudaStream_t s, const TriDev &t, int bs, VType vt, const void *dinv,
                         const void *b, int in_f32, void *x, int out_f32, Control *ctrl,
                         int grid_hint, bool honor_done) {
-  const int nb = t.n / bs;
+  const int nch = t.bnch;
   const int *dfl = honor_done ? &ctrl->done : nullptr;
-  const int per = 32 / bs;
-  const int nch = (nb + per - 1) / per;
   int grid = grid_hint > 0 ? grid_hint : num_sms() * 8;
   int maxgrid = (nch * 32 + kSTPB - 1) / kSTPB;
   if (grid > maxgrid) grid = maxgrid;
   if (grid < 1) grid = 1;
   int *tickets = ctrl->tickets[t.slot];
-  int *epoch_slot = &ctrl->trsv_epoch[t.slot];
   int *status = &ctrl->status;
-#define LACE_BCSR_LAUNCH(CT, VT)                                                                   \
-  if (t.lower)                                                                                     \
-    k_bcsr_sptrsv<CT, VT, true><<<grid, kSTPB, 0, s>>>(nb, bs, t.row, t.col, (const VT *)t.val,  \
-                                                       (const VT *)dinv, b, in_f32, x, out_f32,    \
-                                                       t.ready, tickets, epoch_slot, dfl, status);  \
-  else                                                                                             \
-    k_bcsr_sptrsv<CT, VT, false><<<grid, kSTPB, 0, s>>>(nb, bs, t.row, t.col, (const VT *)t.val, \
-                                                        (const VT *)dinv, b, in_f32, x, out_f32,   \
-                                                        t.ready, tickets, epoch_slot, dfl, status);
-  switch (vt) {
-    case VType::F64: LACE_BCSR_LAUNCH(double, double); break;
-    case VType::F32: LACE_BCSR_LAUNCH(float, float); break;
-    case VType::BF16: LACE_BCSR_LAUNCH(float, __nv_bfloat16); break;
+  // the output starts unsolved (x must not overlap b)
+  cudaMemsetAsync(x, 0xFF, (size_t)t.n * (out_f32 ? 4 : 8), s);
+  if (out_f32) {
+    switch (vt) {
+      case VType::F64: bcsr_launch_bs<double, double, float>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+      case VType::F32: bcsr_launch_bs<float, float, float>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+      case VType::BF16: bcsr_launch_bs<float, __nv_bfloat16, float>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    }
+  } else {
+    switch (vt) {
+      case VType::F64: bcsr_launch_bs<double, double, double>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+      case VType::F32: bcsr_launch_bs<float, float, double>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+      case VType::BF16: bcsr_launch_bs<float, __nv_bfloat16, double>(s, grid, bs, t, dinv, b, in_f32, x, tickets, dfl, status); break;
+    }
   }
-#undef LACE_BCSR_LAUNCH
 }
 
 }  // namespace lace
