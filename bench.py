@@ -23,8 +23,9 @@ exists on the GPU host) on all host cores.
 `config3` times the block system (BCSR 5x5 on 64^3 cells, n = 1,310,720)
 the same way: FP32 factors and solves inside the FP64 FGMRES against the
 all-FP64 path, with its own CPU baseline (the oracle's BCSR path).
-`parilu_parity` reports LACE's one-thread in-place ParILU residual after the
-same sweep count beside the GPU's synchronous one.
+`config4` times the adjoint configuration's forward and backward solves
+(64^3).  `parilu_parity` reports LACE's one-thread in-place ParILU residual
+after the same sweep count beside the GPU's synchronous one.
 """
 from __future__ import annotations
 
@@ -416,6 +417,9 @@ def run_ours(args):
     cfg3 = None
     if not args.skip_config3:
         cfg3 = run_config3(args, lg, torch, stream, local, hbm_peak, rank, world)
+    cfg4 = None
+    if not args.skip_config4:
+        cfg4 = run_config4(args, lg, torch, stream, local)
 
     # launches per solve: ParILU (4 initial-guess copies, the sweeps, 2 gathers,
     # the residual), 2 solve-plan value gathers, and per cycle the residual,
@@ -460,6 +464,7 @@ def run_ours(args):
                     "arnoldi_step_s": step_s},
         "parilu_parity": parity,
         "config3": cfg3,
+        "config4": cfg4,
         "roofline": {"bound": "hbm", "kernel": f"k_hh_step: one Arnoldi step (j = {STEP_J}, 16 basis columns; "
                      "operator, both dot-product sets, new reflector, next Krylov vector), mixed precision",
                      "achieved": step_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": step_gbs / hbm_peak,
@@ -520,6 +525,49 @@ def parilu_parity(ctx, A, pin):
             "note": "LACE's in-place sweep reads values updated earlier in the same sweep (one thread: "
                     "exact ILU(0) after one sweep on this ordering); the synchronous sweeps read only the "
                     "previous sweep's values, so their residual after the same count is larger"}
+
+
+WORKLOAD4 = ("convdiff3d 64^3 (n=262144, nnz=1810432), L = 0.5||x - x_t||^2, x_t~N(0,1) seed 1, b~N(0,1) seed 0: "
+             "forward solve (FP32 ParILU(0) 3 sweeps + FP64 FGMRES-Householder(50) to 1e-10) and the backward "
+             "solve A^T lambda = x - x_t through the transposed factors to 1e-10, dL/db and dL/dA on A's pattern")
+
+
+def run_config4(args, lg, torch, stream, local):
+    """The adjoint configuration: forward and backward solve times (CUDA
+    events on the solver stream), mixed precision."""
+    from lace_gb300 import problems as P
+    A = P.convdiff3d(64)
+    rng = np.random.default_rng(1)
+    xt = torch.tensor(rng.standard_normal(A.n), dtype=torch.float64, device="cuda")
+    b = torch.tensor(P.rhs_normal(A.n, 0), dtype=torch.float64, device="cuda")
+    ctx = lg.Context(local, stream=stream)
+    ctx.set_options(precision="fp32")
+    ctx.upload(A)
+    x = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    gb = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    gA = torch.zeros(A.nnz, dtype=torch.float64, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fwd, bwd, its = [], [], None
+    for it in range(2 + max(3, args.steps)):
+        with torch.cuda.stream(stream):
+            x.zero_()
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        ctx.parilu0(SWEEPS, residual=False)
+        r = ctx.fgmres(b, x, search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+        ev[1].record(stream)
+        with torch.cuda.stream(stream):
+            dLdx = x - xt
+        its = ctx.backward(x, dLdx, gb, gA, search_max=M, restart_max=RESTART_MAX, rtol=RTOL)
+        ev[2].record(stream)
+        ev[2].synchronize()
+        if it >= 2:
+            fwd.append(ev[0].elapsed_time(ev[1]) / 1e3)
+            bwd.append(ev[1].elapsed_time(ev[2]) / 1e3)
+    ctx.close()
+    return {"workload": WORKLOAD4, "forward": {"value": statistics.median(fwd), "unit": "s",
+                                               "iterations": r.total_iterations},
+            "backward": {"value": statistics.median(bwd), "unit": "s", "iterations": its}}
 
 
 def run_config3(args, lg, torch, stream, local, hbm_peak, rank, world):
@@ -640,6 +688,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-config3", action="store_true")
+    ap.add_argument("--skip-config4", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel (the Arnoldi step), if captured")
     ap.add_argument("--trsv-schedule", default=None,

@@ -469,6 +469,16 @@ int lace_gpu_fgmres_mgs(lace_gpu_ctx *ctx, const double *b, double *x,
  * Householder step (LACE_GB300_HH_STEP=0: passes A, B, C).  out: 4 ints. */
 int lace_gpu_get_solve_stats(lace_gpu_ctx *ctx, int *out);
 
+/* The orthogonality monitor of the last FGMRES solve on ctx (options
+ * monitor_orthog = 1): LACE's data_orthogonality_error
+ * (src/orthogonality_error.cpp:46-83), ||I - Q^T Q||_inf of the Krylov
+ * vectors after every search direction, over all cycles in order, which LACE
+ * prints as it goes.  ctx NULL: the context of the LACE-named calls
+ * (data_fgmres_householder_restart with gmres_par->monitorOrthog = 1).
+ * Writes min(capacity, *count) values to out; *count is the number of
+ * directions (0 when the monitor was off). */
+int lace_gpu_get_orthog_history(lace_gpu_ctx *ctx, double *out, int capacity, int *count);
+
 /* Measurement: the mean device time of one launch of the one-kernel Arnoldi
  * step j (method 0 Householder, 1 Gram-Schmidt), replayed reps times on the
  * basis the last FGMRES solve of this context left (j + 2 <= its

@@ -193,6 +193,7 @@ SIGNATURES = {
     "lace_gpu_last_error": (_i, []),
     "lace_gpu_selftest_wait_limit": (_i, [_i, C.POINTER(_i)]),
     "lace_gpu_inject_alloc_failure": (None, [_i]),
+    "lace_gpu_get_orthog_history": (_i, [_p, _p, _i, C.POINTER(_i)]),
     "lace_gpu_error_string": (C.c_char_p, [_i]),
     "lace_gpu_batch_create": (_i, [C.POINTER(_p), _p, _i, _p, _p, _p, _p, _p, _p, _i]),
     "lace_gpu_batch_destroy": (_i, [_p]),

@@ -188,6 +188,16 @@ class Context:
         return {"reorthogonalised": out[0], "conditional_nodes": bool(out[1]), "one_kernel_step": bool(out[2]),
                 "one_kernel_householder_step": bool(out[3])}
 
+    def orthog_history(self) -> np.ndarray:
+        """||I - Q^T Q||_inf after every direction of the last solve (the
+        monitor_orthog option)."""
+        cnt = C.c_int()
+        _chk(self._lib.lace_gpu_get_orthog_history(self.h, None, 0, C.byref(cnt)), "get_orthog_history")
+        out = np.zeros(max(1, cnt.value))
+        _chk(self._lib.lace_gpu_get_orthog_history(self.h, out.ctypes.data, cnt.value, C.byref(cnt)),
+             "get_orthog_history")
+        return out[:cnt.value]
+
     def time_arnoldi_step(self, orthogonalization: str = "householder", j: int = 15, reps: int = 20) -> float:
         """Seconds per launch of the one-kernel Arnoldi step j, replayed on the
         basis of the last solve (overwrites that solve's cycle state)."""

@@ -370,6 +370,20 @@ extern "C" int data_parcsrtrsv(const data_uplo_t uplo, const data_storage_t stor
   return 0;
 }
 
+extern "C" int lace_gpu_get_orthog_history(lace_gpu_ctx *c, double *out, int capacity, int *count) {
+  if (!count || (capacity > 0 && !out)) return set_err(DEV_ERR_INVALID_PTR);
+  std::unique_lock<std::mutex> lk(g_mu, std::defer_lock);
+  if (!c) {  // the LACE-named calls' context
+    lk.lock();
+    int rc = default_ctx(&c);
+    if (rc) return set_err(rc);
+  }
+  const int nh = (int)c->last_orth.size();
+  *count = nh;
+  for (int k = 0; k < nh && k < capacity; ++k) out[k] = c->last_orth[k];
+  return DEV_SUCCESS;
+}
+
 extern "C" int data_z_spmv(dataType alpha, data_d_matrix *A, data_d_matrix *x, dataType beta,
                            data_d_matrix *y) {
   if (!A || !x || !y) return set_err(DEV_ERR_INVALID_PTR);

@@ -631,6 +631,7 @@ int lace_gpu_ctx::analyse(int n_, const int *row, const int *col, int bs_) {
   rc |= map_uc2a.upload(uc2a.data(), 4 * uc2a.size(), stream);
   if (rc) return DEV_ERR_DEVICE_ALLOC;
   sweep_ao = false;
+  sweep_variant = -1;
   if (bs_ <= 5) {  // scalar entries, or blocks whose values fit one warp's lanes
     rc = build_sweep_records(row, col, L, Ur, l2a, ur2a, uc2a);
     if (rc) return rc;
@@ -1212,6 +1213,45 @@ int lace_gpu_ctx::init_factors() {
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
 }
 
+// the CSR sweep's launch shape that runs fastest on this pattern (each
+// candidate sweeps from the initial guess in Fold into Fnew, which the real
+// sweep then overwrites)
+int lace_gpu_ctx::autotune_sweep(const IluArgs &a, const void *Fold, void *Fnew) {
+  const VType t = vtype();
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int pick = 0;
+  double *dstep = (double *)scal_buf.p + 32;
+  for (int v = 0; v < parilu_sweep_variants(); ++v) {
+    float ms = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, stream);
+      launch_parilu_sweep_ao(stream, nnzA, t, (const double *)Aval.p, (const int *)sw_dpos.p, (const int *)sw_pptr.p,
+                             (const int2 *)sw_pairs.p, Fold, Fnew, a.partials, a.counter, dstep, v);
+      cudaEventRecord(e1, stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return DEV_ERR_UNKNOWN;
+      }
+      float tt = 0.f;
+      cudaEventElapsedTime(&tt, e0, e1);
+      if (rep > 0) ms += tt;
+    }
+    if (verbose) printf("%% parilu sweep autotune: variant %d: %.1f us\n", v, ms * 500.f);
+    if (ms < best) {
+      best = ms;
+      pick = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  sweep_variant = pick;
+  return 0;
+}
+
 int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool sync_each,
                          std::vector<double> *steps, double stop_below, int min_sweeps, bool reuse_init) {
   if (!n_blk) return DEV_ERR_NOT_INITIALIZED;
@@ -1239,9 +1279,13 @@ int lace_gpu_ctx::parilu(int sweeps, double *step_out, double *nonlin_out, bool 
                                   sw_dinv.p, Fv[fc].p, Fv[1 - fc].p, a.partials, a.counter, dstep + (s % 32));
       fc = 1 - fc;
     } else if (ao) {
+      if (sweep_variant < 0) {
+        rc = autotune_sweep(a, Fv[fc].p, Fv[1 - fc].p);
+        if (rc) return rc;
+      }
       launch_parilu_sweep_ao(stream, nnzA, t, (const double *)Aval.p, (const int *)sw_dpos.p,
                              (const int *)sw_pptr.p, (const int2 *)sw_pairs.p, Fv[fc].p, Fv[1 - fc].p, a.partials,
-                             a.counter, dstep + (s % 32));
+                             a.counter, dstep + (s % 32), sweep_variant);
       fc = 1 - fc;
     } else {
       launch_parilu_sweep(stream, a, t, Lv[cur].p, Lv[1 - cur].p, Ucv[cur].p, Ucv[1 - cur].p,
@@ -1965,6 +2009,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   bool converged = false;
   int last_cycle = 0, last_steps = 0;
   last_reorth = 0;
+  last_orth.clear();
   double rnorm0 = 0.0, final_res = 0.0;
   for (int restart = 0; restart < restart_max; ++restart) {
     launch_cycle_residual(stream, a, b, x, mgs);
@@ -2037,11 +2082,13 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
     if (capped && ns == m && !hc.converged && !(hc.status & kStatusBreakdown)) return DEV_ERR_NOT_SUPPORTED;
     if (hist)
       for (int k = 0; k < ns; ++k) hist->push_back(h_scal[k]);
-    if (opt.monitor_orthog && verbose) {
+    if (opt.monitor_orthog) {
       std::vector<double> oh(ns);
-      cudaMemcpy(oh.data(), cy->orth, 8 * (size_t)ns, cudaMemcpyDeviceToHost);
-      for (int k = 0; k < ns; ++k)
-        printf("%s_gpu_ortherr(%d) = %.16e;\n", mgs ? "FGMRES" : "FGMRES_Householders", total + k + 1, oh[k]);
+      if (ns > 0) LCHK(cudaMemcpy(oh.data(), cy->orth, 8 * (size_t)ns, cudaMemcpyDeviceToHost));
+      last_orth.insert(last_orth.end(), oh.begin(), oh.end());
+      if (verbose)
+        for (int k = 0; k < ns; ++k)
+          printf("%s_gpu_ortherr(%d) = %.16e;\n", mgs ? "FGMRES" : "FGMRES_Householders", total + k + 1, oh[k]);
     }
     total += ns;
     if (ns > 0) {

@@ -100,6 +100,8 @@ struct lace_gpu_ctx {
   // per-entry records (pair ranges, pairs of A positions, u_jj position)
   DBuf Fv[2], sw_pptr, sw_pairs, sw_dpos, sw_diag, sw_dinv;
   bool sweep_ao = false;
+  int sweep_variant = -1;  // the CSR sweep's launch shape (autotuned)
+  int autotune_sweep(const lace::IluArgs &a, const void *Fold, void *Fnew);
   int cur = 0;
   bool factors_ready = false;
   int fact_version = 0;  // bumped whenever the factor values change
@@ -144,6 +146,7 @@ struct lace_gpu_ctx {
   int last_reorth = 0;     // directions of the last Gram-Schmidt solve that reorthogonalised
   int last_m = 0;          // search directions per cycle of the last FGMRES solve
   std::vector<double> last_hist;
+  std::vector<double> last_orth;  // ||I - Q^T Q||_inf per direction of the last solve (monitor on)
 
   ~lace_gpu_ctx();
   lace::Control *ctrl() const { return (lace::Control *)ctrl_buf.p; }

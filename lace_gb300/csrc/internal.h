@@ -191,9 +191,12 @@ void launch_parilu_sweep(cudaStream_t s, const IluArgs &a, VType t, const void *
                          const void *Uold, void *Unew, double *step);
 // one synchronous sweep over A's entries in A's order on F (factor values in
 // A's order), from the host-built pair records (parilu.cu); *step as above
+// variant: the kernel's entries and pairs in flight per thread and its
+// register budget (0 .. parilu_sweep_variants() - 1), chosen by the autotune
 void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos,
                             const int *pptr, const int2 *pairs, const void *Fold, void *Fnew, double *partials,
-                            int *counter, double *step);
+                            int *counter, double *step, int variant);
+int parilu_sweep_variants();
 // dst[q] = map[q] >= 0 ? src[map[q]] : 1, value type t
 void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, const void *src, void *dst);
 // the block sweep in A's block order (bs <= 5), Dinv: the block inverses of

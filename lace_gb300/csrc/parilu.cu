@@ -402,27 +402,30 @@ static int sweep_grid(int rows) {
 //     F_new[p] = i > j ? s / u_jj : s
 // The step sum (F_new - F_old)^2 is accumulated per thread in the compute
 // type and folded in FP64 across the grid.
-constexpr int kAoU = 4;  // entries per thread in flight
-
-// Each thread takes kAoU entries a grid stride apart (coalesced across the
-// warp): their independent loads first, then the pair operands of all of
-// them round by round, then the arithmetic.
-template <typename FT, typename CT>
-__global__ void __launch_bounds__(kPTPB) k_parilu_sweep_ao(int nnz, const double *__restrict__ Aval,
-                                                           const int *__restrict__ dpos,
-                                                           const int *__restrict__ pptr,
-                                                           const int2 *__restrict__ pairs,
-                                                           const FT *__restrict__ Fold, FT *__restrict__ Fnew,
-                                                           double *partials, int *counter, double *step) {
+// Each thread takes U entries a grid stride apart (coalesced across the
+// warp): their independent loads first, then their pair records PU at a
+// time with all the operands of a batch gathered together, then the
+// arithmetic.  MINB: blocks per SM the register budget is set for.  On the
+// 128^3 convection-diffusion system one entry per thread with three pairs
+// per batch at full occupancy measured fastest (93 us against 113-151 us for
+// two or four entries per thread at lower occupancy); the autotune keeps
+// the choice per pattern.
+template <typename FT, typename CT, int U, int PU, int MINB>
+__global__ void __launch_bounds__(kPTPB, MINB) k_parilu_sweep_ao(int nnz, const double *__restrict__ Aval,
+                                                                 const int *__restrict__ dpos,
+                                                                 const int *__restrict__ pptr,
+                                                                 const int2 *__restrict__ pairs,
+                                                                 const FT *__restrict__ Fold, FT *__restrict__ Fnew,
+                                                                 double *partials, int *counter, double *step) {
   CT acc = (CT)0;
   const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < nnz; base += kAoU * stride) {
-    CT sv[kAoU], dv[kAoU], fo[kAoU];
-    int b[kAoU], cnt[kAoU];
-    bool isl[kAoU];
+  for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < nnz; base += U * stride) {
+    CT sv[U], dv[U], fo[U];
+    int b[U], cnt[U];
+    bool isl[U];
     int most = 0;
 #pragma unroll
-    for (int u = 0; u < kAoU; ++u) {
+    for (int u = 0; u < U; ++u) {
       const int p = base + u * stride;
       b[u] = 0;
       cnt[u] = 0;
@@ -441,22 +444,28 @@ __global__ void __launch_bounds__(kPTPB) k_parilu_sweep_ao(int nnz, const double
       }
       most = max(most, cnt[u]);
     }
-    for (int k = 0; k < most; ++k) {
-      int2 pr[kAoU];
+    for (int k0 = 0; k0 < most; k0 += PU) {
+      int2 pr[U][PU];
 #pragma unroll
-      for (int u = 0; u < kAoU; ++u) pr[u] = k < cnt[u] ? __ldg(pairs + b[u] + k) : make_int2(-1, -1);
-      CT lv[kAoU], uv[kAoU];
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-      for (int u = 0; u < kAoU; ++u) {
-        lv[u] = pr[u].x >= 0 ? cvt<CT>(Fold[pr[u].x]) : (CT)0;
-        uv[u] = pr[u].x >= 0 ? cvt<CT>(Fold[pr[u].y]) : (CT)0;
-      }
+        for (int j = 0; j < PU; ++j) pr[u][j] = k0 + j < cnt[u] ? __ldg(pairs + b[u] + k0 + j) : make_int2(-1, -1);
+      CT lv[U][PU], uv[U][PU];
 #pragma unroll
-      for (int u = 0; u < kAoU; ++u)
-        if (k < cnt[u]) sv[u] = fma(-lv[u], uv[u], sv[u]);
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < PU; ++j) {
+          lv[u][j] = pr[u][j].x >= 0 ? cvt<CT>(Fold[pr[u][j].x]) : (CT)0;
+          uv[u][j] = pr[u][j].x >= 0 ? cvt<CT>(Fold[pr[u][j].y]) : (CT)0;
+        }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < PU; ++j)
+          if (k0 + j < cnt[u]) sv[u] = fma(-lv[u][j], uv[u][j], sv[u]);
     }
 #pragma unroll
-    for (int u = 0; u < kAoU; ++u) {
+    for (int u = 0; u < U; ++u) {
       const int p = base + u * stride;
       if (p < nnz) {
         const CT nv = isl[u] ? sv[u] / dv[u] : sv[u];
@@ -479,21 +488,35 @@ __global__ void k_factor_gather(int count, const int *__restrict__ map, const T 
   }
 }
 
-void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos,
-                            const int *pptr, const int2 *pairs, const void *Fold, void *Fnew, double *partials,
-                            int *counter, double *step) {
-  int grid = (nnz + kPTPB - 1) / kPTPB;
-  const int cap = num_sms() * (2048 / kPTPB);
+template <int U, int PU, int MINB>
+static void sweep_ao_variant(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos, const int *pptr,
+                             const int2 *pairs, const void *Fold, void *Fnew, double *partials, int *counter,
+                             double *step) {
+  int grid = (nnz + kPTPB * U - 1) / (kPTPB * U);
+  const int cap = num_sms() * MINB;
   grid = grid < 1 ? 1 : (grid > cap ? cap : grid);
   if (t == VType::F64)
-    k_parilu_sweep_ao<double, double><<<grid, kPTPB, 0, s>>>(nnz, Aval, dpos, pptr, pairs, (const double *)Fold,
-                                                             (double *)Fnew, partials, counter, step);
+    k_parilu_sweep_ao<double, double, U, PU, MINB><<<grid, kPTPB, 0, s>>>(
+        nnz, Aval, dpos, pptr, pairs, (const double *)Fold, (double *)Fnew, partials, counter, step);
   else if (t == VType::F32)
-    k_parilu_sweep_ao<float, float><<<grid, kPTPB, 0, s>>>(nnz, Aval, dpos, pptr, pairs, (const float *)Fold,
-                                                           (float *)Fnew, partials, counter, step);
+    k_parilu_sweep_ao<float, float, U, PU, MINB><<<grid, kPTPB, 0, s>>>(
+        nnz, Aval, dpos, pptr, pairs, (const float *)Fold, (float *)Fnew, partials, counter, step);
   else
-    k_parilu_sweep_ao<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
+    k_parilu_sweep_ao<__nv_bfloat16, float, U, PU, MINB><<<grid, kPTPB, 0, s>>>(
         nnz, Aval, dpos, pptr, pairs, (const __nv_bfloat16 *)Fold, (__nv_bfloat16 *)Fnew, partials, counter, step);
+}
+
+int parilu_sweep_variants() { return 4; }
+
+void launch_parilu_sweep_ao(cudaStream_t s, int nnz, VType t, const double *Aval, const int *dpos,
+                            const int *pptr, const int2 *pairs, const void *Fold, void *Fnew, double *partials,
+                            int *counter, double *step, int variant) {
+  switch (variant) {
+    case 1: sweep_ao_variant<1, 2, 8>(s, nnz, t, Aval, dpos, pptr, pairs, Fold, Fnew, partials, counter, step); break;
+    case 2: sweep_ao_variant<1, 4, 8>(s, nnz, t, Aval, dpos, pptr, pairs, Fold, Fnew, partials, counter, step); break;
+    case 3: sweep_ao_variant<2, 3, 6>(s, nnz, t, Aval, dpos, pptr, pairs, Fold, Fnew, partials, counter, step); break;
+    default: sweep_ao_variant<1, 3, 8>(s, nnz, t, Aval, dpos, pptr, pairs, Fold, Fnew, partials, counter, step); break;
+  }
 }
 
 void launch_factor_gather(cudaStream_t s, int count, const int *map, VType t, const void *src, void *dst) {
