@@ -1713,7 +1713,7 @@ int lace_gpu_ctx::ensure_krylov(int m, bool monitor) {
   // column on the same memory channels
   ldv = ((size_t)n + 31) / 32 * 32 + 32;
   const size_t vbytes = 8 * ldv * (size_t)(m + 1), zbytes = (zf32 ? 4 : 8) * ldv * (size_t)m;
-  const size_t vfbytes = zf32 ? 4 * ldv * (size_t)(m + 1) : 0;
+  const size_t vfbytes = zf32 ? 2 * 4 * ldv * (size_t)(m + 1) : 0;  // Vf, then Vlo
   if (m > ws_m || zf32 != ws_zf32 || Vb.bytes < vbytes || Zb.bytes < zbytes || Vfb.bytes < vfbytes) {
     drop_graphs();
     rc |= Vb.ensure(vbytes);
@@ -1826,6 +1826,7 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
   a.V = (double *)Vb.p;
   a.ldv = ldv;
   a.Vf = vtype() != VType::F64 ? (float *)Vfb.p : nullptr;
+  a.Vlo = a.Vf ? a.Vf + ldv * (size_t)(m + 1) : nullptr;
   a.Z = Zb.p;
   a.ldz = ldv;
   a.z_f32 = ws_zf32 ? 1 : 0;

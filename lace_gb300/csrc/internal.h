@@ -105,6 +105,10 @@ struct ArnoldiArgs {
   // dimension), when the next Krylov vector q is FP32: pass C forms q from
   // them, reading half the bytes; null otherwise
   float *Vf = nullptr;
+  // with Vf: the remainder v - Vf, also in FP32 (same leading dimension), so
+  // that (Vf, Vlo) hold each reflector entry to about 48 bits and the
+  // one-kernel step forms its products on the FP32 unit; null otherwise
+  float *Vlo = nullptr;
   void *Z = nullptr;     // preconditioned vectors, n x m (float or double)
   size_t ldz = 0;
   int z_f32 = 0;

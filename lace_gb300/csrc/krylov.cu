@@ -289,8 +289,8 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__restrict__ r,
                                                      double *__restrict__ V, float *__restrict__ Vf,
-                                                     QT *__restrict__ q, const Cycle *cy, const Control *ctrl,
-                                                     Prefill pf) {
+                                                     float *__restrict__ Vlo, QT *__restrict__ q, const Cycle *cy,
+                                                     const Control *ctrl, Prefill pf) {
   if (ctrl->done) return;
   const double dd = cy->dd0, ia = cy->inv_alpha0;
   const double rdd = 1.0 / dd;
@@ -298,7 +298,11 @@ __global__ void __launch_bounds__(kTPB) k_cycle_init(int n, const double *__rest
     const double ri = r[i];
     const double v = (i == 0 ? ri + dd : ri) * ia;
     V[i] = v;
-    if (Vf) Vf[i] = dtof_rz(v);
+    if (Vf) {
+      const float2 d = df_split(v);
+      Vf[i] = d.x;
+      if (Vlo) Vlo[i] = d.y;
+    }
     q[i] = (QT)(-ri * rdd);
     prefill_row(pf, i);
   }
@@ -569,7 +573,7 @@ __global__ void __launch_bounds__(kTPB, NS <= 4 ? 3 : 1) k_passB(int n, const do
 // rounds it to FP32 on its first read) the combination runs in FP32.
 template <typename QT>
 __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, float *__restrict__ Vf,
-                                                size_t ldv, int j, const double *__restrict__ w,
+                                                float *__restrict__ Vlo, size_t ldv, int j, const double *__restrict__ w,
                                                 QT *__restrict__ q, const Cycle *cy, const Control *ctrl,
                                                 Prefill pf) {
   if (ctrl->done) return;
@@ -592,8 +596,10 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, f
     const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? wv.y + dd : wv.y) * ia : 0.0;
     *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
     if constexpr (kF32) {
-      const float2 vf = make_float2(dtof_rz(v0), dtof_rz(v1));
+      const float2 d0 = df_split(v0), d1 = df_split(v1);
+      const float2 vf = make_float2(d0.x, d1.x);
       *reinterpret_cast<float2 *>(Vf + (size_t)jp1 * ldv + i) = vf;  // the FP32 copy of v_{j+1}
+      if (Vlo) *reinterpret_cast<float2 *>(Vlo + (size_t)jp1 * ldv + i) = make_float2(d0.y, d1.y);
       const float2 s = vcomb8x2f(Vf, ldv, i, jp1, scf);
       *reinterpret_cast<float2 *>(q + i) = make_float2(((i == jp1 ? 1.f : 0.f) - vf.x * scf[jp1]) - s.x,
                                                        ((i + 1 == jp1 ? 1.f : 0.f) - vf.y * scf[jp1]) - s.y);
@@ -609,7 +615,11 @@ __global__ void __launch_bounds__(kTPB) k_passC(int n, double *__restrict__ V, f
     const int i = n - 1;
     const double v = (i > j) ? (i == jp1 ? w[i] + dd : w[i]) * ia : 0.0;
     vn[i] = v;
-    if (kF32) Vf[(size_t)jp1 * ldv + i] = dtof_rz(v);
+    if (kF32) {
+      const float2 d = df_split(v);
+      Vf[(size_t)jp1 * ldv + i] = d.x;
+      if (Vlo) Vlo[(size_t)jp1 * ldv + i] = d.y;
+    }
     q[i] = (QT)(((i == jp1 ? 1.0 : 0.0) - v * sc[jp1]) - vcomb8(V, ldv, i, jp1, sc));
     prefill_row(pf, i);
   }
@@ -948,6 +958,362 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step(HHStep a, int j) {
   }
 }
 
+// --------------------------- the one-kernel step in double-float arithmetic
+// Mixed precision (FP32 preconditioner) on this part: the step's (j+1)-column
+// dot products and its w -= V y update, 3(j+1) FP64 FMAs per row in the FP64
+// form, run as double-float arithmetic on the FP32 unit from the reflectors'
+// (Vf, Vlo) pair and a (hi, lo) copy of w in shared memory.  FP64 stays in
+// the operator (A z), in w itself between the phases (rebuilt from its pair
+// where it is needed: the update, the norm, the published top rows, the new
+// reflector) and in everything after the grid reductions, which fold FP64
+// partial sums as before.  A lane's double-float sum goes into an FP64
+// accumulator every 32 terms, so its rounding stays at the level of a short
+// FP64 sum.  Same phases, barriers and small-matrix work as k_hh_step.
+
+// block partial sums sacc[k] = sum over this block's rows i > lo of
+// V[k][i] w[i], k < jp1, from the double-float pairs
+__device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, const float *__restrict__ Vlo,
+                                                 size_t ldv, int jp1, int r0, int r1, int lo, const float2 *sw,
+                                                 double *swarp, double *sacc) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nsl = r1 > r0 ? (r1 - r0 + 31) >> 5 : 0;
+  if (jp1 <= 32) {
+    const int G = 32 / jp1;
+    double acc = 0.0;
+    if (wid < G * jp1) {
+      const int k = wid % jp1, g = wid / jp1;
+      const float *Hk = Vf + (size_t)k * ldv + r0, *Lk = Vlo + (size_t)k * ldv + r0;
+      int batch = 0;
+      float sh = 0.f, sl = 0.f;
+      for (int sl0 = g; sl0 < nsl; sl0 += 8 * G) {
+        float vh[8], vl[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int t = 32 * (sl0 + u * G) + lane;
+          const bool ok = sl0 + u * G < nsl && r0 + t < r1;
+          vh[u] = ok ? Hk[t] : 0.f;
+          vl[u] = ok ? Lk[t] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int t = 32 * (sl0 + u * G) + lane;
+          const int i = r0 + t;
+          const float2 wv = (sl0 + u * G < nsl && i < r1 && i > lo) ? sw[t] : make_float2(0.f, 0.f);
+          df_mac(vh[u], vl[u], wv.x, wv.y, sh, sl);
+        }
+        if (++batch == 4) {  // 32 terms per lane: into the FP64 sum
+          acc += to_f64(sh) + to_f64(sl);
+          sh = sl = 0.f;
+          batch = 0;
+        }
+      }
+      acc += to_f64(sh) + to_f64(sl);
+      acc = warp_sum(acc);
+    }
+    if (lane == 0) swarp[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x < jp1) {
+      double t = 0.0;
+      for (int g = 0; g < G; ++g) t += swarp[g * jp1 + threadIdx.x];
+      sacc[threadIdx.x] = t;
+    }
+  } else {
+    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    int batch = 0;
+    for (int sl0 = 0; sl0 < nsl; sl0 += 4) {
+      float2 wv[4];
+      int ii[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = 32 * (sl0 + u) + lane;
+        const int i = r0 + t;
+        const bool ok = sl0 + u < nsl && i < r1 && i > lo;
+        wv[u] = ok ? sw[t] : make_float2(0.f, 0.f);
+        ii[u] = ok ? i : r0;
+      }
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        const int k = wid + 32 * c;
+        if (32 * c < jp1 && k < jp1) {
+          float vh[4], vl[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            vh[u] = Vf[(size_t)k * ldv + ii[u]];
+            vl[u] = Vlo[(size_t)k * ldv + ii[u]];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) df_mac(vh[u], vl[u], wv[u].x, wv[u].y, sh[c], sl[c]);
+        }
+      }
+      if (++batch == 8) {
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          acc[c] += to_f64(sh[c]) + to_f64(sl[c]);
+          sh[c] = sl[c] = 0.f;
+        }
+        batch = 0;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      acc[c] += to_f64(sh[c]) + to_f64(sl[c]);
+      const int k = wid + 32 * c;
+      if (32 * c < jp1) {  // warp-uniform
+        const double v = warp_sum(acc[c]);
+        if (lane == 0 && k < jp1) swarp[k] = v;
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < jp1; k += blockDim.x) sacc[k] = swarp[k];
+  }
+  __syncthreads();
+}
+
+// rows i, i+1 (i even): sum_k V[k][i..i+1] y[k] over k < ncols in
+// double-float from the (Vf, Vlo) pairs and y's pair (yh, yl)
+__device__ __forceinline__ double2 vcomb_df_x2(const float *__restrict__ Vf, const float *__restrict__ Vlo,
+                                               size_t ldv, int i, int ncols, const float *yh, const float *yl) {
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+  for (int k = 0; k < ncols; k += 8) {
+    float2 vh[8], vl[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) {
+        vh[u] = __ldg(reinterpret_cast<const float2 *>(Vf + (size_t)(k + u) * ldv + i));
+        vl[u] = __ldg(reinterpret_cast<const float2 *>(Vlo + (size_t)(k + u) * ldv + i));
+      }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k + u < ncols) {
+        df_mac(vh[u].x, vl[u].x, yh[k + u], yl[k + u], h0, l0);
+        df_mac(vh[u].y, vl[u].y, yh[k + u], yl[k + u], h1, l1);
+      }
+  }
+  return make_double2(to_f64(h0) + to_f64(l0), to_f64(h1) + to_f64(l1));
+}
+
+__device__ __forceinline__ double vcomb_df(const float *__restrict__ Vf, const float *__restrict__ Vlo, size_t ldv,
+                                           int i, int ncols, const float *yh, const float *yl) {
+  float h = 0.f, l = 0.f;
+  for (int k = 0; k < ncols; ++k) df_mac(Vf[(size_t)k * ldv + i], Vlo[(size_t)k * ldv + i], yh[k], yl[k], h, l);
+  return to_f64(h) + to_f64(l);
+}
+
+struct HHStepDF {
+  HHStep base;
+  float *Vlo;
+};
+
+__global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
+  const HHStep &a = ad.base;
+  if (a.ctrl->done) return;
+  extern __shared__ float2 swd[];  // this block's rows of w as (hi, lo)
+  __shared__ double swarp[5 * 32];
+  __shared__ double sacc[kLdT + 1], sres[kLdT + 1];
+  __shared__ double sd[kLdT], srho[kLdT], sc[kLdT];
+  __shared__ float syh[kLdT], syl[kLdT];
+  __shared__ float scf[kLdT];
+  __shared__ double sbuf[kHHTPB];
+  __shared__ double s_dd, s_ia, s_vjj;
+  const int n = a.n, jp1 = j + 1, T = blockDim.x;
+  const int r0 = blockIdx.x * a.rb, r1 = min(n, r0 + a.rb);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const size_t ldv = a.ldv;
+  const float *__restrict__ Vf = a.Vf;
+  const float *__restrict__ Vlo = ad.Vlo;
+  Cycle *cy = a.cy;
+  int phase = 0;
+  // ---- pass A: w = A z_j (FP64, a warp per 32-row slice), kept as a pair
+  {
+    const float *z = (const float *)a.z;
+    for (int sl = (r0 >> 5) + wid; 32 * sl < r1; sl += (T >> 5)) {
+      const int i = 32 * sl + lane;
+      if (i < r1) {
+        const int len = a.op.row[i + 1] - a.op.row[i];
+        const int *cp = a.op.sell_col + a.op.sell_ptr[sl] + lane;
+        const double *vp = a.op.sell_val + (cp - a.op.sell_col);
+        double s = 0.0;
+        for (int t = 0; t < len; t += 8) {
+          int c[8];
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) {
+              c[u] = cp[32 * (t + u)];
+              v[u] = vp[32 * (t + u)];
+            }
+          float zv[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) zv[u] = z[c[u]];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (t + u < len) s = fma(v[u], to_f64(zv[u]), s);
+        }
+        swd[i - r0] = df_split(s);
+      }
+    }
+  }
+  __syncthreads();
+  hh_block_dots_df(Vf, Vlo, ldv, jp1, r0, r1, -1, swd, swarp, sacc);
+  if (!hh_grid_fold(sacc, jp1, a.partials, phase, a.ctrl, sres)) return;
+  // y = T^T s, as a pair
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    double y = 0.0;
+    for (int l = 0; l <= k; ++l) y = fma(cy->T[l + k * kLdT], sres[l], y);
+    const float2 d = df_split(y);
+    syh[k] = d.x;
+    syl[k] = d.y;
+  }
+  __syncthreads();
+  // ---- pass B: w -= V y (a row pair per thread), then V^T w over rows > j
+  // and ||w_{j+1:}||^2; rows 0..j+1 of w published for every block
+  double nrm = 0.0;
+  {
+    const int p0 = r0 >> 1, p1 = r1 >> 1;
+    for (int p = p0 + threadIdx.x; p < p1; p += T) {
+      const int i = 2 * p;
+      const double2 c = vcomb_df_x2(Vf, Vlo, ldv, i, jp1, syh, syl);
+      const double s0 = df_join(swd[i - r0]) - c.x, s1 = df_join(swd[i + 1 - r0]) - c.y;
+      swd[i - r0] = df_split(s0);
+      swd[i + 1 - r0] = df_split(s1);
+      if (i > j) nrm = fma(s0, s0, nrm);
+      if (i + 1 > j) nrm = fma(s1, s1, nrm);
+      if (i <= jp1) cy->wtop[i] = s0;
+      if (i + 1 <= jp1) cy->wtop[i + 1] = s1;
+    }
+    if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {  // the last row of an odd n
+      const int i = r1 - 1;
+      const double s0 = df_join(swd[i - r0]) - vcomb_df(Vf, Vlo, ldv, i, jp1, syh, syl);
+      swd[i - r0] = df_split(s0);
+      if (i > j) nrm = fma(s0, s0, nrm);
+      if (i <= jp1) cy->wtop[i] = s0;
+    }
+  }
+  sbuf[threadIdx.x] = nrm;
+  __syncthreads();
+  hh_block_dots_df(Vf, Vlo, ldv, jp1, r0, r1, j, swd, swarp, sacc);
+  if (wid < 4) {
+    const int quarter = T >> 2;
+    double t = 0.0;
+    for (int k = wid * quarter + lane; k < (wid + 1) * quarter; k += 32) t += sbuf[k];
+    t = warp_sum(t);
+    if (lane == 0) swarp[wid] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sacc[jp1] = ((swarp[0] + swarp[1]) + swarp[2]) + swarp[3];
+  __syncthreads();
+  if (!hh_grid_fold(sacc, jp1 + 1, a.partials, phase, a.ctrl, sres)) return;
+  // ---- pass B's last-block work, in every block (as k_hh_step)
+  if (threadIdx.x == 0) {
+    const double nrm2 = jp1 < n ? sres[jp1] : 0.0;
+    const double wn = sqrt(nrm2);
+    const double wj1 = jp1 < n ? __ldcg(&cy->wtop[jp1]) : 0.0;
+    const double dd = mysgn(wj1) * wn;
+    const double alpha = sqrt(2.0 * (nrm2 + fabs(wj1) * wn));
+    const double ia = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    s_dd = dd;
+    s_ia = ia;
+    s_vjj = (wj1 + dd) * ia;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    const double vk = jp1 < n ? a.V[(size_t)k * ldv + jp1] : 0.0;
+    sd[k] = (sres[k] + s_dd * vk) * s_ia;
+    srho[k] = vk;
+  }
+  if (threadIdx.x == 0) srho[jp1] = s_vjj;
+  __syncthreads();
+  for (int k = threadIdx.x; k < jp1; k += T) {
+    double t = 0.0;
+    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], sd[l], t);
+    sacc[k] = -2.0 * t;
+  }
+  if (threadIdx.x == 0) sacc[jp1] = 2.0;
+  __syncthreads();
+  for (int k = threadIdx.x; k <= jp1; k += T) {
+    double t = 0.0;
+    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], srho[l], t);
+    t = fma(sacc[k], srho[jp1], t);
+    sc[k] = t;
+    scf[k] = (float)t;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    double *Tg = cy->T;
+    for (int k = threadIdx.x; k < kLdT; k += T) Tg[k + jp1 * kLdT] = k <= jp1 ? sacc[k] : 0.0;
+    for (int k = threadIdx.x; k <= jp1; k += T) cy->c[k] = sc[k];
+    if (threadIdx.x == 0) {
+      cy->dd = s_dd;
+      cy->inv_alpha = s_ia;
+      double *sh = sbuf;
+      for (int k = 0; k <= j; ++k) sh[k] = __ldcg(&cy->wtop[k]);
+      for (int k = 0; k < j; ++k) {
+        const double t0 = sh[k], t1 = sh[k + 1];
+        sh[k + 1] = -cy->sn[k] * t0 + cy->cs[k] * t1;
+        sh[k] = cy->cs[k] * t0 + cy->sn[k] * t1;
+      }
+      const double dd = s_dd;
+      double c, sn;
+      givens_rot(sh[j], -dd, 4.9406564584124654e-324, &c, &sn);
+      cy->cs[j] = c;
+      cy->sn[j] = sn;
+      sh[j] = c * sh[j] - sn * dd;
+      const double gj = cy->g[j];
+      cy->g[jp1] = -sn * gj;
+      cy->g[j] = c * gj;
+      const double resid = fabs(-sn * gj);
+      cy->hist[j] = resid;
+      a.ctrl->resid = resid;
+      const bool conv = resid < a.ctrl->rtol_abs;
+      double *R = cy->R + (size_t)j * kLdT;
+      for (int k = 0; k <= j; ++k) R[k] = sh[k];
+      if (conv || j == a.m - 1 || !(resid == resid)) {
+        a.ctrl->nsteps = jp1;
+        a.ctrl->converged = conv ? 1 : 0;
+        if (!(resid == resid)) a.ctrl->status |= kStatusBreakdown;
+        a.ctrl->done = 1;
+      }
+    }
+  }
+  // ---- pass C: v_{j+1} (FP64, and its pair) and q = e_{j+1} - V_{j+1} c (FP32)
+  const double dd = s_dd, ia = s_ia;
+  double *vn = a.V + (size_t)jp1 * ldv;
+  float *vfn = a.Vf + (size_t)jp1 * ldv, *vln = ad.Vlo + (size_t)jp1 * ldv;
+  float *q = (float *)a.q;
+  const int p0 = r0 >> 1, p1 = r1 >> 1;
+  for (int p = p0 + threadIdx.x; p < p1; p += T) {
+    const int i = 2 * p;
+    const double w0 = df_join(swd[i - r0]), w1 = df_join(swd[i + 1 - r0]);
+    const double v0 = (i > j) ? (i == jp1 ? w0 + dd : w0) * ia : 0.0;
+    const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? w1 + dd : w1) * ia : 0.0;
+    *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
+    const float2 d0 = df_split(v0), d1 = df_split(v1);
+    const float2 vf = make_float2(d0.x, d1.x);
+    *reinterpret_cast<float2 *>(vfn + i) = vf;
+    *reinterpret_cast<float2 *>(vln + i) = make_float2(d0.y, d1.y);
+    const float2 sm = vcomb8x2f(a.Vf, ldv, i, jp1, scf);
+    *reinterpret_cast<float2 *>(q + i) = make_float2(((i == jp1 ? 1.f : 0.f) - vf.x * scf[jp1]) - sm.x,
+                                                     ((i + 1 == jp1 ? 1.f : 0.f) - vf.y * scf[jp1]) - sm.y);
+    prefill_row(a.pf, i);
+    prefill_row(a.pf, i + 1);
+  }
+  if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {
+    const int i = r1 - 1;
+    const double wi = df_join(swd[i - r0]);
+    const double v = (i > j) ? (i == jp1 ? wi + dd : wi) * ia : 0.0;
+    vn[i] = v;
+    const float2 d = df_split(v);
+    vfn[i] = d.x;
+    vln[i] = d.y;
+    float sm = 0.f;
+    for (int k = 0; k < jp1; ++k) sm = fmaf(a.Vf[(size_t)k * ldv + i], scf[k], sm);
+    q[i] = ((i == jp1 ? 1.f : 0.f) - d.x * scf[jp1]) - sm;
+    prefill_row(a.pf, i);
+  }
+}
+
 // ----------------------------------------------- orthogonality monitor
 // orth[j+1] = ||I - Q^T Q||_inf over q_0..q_{j} (LACE :628-656 evaluates it on
 // the first search+1 stored vectors); Q columns stored by the host driver.
@@ -1064,9 +1430,10 @@ void launch_cycle_residual(cudaStream_t s, const ArnoldiArgs &a, const double *b
 void launch_cycle_init(cudaStream_t s, const ArnoldiArgs &a) {
   const Prefill pf = prefill_for(a, 0);
   if (a.q_f32)
-    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.Vf, (float *)a.q, a.cy, a.ctrl, pf);
+    k_cycle_init<float><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, a.Vf, a.Vlo, (float *)a.q, a.cy, a.ctrl, pf);
   else
-    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, nullptr, (double *)a.q, a.cy, a.ctrl, pf);
+    k_cycle_init<double><<<rowgrid(a.n), kTPB, 0, s>>>(a.n, a.w, a.V, nullptr, nullptr, (double *)a.q, a.cy, a.ctrl,
+                                                       pf);
 }
 
 
@@ -1126,12 +1493,12 @@ void launch_passC(cudaStream_t s, const ArnoldiArgs &a, int j) {
   const Prefill pf = prefill_for(a, j + 1);  // for the next step's solves
   if (a.q_f32) {
     static const int g = wave_grid(k_passC<float>, num_sms() * 8);
-    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.Vf, a.ldv, j, a.w, (float *)a.q, a.cy,
-                                                                a.ctrl, pf);
+    k_passC<float><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, a.Vf, a.Vlo, a.ldv, j, a.w, (float *)a.q,
+                                                                a.cy, a.ctrl, pf);
   } else {
     static const int g = wave_grid(k_passC<double>, num_sms() * 8);
-    k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, nullptr, a.ldv, j, a.w, (double *)a.q,
-                                                                  a.cy, a.ctrl, pf);
+    k_passC<double><<<std::min(g, rowgrid(a.n)), kTPB, 0, s>>>(a.n, a.V, nullptr, nullptr, a.ldv, j, a.w,
+                                                                  (double *)a.q, a.cy, a.ctrl, pf);
   }
 }
 
@@ -1180,8 +1547,52 @@ static int hh_step_t(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, 
   return 0;
 }
 
+static int hh_step_df(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
+  static const int G = [] {
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(k_hh_step_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kHHSmemMax) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hh_step_df, kHHTPB, kHHSmemMax) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      return 0;
+    }
+    return num_sms();
+  }();
+  if (G == 0) return 1;
+  HHStepDF pd;
+  HHStep &p = pd.base;
+  p.n = a.n;
+  p.rb = ((a.n + G - 1) / G + 31) / 32 * 32;
+  if ((size_t)p.rb * 8 > (size_t)kHHSmemMax || (size_t)G * kLdT * 2 > (size_t)a.grid * kLdT) return 1;
+  p.op = opview(a);
+  p.z = (const char *)a.Z + (size_t)j * a.ldz * sizeof(float);
+  p.V = a.V;
+  p.Vf = a.Vf;
+  p.ldv = a.ldv;
+  p.q = a.q;
+  p.partials = a.partials;
+  p.cy = a.cy;
+  p.ctrl = a.ctrl;
+  p.m = a.m;
+  p.pf = prefill_for(a, j + 1);
+  if (mark_t && p.pf.t) {
+    p.pf.t = mark_t;
+    p.pf.z = mark_z;
+  }
+  pd.Vlo = a.Vlo;
+  void *args[] = {&pd, &j};
+  if (cudaLaunchCooperativeKernel((const void *)k_hh_step_df, dim3(G), dim3(kHHTPB), args, (size_t)p.rb * 8, s) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 2;
+  }
+  return 0;
+}
+
 int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   if (a.bs || !a.sell_ptr) return 1;
+  if (a.z_f32 && a.q_f32 && a.Vf && a.Vlo) return hh_step_df(s, a, j, mark_t, mark_z);
   if (a.z_f32 && a.q_f32 && a.Vf) return hh_step_t<float, float>(s, a, j, mark_t, mark_z);
   if (!a.z_f32 && !a.q_f32) return hh_step_t<double, double>(s, a, j, mark_t, mark_z);
   return 1;

@@ -121,6 +121,29 @@ __device__ __forceinline__ float dtof_rz(double x) {
   return __uint_as_float((hi & 0x80000000u) | mag);
 }
 
+// Double-float values: an FP64 value x as hi = dtof_rz(x) and lo =
+// dtof_rz(x - hi), about 48 bits together (finite |x| < 2^128; lo of values
+// near the FP32 underflow flushes to 0), so that products and sums of FP64
+// data run on the FP32 unit - 64 times the FP64 unit's rate on this part -
+// with FP64-like accuracy.  Conversions use integer operations.
+__device__ __forceinline__ float2 df_split(double x) {
+  const float h = dtof_rz(x);
+  return make_float2(h, dtof_rz(x - to_f64(h)));
+}
+__device__ __forceinline__ double df_join(float2 v) { return to_f64(v.x) + to_f64(v.y); }
+// (sh, sl) += (ah + al) * (bh + bl): the high product exactly (an FMA gives
+// its rounding error), the cross terms in FP32, al*bl dropped (2^-48
+// relative), the high parts summed error-free (TwoSum), the rest into sl
+__device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, float &sh, float &sl) {
+  const float p = ah * bh;
+  const float pe = fmaf(ah, bl, fmaf(al, bh, fmaf(ah, bh, -p)));
+  const float t = sh + p;
+  const float z = t - sh;
+  const float e = (sh - (t - z)) + (p - z);
+  sh = t;
+  sl += e + pe;
+}
+
 // the unsolved pattern (all ones) into row i of an FP32 or FP64 vector: the
 // sync-free solve that writes the vector polls it until the pattern is gone
 __device__ __forceinline__ void mark_unsolved(void *x, int f32, size_t i) {
