@@ -1767,6 +1767,7 @@ int lace_gpu_ctx::ensure_sell() {
     rc |= sell_col.upload(col.data(), 4 * col.size(), stream);
     rc |= sell_map.upload(map.data(), 4 * map.size(), stream);
     rc |= sell_val.ensure(8 * col.size());
+    rc |= sell_pair.ensure(8 * col.size());
     if (rc) return DEV_ERR_DEVICE_ALLOC;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
     sell_slots = (size_t)ptr[nsl];
@@ -1776,7 +1777,7 @@ int lace_gpu_ctx::ensure_sell() {
   }
   if (sell_version != aval_version) {
     launch_sell_values(stream, sell_slots, (const int *)sell_map.p, (const double *)Aval.p,
-                       (double *)sell_val.p);
+                       (double *)sell_val.p, (float2 *)sell_pair.p);
     sell_version = aval_version;
   }
   return cudaGetLastError() == cudaSuccess ? 0 : DEV_ERR_UNKNOWN;
@@ -1820,6 +1821,7 @@ ArnoldiArgs lace_gpu_ctx::arnoldi_args(int m, bool adjoint) {
       a.sell_ptr = (const int *)sell_ptr.p;
       a.sell_col = (const int *)sell_col.p;
       a.sell_val = (const double *)sell_val.p;
+      a.sell_pair = (const float2 *)sell_pair.p;
     }
   }
   a.lanes = lanes;

@@ -80,7 +80,7 @@ struct lace_gpu_ctx {
   int aval_version = 0;  // bumped whenever A's values change
   // A in sliced ELL for the Arnoldi operator (CSR only): slice offsets, columns,
   // source CSR entry of each slot (-1: padding) and the gathered values
-  DBuf sell_ptr, sell_col, sell_map, sell_val;
+  DBuf sell_ptr, sell_col, sell_map, sell_val, sell_pair;
   size_t sell_slots = 0;
   bool sell_valid = false;
   int sell_version = -1;

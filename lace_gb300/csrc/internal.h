@@ -47,6 +47,10 @@ struct Cycle {
   // rows 0..j+1 of w after the step's update, published by the blocks that
   // own them (the one-kernel Householder step)
   double wtop[kLdT];
+  // the Gram matrix V^T V of the reflectors (column-major, diagonal 1): its
+  // column j+1 is V^T v_{j+1}, which step j forms for T anyway; the
+  // double-float one-kernel step takes V^T w over rows > j from it
+  double G[kLdT * kLdT];
 };
 
 // Handles for the two triangles of one solve direction.
@@ -99,6 +103,7 @@ struct ArnoldiArgs {
   // absent
   const int *sell_ptr = nullptr, *sell_col = nullptr;
   const double *sell_val = nullptr;
+  const float2 *sell_pair = nullptr;  // sell_val as (hi, lo) pairs
   double *V = nullptr;   // reflectors, n x (m+1) column-major
   size_t ldv = 0;
   // the reflectors again in FP32 (rounded toward zero, same leading
@@ -223,7 +228,8 @@ void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
                    const void *L, const void *Ur, const void *Uc, double *out3);
 // the sliced-ELL values of the operator: dst[q] = map[q] >= 0 ? src[map[q]] : 0
-void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst);
+void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst,
+                        float2 *pair);
 // gather: dst[p] = src[perm[p]] with type conversion
 void launch_gather(cudaStream_t s, int count, const int *perm, VType ts, const void *src, VType td,
                    void *dst);

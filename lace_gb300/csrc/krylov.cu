@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(kTPB) k_cycle_residual(int n, OpView op, const
       cy->inv_alpha0 = alpha > 0.0 ? 1.0 / alpha : 0.0;
       cy->g[0] = -dd;
       cy->T[0] = 2.0;
+      cy->G[0] = 1.0;
       ctrl->done = 0;
       ctrl->converged = 0;
     }
@@ -734,10 +735,10 @@ __device__ __forceinline__ void hh_block_dots(const double *__restrict__ V, size
 // sres[k] = sum over the grid of the blocks' sacc[k], k < nv, the same in
 // every block (warp w folds k = w, w+32, ...; lanes stride over the blocks)
 __device__ __forceinline__ bool hh_grid_fold(const double *sacc, int nv, double *partials, int &phase,
-                                             Control *ctrl, double *sres) {
+                                             Control *ctrl, double *sres, int cap = kLdT) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int G = gridDim.x;
-  double *P = partials + (size_t)phase * kLdT * G;
+  double *P = partials + (size_t)phase * cap * G;
   for (int k = threadIdx.x; k < nv; k += blockDim.x) P[(size_t)k * G + blockIdx.x] = sacc[k];
   if (!grid_barrier(ctrl)) return false;
   for (int k = wid; k < nv; k += (int)(blockDim.x >> 5)) {
@@ -970,18 +971,26 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step(HHStep a, int j) {
 // accumulator every 32 terms, so its rounding stays at the level of a short
 // FP64 sum.  Same phases, barriers and small-matrix work as k_hh_step.
 
+// operand of the block dot products: the block's rows of a vector as
+// pairs in shared memory
+struct DfShared {
+  const float2 *sw;
+  __device__ __forceinline__ float2 get(int t, int) const { return sw[t]; }
+};
+
 // block partial sums sacc[k] = sum over this block's rows i > lo of
-// V[k][i] w[i], k < jp1, from the double-float pairs
+// V[k][i] x[i], k < ncols, from the double-float pairs (ncols >= 1)
+template <class OP>
 __device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, const float *__restrict__ Vlo,
-                                                 size_t ldv, int jp1, int r0, int r1, int lo, const float2 *sw,
+                                                 size_t ldv, int ncols, int r0, int r1, int lo, OP x,
                                                  double *swarp, double *sacc) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nsl = r1 > r0 ? (r1 - r0 + 31) >> 5 : 0;
-  if (jp1 <= 32) {
-    const int G = 32 / jp1;
+  if (ncols <= 32) {
+    const int G = 32 / ncols;
     double acc = 0.0;
-    if (wid < G * jp1) {
-      const int k = wid % jp1, g = wid / jp1;
+    if (wid < G * ncols) {
+      const int k = wid % ncols, g = wid / ncols;
       const float *Hk = Vf + (size_t)k * ldv + r0, *Lk = Vlo + (size_t)k * ldv + r0;
       int batch = 0;
       float sh = 0.f, sl = 0.f;
@@ -998,7 +1007,7 @@ __device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, c
         for (int u = 0; u < 8; ++u) {
           const int t = 32 * (sl0 + u * G) + lane;
           const int i = r0 + t;
-          const float2 wv = (sl0 + u * G < nsl && i < r1 && i > lo) ? sw[t] : make_float2(0.f, 0.f);
+          const float2 wv = (sl0 + u * G < nsl && i < r1 && i > lo) ? x.get(t, i) : make_float2(0.f, 0.f);
           df_mac(vh[u], vl[u], wv.x, wv.y, sh, sl);
         }
         if (++batch == 4) {  // 32 terms per lane: into the FP64 sum
@@ -1012,9 +1021,9 @@ __device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, c
     }
     if (lane == 0) swarp[wid] = acc;
     __syncthreads();
-    if (threadIdx.x < jp1) {
+    if (threadIdx.x < ncols) {
       double t = 0.0;
-      for (int g = 0; g < G; ++g) t += swarp[g * jp1 + threadIdx.x];
+      for (int g = 0; g < G; ++g) t += swarp[g * ncols + threadIdx.x];
       sacc[threadIdx.x] = t;
     }
   } else {
@@ -1029,13 +1038,13 @@ __device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, c
         const int t = 32 * (sl0 + u) + lane;
         const int i = r0 + t;
         const bool ok = sl0 + u < nsl && i < r1 && i > lo;
-        wv[u] = ok ? sw[t] : make_float2(0.f, 0.f);
+        wv[u] = ok ? x.get(t, i) : make_float2(0.f, 0.f);
         ii[u] = ok ? i : r0;
       }
 #pragma unroll
       for (int c = 0; c < 5; ++c) {
         const int k = wid + 32 * c;
-        if (32 * c < jp1 && k < jp1) {
+        if (32 * c < ncols && k < ncols) {
           float vh[4], vl[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
@@ -1059,21 +1068,86 @@ __device__ __forceinline__ void hh_block_dots_df(const float *__restrict__ Vf, c
     for (int c = 0; c < 5; ++c) {
       acc[c] += to_f64(sh[c]) + to_f64(sl[c]);
       const int k = wid + 32 * c;
-      if (32 * c < jp1) {  // warp-uniform
+      if (32 * c < ncols) {  // warp-uniform
         const double v = warp_sum(acc[c]);
-        if (lane == 0 && k < jp1) swarp[k] = v;
+        if (lane == 0 && k < ncols) swarp[k] = v;
       }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < jp1; k += blockDim.x) sacc[k] = swarp[k];
+    for (int k = threadIdx.x; k < ncols; k += blockDim.x) sacc[k] = swarp[k];
   }
   __syncthreads();
 }
 
+// (h, l) summed over the warp in double-float (TwoSum at each level; every
+// lane ends with the same pair)
+__device__ __forceinline__ void warp_sum_df(float &h, float &l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+    const float t = h + h2, z = t - h;
+    const float e = (h - (t - z)) + (h2 - z);
+    h = t;
+    l = (l + l2) + e;
+  }
+}
+
+// pass C's sweep over the basis, a thread per row, eight columns at a
+// time: sgx[k] = sum over the block's rows of V[k][i] x[i] (k < ncols, x =
+// v_{j+1} as pairs in sx; double-float per thread, then over the warp, then
+// over the warps in FP64 in a fixed order) and q[i] = q0_i - sum_k V[k][i]
+// c[k] in FP32, the columns in ascending order (q0_i = e_{j+1} - v_{j+1,i}
+// c_{j+1}): each thread keeps its rows from chunk to chunk, so q is
+// deterministic.  swarp2 holds 32 x 8 pairs.
+__device__ __forceinline__ void hh_passC_rows(const float *__restrict__ Vf, const float *__restrict__ Vlo,
+                                              size_t ldv, int ncols, int r0, int r1, int jp1, const float2 *sx,
+                                              const float *scf, float *q, float2 *swarp2, double *sgx) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, T = blockDim.x;
+  const float cj1 = scf[jp1];
+  for (int k0 = 0; k0 < ncols; k0 += 8) {
+    float cf[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) cf[c] = k0 + c < ncols ? scf[k0 + c] : 0.f;
+    float sh[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, sl[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int i = r0 + threadIdx.x; i < r1; i += T) {
+      float vh[8], vl[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const bool ok = k0 + c < ncols;
+        vh[c] = ok ? Vf[(size_t)(k0 + c) * ldv + i] : 0.f;
+        vl[c] = ok ? Vlo[(size_t)(k0 + c) * ldv + i] : 0.f;
+      }
+      const float2 x = sx[i - r0];
+      float qp = k0 == 0 ? (i == jp1 ? 1.f : 0.f) - x.x * cj1 : q[i];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        df_mac(vh[c], vl[c], x.x, x.y, sh[c], sl[c]);
+        qp = fmaf(-vh[c], cf[c], qp);
+      }
+      q[i] = qp;
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      warp_sum_df(sh[c], sl[c]);
+      if (lane == 0) swarp2[wid * 8 + c] = make_float2(sh[c], sl[c]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 8 && k0 + (int)threadIdx.x < ncols) {
+      double t = 0.0;
+      for (int w = 0; w < (T >> 5); ++w) {
+        const float2 v = swarp2[w * 8 + threadIdx.x];
+        t += to_f64(v.x) + to_f64(v.y);
+      }
+      sgx[k0 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
 // rows i, i+1 (i even): sum_k V[k][i..i+1] y[k] over k < ncols in
-// double-float from the (Vf, Vlo) pairs and y's pair (yh, yl)
-__device__ __forceinline__ double2 vcomb_df_x2(const float *__restrict__ Vf, const float *__restrict__ Vlo,
-                                               size_t ldv, int i, int ncols, const float *yh, const float *yl) {
+// double-float from the (Vf, Vlo) pairs and y's pair (yh, yl), as two pairs
+__device__ __forceinline__ float4 vcomb_df_x2(const float *__restrict__ Vf, const float *__restrict__ Vlo,
+                                              size_t ldv, int i, int ncols, const float *yh, const float *yl) {
   float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
   for (int k = 0; k < ncols; k += 8) {
     float2 vh[8], vl[8];
@@ -1090,53 +1164,74 @@ __device__ __forceinline__ double2 vcomb_df_x2(const float *__restrict__ Vf, con
         df_mac(vh[u].y, vl[u].y, yh[k + u], yl[k + u], h1, l1);
       }
   }
-  return make_double2(to_f64(h0) + to_f64(l0), to_f64(h1) + to_f64(l1));
+  return make_float4(h0, l0, h1, l1);
 }
 
-__device__ __forceinline__ double vcomb_df(const float *__restrict__ Vf, const float *__restrict__ Vlo, size_t ldv,
+__device__ __forceinline__ float2 vcomb_df(const float *__restrict__ Vf, const float *__restrict__ Vlo, size_t ldv,
                                            int i, int ncols, const float *yh, const float *yl) {
   float h = 0.f, l = 0.f;
   for (int k = 0; k < ncols; ++k) df_mac(Vf[(size_t)k * ldv + i], Vlo[(size_t)k * ldv + i], yh[k], yl[k], h, l);
-  return to_f64(h) + to_f64(l);
+  return make_float2(h, l);
 }
 
 struct HHStepDF {
   HHStep base;
   float *Vlo;
+  const float2 *sell_pair;  // the operator's sliced-ELL values as pairs
+  double *carry;  // block partials of V_j^T v_{j+1}, left for the next step
 };
 
+// One Arnoldi step as one cooperative kernel, double-float dot products.
+// Pass A: w = A z_j and s = V^T w.  With g = V_j^T v_j (its block partials
+// left by the previous step), one grid fold gives s and the exact column j
+// of T and of the Gram matrix G = V^T V; y = T^T s.  Pass B: w -= V y and
+// ||w_{j+1:}||^2 (a second fold).  Then the new reflector and a
+// provisional column j+1 of T from V^T w_{j+1:} = s - G y - V_top^T w_top
+// (no pass over V, but its rounding grows with ||w|| / ||w_{j+1:}||): it
+// only forms this step's q = e_{j+1} - V T V^T e_{j+1}, the vector the
+// preconditioner is applied to next, which need not be exact - the Arnoldi
+// relation holds for any q.  Pass C: v_{j+1}, then one sweep over V forms q
+// and the exact V_j^T v_{j+1} for the next step.  The Hessenberg column and
+// its Givens rotation run last, in the block with the fewest rows.
 __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
   const HHStep &a = ad.base;
   if (a.ctrl->done) return;
-  extern __shared__ float2 swd[];  // this block's rows of w as (hi, lo)
+  extern __shared__ float2 swd[];  // this block's rows of w, then of v_{j+1}, as (hi, lo)
+  constexpr int kCap = 2 * kLdT;   // values per grid fold
   __shared__ double swarp[5 * 32];
-  __shared__ double sacc[kLdT + 1], sres[kLdT + 1];
+  __shared__ double sacc[kCap], sres[kCap];
   __shared__ double sd[kLdT], srho[kLdT], sc[kLdT];
+  __shared__ double sy[kLdT], ss[kLdT], stc[kLdT], sg[kLdT], s2[kLdT];
   __shared__ float syh[kLdT], syl[kLdT];
   __shared__ float scf[kLdT];
   __shared__ double sbuf[kHHTPB];
   __shared__ double s_dd, s_ia, s_vjj;
-  const int n = a.n, jp1 = j + 1, T = blockDim.x;
+  const int n = a.n, jp1 = j + 1, T = blockDim.x, nw = T >> 5;
   const int r0 = blockIdx.x * a.rb, r1 = min(n, r0 + a.rb);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const size_t ldv = a.ldv;
   const float *__restrict__ Vf = a.Vf;
   const float *__restrict__ Vlo = ad.Vlo;
   Cycle *cy = a.cy;
+  const int G = gridDim.x;
   int phase = 0;
-  // ---- pass A: w = A z_j (FP64, a warp per 32-row slice), kept as a pair
+  // g's block partials from the previous step, folded with s below
+  for (int k = threadIdx.x; k < j; k += T) sacc[jp1 + k] = __ldcg(&ad.carry[(size_t)k * G + blockIdx.x]);
+  // ---- pass A: w = A z_j in pair arithmetic (the operator's values as
+  // pairs, z in FP32: each product's high part exact), a warp per 32-row
+  // slice
   {
     const float *z = (const float *)a.z;
-    for (int sl = (r0 >> 5) + wid; 32 * sl < r1; sl += (T >> 5)) {
+    for (int sl = (r0 >> 5) + wid; 32 * sl < r1; sl += nw) {
       const int i = 32 * sl + lane;
       if (i < r1) {
         const int len = a.op.row[i + 1] - a.op.row[i];
         const int *cp = a.op.sell_col + a.op.sell_ptr[sl] + lane;
-        const double *vp = a.op.sell_val + (cp - a.op.sell_col);
-        double s = 0.0;
+        const float2 *vp = ad.sell_pair + (cp - a.op.sell_col);
+        float sh = 0.f, sl2 = 0.f;
         for (int t = 0; t < len; t += 8) {
           int c[8];
-          double v[8];
+          float2 v[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u)
             if (t + u < len) {
@@ -1149,51 +1244,77 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
             if (t + u < len) zv[u] = z[c[u]];
 #pragma unroll
           for (int u = 0; u < 8; ++u)
-            if (t + u < len) s = fma(v[u], to_f64(zv[u]), s);
+            if (t + u < len) df_mac1(v[u].x, v[u].y, zv[u], sh, sl2);
         }
-        swd[i - r0] = df_split(s);
+        swd[i - r0] = df_renorm(sh, sl2);
       }
     }
   }
   __syncthreads();
-  hh_block_dots_df(Vf, Vlo, ldv, jp1, r0, r1, -1, swd, swarp, sacc);
-  if (!hh_grid_fold(sacc, jp1, a.partials, phase, a.ctrl, sres)) return;
-  // y = T^T s, as a pair
-  for (int k = threadIdx.x; k < jp1; k += T) {
-    double y = 0.0;
-    for (int l = 0; l <= k; ++l) y = fma(cy->T[l + k * kLdT], sres[l], y);
-    const float2 d = df_split(y);
-    syh[k] = d.x;
-    syl[k] = d.y;
+  hh_block_dots_df(Vf, Vlo, ldv, jp1, r0, r1, -1, DfShared{swd}, swarp, sacc);
+  if (!hh_grid_fold(sacc, jp1 + j, a.partials, phase, a.ctrl, sres, kCap)) return;
+  // T(:, j) = [-2 T_j g ; 2] and G(:, j) = [g ; 1] (a warp per entry)
+  for (int k = wid; k <= j; k += nw) {
+    double t = 0.0;
+    for (int l = k + lane; l < j; l += 32) t = fma(cy->T[k + l * kLdT], sres[jp1 + l], t);
+    t = warp_sum(t);
+    if (lane == 0) {
+      stc[k] = k < j ? -2.0 * t : 2.0;
+      sg[k] = k < j ? sres[jp1 + k] : 1.0;
+    }
   }
   __syncthreads();
-  // ---- pass B: w -= V y (a row pair per thread), then V^T w over rows > j
-  // and ||w_{j+1:}||^2; rows 0..j+1 of w published for every block
-  double nrm = 0.0;
+  // y = T^T s, as a pair (and in FP64); s kept for the second dot set
+  for (int k = wid; k < jp1; k += nw) {
+    double t = 0.0;
+    for (int l = lane; l <= k; l += 32) t = fma(k < j ? cy->T[l + k * kLdT] : stc[l], sres[l], t);
+    t = warp_sum(t);
+    if (lane == 0) {
+      const float2 d = df_split(t);
+      syh[k] = d.x;
+      syl[k] = d.y;
+      sy[k] = t;
+      ss[k] = sres[k];
+    }
+  }
+  if (blockIdx.x == 0) {  // read by the later steps only
+    for (int k = threadIdx.x; k < kLdT; k += T) cy->T[k + j * kLdT] = k <= j ? stc[k] : 0.0;
+    for (int k = threadIdx.x; k <= j; k += T) {
+      cy->G[k + j * kLdT] = sg[k];
+      cy->G[j + k * kLdT] = sg[k];
+    }
+  }
+  __syncthreads();
+  // ---- pass B: w -= V y (a row pair per thread) and ||w_{j+1:}||^2, in
+  // pair arithmetic; rows 0..j+1 of w published for every block
+  double nrm;
   {
+    float nh = 0.f, nl = 0.f;
     const int p0 = r0 >> 1, p1 = r1 >> 1;
     for (int p = p0 + threadIdx.x; p < p1; p += T) {
       const int i = 2 * p;
-      const double2 c = vcomb_df_x2(Vf, Vlo, ldv, i, jp1, syh, syl);
-      const double s0 = df_join(swd[i - r0]) - c.x, s1 = df_join(swd[i + 1 - r0]) - c.y;
-      swd[i - r0] = df_split(s0);
-      swd[i + 1 - r0] = df_split(s1);
-      if (i > j) nrm = fma(s0, s0, nrm);
-      if (i + 1 > j) nrm = fma(s1, s1, nrm);
-      if (i <= jp1) cy->wtop[i] = s0;
-      if (i + 1 <= jp1) cy->wtop[i + 1] = s1;
+      const float4 c = vcomb_df_x2(Vf, Vlo, ldv, i, jp1, syh, syl);
+      const float2 s0 = df_add(swd[i - r0], make_float2(-c.x, -c.y));
+      const float2 s1 = df_add(swd[i + 1 - r0], make_float2(-c.z, -c.w));
+      swd[i - r0] = s0;
+      swd[i + 1 - r0] = s1;
+      if (i > j) df_mac(s0.x, s0.y, s0.x, s0.y, nh, nl);
+      if (i + 1 > j) df_mac(s1.x, s1.y, s1.x, s1.y, nh, nl);
+      if (i <= jp1) cy->wtop[i] = df_join(s0);
+      if (i + 1 <= jp1) cy->wtop[i + 1] = df_join(s1);
     }
     if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {  // the last row of an odd n
       const int i = r1 - 1;
-      const double s0 = df_join(swd[i - r0]) - vcomb_df(Vf, Vlo, ldv, i, jp1, syh, syl);
-      swd[i - r0] = df_split(s0);
-      if (i > j) nrm = fma(s0, s0, nrm);
-      if (i <= jp1) cy->wtop[i] = s0;
+      const float2 c = vcomb_df(Vf, Vlo, ldv, i, jp1, syh, syl);
+      const float2 s0 = df_add(swd[i - r0], make_float2(-c.x, -c.y));
+      swd[i - r0] = s0;
+      if (i > j) df_mac(s0.x, s0.y, s0.x, s0.y, nh, nl);
+      if (i <= jp1) cy->wtop[i] = df_join(s0);
     }
+    nrm = to_f64(nh) + to_f64(nl);
   }
   sbuf[threadIdx.x] = nrm;
   __syncthreads();
-  hh_block_dots_df(Vf, Vlo, ldv, jp1, r0, r1, j, swd, swarp, sacc);
   if (wid < 4) {
     const int quarter = T >> 2;
     double t = 0.0;
@@ -1202,12 +1323,23 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
     if (lane == 0) swarp[wid] = t;
   }
   __syncthreads();
-  if (threadIdx.x == 0) sacc[jp1] = ((swarp[0] + swarp[1]) + swarp[2]) + swarp[3];
+  if (threadIdx.x == 0) sacc[0] = ((swarp[0] + swarp[1]) + swarp[2]) + swarp[3];
   __syncthreads();
-  if (!hh_grid_fold(sacc, jp1 + 1, a.partials, phase, a.ctrl, sres)) return;
-  // ---- pass B's last-block work, in every block (as k_hh_step)
+  if (!hh_grid_fold(sacc, 1, a.partials, phase, a.ctrl, sres, kCap)) return;
+  const double nrm2 = jp1 < n ? sres[0] : 0.0;
+  // V^T w over rows > j after the update, without a pass over V:
+  // s - G y over all rows, less the rows <= j that their owners published
+  for (int k = wid; k < jp1; k += nw) {
+    double t = 0.0;
+    for (int l = lane; l < jp1; l += 32) {
+      const double gkl = l == j ? sg[k] : (k == j ? sg[l] : cy->G[k + l * kLdT]);
+      t = fma(gkl, sy[l], t);
+    }
+    for (int i = k + lane; i <= j; i += 32) t = fma(a.V[(size_t)k * ldv + i], __ldcg(&cy->wtop[i]), t);
+    t = warp_sum(t);
+    if (lane == 0) s2[k] = ss[k] - t;
+  }
   if (threadIdx.x == 0) {
-    const double nrm2 = jp1 < n ? sres[jp1] : 0.0;
     const double wn = sqrt(nrm2);
     const double wj1 = jp1 < n ? __ldcg(&cy->wtop[jp1]) : 0.0;
     const double dd = mysgn(wj1) * wn;
@@ -1220,24 +1352,29 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
   __syncthreads();
   for (int k = threadIdx.x; k < jp1; k += T) {
     const double vk = jp1 < n ? a.V[(size_t)k * ldv + jp1] : 0.0;
-    sd[k] = (sres[k] + s_dd * vk) * s_ia;
+    sd[k] = (s2[k] + s_dd * vk) * s_ia;
     srho[k] = vk;
   }
   if (threadIdx.x == 0) srho[jp1] = s_vjj;
   __syncthreads();
-  for (int k = threadIdx.x; k < jp1; k += T) {
+  // T's column j+1 (provisional, see above), then c = T_{j+1} rho
+  for (int k = wid; k < jp1; k += nw) {
     double t = 0.0;
-    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], sd[l], t);
-    sacc[k] = -2.0 * t;
+    for (int l = k + lane; l <= j; l += 32) t = fma(l == j ? stc[k] : cy->T[k + l * kLdT], sd[l], t);
+    t = warp_sum(t);
+    if (lane == 0) sacc[k] = -2.0 * t;
   }
   if (threadIdx.x == 0) sacc[jp1] = 2.0;
   __syncthreads();
-  for (int k = threadIdx.x; k <= jp1; k += T) {
+  for (int k = wid; k <= jp1; k += nw) {
     double t = 0.0;
-    for (int l = k; l < jp1; ++l) t = fma(cy->T[k + l * kLdT], srho[l], t);
-    t = fma(sacc[k], srho[jp1], t);
-    sc[k] = t;
-    scf[k] = (float)t;
+    for (int l = k + lane; l <= j; l += 32) t = fma(l == j ? stc[k] : cy->T[k + l * kLdT], srho[l], t);
+    t = warp_sum(t);
+    if (lane == 0) {
+      t = fma(sacc[k], srho[jp1], t);
+      sc[k] = t;
+      scf[k] = (float)t;
+    }
   }
   __syncthreads();
   if (blockIdx.x == 0) {
@@ -1247,14 +1384,65 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
     if (threadIdx.x == 0) {
       cy->dd = s_dd;
       cy->inv_alpha = s_ia;
-      double *sh = sbuf;
-      for (int k = 0; k <= j; ++k) sh[k] = __ldcg(&cy->wtop[k]);
+    }
+  }
+  // ---- pass C: v_{j+1} (pairs; FP64 for the top rows the small-matrix
+  // work reads; its pairs replace w in shared memory), then q and
+  // V_j^T v_{j+1} from one sweep over V
+  const double dd = s_dd, ia = s_ia;
+  const int ntop = a.m + 2;
+  double *vn = a.V + (size_t)jp1 * ldv;
+  float *vfn = a.Vf + (size_t)jp1 * ldv, *vln = ad.Vlo + (size_t)jp1 * ldv;
+  {
+    const float2 iad = df_split(ia);
+    const int p0 = r0 >> 1, p1 = r1 >> 1;
+    for (int p = p0 + threadIdx.x; p < p1; p += T) {
+      const int i = 2 * p;
+      const float2 z2 = make_float2(0.f, 0.f);
+      const float2 d0 = i > j ? (i == jp1 ? df_split((df_join(swd[i - r0]) + dd) * ia) : df_mul(swd[i - r0], iad)) : z2;
+      const float2 d1 =
+          i + 1 > j ? (i + 1 == jp1 ? df_split((df_join(swd[i + 1 - r0]) + dd) * ia) : df_mul(swd[i + 1 - r0], iad))
+                    : z2;
+      if (i < ntop) *reinterpret_cast<double2 *>(vn + i) = make_double2(df_join(d0), df_join(d1));
+      *reinterpret_cast<float2 *>(vfn + i) = make_float2(d0.x, d1.x);
+      *reinterpret_cast<float2 *>(vln + i) = make_float2(d0.y, d1.y);
+      swd[i - r0] = d0;
+      swd[i + 1 - r0] = d1;
+      prefill_row(a.pf, i);
+      prefill_row(a.pf, i + 1);
+    }
+    if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {
+      const int i = r1 - 1;
+      const float2 d = i > j ? (i == jp1 ? df_split((df_join(swd[i - r0]) + dd) * ia) : df_mul(swd[i - r0], iad))
+                             : make_float2(0.f, 0.f);
+      if (i < ntop) vn[i] = df_join(d);
+      vfn[i] = d.x;
+      vln[i] = d.y;
+      swd[i - r0] = d;
+      prefill_row(a.pf, i);
+    }
+  }
+  __syncthreads();
+  hh_passC_rows(Vf, Vlo, ldv, jp1, r0, r1, jp1, swd, scf, (float *)a.q, reinterpret_cast<float2 *>(sbuf), sg);
+  for (int k = threadIdx.x; k < jp1; k += T) ad.carry[(size_t)k * G + blockIdx.x] = sg[k];
+  // ---- the Hessenberg column j (rows 0..j of w, -dd below), its Givens
+  // rotation and the convergence test, in the last block (the fewest rows)
+  if (blockIdx.x == G - 1) {
+    double *sh = sbuf, *scs = sbuf + 256, *ssn = sbuf + 512;
+    if (wid == 0) {
+      for (int k = lane; k <= j; k += 32) sh[k] = __ldcg(&cy->wtop[k]);
+      for (int k = lane; k < j; k += 32) {
+        scs[k] = cy->cs[k];
+        ssn[k] = cy->sn[k];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
       for (int k = 0; k < j; ++k) {
         const double t0 = sh[k], t1 = sh[k + 1];
-        sh[k + 1] = -cy->sn[k] * t0 + cy->cs[k] * t1;
-        sh[k] = cy->cs[k] * t0 + cy->sn[k] * t1;
+        sh[k + 1] = -ssn[k] * t0 + scs[k] * t1;
+        sh[k] = scs[k] * t0 + ssn[k] * t1;
       }
-      const double dd = s_dd;
       double c, sn;
       givens_rot(sh[j], -dd, 4.9406564584124654e-324, &c, &sn);
       cy->cs[j] = c;
@@ -1276,41 +1464,6 @@ __global__ void __launch_bounds__(kHHTPB, 1) k_hh_step_df(HHStepDF ad, int j) {
         a.ctrl->done = 1;
       }
     }
-  }
-  // ---- pass C: v_{j+1} (FP64, and its pair) and q = e_{j+1} - V_{j+1} c (FP32)
-  const double dd = s_dd, ia = s_ia;
-  double *vn = a.V + (size_t)jp1 * ldv;
-  float *vfn = a.Vf + (size_t)jp1 * ldv, *vln = ad.Vlo + (size_t)jp1 * ldv;
-  float *q = (float *)a.q;
-  const int p0 = r0 >> 1, p1 = r1 >> 1;
-  for (int p = p0 + threadIdx.x; p < p1; p += T) {
-    const int i = 2 * p;
-    const double w0 = df_join(swd[i - r0]), w1 = df_join(swd[i + 1 - r0]);
-    const double v0 = (i > j) ? (i == jp1 ? w0 + dd : w0) * ia : 0.0;
-    const double v1 = (i + 1 > j) ? (i + 1 == jp1 ? w1 + dd : w1) * ia : 0.0;
-    *reinterpret_cast<double2 *>(vn + i) = make_double2(v0, v1);
-    const float2 d0 = df_split(v0), d1 = df_split(v1);
-    const float2 vf = make_float2(d0.x, d1.x);
-    *reinterpret_cast<float2 *>(vfn + i) = vf;
-    *reinterpret_cast<float2 *>(vln + i) = make_float2(d0.y, d1.y);
-    const float2 sm = vcomb8x2f(a.Vf, ldv, i, jp1, scf);
-    *reinterpret_cast<float2 *>(q + i) = make_float2(((i == jp1 ? 1.f : 0.f) - vf.x * scf[jp1]) - sm.x,
-                                                     ((i + 1 == jp1 ? 1.f : 0.f) - vf.y * scf[jp1]) - sm.y);
-    prefill_row(a.pf, i);
-    prefill_row(a.pf, i + 1);
-  }
-  if ((r1 & 1) && r1 > r0 && threadIdx.x == 0) {
-    const int i = r1 - 1;
-    const double wi = df_join(swd[i - r0]);
-    const double v = (i > j) ? (i == jp1 ? wi + dd : wi) * ia : 0.0;
-    vn[i] = v;
-    const float2 d = df_split(v);
-    vfn[i] = d.x;
-    vln[i] = d.y;
-    float sm = 0.f;
-    for (int k = 0; k < jp1; ++k) sm = fmaf(a.Vf[(size_t)k * ldv + i], scf[k], sm);
-    q[i] = ((i == jp1 ? 1.f : 0.f) - d.x * scf[jp1]) - sm;
-    prefill_row(a.pf, i);
   }
 }
 
@@ -1400,17 +1553,20 @@ __global__ void __launch_bounds__(kTPB) k_xupdate(int n, const ZT *__restrict__ 
 
 
 __global__ void k_sell_values(size_t count, const int *__restrict__ map, const double *__restrict__ src,
-                              double *__restrict__ dst) {
+                              double *__restrict__ dst, float2 *__restrict__ pair) {
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (size_t)gridDim.x * blockDim.x) {
     const int e = map[q];
-    dst[q] = e >= 0 ? src[e] : 0.0;
+    const double v = e >= 0 ? src[e] : 0.0;
+    dst[q] = v;
+    pair[q] = df_split(v);
   }
 }
 
-void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst) {
+void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst,
+                        float2 *pair) {
   if (count == 0) return;
   const int grid = (int)std::min<size_t>((size_t)num_sms() * 8, (count + 255) / 256);
-  k_sell_values<<<grid, 256, 0, s>>>(count, map, src, dst);
+  k_sell_values<<<grid, 256, 0, s>>>(count, map, src, dst, pair);
 }
 
 
@@ -1564,7 +1720,9 @@ static int hh_step_df(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t,
   HHStep &p = pd.base;
   p.n = a.n;
   p.rb = ((a.n + G - 1) / G + 31) / 32 * 32;
-  if ((size_t)p.rb * 8 > (size_t)kHHSmemMax || (size_t)G * kLdT * 2 > (size_t)a.grid * kLdT) return 1;
+  // two phases of 2 kLdT fold values per block, then the carried partials,
+  // in the partials buffer
+  if ((size_t)p.rb * 8 > (size_t)kHHSmemMax || (size_t)G * kLdT * 5 > (size_t)a.grid * kLdT) return 1;
   p.op = opview(a);
   p.z = (const char *)a.Z + (size_t)j * a.ldz * sizeof(float);
   p.V = a.V;
@@ -1581,6 +1739,8 @@ static int hh_step_df(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t,
     p.pf.z = mark_z;
   }
   pd.Vlo = a.Vlo;
+  pd.carry = a.partials + (size_t)4 * kLdT * G;
+  pd.sell_pair = a.sell_pair;
   void *args[] = {&pd, &j};
   if (cudaLaunchCooperativeKernel((const void *)k_hh_step_df, dim3(G), dim3(kHHTPB), args, (size_t)p.rb * 8, s) !=
       cudaSuccess) {
@@ -1592,7 +1752,7 @@ static int hh_step_df(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t,
 
 int launch_hh_step(cudaStream_t s, const ArnoldiArgs &a, int j, void *mark_t, void *mark_z) {
   if (a.bs || !a.sell_ptr) return 1;
-  if (a.z_f32 && a.q_f32 && a.Vf && a.Vlo) return hh_step_df(s, a, j, mark_t, mark_z);
+  if (a.z_f32 && a.q_f32 && a.Vf && a.Vlo && a.sell_pair) return hh_step_df(s, a, j, mark_t, mark_z);
   if (a.z_f32 && a.q_f32 && a.Vf) return hh_step_t<float, float>(s, a, j, mark_t, mark_z);
   if (!a.z_f32 && !a.q_f32) return hh_step_t<double, double>(s, a, j, mark_t, mark_z);
   return 1;

@@ -142,6 +142,35 @@ __device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, f
   const float e = (sh - (t - z)) + (p - z);
   sh = t;
   sl += e + pe;
+}// (sh, sl) += (ah + al) * b for an FP32 b
+__device__ __forceinline__ void df_mac1(float ah, float al, float b, float &sh, float &sl) {
+  const float p = ah * b;
+  const float pe = fmaf(al, b, fmaf(ah, b, -p));
+  const float t = sh + p;
+  const float z = t - sh;
+  const float e = (sh - (t - z)) + (p - z);
+  sh = t;
+  sl += e + pe;
+}
+
+// pair arithmetic for values kept as pairs: h + l as an unevaluated sum
+// renormalised (TwoSum: exact for any magnitudes), a + b (the high parts
+// summed error-free, the low parts added) and a * b (the high product
+// exactly, the cross terms in FP32, a.lo * b.lo dropped)
+__device__ __forceinline__ float2 df_renorm(float h, float l) {
+  const float t = h + l, z = t - h;
+  return make_float2(t, (h - (t - z)) + (l - z));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float t = a.x + b.x, z = t - a.x;
+  const float e = (a.x - (t - z)) + (b.x - z);
+  return df_renorm(t, e + (a.y + b.y));
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  const float e = fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p)));
+  const float s = p + e;  // |e| <= |p| up to rounding: Fast2Sum
+  return make_float2(s, e - (s - p));
 }
 
 // the unsolved pattern (all ones) into row i of an FP32 or FP64 vector: the
