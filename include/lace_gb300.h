@@ -288,12 +288,24 @@ int data_zmconvert(data_d_matrix A, data_d_matrix *B, data_storage_t old_format,
 int data_zmtranspose(data_d_matrix A, data_d_matrix *B);
 int data_rowindex(data_d_matrix *A, int **rowidx);
 
-/* Replaces control/norms.cpp:301 for the nonlinear residual: *nonlinres =
- * ||(A - L U)|_S(A)||_F computed on the GPU on A's pattern; *res receives
- * the same value (the fill-in part of LACE's res is not formed) and LU is
- * left untouched.  L: Magma_CSRL, U: Magma_CSCU or Magma_CSRU. */
+/* Replaces control/norms.cpp:301: *res = ||A - L U||_F over the product's
+ * pattern (fill-in included) and *nonlinres = the same over the entries of
+ * A the product holds, on the GPU without forming L U.  L: CSRL with its
+ * unit diagonal stored (L.row[1] == 1) or strictly lower (L.row[1] == 0),
+ * U: Magma_CSCU or Magma_CSRU.  LU is not formed; the caller's matrix is
+ * left as passed. */
 int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U,
                  data_d_matrix *LU, dataType *res, dataType *nonlinres);
+
+/* Replaces control/norms.cpp:409 (data_zilures_bcsr): L and U read as BCSR
+ * (num_rows block rows of blocksize^2 row-major blocks), every block entry
+ * expanded to scalar CSR as LACE's BCSR -> CSR conversion does, their
+ * product measured against A (scalar CSR, num_rows = blocks x blocksize)
+ * as data_zilures does, L's values as stored.  LACE reads both factors with
+ * the BCSR reader whatever their storage tag, and so does this.  LU is not
+ * formed. */
+int data_zilures_bcsr(data_d_matrix A, data_d_matrix L, data_d_matrix U,
+                      data_d_matrix *LU, dataType *res, dataType *nonlinres);
 
 /* ------------------------------------------------------------------------
  * 2. GPU-resident API

@@ -157,6 +157,7 @@ SIGNATURES = {
     "data_fgmres_restart": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_fgmres": (_i, [_DM, _DM, _DM, _DM, _DM, C.POINTER(GmresParam), C.POINTER(GmresLog)]),
     "data_zilures": (_i, [DataMatrix, DataMatrix, DataMatrix, _DM, C.POINTER(_d), C.POINTER(_d)]),
+    "data_zilures_bcsr": (_i, [DataMatrix, DataMatrix, DataMatrix, _DM, C.POINTER(_d), C.POINTER(_d)]),
     "read_z_csr_from_mtx": (_i, [C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), C.POINTER(_p),
                                  C.POINTER(_p), C.POINTER(_p), C.c_char_p]),
     "data_z_csr_mtx": (_i, [_DM, C.c_char_p]),

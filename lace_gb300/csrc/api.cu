@@ -3,6 +3,7 @@
 // runs on the GPU through a process-wide context and writes the results back
 // into the same containers, allocating output arrays the way LACE does
 // (64-byte aligned, released with free() by data_zmfree).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -531,11 +532,39 @@ extern "C" int data_fgmres(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0
   return fgmres_dropin(A, b, x0, L, U, gmres_par, gmres_log, 1, 1, 0);
 }
 
+// LACE's ILU residual pair (control/norms.cpp:301-405): res = ||A - LU||_F
+// over the product's pattern (fill included) and nonlinres over the entries
+// of A it holds, without forming LU.  L: CSRL with its unit diagonal stored
+// (L.row[1] == 1), or strictly lower (L.row[1] == 0: the unit diagonal is
+// implied, :327-349), as LACE tells them apart; U: CSRU or CSCU.  *LU is not
+// formed: the caller's matrix is left as passed (LACE's callers only free it).
 extern "C" int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U, data_d_matrix *LU,
                             dataType *res, dataType *nonlinres) {
   (void)LU;
   if (!res || !nonlinres) return set_err(DEV_ERR_INVALID_PTR);
-  if (!is_csr(A.storage_type)) return set_err(DEV_ERR_NOT_SUPPORTED);
+  if (!is_csr(A.storage_type) || !L.row || !U.row) return set_err(DEV_ERR_NOT_SUPPORTED);
+  const int n = A.num_rows;
+  if (L.num_rows != n || U.num_rows != n || n < 1) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  std::vector<int> lp, li;
+  std::vector<double> lv;
+  if (L.row[1] == 1) {
+    lp.assign(L.row, L.row + n + 1);
+    li.assign(L.col, L.col + L.row[n]);
+    lv.assign(L.val, L.val + L.row[n]);
+  } else if (L.row[1] == 0) {  // strictly lower: the unit diagonal appended to each row
+    lp.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+      for (int p = L.row[i]; p < L.row[i + 1]; ++p) {
+        li.push_back(L.col[p]);
+        lv.push_back(L.val[p]);
+      }
+      li.push_back(i);
+      lv.push_back(1.0);
+      lp[i + 1] = (int)li.size();
+    }
+  } else {
+    return set_err(DEV_ERR_NOT_SUPPORTED);  // LACE: "L neither lower nor strictly lower triangular"
+  }
   std::lock_guard<std::mutex> lk(g_mu);
   lace_gpu_ctx *c = nullptr;
   int rc = default_ctx(&c);
@@ -543,21 +572,121 @@ extern "C" int data_zilures(data_d_matrix A, data_d_matrix L, data_d_matrix U, d
   lace_gpu_options o;
   lace_gpu_default_options(&o);
   lace_gpu_set_options(c, &o);
-  const int n = A.num_rows;
   rc = lace_gpu_upload_csr_host(c, n, A.row[n], A.row, A.col, A.val);
   if (rc) return set_err(rc);
   std::vector<int> up, ui;
   std::vector<double> uv;
   u_as_csr(&U, up, ui, uv);
-  rc = c->set_factors_host(n, L.row, L.col, L.val, up.data(), ui.data(), uv.data());
+  rc = c->set_factors_host(n, lp.data(), li.data(), lv.data(), up.data(), ui.data(), uv.data());
+  if (!rc) rc = c->ilu_residuals(res, nonlinres);
+  return rc ? set_err(rc) : DEV_SUCCESS;
+}
+
+namespace {
+
+// a BCSR matrix (block rows nb, blocks bs x bs stored row-major) as scalar
+// CSR holding every entry of every block, rows sorted by column (LACE's
+// BCSR -> CSR conversion through mkl_dcsrbsr, control/magma_zmconverter.cpp:
+// 802-836)
+int bcsr_expand(const data_d_matrix &B, int nb, int bs, std::vector<int> &ptr, std::vector<int> &idx,
+                std::vector<double> &val) {
+  if (!B.row || !B.col || !B.val || B.row[0] != 0) return DEV_ERR_ILLEGAL_VALUE;
+  const int ld = bs * bs;
+  for (int I = 0; I < nb; ++I)
+    if (B.row[I + 1] < B.row[I]) return DEV_ERR_ILLEGAL_VALUE;
+  for (int p = 0; p < B.row[nb]; ++p)
+    if (B.col[p] < 0 || B.col[p] >= nb) return DEV_ERR_ILLEGAL_VALUE;
+  const int n = nb * bs;
+  ptr.assign(n + 1, 0);
+  for (int I = 0; I < nb; ++I)
+    for (int r = 0; r < bs; ++r) ptr[I * bs + r + 1] = (B.row[I + 1] - B.row[I]) * bs;
+  for (int i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
+  idx.resize(ptr[n]);
+  val.resize(ptr[n]);
+  std::vector<std::pair<int, double>> row;
+  for (int I = 0; I < nb; ++I)
+    for (int r = 0; r < bs; ++r) {
+      row.clear();
+      for (int p = B.row[I]; p < B.row[I + 1]; ++p)
+        for (int c = 0; c < bs; ++c) row.emplace_back(B.col[p] * bs + c, B.val[(size_t)p * ld + r * bs + c]);
+      std::stable_sort(row.begin(), row.end(),
+                       [](const std::pair<int, double> &x, const std::pair<int, double> &y) { return x.first < y.first; });
+      int q = ptr[I * bs + r];
+      for (const auto &e : row) {
+        idx[q] = e.first;
+        val[q++] = e.second;
+      }
+    }
+  return 0;
+}
+
+}  // namespace
+
+// data_zilures_bcsr (control/norms.cpp:409-468): L and U are read as BCSR
+// (block rows L.num_rows, blocks L.blocksize^2, row-major) and expanded to
+// scalar CSR with every block entry, their product measured against A
+// (scalar CSR, num_rows = blocks x blocksize) as data_zilures does, L's
+// values as stored.  LACE converts both factors with the BCSR reader
+// whatever their storage tag, so a BCSCU U is read as its block transpose
+// there and here alike.  *LU is not formed.
+extern "C" int data_zilures_bcsr(data_d_matrix A, data_d_matrix L, data_d_matrix U, data_d_matrix *LU,
+                                 dataType *res, dataType *nonlinres) {
+  (void)LU;
+  if (!res || !nonlinres) return set_err(DEV_ERR_INVALID_PTR);
+  if (!is_csr(A.storage_type) || !A.row) return set_err(DEV_ERR_NOT_SUPPORTED);
+  const int bs = L.blocksize, nb = L.num_rows;
+  if (bs <= 0 || U.blocksize != bs || U.num_rows != nb || nb < 1) return set_err(DEV_ERR_NOT_SUPPORTED);
+  const int n = nb * bs;
+  if (A.num_rows != n) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  std::vector<int> lp, li, up, ui;
+  std::vector<double> lv, uv;
+  int rc = bcsr_expand(L, nb, bs, lp, li, lv);
+  if (!rc) rc = bcsr_expand(U, nb, bs, up, ui, uv);
   if (rc) return set_err(rc);
-  // the residual kernel walks A's rows with L (CSRL) and U (CSCU) current values
+  for (int p = 0; p < A.row[n]; ++p)
+    if (A.col[p] < 0 || A.col[p] >= n) return set_err(DEV_ERR_ILLEGAL_VALUE);
+  // U's CSC image for the entries of A
+  Pattern P, Tp;
+  P.n = n;
+  P.ptr = up;
+  P.idx = ui;
+  std::vector<int> t2p;
+  transpose_pattern(P, Tp, t2p);
+  std::vector<double> ucv(t2p.size());
+  for (size_t q = 0; q < t2p.size(); ++q) ucv[q] = uv[t2p[q]];
+  std::lock_guard<std::mutex> lk(g_mu);
+  lace_gpu_ctx *c = nullptr;
+  rc = default_ctx(&c);
+  if (rc) return set_err(rc);
+  DBuf dAr, dAc, dAv, dLr, dLc, dLv, dUr, dUc, dUv, dCp, dCi, dCv;
+  const cudaStream_t s = c->stream;
+  if (dAr.upload(A.row, 4 * (size_t)(n + 1), s) || dAc.upload(A.col, 4 * (size_t)A.row[n] + 4, s) ||
+      dAv.upload(A.val, 8 * (size_t)A.row[n] + 8, s) || dLr.upload(lp.data(), 4 * lp.size(), s) ||
+      dLc.upload(li.data(), 4 * li.size() + 4, s) || dLv.upload(lv.data(), 8 * lv.size() + 8, s) ||
+      dUr.upload(up.data(), 4 * up.size(), s) || dUc.upload(ui.data(), 4 * ui.size() + 4, s) ||
+      dUv.upload(uv.data(), 8 * uv.size() + 8, s) || dCp.upload(Tp.ptr.data(), 4 * Tp.ptr.size(), s) ||
+      dCi.upload(Tp.idx.data(), 4 * Tp.idx.size() + 4, s) || dCv.upload(ucv.data(), 8 * ucv.size() + 8, s))
+    return set_err(DEV_ERR_DEVICE_ALLOC);
   IluArgs a = c->ilu_args();
-  launch_ilu_residual(c->stream, a, c->vtype(), c->Lv[c->cur].p, c->Ucv[c->cur].p, (double *)c->scal_buf.p + 41);
-  cudaMemcpyAsync(c->h_scal + 41, (double *)c->scal_buf.p + 41, 8, cudaMemcpyDeviceToHost, c->stream);
-  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return set_err(DEV_ERR_UNKNOWN);
-  *nonlinres = std::sqrt(c->h_scal[41]);
-  *res = *nonlinres;
+  a.n = n;
+  a.nnzA = A.row[n];
+  a.Arow = (const int *)dAr.p;
+  a.Acol = (const int *)dAc.p;
+  a.Aval = (const double *)dAv.p;
+  a.Lrow = (const int *)dLr.p;
+  a.Lcol = (const int *)dLc.p;
+  a.Ucp = (const int *)dCp.p;
+  a.Uri = (const int *)dCi.p;
+  a.bs = 0;
+  if (!a.partials) return set_err(DEV_ERR_DEVICE_ALLOC);
+  double *d = (double *)c->scal_buf.p + 42;
+  launch_lu_fro(s, a, VType::F64, (const int *)dUr.p, (const int *)dUc.p, dLv.p, dUv.p, dCv.p, d, 0);
+  if (cudaMemcpyAsync(c->h_scal + 42, d, 3 * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return set_err(DEV_ERR_UNKNOWN);
+  const double fro = c->h_scal[42], onS = c->h_scal[43], nl2 = c->h_scal[44];
+  *nonlinres = std::sqrt(nl2);
+  *res = std::sqrt(std::max(0.0, nl2 + fro - onS));
   return DEV_SUCCESS;
 }
 

@@ -1338,7 +1338,7 @@ int lace_gpu_ctx::ilu_residuals(double *res, double *nonlin) {
   const VType t = vtype();
   // one kernel: ||LU||^2, sum over S(A) of (LU)_ij^2 and of (LU - A)_ij^2
   double *d = (double *)scal_buf.p + 42;
-  launch_lu_fro(stream, a, t, (const int *)Urow.p, (const int *)Ucol.p, Lv[cur].p, Urv.p, Ucv[cur].p, d);
+  launch_lu_fro(stream, a, t, (const int *)Urow.p, (const int *)Ucol.p, Lv[cur].p, Urv.p, Ucv[cur].p, d, 1);
   LCHK(cudaMemcpyAsync(h_scal + 42, d, 3 * 8, cudaMemcpyDeviceToHost, stream));
   LCHK(cudaStreamSynchronize(stream));
   const double fro = h_scal[42], onS = h_scal[43], nl2 = h_scal[44];

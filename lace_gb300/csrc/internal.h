@@ -223,10 +223,12 @@ void launch_factor_gather_blk(cudaStream_t s, int count, int bs, const int *map,
 // ||(A - LU)|_S||_F^2 to *out (device)
 void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *L, const void *U,
                          double *out);
-// out2 = {||LU||_F^2, sum over S(A) of (LU)_ij^2}; Urow/Ucol/Ur: U in CSR,
-// a.Ucp/a.Uri + Uc: U in CSC (same values)
+// out3 = {||LU||_F^2, sum over S of (LU)_ij^2, sum over S of (LU - A)_ij^2}
+// with S the entries of A the product's pattern holds; Urow/Ucol/Ur: U in
+// CSR, a.Ucp/a.Uri + Uc: U in CSC (same values); unit: L's diagonal counts
+// as 1
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
-                   const void *L, const void *Ur, const void *Uc, double *out3);
+                   const void *L, const void *Ur, const void *Uc, double *out3, int unit);
 // the sliced-ELL values of the operator: dst[q] = map[q] >= 0 ? src[map[q]] : 0
 void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst,
                         float2 *pair);

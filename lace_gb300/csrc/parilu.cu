@@ -135,23 +135,26 @@ __global__ void __launch_bounds__(kPTPB) k_ilu_residual(
 // sum_k l_ik U(k,:), so ||(LU)(i,:)||^2 = sum_{k,k'} l_ik l_ik' <U(k,:),U(k',:)>
 // (sparse dots of U's CSR rows).  With the S(A) part of the ILU residual this
 // gives LACE's full residual ||LU - A|| over pattern(LU) (control/norms.cpp:
-// 389-398) without forming LU:  res^2 = sum_S (LU-A)^2 + ||LU||^2 - sum_S LU^2.
+// 389-398) without forming LU:  res^2 = sum_S (LU-A)^2 + ||LU||^2 - sum_S LU^2,
+// S = the entries of A that the product's pattern holds (LACE skips the
+// others, :380-388).  unit: L's diagonal entries count as 1 (a CSRL L with
+// unit diagonal); otherwise L's values as stored (data_zilures_bcsr).
 template <typename FT, typename CT>
 __global__ void __launch_bounds__(kPTPB) k_lu_fro(
     int n, const int *__restrict__ Arow, const int *__restrict__ Acol, const double *__restrict__ Aval,
     const int *__restrict__ Lrow, const int *__restrict__ Lcol, const FT *__restrict__ L,
     const int *__restrict__ Urow, const int *__restrict__ Ucol, const FT *__restrict__ Ur,
     const int *__restrict__ Ucp, const int *__restrict__ Uri, const FT *__restrict__ Uc, double *partials,
-    int *counter, double *out3) {
+    int *counter, double *out3, int unit) {
   double fro = 0.0, onS = 0.0, nl = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int lb = Lrow[i], le = Lrow[i + 1];
     for (int a = lb; a < le; ++a) {
       const int k = Lcol[a];
-      const double lk = (k == i) ? 1.0 : fval(L[a]);
+      const double lk = (unit && k == i) ? 1.0 : fval(L[a]);
       for (int b = a; b < le; ++b) {
         const int k2 = Lcol[b];
-        const double lk2 = (k2 == i) ? 1.0 : fval(L[b]);
+        const double lk2 = (unit && k2 == i) ? 1.0 : fval(L[b]);
         double dot = 0.0;
         int p = Urow[k], q = Urow[k2];
         const int pe = Urow[k + 1], qe = Urow[k2 + 1];
@@ -173,12 +176,14 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
     for (int p = Arow[i]; p < Arow[i + 1]; ++p) {
       const int j = Acol[p];
       double t = 0.0;
+      bool hit = false;
       int il = lb, iu = Ucp[j];
       const int ue = Ucp[j + 1];
       while (il < le && iu < ue) {
         const int jl = Lcol[il], ju = Uri[iu];
         if (jl == ju) {
-          t = fma(jl == i ? 1.0 : fval(L[il]), fval(Uc[iu]), t);
+          t = fma((unit && jl == i) ? 1.0 : fval(L[il]), fval(Uc[iu]), t);
+          hit = true;
           ++il;
           ++iu;
         } else if (jl < ju) {
@@ -187,6 +192,7 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
           ++iu;
         }
       }
+      if (!hit) continue;  // (i, j) is not in the product's pattern
       onS = fma(t, t, onS);
       const double d = t - Aval[p];  // the nonlinear residual's entry, from the same product
       nl = fma(d, d, nl);
@@ -213,20 +219,20 @@ __global__ void __launch_bounds__(kPTPB) k_lu_fro(
 }
 
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
-                   const void *L, const void *Ur, const void *Uc, double *out3) {
+                   const void *L, const void *Ur, const void *Uc, double *out3, int unit) {
   const int grid = sweep_grid_pub(a.n);
   if (t == VType::F64)
     k_lu_fro<double, double><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const double *)L,
                                                     Urow, Ucol, (const double *)Ur, a.Ucp, a.Uri,
-                                                    (const double *)Uc, a.partials, a.counter, out3);
+                                                    (const double *)Uc, a.partials, a.counter, out3, unit);
   else if (t == VType::F32)
     k_lu_fro<float, float><<<grid, kPTPB, 0, s>>>(a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const float *)L,
                                                   Urow, Ucol, (const float *)Ur, a.Ucp, a.Uri, (const float *)Uc,
-                                                  a.partials, a.counter, out3);
+                                                  a.partials, a.counter, out3, unit);
   else
     k_lu_fro<__nv_bfloat16, float><<<grid, kPTPB, 0, s>>>(
         a.n, a.Arow, a.Acol, a.Aval, a.Lrow, a.Lcol, (const __nv_bfloat16 *)L, Urow, Ucol,
-        (const __nv_bfloat16 *)Ur, a.Ucp, a.Uri, (const __nv_bfloat16 *)Uc, a.partials, a.counter, out3);
+        (const __nv_bfloat16 *)Ur, a.Ucp, a.Uri, (const __nv_bfloat16 *)Uc, a.partials, a.counter, out3, unit);
 }
 
 // ---------------------------------------------------------------- BCSR

@@ -298,3 +298,12 @@ def zilures(A: Mat, L: Mat, U: Mat):
     LU = DataMatrix()
     rc = lib().data_zilures(A.m, L.m, U.m, C.byref(LU), C.byref(res), C.byref(nl))
     return res.value, nl.value, rc
+
+
+def zilures_bcsr(A: Mat, L: Mat, U: Mat):
+    """data_zilures_bcsr: A a scalar CSR container, L and U BCSR containers."""
+    res = C.c_double()
+    nl = C.c_double()
+    LU = DataMatrix()
+    rc = lib().data_zilures_bcsr(A.m, L.m, U.m, C.byref(LU), C.byref(res), C.byref(nl))
+    return res.value, nl.value, rc

@@ -278,6 +278,55 @@ def zilures(row, col, val, F: Factors) -> tuple[float, float]:
     return r.value, nl.value
 
 
+def bcsr_expand(row, col, val, bs):
+    """LACE's BCSR -> CSR conversion (control/magma_zmconverter.cpp:802-836,
+    through mkl_dcsrbsr): every entry of every block, blocks row-major ->
+    (ptr, idx, val) scalar CSR, each row in block order."""
+    row = np.asarray(row)
+    col = np.asarray(col)
+    blk = np.asarray(val, dtype=np.float64).reshape(-1, bs, bs)
+    nb = len(row) - 1
+    ptr = [0]
+    idx = []
+    out = []
+    for I in range(nb):
+        for r in range(bs):
+            for p in range(row[I], row[I + 1]):
+                idx.extend(range(col[p] * bs, col[p] * bs + bs))
+                out.extend(blk[p, r, :].tolist())
+            ptr.append(len(idx))
+    return np.array(ptr, np.int32), np.array(idx, np.int32), np.array(out)
+
+
+def zilures_bcsr(arow, acol, aval, L, U, bs) -> tuple[float, float]:
+    """data_zilures_bcsr (control/norms.cpp:409-468) -> (res, nonlinres).
+    A scalar CSR; L and U as (row, col, val) BCSR triples read with the BCSR
+    reader (:427-432), every block entry kept; LU = L U with the structural
+    pattern of the sparse product (:436); then LACE's two sums (:439-460):
+    entries of A the product holds become LU - A, nonlinres over those, res
+    over all of LU.  Loops: small cases only."""
+    lp, li, lv = bcsr_expand(*L, bs)
+    up, ui, uv = bcsr_expand(*U, bs)
+    n = len(lp) - 1
+    res = 0.0
+    nl = 0.0
+    for i in range(n):
+        lu = {}
+        for a in range(lp[i], lp[i + 1]):
+            k = li[a]
+            for b in range(up[k], up[k + 1]):
+                lu[ui[b]] = lu.get(ui[b], 0.0) + lv[a] * uv[b]
+        for p in range(arow[i], arow[i + 1]):
+            j = int(acol[p])
+            if j in lu:
+                t = lu[j] - aval[p]
+                lu[j] = t
+                nl += t * t
+        for v in lu.values():
+            res += v * v
+    return float(np.sqrt(res)), float(np.sqrt(nl))
+
+
 # ------------------------------------------------------------ kernels
 
 def spmv(row, col, val, x, alpha=1.0, beta=0.0, y=None) -> np.ndarray:

@@ -54,6 +54,22 @@ int ref_zilures(const data_d_matrix *A, const data_d_matrix *L,
   return info;
 }
 
+/* LACE's BCSR -> CSR conversion sizes the CSR row pointers by the block
+ * rows (control/magma_zmconverter.cpp:250-255, 285) while mkl_dcsrbsr writes
+ * one per scalar row (:836): with blocksize > 1 that overruns the array.
+ * LACE's own pad_rows / pad_cols size it; the copies passed here carry the
+ * scalar size so that the routine runs as written. */
+int ref_zilures_bcsr(const data_d_matrix *A, const data_d_matrix *L,
+                     const data_d_matrix *U, double *res, double *nonlinres) {
+  data_d_matrix LU = {Magma_CSR};
+  data_d_matrix Lc = *L, Uc = *U;
+  Lc.pad_rows = Lc.pad_cols = L->num_rows * L->blocksize;
+  Uc.pad_rows = Uc.pad_cols = U->num_rows * U->blocksize;
+  int info = data_zilures_bcsr(*A, Lc, Uc, &LU, res, nonlinres);
+  data_zmfree(&LU);
+  return info;
+}
+
 int ref_spmv(double alpha, data_d_matrix *A, const double *x, double beta,
              double *y) {
   data_d_matrix *xv = ref_vec_new(A->num_cols, x);

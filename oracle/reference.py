@@ -78,6 +78,7 @@ def _load(path: str) -> C.CDLL:
         if path == LIB:
             L.ref_parilu.argtypes = [vp, C.c_double, C.c_int, C.POINTER(vp), C.POINTER(vp), vp]
             L.ref_zilures.argtypes = [vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.ref_zilures_bcsr.argtypes = [vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.ref_spmv.argtypes = [C.c_double, vp, vp, C.c_double, vp]
             L.ref_parcsrtrsv.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp,
                                          C.c_double, C.POINTER(C.c_int)]
@@ -193,6 +194,15 @@ def zilures(A: Mat, Lm: Mat, Um: Mat):
     r = C.c_double()
     nl = C.c_double()
     lib().ref_zilures(A.h, Lm.h, Um.h, C.byref(r), C.byref(nl))
+    return r.value, nl.value
+
+
+def zilures_bcsr(A: Mat, Lm: Mat, Um: Mat):
+    """LACE's data_zilures_bcsr (control/norms.cpp:409-468): A scalar CSR,
+    L and U BCSR handles."""
+    r = C.c_double()
+    nl = C.c_double()
+    lib().ref_zilures_bcsr(A.h, Lm.h, Um.h, C.byref(r), C.byref(nl))
     return r.value, nl.value
 
 

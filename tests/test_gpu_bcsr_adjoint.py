@@ -263,3 +263,25 @@ def test_adjoint_at_64_cubed(lg, torch_cuda):
                     search_max=50, restart_max=40, rtol=1e-13)
     assert ra.converged
     assert relmax(gb, ra.x) <= 1e-8
+
+
+@pytest.mark.parametrize("case", ["lace_layout", "bcsr_u", "random"])
+def test_dropin_zilures_bcsr(lg, case):
+    """data_zilures_bcsr on the GPU against the oracle's restatement (pinned
+    to LACE's build in test_oracle.py): res over the product's pattern and
+    nonlinres over A's entries it holds, 1e-12 relative."""
+    from lace_gb300 import dropin
+    from test_oracle import _zilures_bcsr_cases
+    A, L, U, bs = _zilures_bcsr_cases()[case]
+    r_or, nl_or = orc.zilures_bcsr(A.row, A.col, A.val, L, U, bs)
+    nb = len(L[0]) - 1
+    Lb = dropin.bcsr(P.BCSR(nb, bs, L[0], L[1], np.asarray(L[2]).reshape(-1, bs, bs)))
+    Ub = dropin.bcsr(P.BCSR(nb, bs, U[0], U[1], np.asarray(U[2]).reshape(-1, bs, bs)))
+    r, nl, rc = dropin.zilures_bcsr(dropin.csr(A.row, A.col, A.val, A.n), Lb, Ub)
+    assert rc == 0
+    assert r == pytest.approx(r_or, rel=1e-12)
+    assert nl == pytest.approx(nl_or, rel=1e-10, abs=1e-13 * r_or)
+    # an A whose size is not blocks x blocksize answers with a code
+    S = P.laplace2d(4)
+    _, _, rc = dropin.zilures_bcsr(dropin.csr(S.row, S.col, S.val, S.n), Lb, Ub)
+    assert rc == -104

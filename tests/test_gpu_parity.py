@@ -136,6 +136,10 @@ def test_parilu_sync_sweeps(lg, name, sweeps):
                                  dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU))
     assert rc == 0
     assert abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14 * info["A_Frobenius"]
+    # and LACE's res, over the product's pattern (fill-in included)
+    res_or, _ = orc.zilures(A.row, A.col, A.val, F)
+    assert abs(r2 - res_or) <= 1e-12 * res_or
+    assert r2 > nl2
 
 
 @pytest.mark.parametrize("name", ["lap64", "cd16"])
@@ -560,6 +564,7 @@ def test_dropin_parilu_vs_exact_ilu0(lg):
     U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
     r2, nl2, rc = dropin.zilures(Am, L, U)
     assert rc == 0 and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-13
+    assert abs(r2 - res) <= 1e-12 * res
 
 
 def test_dropin_spmv_and_parcsrtrsv(lg):
@@ -669,3 +674,23 @@ def test_orthogonality_monitor_matches_oracle(lg, torch_cuda, prec):
         assert np.all(oh < 1e-12) and np.all(np.abs(oh[:k] - r.orth_hist[:k]) <= 1e-13)
     else:
         assert np.all(oh < 1e-5)
+
+
+def test_dropin_zilures_strictly_lower_l(lg):
+    """data_zilures tells a CSRL L with its unit diagonal stored (L.row[1] ==
+    1) from a strictly lower one (L.row[1] == 0, the diagonal implied;
+    control/norms.cpp:322-349): both give LACE's pair, the oracle's."""
+    from lace_gb300 import dropin
+    A = P.convdiff3d(6)
+    F = orc.parilu(A.row, A.col, A.val, 2, mode="sync")
+    res, nl = orc.zilures(A.row, A.col, A.val, F)
+    Am = dropin.csr(A.row, A.col, A.val, A.n)
+    U = dropin.csr(F.U.ptr, F.U.idx, F.U.val, A.n, dropin.Magma_CSCU)
+    keep = np.ones(len(F.L.idx), bool)
+    keep[F.L.ptr[1:] - 1] = False  # each row's diagonal, stored last
+    sp = (F.L.ptr - np.arange(A.n + 1)).astype(np.int32)
+    for L in (dropin.csr(F.L.ptr, F.L.idx, F.L.val, A.n, dropin.Magma_CSRL),
+              dropin.csr(sp, F.L.idx[keep], F.L.val[keep], A.n, dropin.Magma_CSRL)):
+        r2, nl2, rc = dropin.zilures(Am, L, U)
+        assert rc == 0
+        assert abs(r2 - res) <= 1e-12 * res and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14

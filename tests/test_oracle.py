@@ -341,3 +341,51 @@ def test_live_reference_fgmres_mgs(restarted):
 def test_live_reference_block_inverse():
     a = np.eye(5) * 5 + 0.1 * np.random.default_rng(0).standard_normal((5, 5))
     assert np.allclose(ref.dense_inverse(a), orc.block_inverse(a), rtol=1e-12, atol=1e-14)
+
+
+def _zilures_bcsr_cases():
+    """(A scalar CSR, L triple, U triple, bs) for data_zilures_bcsr: LACE's
+    own factor layout (BCSRL, and BCSCU read as BCSR as LACE does), U as
+    genuine block rows, and random block patterns."""
+    B = P.bcsr3d(3, seed=2)
+    A = B.to_csr()
+    F = orc.bcsr_parilu(B, 1, mode="async")
+    L = (F.L.ptr, F.L.idx, F.L.val)
+    U_bcsc = (F.U.ptr, F.U.idx, F.U.val)
+    # the same U with its blocks gathered by block row
+    nb = B.nb
+    cols = np.repeat(np.arange(nb), np.diff(F.U.ptr))
+    order = np.lexsort((cols, F.U.idx))
+    rp = np.zeros(nb + 1, dtype=np.int32)
+    np.cumsum(np.bincount(F.U.idx, minlength=nb), out=rp[1:])
+    U_bcsr = (rp, cols[order].astype(np.int32), np.asarray(F.U.val).reshape(-1, B.bs, B.bs)[order])
+    rng = np.random.default_rng(5)
+    def rand_bcsr(nb, bs, per_row):
+        ptr = [0]
+        idx = []
+        for _ in range(nb):
+            c = sorted(set(rng.integers(0, nb, size=per_row).tolist()))
+            idx += c
+            ptr.append(len(idx))
+        return (np.array(ptr, np.int32), np.array(idx, np.int32), rng.standard_normal((len(idx), bs, bs)))
+    R = P.bcsr3d(2, bs=3, seed=7)
+    return {"lace_layout": (A, L, U_bcsc, B.bs), "bcsr_u": (A, L, U_bcsr, B.bs),
+            "random": (R.to_csr(), rand_bcsr(R.nb, 3, 3), rand_bcsr(R.nb, 3, 4), 3)}
+
+
+@needs_ref
+@pytest.mark.parametrize("case", ["lace_layout", "bcsr_u", "random"])
+def test_live_reference_zilures_bcsr(case):
+    """The oracle's data_zilures_bcsr against LACE's own (control/norms.cpp:
+    409-468) built here."""
+    A, L, U, bs = _zilures_bcsr_cases()[case]
+    Am = ref.Mat.from_arrays(ref.Magma_CSR, A.n, A.n, A.row, A.col, A.val)
+    nb = len(L[0]) - 1
+    Lm = ref.Mat.from_arrays(ref.Magma_BCSR, nb, nb, L[0], L[1], np.asarray(L[2]).ravel(), blocksize=bs)
+    Um = ref.Mat.from_arrays(ref.Magma_BCSR, nb, nb, U[0], U[1], np.asarray(U[2]).ravel(), blocksize=bs)
+    r_ref, nl_ref = ref.zilures_bcsr(Am, Lm, Um)
+    r, nl = orc.zilures_bcsr(A.row, A.col, A.val, L, U, bs)
+    assert r == pytest.approx(r_ref, rel=1e-12)
+    assert nl == pytest.approx(nl_ref, rel=1e-10, abs=1e-13 * r_ref)
+    if case == "bcsr_u":  # the genuine product: block ILU(0) after one in-place sweep
+        assert nl < 1e-10 * r
