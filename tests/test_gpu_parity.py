@@ -136,9 +136,13 @@ def test_parilu_sync_sweeps(lg, name, sweeps):
                                  dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU))
     assert rc == 0
     assert abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14 * info["A_Frobenius"]
-    # and LACE's res, over the product's pattern (fill-in included)
-    res_or, _ = orc.zilures(A.row, A.col, A.val, F)
-    assert abs(r2 - res_or) <= 1e-12 * res_or
+    # and LACE's res, over the product's pattern (fill-in included), against
+    # the oracle on the same factors; the GPU forms the fill part as
+    # ||LU||^2 - sum_S (LU)^2 without forming LU, which cancels to about
+    # 1e-16 ||LU||^2 / res^2 relative
+    G = orc.Factors(orc.Tri(lp, li, lv), orc.Tri(up, ui, uv), [])
+    res_or, _ = orc.zilures(A.row, A.col, A.val, G)
+    assert abs(r2 - res_or) <= 1e-10 * res_or
     assert r2 > nl2
 
 
@@ -564,7 +568,7 @@ def test_dropin_parilu_vs_exact_ilu0(lg):
     U = dropin.csr(up, ui, uv, A.n, dropin.Magma_CSCU)
     r2, nl2, rc = dropin.zilures(Am, L, U)
     assert rc == 0 and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-13
-    assert abs(r2 - res) <= 1e-12 * res
+    assert abs(r2 - res) <= 1e-10 * res
 
 
 def test_dropin_spmv_and_parcsrtrsv(lg):
@@ -693,4 +697,4 @@ def test_dropin_zilures_strictly_lower_l(lg):
               dropin.csr(sp, F.L.idx[keep], F.L.val[keep], A.n, dropin.Magma_CSRL)):
         r2, nl2, rc = dropin.zilures(Am, L, U)
         assert rc == 0
-        assert abs(r2 - res) <= 1e-12 * res and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14
+        assert abs(r2 - res) <= 1e-10 * res and abs(nl2 - nl) <= 1e-12 * max(nl, 1e-300) + 1e-14
