@@ -314,7 +314,9 @@ int data_zilures_bcsr(data_d_matrix A, data_d_matrix L, data_d_matrix U,
 typedef struct lace_gpu_ctx lace_gpu_ctx;
 
 /* precision of the ParILU factors and of both triangular solves; the outer
- * FGMRES, its SpMV and the reflectors are always FP64 */
+ * FGMRES, its SpMV and the reflectors are FP64-class: FP64, or in the
+ * one-kernel Householder step of FP32/BF16 runs double-float pairs (about 48
+ * bits, on the FP32 pipe); each cycle's true residual is FP64 */
 enum { LACE_PREC_FP64 = 0, LACE_PREC_FP32 = 1, LACE_PREC_BF16_STORE = 2 };
 /* how M^{-1} is applied */
 enum {
