@@ -201,6 +201,9 @@ def run_ours(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
+    if args.only_config5:
+        print(json.dumps({"config5": run_config5(args, lg, torch, torch.cuda.Stream(), local)}))
+        return
     A, b = build_problem(args.grid if (args.only_mgs or args.only_householder or args.only_kernels) else GRID)
     stream = torch.cuda.Stream()
     ctx = lg.Context(local, stream=stream)
@@ -347,6 +350,37 @@ def run_ours(args):
     traffic_sweep = profiled_traffic("parilu_sweep_convdiff128.txt", "dram_bytes_per_launch")
     traffic_spmv = profiled_traffic("spmv_convdiff128.txt", "dram_bytes_per_launch")
     traffic_pair = profiled_traffic("sptrsv_pair_convdiff128.txt", "dram_bytes_per_pair")
+    # ---- the bandwidth-bound alternative to the exact solves: k synchronous
+    # Jacobi sweeps per triangle (the GPU-native inexact M^-1), the sweeps'
+    # rate and what the inexact solves cost in directions
+    jacobi = None
+    if not args.skip_jacobi:
+        jacobi = {}
+        n = A.n
+        sweep_pair_b = ab["sptrsv_pair"] + 2 * n * 4  # a sweep also reads the previous iterate
+        for k in (2, 4, 8):
+            ctx.set_options(precision="fp32", trsv="jacobi", jacobi_sweeps=k, **pin)
+            ctx.parilu0(SWEEPS, residual=False)
+            ctx.apply_precond(q, z)
+            for _ in range(3):
+                ctx.precond_enqueue(q32, z32)
+            ev0.record(stream)
+            for _ in range(reps):
+                ctx.precond_enqueue(q32, z32)
+            ev1.record(stream)
+            ev1.synchronize()
+            pair_s = ev0.elapsed_time(ev1) / 1e3 / reps
+            tj, _, rj = timed("fp32", 2, 1)
+            jacobi[f"sweeps_{k}"] = {
+                "precond_pair_s": pair_s, "sweep_pair_gbs": k * sweep_pair_b / pair_s / 1e9,
+                "sweep_pair_frac": k * sweep_pair_b / pair_s / 1e9 / hbm_peak,
+                "solve_s": statistics.median(tj), "iterations": rj.total_iterations,
+                "converged": bool(rj.converged)}
+        ctx.set_options(trsv="syncfree")
+        jacobi["note"] = ("M^-1 by k synchronous Jacobi sweeps per triangle (LACE_TRSV_JACOBI): streams at "
+                          "HBM rate but is inexact, so FGMRES needs more directions than with the exact "
+                          "sync-free solves (the headline)")
+
     # ---- the dominant kernel: the one-kernel Arnoldi step (Householder),
     # replayed at step STEP_J on the basis of the last mixed-precision solve
     ctx.set_options(precision="fp32", **pin)
@@ -424,6 +458,9 @@ def run_ours(args):
     cfg4 = None
     if not args.skip_config4:
         cfg4 = run_config4(args, lg, torch, stream, local)
+    cfg5 = None
+    if not args.skip_config5:
+        cfg5 = run_config5(args, lg, torch, stream, local)
 
     # launches per solve: ParILU (4 initial-guess copies, the sweeps, 2 gathers,
     # the residual), 2 solve-plan value gathers, and per cycle the residual,
@@ -467,8 +504,10 @@ def run_ours(args):
                     "parilu_sweep_traffic": traffic_sweep,
                     "arnoldi_step_s": step_s},
         "parilu_parity": parity,
+        "jacobi_precond": jacobi,
         "config3": cfg3,
         "config4": cfg4,
+        "config5": cfg5,
         "roofline": {"bound": "hbm", "kernel": f"k_hh_step_df: one Arnoldi step (j = {STEP_J}, 16 basis columns; "
                      "operator, V^T w, w -= V y, new reflector, q and V^T v_{{j+1}}), mixed precision, "
                      "double-float pairs",
@@ -573,6 +612,72 @@ def run_config4(args, lg, torch, stream, local):
     return {"workload": WORKLOAD4, "forward": {"value": statistics.median(fwd), "unit": "s",
                                                "iterations": r.total_iterations},
             "backward": {"value": statistics.median(bwd), "unit": "s", "iterations": its}}
+
+
+WORKLOAD5 = ("batch_aniso: 256 independent 2D 5-pt anisotropic Laplacians, side U{32..256}, eps logU[1e-3, 1] "
+             "(seed 0), 4 RHS N(0,1) each; ParILU(0) 3 sync sweeps in FP32 for every system, "
+             "FGMRES-Householder(30) per (system, rhs) to 1e-10 rel, FP64 outer")
+RESTART5 = 100
+
+
+def run_config5(args, lg, torch, stream, local):
+    """The batched configuration through lace_gpu_batch_* (one persistent
+    launch: every system's ParILU and every (system, rhs) FGMRES process):
+    solve time (CUDA events on the solver stream around the call),
+    directions per (system, rhs), true residuals on the host."""
+    import ctypes as C
+    from lace_gb300 import problems as P
+    systems = P.batch_aniso(count=256, side_lo=32, side_hi=256, nrhs=4, seed=0)
+    nrhs = 4
+    n = np.array([sy.A.n for sy in systems], dtype=np.int32)
+    row_off = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int32)
+    nnz_off = np.concatenate([[0], np.cumsum([sy.A.nnz for sy in systems])[:-1]]).astype(np.int32)
+    row = np.concatenate([sy.A.row for sy in systems]).astype(np.int32)
+    col = np.concatenate([sy.A.col for sy in systems]).astype(np.int32)
+    val = np.concatenate([sy.A.val for sy in systems])
+    N = int(n.sum())
+    B = np.zeros((nrhs, N))
+    for s, sy in enumerate(systems):
+        B[:, row_off[s]:row_off[s] + n[s]] = sy.B
+    L = lg.lib()
+    ctx = lg.Context(local, stream=stream)
+    ctx.set_options(precision="fp32")
+    bh = C.c_void_p()
+    rc = L.lace_gpu_batch_create(C.byref(bh), ctx.h, len(systems), n.ctypes.data, row_off.ctypes.data,
+                                 nnz_off.ctypes.data, row.ctypes.data, col.ctypes.data, val.ctypes.data, nrhs)
+    if rc != 0:
+        ctx.close()
+        return {"workload": WORKLOAD5, "error": int(rc)}
+    bd = torch.tensor(B.ravel(), dtype=torch.float64, device="cuda")
+    xd = torch.zeros(nrhs * N, dtype=torch.float64, device="cuda")
+    iters = np.zeros(len(systems) * nrhs, dtype=np.int32)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    times = []
+    for it in range(1 + max(1, min(3, args.steps))):
+        with torch.cuda.stream(stream):
+            xd.zero_()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        rc = L.lace_gpu_batch_solve(bh, SWEEPS, 30, RESTART5, RTOL, bd.data_ptr(), xd.data_ptr(), iters.ctypes.data)
+        ev1.record(stream)
+        ev1.synchronize()
+        if it >= 1:
+            times.append(ev0.elapsed_time(ev1) / 1e3)
+    L.lace_gpu_batch_destroy(bh)
+    X = xd.cpu().numpy().reshape(nrhs, N)
+    ctx.close()
+    worst = 0.0
+    for s, sy in enumerate(systems):
+        for r in range(nrhs):
+            x = X[r, row_off[s]:row_off[s] + n[s]]
+            worst = max(worst, float(np.linalg.norm(sy.B[r] - sy.A.matvec(x)) / np.linalg.norm(sy.B[r])))
+    return {"workload": WORKLOAD5, "rows": N, "nnz": int(len(col)), "rhs": nrhs,
+            "fp32": {"value": statistics.median(times), "unit": "s", "code": int(rc),
+                     "directions_total": int(iters.sum()), "directions_max": int(iters.max()),
+                     "directions_mean": float(iters.mean()), "worst_true_rel_resid": worst},
+            "launch": "one persistent launch (captured in a CUDA graph): CTAs take (system, rhs group) jobs "
+                      "from a queue, largest systems first, and run each through ParILU and FGMRES alone"}
 
 
 def run_config3(args, lg, torch, stream, local, hbm_peak, rank, world):
@@ -694,6 +799,10 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-config3", action="store_true")
     ap.add_argument("--skip-config4", action="store_true")
+    ap.add_argument("--skip-config5", action="store_true")
+    ap.add_argument("--skip-jacobi", action="store_true")
+    ap.add_argument("--only-config5", action="store_true",
+                    help="profiling aid: the batched configuration alone (its JSON object, no contract line)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel (the Arnoldi step), if captured")
     ap.add_argument("--trsv-schedule", default=None,

@@ -159,4 +159,21 @@ template <> __device__ __forceinline__ double fval<__nv_bfloat16>(__nv_bfloat16 
 // mysgn of LACE (include/sparse.h:1129-1133): +1 for v >= 0, -1 otherwise
 __device__ __forceinline__ double mysgn(double v) { return v >= 0.0 ? 1.0 : -1.0; }
 
+// LACE's Givens rotation (src/givens.cpp:46-67): (c, s) with
+// [c s; -s c]^T-style sign convention of the reference
+__device__ __forceinline__ void givens_rot(double a, double b, double tol, double *c, double *s) {
+  if (fabs(b) <= tol) {
+    *c = 1.0;
+    *s = 0.0;
+  } else if (fabs(b) > fabs(a)) {
+    const double temp = a / b;
+    *s = 1.0 / sqrt(1.0 + temp * temp);
+    *c = temp * (*s);
+  } else {
+    const double temp = b / a;
+    *c = 1.0 / sqrt(1.0 + temp * temp);
+    *s = temp * (*c);
+  }
+}
+
 }  // namespace lace

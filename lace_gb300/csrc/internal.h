@@ -230,6 +230,33 @@ void launch_ilu_residual(cudaStream_t s, const IluArgs &a, VType t, const void *
 void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, const int *Ucol,
                    const void *L, const void *Ur, const void *Uc, double *out3, int unit);
 // the sliced-ELL values of the operator: dst[q] = map[q] >= 0 ? src[map[q]] : 0
+// batched solves as one persistent launch (batch_persist.cu): systems from a
+// queue, largest first, each carried by one CTA through ParILU and
+// FGMRES-Householder for all its right-hand sides
+constexpr int kBatchMaxM = 64;  // largest search_max of the batched solver
+struct PBatchHost {
+  int nsys = 0, nrhs = 0, m = 0, restart_max = 0, sweeps = 0, N = 0, grid = 0, f32 = 1;
+  double rtol = 0.0;
+  int njobs = 0;
+  const int *jsys = nullptr, *jrhs = nullptr, *jnr = nullptr;  // jobs: system, first rhs, rhs count
+  const int *n = nullptr, *roff = nullptr, *lsys = nullptr, *usys = nullptr;
+  const int *Arow = nullptr, *Acol = nullptr;
+  const double *Aval = nullptr;
+  const int *pptr = nullptr, *dpos = nullptr, *diag = nullptr;
+  const int2 *pairs = nullptr;
+  void *F = nullptr;  // per CTA two factor buffers of fstride entries
+  size_t fstride = 0;
+  const int *lptr = nullptr, *lrows = nullptr, *uptr = nullptr, *urows = nullptr;
+  const double *b = nullptr;
+  double *x = nullptr;
+  size_t nmax = 0;
+  double *V = nullptr, *W = nullptr, *Tm = nullptr, *Rm = nullptr;
+  void *Z = nullptr, *Q = nullptr, *Tt = nullptr;
+  int *next = nullptr, *iters = nullptr, *conv = nullptr;
+};
+int launch_batch_persist(cudaStream_t s, const PBatchHost &h);
+int batch_persist_threads();
+int batch_persist_rhs();
 void launch_sell_values(cudaStream_t s, size_t count, const int *map, const double *src, double *dst,
                         float2 *pair);
 // gather: dst[p] = src[perm[p]] with type conversion

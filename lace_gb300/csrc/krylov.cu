@@ -414,22 +414,6 @@ __global__ void __launch_bounds__(kTPB, NS <= 2 ? 5 : 1) k_passA(int n, OpView o
 
 // ------------------------------------------------------------- pass B
 
-__device__ void givens_rot(double a, double b, double tol, double *c, double *s) {
-  // src/givens.cpp:46-67
-  if (fabs(b) <= tol) {
-    *c = 1.0;
-    *s = 0.0;
-  } else if (fabs(b) > fabs(a)) {
-    double temp = a / b;
-    *s = 1.0 / sqrt(1.0 + temp * temp);
-    *c = temp * (*s);
-  } else {
-    double temp = b / a;
-    *c = 1.0 / sqrt(1.0 + temp * temp);
-    *s = temp * (*c);
-  }
-}
-
 // three blocks per SM for up to 32 basis columns (a few bytes of spill; the
 // occupancy matters more: measured 2.8 % faster FGMRES)
 template <int NS>
