@@ -23,6 +23,9 @@ struct lace_gpu_batch {
   int nsys = 0, nrhs = 0, N = 0, nmax = 0;
   std::vector<int> n, row_off;
   DBuf dn, droff, lsys, lptr, lrows, usys, uptr, urows;  // per system and its levels
+  DBuf cL, fL, cU, fU, dU;                               // level-ordered row records (columns, A positions)
+  int w = 0;                                             // record width
+  DBuf vrec;                                             // per CTA: the records' factor values
   DBuf jsys, jrhs, jnr;                                  // jobs: (system, first rhs, rhs count)
   int njobs = 0;
   size_t nnzmax = 0;                                     // the largest system's entries
@@ -132,6 +135,45 @@ extern "C" int lace_gpu_batch_create(lace_gpu_batch **out, lace_gpu_ctx *ctx, in
   usys[nsys] = (int)uptr.size();
   lptr.push_back(N);
   uptr.push_back(N);
+  // level-ordered records of the two triangles: for the k-th row of the
+  // level order, its off-diagonal entries' local columns and A positions
+  // (W of them, -1 beyond the row's count) and, for U, its diagonal's position
+  std::vector<int> dpos_row(N), sys_of(N);
+  int W = 0;
+  for (int s = 0; s < nsys; ++s)
+    for (int i = row_off[s]; i < row_off[s] + n[s]; ++i) {
+      sys_of[i] = s;
+      int d = -1;
+      for (int q = Sr[i]; q < Sr[i + 1]; ++q)
+        if (Sc[q] == i) d = q;
+      if (d < 0) {  // the upload checked this already
+        delete B;
+        return set_err(DEV_ERR_NOT_SUPPORTED);
+      }
+      dpos_row[i] = d;
+      W = std::max(W, std::max(d - Sr[i], Sr[i + 1] - d - 1));
+    }
+  if (W > kBatchMaxW) {
+    delete B;
+    return set_err(DEV_ERR_NOT_SUPPORTED);
+  }
+  W = std::max(W, 1);
+  B->w = W;
+  std::vector<int> cLh((size_t)N * W, -1), fLh((size_t)N * W, -1), cUh((size_t)N * W, -1), fUh((size_t)N * W, -1),
+      dUh(N);
+  for (int k = 0; k < N; ++k) {
+    const int gl = lrows[k], gu = urows[k];
+    const int rl = row_off[sys_of[gl]], ru = row_off[sys_of[gu]];
+    for (int q = Sr[gl], w = 0; q < dpos_row[gl]; ++q, ++w) {
+      cLh[(size_t)k * W + w] = Sc[q] - rl;
+      fLh[(size_t)k * W + w] = q;
+    }
+    for (int q = dpos_row[gu] + 1, w = 0; q < Sr[gu + 1]; ++q, ++w) {
+      cUh[(size_t)k * W + w] = Sc[q] - ru;
+      fUh[(size_t)k * W + w] = q;
+    }
+    dUh[k] = dpos_row[gu];
+  }
   // jobs, largest systems first: a system of at least kSplitRows rows gives
   // each right-hand side its own job (its FGMRES processes run on different
   // SMs: the longest of them sets the launch's time), a smaller one takes its
@@ -159,7 +201,9 @@ extern "C" int lace_gpu_batch_create(lace_gpu_batch **out, lace_gpu_ctx *ctx, in
       B->jnr.upload(jnr.data(), 4 * jnr.size(), st) || B->lsys.upload(lsys.data(), 4 * lsys.size(), st) ||
       B->usys.upload(usys.data(), 4 * usys.size(), st) || B->lptr.upload(lptr.data(), 4 * lptr.size(), st) ||
       B->uptr.upload(uptr.data(), 4 * uptr.size(), st) || B->lrows.upload(lrows.data(), 4 * lrows.size(), st) ||
-      B->urows.upload(urows.data(), 4 * urows.size(), st)) {
+      B->urows.upload(urows.data(), 4 * urows.size(), st) || B->cL.upload(cLh.data(), 4 * cLh.size(), st) ||
+      B->fL.upload(fLh.data(), 4 * fLh.size(), st) || B->cU.upload(cUh.data(), 4 * cUh.size(), st) ||
+      B->fU.upload(fUh.data(), 4 * fUh.size(), st) || B->dU.upload(dUh.data(), 4 * dUh.size(), st)) {
     delete B;
     return set_err(DEV_ERR_DEVICE_ALLOC);
   }
@@ -190,6 +234,7 @@ static int batch_workspace(lace_gpu_batch *B, int m, bool f32) {
   const size_t fb = f32 ? 4 : 8;
   int rc = 0;
   rc |= B->F.ensure(fb * G * 2 * (B->nnzmax + 4));
+  rc |= B->vrec.ensure(fb * G * (2 * (size_t)B->w + 1) * nmax);
   rc |= B->V.ensure(8 * G * R * (m + 1) * nmax);
   rc |= B->W.ensure(8 * G * R * nmax);
   rc |= B->Tm.ensure(8 * G * R * ld * ld);
@@ -248,6 +293,13 @@ extern "C" int lace_gpu_batch_solve(lace_gpu_batch *B, int sweeps, int search_ma
   h.F = B->F.p;
   h.fstride = B->nnzmax + 4;
   h.lptr = (const int *)B->lptr.p;
+  h.w = B->w;
+  h.cL = (const int *)B->cL.p;
+  h.fL = (const int *)B->fL.p;
+  h.cU = (const int *)B->cU.p;
+  h.fU = (const int *)B->fU.p;
+  h.dU = (const int *)B->dU.p;
+  h.vrec = B->vrec.p;
   h.lrows = (const int *)B->lrows.p;
   h.uptr = (const int *)B->uptr.p;
   h.urows = (const int *)B->urows.p;

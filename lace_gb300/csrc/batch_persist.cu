@@ -31,6 +31,7 @@ namespace lace {
 constexpr int kPBThreads = 512;
 constexpr int kPBRhs = 4;            // right-hand sides in lockstep
 constexpr int kPBMaxLd = kBatchMaxM + 2;  // the small matrices' largest leading dimension
+constexpr int kPBMaxW = kBatchMaxW;       // off-diagonal entries a triangle's row holds at most
 
 template <typename T>
 __device__ __forceinline__ double pb_f64(T v) {
@@ -91,6 +92,9 @@ struct PBatch {
   const int2 *pairs;
   void *F;                          // per CTA: two buffers of factor values in A's order (FT), fstride each
   const int *lptr, *lrows, *uptr, *urows;  // levels: row ranges and rows
+  int w;                            // record width (off-diagonals per row, <= kPBMaxW)
+  const int *cL, *fL, *cU, *fU, *dU;  // level-ordered records: local columns (-1: none), A positions
+  void *vrec;                       // per CTA: the records' values, L then U then U's diagonal (FT)
   const double *b;
   double *x;
   int N;                            // rows of all systems (vector stride between rhs)
@@ -147,6 +151,9 @@ __global__ void __launch_bounds__(kPBThreads, 1) k_batch_persist(PBatch P) {
   FT *Q0 = (FT *)P.Q + (size_t)blockIdx.x * kPBRhs * nmax;
   FT *Tt0 = (FT *)P.Tt + (size_t)blockIdx.x * kPBRhs * nmax;
   FT *Fcta = (FT *)P.F + (size_t)blockIdx.x * 2 * P.fstride;
+  const int W = P.w;
+  FT *vL0 = (FT *)P.vrec + (size_t)blockIdx.x * (2 * W + 1) * nmax;
+  FT *vU0 = vL0 + (size_t)W * nmax, *vD0 = vU0 + (size_t)W * nmax;
   for (;;) {
     if (tid == 0) s_job = atomicAdd(P.next, 1);
     __syncthreads();
@@ -177,6 +184,15 @@ __global__ void __launch_bounds__(kPBThreads, 1) k_batch_persist(PBatch P) {
       Fb = t;
     }
     const FT *F = Fa;
+    // the factor values into the level-ordered records of the two triangles
+    const int kbL = P.lptr[P.lsys[sys]], kbU = P.uptr[P.usys[sys]];
+    for (int t = tid; t < n * W; t += T) {
+      const int fl = P.fL[(size_t)kbL * W + t], fu = P.fU[(size_t)kbU * W + t];
+      vL0[t] = fl >= 0 ? F[fl] : (FT)0;
+      vU0[t] = fu >= 0 ? F[fu] : (FT)0;
+    }
+    for (int t = tid; t < n; t += T) vD0[t] = F[P.dU[kbU + t]];
+    __syncthreads();
     // ---- FGMRES-Householder for the job's right-hand sides, in lockstep
     {
       const int rg = P.jrhs[job];
@@ -251,36 +267,71 @@ __global__ void __launch_bounds__(kPBThreads, 1) k_batch_persist(PBatch P) {
           for (int c = 0; c < nr; ++c) any = any || s_live[c];
           if (!any) break;
           const int jp1 = j + 1;
-          // ---- z_j = U^-1 L^-1 q_j (level by level, all live rhs per pass)
-          for (int lv = P.lsys[sys]; lv < P.lsys[sys + 1]; ++lv) {
-            for (int k = P.lptr[lv] + tid; k < P.lptr[lv + 1]; k += T) {
-              const int gi = P.lrows[k], i = gi - r0;
-              const int pe = P.diag[gi];
-              for (int c = 0; c < nr; ++c) {
-                if (!s_live[c]) continue;
-                const FT *qv = Q0 + (size_t)c * nmax;
-                FT *tv = Tt0 + (size_t)c * nmax;
-                FT s = qv[i];
-                for (int p = P.Arow[gi]; p < pe; ++p) s = fma(-F[p], tv[P.Acol[p] - r0], s);
-                tv[i] = s;
+          // ---- z_j = U^-1 L^-1 q_j, level by level, all live rhs per pass: a
+          // row's record (columns, values, right-hand side) is loaded for the
+          // next level before the barrier, so a level waits for one load
+          // (the solved values it reads)
+          {
+            bool live[kPBRhs];
+#pragma unroll
+            for (int c = 0; c < kPBRhs; ++c) live[c] = c < nr && s_live[c];
+            for (int pass = 0; pass < 2; ++pass) {
+              const bool lower = pass == 0;
+              const int *lp = lower ? P.lptr : P.uptr;
+              const int *lr = lower ? P.lrows : P.urows;
+              const int *cw = lower ? P.cL : P.cU;
+              const FT *vw = lower ? vL0 : vU0;
+              const int kb0 = lower ? kbL : kbU;
+              const int l0 = lower ? P.lsys[sys] : P.usys[sys], l1 = lower ? P.lsys[sys + 1] : P.usys[sys + 1];
+              FT *out[kPBRhs];
+              const FT *in[kPBRhs];
+#pragma unroll
+              for (int c = 0; c < kPBRhs; ++c) {
+                out[c] = lower ? Tt0 + (size_t)c * nmax : Z0 + ((size_t)c * m + j) * nmax;
+                in[c] = lower ? Q0 + (size_t)c * nmax : Tt0 + (size_t)c * nmax;
+              }
+              // one row's record
+              int ri = -1, rc[kPBMaxW];
+              FT rv[kPBMaxW], rq[kPBRhs], rd = (FT)1;
+              auto load = [&](int k) {
+                ri = k >= 0 ? lr[k] - r0 : -1;
+#pragma unroll
+                for (int w = 0; w < kPBMaxW; ++w) {
+                  rc[w] = (k >= 0 && w < W) ? cw[(size_t)k * W + w] : -1;
+                  rv[w] = (k >= 0 && w < W) ? vw[(size_t)(k - kb0) * W + w] : (FT)0;
+                }
+#pragma unroll
+                for (int c = 0; c < kPBRhs; ++c) rq[c] = (k >= 0 && live[c]) ? in[c][ri] : (FT)0;
+                if (!lower && k >= 0) rd = vD0[k - kb0];
+              };
+              auto solve = [&]() {
+#pragma unroll
+                for (int c = 0; c < kPBRhs; ++c) {
+                  if (!live[c]) continue;
+                  FT acc = rq[c];
+#pragma unroll
+                  for (int w = 0; w < kPBMaxW; ++w)
+                    if (rc[w] >= 0) acc = fma(-rv[w], out[c][rc[w]], acc);
+                  out[c][ri] = lower ? acc : acc / rd;
+                }
+              };
+              int lv = l0, kb = lp[lv], ke = lp[lv + 1];
+              load(kb + tid < ke ? kb + tid : -1);
+              while (lv < l1) {
+                if (ri >= 0) solve();
+                for (int k = kb + tid + T; k < ke; k += T) {  // levels wider than the CTA
+                  load(k);
+                  solve();
+                }
+                ++lv;
+                if (lv < l1) {
+                  kb = lp[lv];
+                  ke = lp[lv + 1];
+                  load(kb + tid < ke ? kb + tid : -1);
+                }
+                __syncthreads();
               }
             }
-            __syncthreads();
-          }
-          for (int lv = P.usys[sys]; lv < P.usys[sys + 1]; ++lv) {
-            for (int k = P.uptr[lv] + tid; k < P.uptr[lv + 1]; k += T) {
-              const int gi = P.urows[k], i = gi - r0;
-              const int pd = P.diag[gi];
-              for (int c = 0; c < nr; ++c) {
-                if (!s_live[c]) continue;
-                const FT *tv = Tt0 + (size_t)c * nmax;
-                FT *zv = Z0 + ((size_t)c * m + j) * nmax;
-                FT s = tv[i];
-                for (int p = pd + 1; p < P.Arow[gi + 1]; ++p) s = fma(-F[p], zv[P.Acol[p] - r0], s);
-                zv[i] = s / F[pd];
-              }
-            }
-            __syncthreads();
           }
           // ---- w = A z_j
           for (int c = 0; c < nr; ++c) {
@@ -469,6 +520,13 @@ int launch_batch_persist(cudaStream_t s, const PBatchHost &h) {
   P.F = h.F;
   P.fstride = h.fstride;
   P.lptr = h.lptr;
+  P.w = h.w;
+  P.cL = h.cL;
+  P.fL = h.fL;
+  P.cU = h.cU;
+  P.fU = h.fU;
+  P.dU = h.dU;
+  P.vrec = h.vrec;
   P.lrows = h.lrows;
   P.uptr = h.uptr;
   P.urows = h.urows;

@@ -234,6 +234,7 @@ void launch_lu_fro(cudaStream_t s, const IluArgs &a, VType t, const int *Urow, c
 // queue, largest first, each carried by one CTA through ParILU and
 // FGMRES-Householder for all its right-hand sides
 constexpr int kBatchMaxM = 64;  // largest search_max of the batched solver
+constexpr int kBatchMaxW = 4;   // off-diagonal entries per row of a triangle the batched solver takes
 struct PBatchHost {
   int nsys = 0, nrhs = 0, m = 0, restart_max = 0, sweeps = 0, N = 0, grid = 0, f32 = 1;
   double rtol = 0.0;
@@ -247,6 +248,9 @@ struct PBatchHost {
   void *F = nullptr;  // per CTA two factor buffers of fstride entries
   size_t fstride = 0;
   const int *lptr = nullptr, *lrows = nullptr, *uptr = nullptr, *urows = nullptr;
+  int w = 0;
+  const int *cL = nullptr, *fL = nullptr, *cU = nullptr, *fU = nullptr, *dU = nullptr;
+  void *vrec = nullptr;
   const double *b = nullptr;
   double *x = nullptr;
   size_t nmax = 0;
