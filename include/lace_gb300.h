@@ -516,8 +516,10 @@ const char *lace_gpu_error_string(int code);
 
 /* ------------------------------------------------------------------------
  * Batched solves: many independent CSR systems, several right-hand sides
- * each, all ParILU sweeps and all FGMRES cycles advanced together in a few
- * persistent launches per Arnoldi step (captured in a CUDA graph).
+ * each; every system's ParILU sweeps and FGMRES-Householder for every
+ * (system, rhs) pair in one persistent launch (captured in a CUDA graph when
+ * the context's use_graph option is on).  Each row of a system's triangles
+ * may hold at most 4 off-diagonal entries (DEV_ERR_NOT_SUPPORTED otherwise).
  * ---------------------------------------------------------------------- */
 typedef struct lace_gpu_batch lace_gpu_batch;
 
