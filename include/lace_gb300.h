@@ -515,6 +515,38 @@ int lace_gpu_last_error(void);
 const char *lace_gpu_error_string(int code);
 
 /* ------------------------------------------------------------------------
+ * GPU-side setup conversions on device arrays (zero-based CSR), the GPU form
+ * of the conversions the factorisation path runs: data_rowindex
+ * (control/magma_zmconverter.cpp:145), the CSR -> CSRL/CSRU split (:304),
+ * the CSR transpose (control/magma_zmtranspose.cpp:85) and CSR -> BCSR
+ * (:614).  Results equal the host data_zmconvert / data_zmtranspose /
+ * data_rowindex array for array; work runs on the context's stream and the
+ * calls return once it is done.
+ * ---------------------------------------------------------------------- */
+/* rowidx[p] = the row of entry p */
+int lace_gpu_rowindex_device(lace_gpu_ctx *ctx, int n, const int *row, int *rowidx);
+/* lower = 1: CSRL, 0: CSRU, with data_diagorder_t diagorder as LACE's
+ * B->diagorder_type (Magma_UNITY, Magma_VALUE, Magma_ZERO, Magma_NODIAG or
+ * another value for LACE's default).  *nnz_out = the entries the rows hold
+ * (LACE's nnz field also counts a lower split's default diagonal, which no
+ * row holds).  brow (n + 1 ints) may be NULL for a size query; bcol and bval
+ * (nnz_out entries) NULL skip the fill. */
+int lace_gpu_csr_split_device(lace_gpu_ctx *ctx, int n, const int *row, const int *col, const double *val,
+                              int lower, int diagorder, int *nnz_out, int *brow, int *bcol, double *bval);
+/* the transpose as CSR (tptr: ncols + 1; tidx, tval: nnz), each row of the
+ * transpose by ascending column; DEV_ERR_ILLEGAL_VALUE for a column index
+ * outside [0, ncols) */
+int lace_gpu_csr_transpose_device(lace_gpu_ctx *ctx, int n, int ncols, const int *row, const int *col,
+                                  const double *val, int *tptr, int *tidx, double *tval);
+/* CSR -> BCSR with bs x bs row-major blocks, block columns ascending in each
+ * block row, zero-filled; *nblocks_out = blocks; brow ((n+bs-1)/bs + 1 ints)
+ * may be NULL for a size query; bcol, bval (nblocks, nblocks*bs*bs) NULL skip
+ * the fill.  DEV_ERR_NOT_SUPPORTED for a block row with more than 256 block
+ * columns. */
+int lace_gpu_csr_to_bcsr_device(lace_gpu_ctx *ctx, int n, const int *row, const int *col, const double *val,
+                                int bs, int *nblocks_out, int *brow, int *bcol, double *bval);
+
+/* ------------------------------------------------------------------------
  * Batched solves: many independent CSR systems, several right-hand sides
  * each; every system's ParILU sweeps and FGMRES-Householder for every
  * (system, rhs) pair in one persistent launch (captured in a CUDA graph when

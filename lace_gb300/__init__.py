@@ -196,6 +196,10 @@ SIGNATURES = {
     "lace_gpu_inject_alloc_failure": (None, [_i]),
     "lace_gpu_get_orthog_history": (_i, [_p, _p, _i, C.POINTER(_i)]),
     "lace_gpu_error_string": (C.c_char_p, [_i]),
+    "lace_gpu_rowindex_device": (_i, [_p, _i, _p, _p]),
+    "lace_gpu_csr_split_device": (_i, [_p, _i, _p, _p, _p, _i, _i, C.POINTER(_i), _p, _p, _p]),
+    "lace_gpu_csr_transpose_device": (_i, [_p, _i, _i, _p, _p, _p, _p, _p, _p]),
+    "lace_gpu_csr_to_bcsr_device": (_i, [_p, _i, _p, _p, _p, _i, C.POINTER(_i), _p, _p, _p]),
     "lace_gpu_batch_create": (_i, [C.POINTER(_p), _p, _i, _p, _p, _p, _p, _p, _p, _i]),
     "lace_gpu_batch_destroy": (_i, [_p]),
     "lace_gpu_batch_solve": (_i, [_p, _i, _i, _i, _d, _p, _p, _p]),
