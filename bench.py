@@ -413,8 +413,11 @@ def run_ours(args):
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 L, U, info = dropin.parilu_mats(Am, max_sweeps=SWEEPS)
+                # x0 = 0 in a fresh array the solution overwrites, as a C
+                # caller's data_zvinit container
                 x, rc, glog = dropin.fgmres_householder_restart(Am, b, np.zeros(A.n), L, U, search_max=M,
-                                                               restart_max=RESTART_MAX, rtol=RTOL, tol_type=1)
+                                                               restart_max=RESTART_MAX, rtol=RTOL, tol_type=1,
+                                                               x0_inplace=True)
                 del L, U
                 torch.cuda.synchronize()
                 times.append(time.perf_counter() - t0)

@@ -115,8 +115,35 @@ bool is_csr(data_storage_t s) {
 // (allocation, the pattern, the values' pages mapped) needs nothing from the
 // GPU and can run while it works; the FP64 values on the device then go
 // straight into the container's array.
+// one piece of the output containers' bulk fill: a copy of src, or zeros
+struct FillPiece {
+  char *dst;
+  const char *src;
+  size_t bytes;
+};
+
+// the pieces as one byte range cut evenly over the host threads
+void fill_pieces(const std::vector<FillPiece> &pc) {
+  size_t total = 0;
+  for (const FillPiece &p : pc) total += p.bytes;
+  const int nt = host_threads(total);
+  par_run(nt, [&](int t) {
+    const size_t b = total * t / nt, e = total * (t + 1) / nt;
+    size_t base = 0;
+    for (const FillPiece &p : pc) {
+      const size_t s = std::max(b, base), f = std::min(e, base + p.bytes);
+      if (s < f) {
+        if (p.src) memcpy(p.dst + (s - base), p.src + (s - base), f - s);
+        else memset(p.dst + (s - base), 0, f - s);
+      }
+      base += p.bytes;
+    }
+  });
+}
+
+// the container's fields and arrays; its bulk fill appended to `pieces`
 int prepare_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n, const std::vector<int> &ptr,
-                    const std::vector<int> &idx, int blocksize) {
+                    const std::vector<int> &idx, int blocksize, std::vector<FillPiece> &pieces) {
   release_members(B);
   const int ld = blocksize > 0 ? blocksize * blocksize : 1;
   const size_t nval = idx.size() * ld;
@@ -131,9 +158,9 @@ int prepare_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n
   if (!B->row || !B->col || !B->val) return DEV_ERR_HOST_ALLOC;
   // the values' pages mapped by host threads now, so that the copy into them
   // runs at full speed (faults taken inside it cost several times more)
-  par_zero(B->val, 8 * nval);
-  par_copy(B->row, ptr.data(), 4 * ptr.size());
-  par_copy(B->col, idx.data(), 4 * idx.size());
+  pieces.push_back({(char *)B->val, nullptr, 8 * nval});
+  pieces.push_back({(char *)B->row, (const char *)ptr.data(), 4 * ptr.size()});
+  pieces.push_back({(char *)B->col, (const char *)idx.data(), 4 * idx.size()});
   if (blocksize > 0) {
     B->blocksize = blocksize;
     B->ldblock = ld;
@@ -147,10 +174,10 @@ int prepare_csr_out(data_d_matrix *B, data_storage_t st, data_uplo_t fill, int n
 }
 
 // The output containers' host part for L (CSRL) and U (CSCU) of the
-// context's factor patterns, on two host threads (each spreading its bulk
-// work further), running while the GPU works.
+// context's factor patterns, on a host thread (spreading the bulk fill of
+// both over the host pool), running while the GPU works.
 struct OutPrep {
-  std::thread tl, tu;
+  std::thread th;
   int rcl = 0, rcu = 0;
   double ms = 0.0;
   std::chrono::steady_clock::time_point t0;
@@ -159,17 +186,18 @@ struct OutPrep {
     L->diagorder_type = Magma_UNITY;
     U->diagorder_type = Magma_VALUE;
     t0 = std::chrono::steady_clock::now();
-    tl = std::thread([this, L, c, bcsr, n, blocksize] {
-      rcl = prepare_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, blocksize);
-    });
-    tu = std::thread([this, U, c, bcsr, n, blocksize] {
-      rcu = prepare_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, blocksize);
+    th = std::thread([this, L, U, c, bcsr, n, blocksize] {
+      std::vector<FillPiece> pieces;
+      rcl = prepare_csr_out(L, bcsr ? Magma_BCSR : Magma_CSRL, MagmaLower, n, c->hL.ptr, c->hL.idx, blocksize,
+                            pieces);
+      rcu = prepare_csr_out(U, bcsr ? Magma_BCSCU : Magma_CSCU, MagmaUpper, n, c->hUc.ptr, c->hUc.idx, blocksize,
+                            pieces);
+      if (!rcl && !rcu) fill_pieces(pieces);
     });
     started = true;
   }
   int join() {
-    if (tl.joinable()) tl.join();
-    if (tu.joinable()) tu.join();
+    if (th.joinable()) th.join();
     if (started) ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     started = false;
     return rcl ? rcl : rcu;

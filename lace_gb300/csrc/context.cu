@@ -541,10 +541,19 @@ extern "C" int lace_gpu_set_options(lace_gpu_ctx *c, const lace_gpu_options *o) 
       !(o->trsv_cluster == 0 || o->trsv_cluster == 1 || o->trsv_cluster == 2 || o->trsv_cluster == 4 ||
         o->trsv_cluster == 8 || o->trsv_cluster == 16))
     return set_err(DEV_ERR_ILLEGAL_VALUE);
-  const bool prec_changed = o->precision != c->opt.precision;
+  const lace_gpu_options &p = c->opt;
+  // the drop-in entry points set their options on every call: the same
+  // options keep the captured cycle graphs and the tuned schedules
+  if (o->precision == p.precision && o->trsv_mode == p.trsv_mode && o->jacobi_sweeps == p.jacobi_sweeps &&
+      o->jacobi_tol == p.jacobi_tol && o->use_graph == p.use_graph && o->spmv_lanes == p.spmv_lanes &&
+      o->trsv_rows_per_lane == p.trsv_rows_per_lane && o->monitor_orthog == p.monitor_orthog &&
+      o->trsv_chunks_per_block == p.trsv_chunks_per_block && o->trsv_warps == p.trsv_warps &&
+      o->trsv_cluster == p.trsv_cluster)
+    return DEV_SUCCESS;
+  const bool prec_changed = o->precision != p.precision;
   // a new schedule choice: tuned again before the next solve
-  if (o->trsv_rows_per_lane != c->opt.trsv_rows_per_lane || o->trsv_chunks_per_block != c->opt.trsv_chunks_per_block ||
-      o->trsv_warps != c->opt.trsv_warps || o->trsv_cluster != c->opt.trsv_cluster)
+  if (o->trsv_rows_per_lane != p.trsv_rows_per_lane || o->trsv_chunks_per_block != p.trsv_chunks_per_block ||
+      o->trsv_warps != p.trsv_warps || o->trsv_cluster != p.trsv_cluster)
     c->trsv_tuned = false;
   c->opt = *o;
   c->drop_graphs();

@@ -7,13 +7,92 @@
 // loops, not the copies, set the time.
 #pragma once
 
+#include <unistd.h>
+
 #include <algorithm>
+#include <condition_variable>
 #include <cstddef>
 #include <cstring>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
 namespace lace {
+
+// Parked host threads for the bulk loops below: waking one costs a few
+// microseconds where creating and joining one costs tens, and a drop-in call
+// runs several of these loops.  One region runs at a time.  A region asked
+// for while another runs (from another thread, or from inside a region) and
+// any region in a forked child (whose copy of the pool has no threads) get
+// threads of their own instead.  The pool lives until the process exits.
+class HostPool {
+ public:
+  static HostPool *get() {
+    static HostPool *pool = new HostPool(
+        (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())) - 1);
+    return pool;
+  }
+  // f(t) for t in [0, nt) on the caller (t = 0) and nt - 1 parked threads;
+  // false (nothing run) when the pool cannot take the region now
+  bool try_run(int nt, const std::function<void(int)> &f) {
+    if (nt - 1 > workers_ || getpid() != pid_) return false;
+    std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+    if (!busy.owns_lock()) return false;
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      job_ = &f;
+      nt_ = nt;
+      left_ = nt - 1;
+      ++gen_;
+    }
+    wake_.notify_all();
+    f(0);
+    std::unique_lock<std::mutex> l(mu_);
+    done_.wait(l, [&] { return left_ == 0; });
+    job_ = nullptr;
+    return true;
+  }
+
+ private:
+  explicit HostPool(int workers) : workers_(std::max(0, workers)), pid_(getpid()) {
+    for (int t = 1; t <= workers_; ++t) std::thread([this, t] { loop(t); }).detach();
+  }
+  void loop(int id) {
+    unsigned long seen = 0;
+    std::unique_lock<std::mutex> l(mu_);
+    for (;;) {
+      wake_.wait(l, [&] { return gen_ != seen; });
+      seen = gen_;
+      if (id >= nt_) continue;
+      const std::function<void(int)> *f = job_;
+      l.unlock();
+      (*f)(id);
+      l.lock();
+      if (--left_ == 0) done_.notify_one();
+    }
+  }
+  const int workers_;
+  const pid_t pid_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable wake_, done_;
+  const std::function<void(int)> *job_ = nullptr;
+  int nt_ = 0, left_ = 0;
+  unsigned long gen_ = 0;
+};
+
+// f(t) for t in [0, nt): on the pool, else on threads started for it
+inline void par_run(int nt, const std::function<void(int)> &f) {
+  if (nt <= 1) {
+    f(0);
+    return;
+  }
+  if (HostPool::get()->try_run(nt, f)) return;
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(f, t);
+  f(0);
+  for (auto &x : th) x.join();
+}
 
 // threads for a bulk operation over `bytes`: one per 4 MB, at most 16
 inline int host_threads(size_t bytes) {
@@ -32,14 +111,10 @@ void par_ranges(size_t bytes, F f) {
     return;
   }
   const size_t per = ((bytes + nt - 1) / nt + 63) & ~(size_t)63;
-  std::vector<std::thread> th;
-  for (int t = 1; t < nt; ++t) {
+  par_run(nt, [&](int t) {
     const size_t o = per * t;
-    if (o >= bytes) break;
-    th.emplace_back(f, o, std::min(per, bytes - o));
-  }
-  f((size_t)0, std::min(per, bytes));
-  for (auto &x : th) x.join();
+    if (o < bytes) f(o, std::min(per, bytes - o));
+  });
 }
 
 // f(begin, end) over [0, count) cut into one range per thread (`grain`
@@ -53,14 +128,10 @@ void par_for(size_t count, size_t grain, F f) {
     return;
   }
   const size_t per = (count + nt - 1) / nt;
-  std::vector<std::thread> th;
-  for (size_t t = 1; t < nt; ++t) {
+  par_run((int)nt, [&](int t) {
     const size_t b = per * t;
-    if (b >= count) break;
-    th.emplace_back(f, b, std::min(count, b + per));
-  }
-  f((size_t)0, std::min(count, per));
-  for (auto &x : th) x.join();
+    if (b < count) f(b, std::min(count, b + per));
+  });
 }
 
 inline bool par_equal(const void *a, const void *b, size_t bytes) {

@@ -203,11 +203,15 @@ def parilu_mats(A: Mat, reduction: float = 1e-15, max_sweeps: int | None = None)
 
 
 def fgmres_householder_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
-                               rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, single_cycle=False):
-    """data_fgmres_householder_restart (or data_fgmres_householder)."""
+                               rtol=1e-3, tol_type=0, choice=0, monitor_orthog=0, single_cycle=False,
+                               x0_inplace=False):
+    """data_fgmres_householder_restart (or data_fgmres_householder).
+    x0_inplace: the solution overwrites x0 (a contiguous float64 array), as
+    LACE overwrites its caller's x0 container; otherwise x0 is copied first."""
     f = lib()
     fn = f.data_fgmres_householder if single_cycle else f.data_fgmres_householder_restart
-    return _fgmres_call(fn, A, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog, 0)
+    return _fgmres_call(fn, A, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog, 0,
+                        x0_inplace)
 
 
 def fgmres_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, restart_max=20,
@@ -221,9 +225,11 @@ def fgmres_restart(A: Mat, b, x0, L: Mat | None, U: Mat | None, search_max=20, r
 
 
 def _fgmres_call(fn, A: Mat, b, x0, L, U, search_max, restart_max, rtol, tol_type, choice, monitor_orthog,
-                 reorth):
+                 reorth, x0_inplace=False):
     bv = dense(b, copy=False)
-    xv = dense(x0)
+    if x0_inplace and not (isinstance(x0, np.ndarray) and x0.dtype == np.float64 and x0.flags.c_contiguous):
+        raise ValueError("x0_inplace needs a contiguous float64 array")
+    xv = dense(x0, copy=not x0_inplace)
     par = GmresParam()
     par.search_max = search_max
     par.restart_max = restart_max
