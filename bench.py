@@ -22,7 +22,10 @@ exists on the GPU host) on all host cores.
 
 `config3` times the block system (BCSR 5x5 on 64^3 cells, n = 1,310,720)
 the same way: FP32 factors and solves inside the FP64 FGMRES against the
-all-FP64 path, with its own CPU baseline (the oracle's BCSR path).
+all-FP64 path, end to end through the LACE-named calls on the Magma_BCSR
+operator (its `e2e`, `e2e_fp64`; LACE's own FGMRES takes CSR only, so the
+BCSR operator there is this library's extension), with its own CPU baseline
+(the oracle's BCSR path).
 `config4` times the adjoint configuration's forward and backward solves
 (64^3).  `parilu_parity` reports LACE's one-thread in-place ParILU residual
 after the same sweep count beside the GPU's synchronous one.
@@ -685,6 +688,7 @@ def run_config5(args, lg, torch, stream, local):
 
 def run_config3(args, lg, torch, stream, local, hbm_peak, rank, world):
     """The block system: solves in FP32/BF16-stored factors and in FP64, the
+    same solves end to end through the LACE-named calls from host buffers, the
     block SpMV, a CPU baseline (the oracle's BCSR path) on rank 0."""
     from lace_gb300 import problems as P
     B = P.bcsr3d(BCSR_CELLS)
@@ -729,6 +733,40 @@ def run_config3(args, lg, torch, stream, local, hbm_peak, rank, world):
         out[prec] = {"value": t, "unit": "s", "iterations": r.total_iterations, "true_rel_resid": rel(x),
                      "converged": r.converged}
     out["speedup_mixed_vs_fp64"] = out["fp64"]["value"] / out["fp32"]["value"]
+    if not args.skip_e2e:
+        # the same solve through the LACE-named calls from host buffers:
+        # data_PariLU_v0_3_prescribedSweeps on the Magma_BCSR operator, then
+        # data_fgmres_householder_restart with the BCSR operator and the BCSR /
+        # BCSC factors it returned (an extension: LACE's FGMRES takes CSR)
+        from lace_gb300 import dropin
+        Am = dropin.bcsr(B)
+        ld = B.bs * B.bs
+
+        def e2e_runs(prec, count):
+            dropin.set_options(precision=prec)
+            times, nf, x = [], 0, None
+            for _ in range(count):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                L, U, info = dropin.parilu_mats(Am, max_sweeps=SWEEPS)
+                x, rc, glog = dropin.fgmres_householder_restart(Am, b, np.zeros(B.n), L, U, search_max=M,
+                                                               restart_max=RESTART_MAX, rtol=RTOL, tol_type=1,
+                                                               x0_inplace=True)
+                nf = L.m.nnz + U.m.nnz
+                del L, U
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t0)
+            dropin.set_options()
+            # A's values twice, the factors up, b and x0 up; the factors and x down
+            h2d = 2 * B.nblk * ld * 8 + nf * 8 + 2 * B.n * 8
+            d2h = nf * 8 + B.n * 8
+            return statistics.median(times[1:]), h2d, d2h, x
+
+        path = "data_PariLU_v0_3_prescribedSweeps + data_fgmres_householder_restart on the Magma_BCSR operator"
+        for key, prec in (("e2e", "fp32"), ("e2e_fp64", "fp64")):
+            t, h2d, d2h, x = e2e_runs(prec, 1 + max(3, args.steps))
+            out[key] = {"value": t, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                        "true_rel_resid": rel(x), "path": f"{path} ({prec} factors)"}
     # block SpMV (FP64) alone
     q = torch.randn(B.n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(q)

@@ -480,7 +480,11 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
                   data_d_matrix *U, data_d_gmres_param *par, data_d_gmres_log *log, int restart_max,
                   int method, int restarted) {
   if (!A || !b || !x0 || !par || !log) return set_err(DEV_ERR_INVALID_PTR);
-  if (!is_csr(A->storage_type)) return set_err(DEV_ERR_NOT_SUPPORTED);
+  // CSR, as LACE; a BCSR operator (with the BCSR / BCSC factors
+  // data_PariLU_v0_3 returns for it) is this library's extension: LACE's
+  // data_z_spmv and solves take CSR only
+  const bool bcsr = A->storage_type == Magma_BCSR;
+  if (!is_csr(A->storage_type) && !bcsr) return set_err(DEV_ERR_NOT_SUPPORTED);
   std::lock_guard<std::mutex> lk(g_mu);
   auto t0 = std::chrono::steady_clock::now();
   lace_gpu_ctx *c = nullptr;
@@ -497,17 +501,31 @@ int fgmres_dropin(data_d_matrix *A, data_d_matrix *b, data_d_matrix *x0, data_d_
   else if (o.trsv_mode != LACE_TRSV_LEVELS) o.trsv_mode = LACE_TRSV_SYNCFREE;
   lace_gpu_set_options(c, &o);
   PhaseClock pc(c->verbose, "fgmres");
-  const int n = A->num_rows;
-  rc = lace_gpu_upload_csr_host(c, n, A->row[n], A->row, A->col, A->val);
+  // rows of the pattern (block rows for BCSR) and of the vectors
+  const int nr = A->num_rows;
+  const int n = bcsr ? nr * A->blocksize : nr;
+  if (bcsr)
+    rc = lace_gpu_upload_bcsr_host(c, nr, A->blocksize, A->numblocks > 0 ? A->numblocks : A->row[nr], A->row, A->col,
+                                   A->val);
+  else
+    rc = lace_gpu_upload_csr_host(c, nr, A->row[nr], A->row, A->col, A->val);
   if (rc) return set_err(rc);
   pc.mark("upload A");
   if (choice != 2) {
     if (!L || !U) return set_err(DEV_ERR_INVALID_PTR);
-    // factors as ParILU returned them (U in CSC, the context's own patterns):
-    // values go up as they are; anything else is converted on the host
+    // factors as ParILU returned them (U in CSC, or BCSC for a BCSR operator;
+    // the context's own patterns): values go up as they are; CSR factors in
+    // other layouts are converted on the host
     rc = 1;
-    if ((U->storage_type == Magma_CSCU || U->storage_type == Magma_CSC) && L->num_rows == n && U->num_rows == n)
+    if (bcsr) {
+      if (L->storage_type == Magma_BCSR && U->storage_type == Magma_BCSCU && L->num_rows == nr &&
+          U->num_rows == nr && L->blocksize == A->blocksize && U->blocksize == A->blocksize)
+        rc = c->set_factors_csc_host(nr, L->row, L->col, L->val, U->row, U->col, U->val);
+      if (rc == 1) return set_err(DEV_ERR_NOT_SUPPORTED);
+    } else if ((U->storage_type == Magma_CSCU || U->storage_type == Magma_CSC) && L->num_rows == n &&
+               U->num_rows == n) {
       rc = c->set_factors_csc_host(n, L->row, L->col, L->val, U->row, U->col, U->val);
+    }
     if (rc == 1) {
       std::vector<int> up, ui;
       std::vector<double> uv;

@@ -851,12 +851,15 @@ int lace_gpu_ctx::same_on_device(int parts, const int *const *h, const int *cons
 
 int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lcol, const double *lval,
                                        const int *ucp, const int *uri, const double *ucval) {
-  if (bs || nrows != n || (int)hL.ptr.size() != n + 1 || (int)hUc.ptr.size() != n + 1) return 1;
-  if (lrow[n] != nnzL || ucp[n] != nnzU) return 1;
+  // rows (block rows for BCSR factors) and values per pattern entry
+  const int nr = n_blk;
+  const size_t ld = bs ? (size_t)bs * bs : 1;
+  if (nrows != nr || (int)hL.ptr.size() != nr + 1 || (int)hUc.ptr.size() != nr + 1) return 1;
+  if (lrow[nr] != nnzL || ucp[nr] != nnzU) return 1;
   {
     const int *h[4] = {lrow, ucp, lcol, uri};
     const int *d[4] = {(const int *)Lrow.p, (const int *)Ucp.p, (const int *)Lcol.p, (const int *)Uri.p};
-    const size_t cnt[4] = {(size_t)n + 1, (size_t)n + 1, (size_t)nnzL, (size_t)nnzU};
+    const size_t cnt[4] = {(size_t)nr + 1, (size_t)nr + 1, (size_t)nnzL, (size_t)nnzU};
     bool same = false;
     const int rc = same_on_device(4, h, d, cnt, &same);
     if (rc) return rc;
@@ -866,22 +869,25 @@ int lace_gpu_ctx::set_factors_csc_host(int nrows, const int *lrow, const int *lc
   if (rc) return rc;
   const VType t = vtype();
   cur = 0;
+  const size_t nl = (size_t)nnzL * ld, nu = (size_t)nnzU * ld;
   if (t == VType::F64) {
-    if (cudaMemcpyAsync(Lv[0].p, lval, 8 * (size_t)nnzL, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
-        cudaMemcpyAsync(Ucv[0].p, ucval, 8 * (size_t)nnzU, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+    if (cudaMemcpyAsync(Lv[0].p, lval, 8 * nl, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(Ucv[0].p, ucval, 8 * nu, cudaMemcpyHostToDevice, stream) != cudaSuccess)
       return DEV_ERR_UNKNOWN;
   } else {
     // FP64 values through a staging buffer the context keeps (no allocation
     // per call), converted on the GPU
-    if (stage64.ensure(8 * (size_t)(nnzL + nnzU))) return DEV_ERR_DEVICE_ALLOC;
-    double *tl = (double *)stage64.p, *tu = tl + nnzL;
-    if (cudaMemcpyAsync(tl, lval, 8 * (size_t)nnzL, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
-        cudaMemcpyAsync(tu, ucval, 8 * (size_t)nnzU, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+    if (stage64.ensure(8 * (nl + nu))) return DEV_ERR_DEVICE_ALLOC;
+    double *tl = (double *)stage64.p, *tu = tl + nl;
+    if (cudaMemcpyAsync(tl, lval, 8 * nl, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+        cudaMemcpyAsync(tu, ucval, 8 * nu, cudaMemcpyHostToDevice, stream) != cudaSuccess)
       return DEV_ERR_UNKNOWN;
-    launch_convert(stream, nnzL, VType::F64, tl, t, Lv[0].p);
-    launch_convert(stream, nnzU, VType::F64, tu, t, Ucv[0].p);
+    launch_convert(stream, (int)nl, VType::F64, tl, t, Lv[0].p);
+    launch_convert(stream, (int)nu, VType::F64, tu, t, Ucv[0].p);
   }
-  rc = finish_factors();  // U's CSR image and L^T, gathered on the GPU
+  // U's CSR image and L^T (for BCSR: U's block-row image and the inverses
+  // of the diagonal blocks), on the GPU
+  rc = finish_factors();
   if (rc) return rc;
   if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
   return 0;
@@ -973,11 +979,12 @@ int lace_gpu_ctx::upload_common(int n_, int nnz_, const int *hrow, const int *hc
   return 0;
 }
 
-// new values for the resident CSR pattern (the caller has checked that the
-// pattern is the same): the analysis, plans and maps are kept
+// new values for the resident CSR or BCSR pattern (the caller has checked
+// that the pattern is the same): the analysis, plans and maps are kept
 int lace_gpu_ctx::upload_values_same_pattern(const double *val) {
   ++aval_version;
-  if (Aval.upload(val, 8 * (size_t)nnzA, stream)) return DEV_ERR_DEVICE_ALLOC;
+  const size_t ld = bs ? (size_t)bs * bs : 1;
+  if (Aval.upload(val, 8 * (size_t)nnzA * ld, stream)) return DEV_ERR_DEVICE_ALLOC;
   factors_ready = false;
   const int rc = device_anorm();
   if (rc) return rc;
@@ -1046,6 +1053,19 @@ extern "C" int lace_gpu_upload_bcsr_host(lace_gpu_ctx *c, int nb, int bs, int nb
   if (!c || !row || (nblk > 0 && (!col || !val))) return set_err(DEV_ERR_INVALID_PTR);
   if (bs < 1 || bs > 8) return set_err(DEV_ERR_NOT_SUPPORTED);
   cudaSetDevice(c->device);
+  // same block pattern as the resident matrix: only the values travel
+  bool same = c->bs == bs && c->n_blk == nb && c->nnzA == nblk && row[nb] == nblk;
+  if (same) {  // compared with the resident pattern on the GPU
+    const int *h[2] = {row, col};
+    const int *d[2] = {(const int *)c->Arow.p, (const int *)c->Acol.p};
+    const size_t cnt[2] = {(size_t)nb + 1, (size_t)nblk};
+    const int rc = c->same_on_device(2, h, d, cnt, &same);
+    if (rc) return set_err(rc);
+  }
+  if (same) {
+    const int rc = c->upload_values_same_pattern(val);
+    return rc ? set_err(rc) : DEV_SUCCESS;
+  }
   int rc = validate_csr(nb, nblk, row, col);
   if (rc) return set_err(rc);
   const size_t ld = (size_t)bs * bs;
