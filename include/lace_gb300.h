@@ -214,6 +214,11 @@ int data_z_spmv(dataType alpha, data_d_matrix *A, data_d_matrix *x,
  * SpTRSV), 1 ParCSRTRSV with tol 1.0 (in LACE's sweep order the first sweep
  * is the exact substitution and the second changes nothing, so the
  * preconditioned vectors are the exact solves'), 2 no preconditioner.
+ * Beyond LACE (whose data_z_spmv and solves take CSR only): A may be
+ * Magma_BCSR (num_rows = block rows; b, x0 of num_rows * blocksize rows)
+ * with the factors data_PariLU_v0_3 returns for it, L Magma_BCSR and U
+ * Magma_BCSCU of the same block pattern (other factor layouts:
+ * DEV_ERR_NOT_SUPPORTED); this holds for every FGMRES entry point below.
  * x0 is overwritten with the solution (LACE frees and re-allocates
  * x0->val; this replacement writes into the existing array).  Returns
  * DEV_SUCCESS when the residual target was reached, DEV_NOTCONVERGED
