@@ -293,6 +293,32 @@ int data_zmconvert(data_d_matrix A, data_d_matrix *B, data_storage_t old_format,
 int data_zmtranspose(data_d_matrix A, data_d_matrix *B);
 int data_rowindex(data_d_matrix *A, int **rowidx);
 
+/* Cuthill-McKee orderings (src/cuthill_mckee.cpp:53), on the host:
+ * nn_map[old] = new.  The seed is the lowest-numbered node of maximum degree
+ * (off-diagonal entries of its row), nodes are numbered breadth first over
+ * A's rows, each node's unnumbered neighbours in order of decreasing degree
+ * (lower index first among equals), each further component from its own
+ * seed; reverse gives new' = n - 1 - new.  This is the ordering LACE's
+ * source describes; LACE's routine itself reads outside its arrays on
+ * ordinary meshes, so its results are not reproducible (a null argument or a
+ * malformed pattern sets lace_gpu_last_error() and leaves nn_map alone). */
+#if defined(__cplusplus) && !defined(SPARSE_Z_H)
+void data_reorder_cuthill_mckee(data_d_matrix *A, int *nn_map, bool reverse = false);
+#elif defined(__cplusplus)
+void data_reorder_cuthill_mckee(data_d_matrix *A, int *nn_map, bool reverse);
+#else
+void data_reorder_cuthill_mckee(data_d_matrix *A, int *nn_map, _Bool reverse);
+#endif
+
+/* src/reorder.cpp:167: reorder 1 Cuthill-McKee, 2 reverse Cuthill-McKee,
+ * anything else but 3 none; A (Magma_CSR, or Magma_BCSR by block rows) is
+ * replaced in place by A in the new numbering, rows sorted by column, its
+ * arrays reallocated as LACE's are.  P[new] = old and Pinv[old] = new (LACE
+ * hands the old-to-new map to its permutation as P and so applies the inverse
+ * ordering).  3 (AMD, SuiteSparse in LACE) returns DEV_ERR_NOT_SUPPORTED with
+ * A untouched.  Nothing is printed. */
+int data_sparse_reorder(data_d_matrix *A, int *P, int *Pinv, int reorder);
+
 /* Replaces control/norms.cpp:301: *res = ||A - L U||_F over the product's
  * pattern (fill-in included) and *nonlinres = the same over the entries of
  * A the product holds, on the GPU without forming L U.  L: CSRL with its

@@ -167,6 +167,8 @@ SIGNATURES = {
     "data_zmconvert": (_i, [DataMatrix, _DM, _i, _i]),
     "data_zmtranspose": (_i, [DataMatrix, _DM]),
     "data_rowindex": (_i, [_DM, C.POINTER(_p)]),
+    "data_reorder_cuthill_mckee": (None, [_DM, C.POINTER(_i), C.c_bool]),
+    "data_sparse_reorder": (_i, [_DM, C.POINTER(_i), C.POINTER(_i), _i]),
     "data_zwrite_csr_mtx": (_i, [DataMatrix, _i, C.c_char_p]),
     "lace_gpu_default_options": (None, [C.POINTER(GpuOptions)]),
     "lace_gpu_dropin_set_options": (_i, [C.POINTER(GpuOptions)]),

@@ -602,3 +602,62 @@ def ilu_precond_adjoint(F: Factors, kind: str = "trsv") -> dict:
     lp, li, lv, _ = transpose(F.L.ptr, F.L.idx, F.L.val, n)
     return {"kind": kind, "t1": F.U, "t1_lower": True, "t1_unit": False,
             "t2": Tri(lp, li, lv), "t2_lower": False, "t2_unit": True}
+
+
+# ------------------------------------------------------------ orderings
+
+def cuthill_mckee(n: int, row, col, reverse: bool = False) -> np.ndarray:
+    """nn_map[old] = new, the Cuthill-McKee numbering of A's row graph as
+    src/cuthill_mckee.cpp states it: degree = off-diagonal entries of a row
+    (:98-113), the seed a node of maximum degree (:128-139), breadth first,
+    each node's unnumbered neighbours in order of decreasing degree
+    (compare_degree, :31-41, popped in that order :192-207), nn_map[old] = new
+    (:224-225).  The cases LACE's routine leaves undefined are fixed as the
+    library fixes them: ties to the lower index, a new component from the
+    next node of maximum degree, new' = n - 1 - new when reversed."""
+    row = np.asarray(row, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    deg = [int(np.count_nonzero(col[row[i]:row[i + 1]] != i)) for i in range(n)]
+    key = lambda v: (-deg[v], v)  # noqa: E731
+    seeds = sorted(range(n), key=key)
+    seen = [False] * n
+    order: list[int] = []
+    head = nxt = 0
+    while len(order) < n:
+        if head == len(order):
+            while seen[seeds[nxt]]:
+                nxt += 1
+            seen[seeds[nxt]] = True
+            order.append(seeds[nxt])
+        v = order[head]
+        head += 1
+        nb = []
+        for u in col[row[v]:row[v + 1]]:
+            u = int(u)
+            if u != v and not seen[u]:
+                seen[u] = True
+                nb.append(u)
+        order.extend(sorted(nb, key=key))
+    nn_map = np.empty(n, dtype=np.int64)
+    for k, v in enumerate(order):
+        nn_map[v] = n - 1 - k if reverse else k
+    return nn_map
+
+
+def permute_csr(row, col, val, P, Pinv, ld: int = 1):
+    """src/reorder.cpp:86-122 then :127-165: row i of the result is row P[i]
+    of A with columns c -> Pinv[c], each row sorted by column (ld values per
+    entry)."""
+    row = np.asarray(row)
+    n = len(row) - 1
+    val = np.asarray(val).reshape(-1, ld)
+    r2, c2, v2 = [0], [], []
+    for i in range(n):
+        o = P[i]
+        cols = np.asarray(Pinv)[np.asarray(col[row[o]:row[o + 1]], dtype=np.int64)]
+        order = np.argsort(cols, kind="stable")
+        c2.extend(cols[order].tolist())
+        v2.append(val[row[o]:row[o + 1]][order])
+        r2.append(r2[-1] + len(cols))
+    vals = np.concatenate(v2).reshape(-1) if v2 else np.zeros(0)
+    return np.array(r2, dtype=np.int32), np.array(c2, dtype=np.int32), vals
