@@ -399,6 +399,53 @@ int upload_blk_plan(const HostPlan &hp, PlanBufs &pb, cudaStream_t s) {
   return 0;
 }
 
+// dst <- a device copy of src's plan (its buffers, shape and gathered values)
+int copy_blk_plan(const PlanBufs &src, PlanBufs &dst, cudaStream_t s) {
+  dst.valid = false;
+  const DBuf *from[10] = {&src.blk, &src.urec, &src.ucode, &src.umap, &src.udiag,
+                          &src.uprev, &src.uflag, &src.uvs, &src.uaps, &src.urd};
+  DBuf *to[10] = {&dst.blk, &dst.urec, &dst.ucode, &dst.umap, &dst.udiag, &dst.uprev, &dst.uflag, &dst.uvs, &dst.uaps,
+                  &dst.urd};
+  for (int k = 0; k < 10; ++k) {
+    if (to[k]->ensure(from[k]->bytes)) return DEV_ERR_DEVICE_ALLOC;
+    if (from[k]->bytes &&
+        cudaMemcpyAsync(to[k]->p, from[k]->p, from[k]->bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return DEV_ERR_UNKNOWN;
+  }
+  dst.dev = src.dev;
+  TriBlkPlan &d = dst.dev;
+  d.blk = (const int4 *)dst.blk.p;
+  d.urec = (const int4 *)dst.urec.p;
+  d.ucode = (const int *)dst.ucode.p;
+  d.umap = (const int *)dst.umap.p;
+  d.udiag = (const int *)dst.udiag.p;
+  d.uprev = (const int *)dst.uprev.p;
+  d.uflag = (const int *)dst.uflag.p;
+  d.uvs = dst.uvs.p;
+  d.uaps = dst.uaps.p;
+  d.urd = dst.urd.p;
+  dst.vals_version = src.vals_version;
+  dst.vals_type = src.vals_type;
+  dst.vals_src = src.vals_src;
+  dst.valid = src.valid;
+  return 0;
+}
+
+// exchange two plans (buffers move with the pointers into them)
+void swap_blk_plans(PlanBufs &a, PlanBufs &b) {
+  DBuf *x[10] = {&a.blk, &a.urec, &a.ucode, &a.umap, &a.udiag, &a.uprev, &a.uflag, &a.uvs, &a.uaps, &a.urd};
+  DBuf *y[10] = {&b.blk, &b.urec, &b.ucode, &b.umap, &b.udiag, &b.uprev, &b.uflag, &b.uvs, &b.uaps, &b.urd};
+  for (int k = 0; k < 10; ++k) {
+    std::swap(x[k]->p, y[k]->p);
+    std::swap(x[k]->bytes, y[k]->bytes);
+  }
+  std::swap(a.dev, b.dev);
+  std::swap(a.valid, b.valid);
+  std::swap(a.vals_version, b.vals_version);
+  std::swap(a.vals_type, b.vals_type);
+  std::swap(a.vals_src, b.vals_src);
+}
+
 int build_blk_plan(const Pattern &T, bool lower, bool unit, int R, int cpb, PlanBufs &pb, cudaStream_t s) {
   HostPlan hp;
   const int rc = build_blk_plan_host(T, lower, unit, R, cpb, hp);
@@ -1545,6 +1592,7 @@ int lace_gpu_ctx::autotune_trsv() {
   // distributed shared memory
   struct Cand {
     int R, cpb, w, cl;
+    int fam = 0, grp = 0;  // shape family, and the group whose plans are built together
   };
   // blocks up to the shared-memory window (160 KB of solved rows: 40960 rows
   // in FP32, 20480 in FP64) keep every in-block dependency on chip; a block
@@ -1568,24 +1616,57 @@ int lace_gpu_ctx::autotune_trsv() {
   cands.erase(std::remove_if(cands.begin(), cands.end(),
                              [&](const Cand &c) { return c.cpb > 1 && c.cpb * 32 * c.R > 2 * n && cands.size() > 1; }),
               cands.end());
+  // Families of shapes: one row per lane in multi-chunk blocks (tried in
+  // full), two rows, four rows, and one chunk per block.  The other families
+  // are tried through one representative first; their other shapes, whose
+  // times stay within about 15 % of one another, are built and timed only if
+  // the representative comes within 1.5x of the best so far.
+  auto family = [](const Cand &c) { return c.cpb == 1 ? 3 : (c.R == 1 ? 0 : (c.R == 2 ? 1 : 2)); };
+  const Cand reps[4] = {{1, 0, 0, 0}, {2, 256, 16, 1}, {4, 128, 16, 1}, {1, 1, 1, 1}};
+  for (int f = 1; f < 4; ++f) {
+    bool have_rep = false;
+    for (auto &c : cands)
+      have_rep |= family(c) == f && c.R == reps[f].R && c.cpb == reps[f].cpb && c.w == reps[f].w && c.cl == reps[f].cl;
+    bool first = !have_rep;
+    for (auto &c : cands)
+      if (family(c) == f) {
+        const bool is_rep = have_rep ? (c.R == reps[f].R && c.cpb == reps[f].cpb && c.w == reps[f].w &&
+                                        c.cl == reps[f].cl)
+                                     : first;
+        first = false;
+        c.grp = is_rep ? 2 * f - 1 : 2 * f;
+      }
+  }
+  for (auto &c : cands) c.fam = family(c);
+  float rep_ms[4] = {0.f, 0.f, 0.f, 0.f};
+  PlanBufs kept[2];  // the fastest candidate's plans so far
   // The host halves of the candidates' plans (L and U) are built in parallel
-  // ahead of their turn, in batches of about 4 GB of host memory.
+  // ahead of their turn, a group at a time, in batches of about 4 GB of host
+  // memory.
   const size_t plan_bytes = (size_t)n * 48 + ((size_t)1 << 20);
-  const size_t batch = std::max<size_t>(2, std::min<size_t>(16, ((size_t)4 << 30) / plan_bytes));
-  // candidates of one plan shape next to each other: the plan is built once
-  std::stable_sort(cands.begin(), cands.end(),
-                   [](const Cand &a, const Cand &b) { return a.R != b.R ? a.R < b.R : a.cpb < b.cpb; });
+  const size_t batch = std::max<size_t>(2, std::min<size_t>(24, ((size_t)4 << 30) / plan_bytes));
+  // groups in order; in a group, candidates of one plan shape next to each
+  // other: the plan is built once
+  std::stable_sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) {
+    return a.grp != b.grp ? a.grp < b.grp : (a.R != b.R ? a.R < b.R : a.cpb < b.cpb);
+  });
   auto have = [&](int w, int R, int cpb) {
     return prebuilt.count(std::make_tuple(w, R, cpb)) || (plans[w].valid && plans[w].dev.R == R && plans[w].dev.cpb == cpb);
   };
   auto prebuild_from = [&](size_t first) {
+    // the shapes tried in any case (the first family and every other
+    // family's first shape) are built together; the rest of a family when
+    // its turn comes
+    auto eager = [](const Cand &c) { return c.grp == 0 || c.grp % 2 == 1; };
     std::vector<std::tuple<int, int, int>> keys;
-    for (size_t c = first; c < cands.size() && keys.size() < batch; ++c)
+    for (size_t c = first; c < cands.size() && keys.size() < batch; ++c) {
+      if (eager(cands[first]) ? !eager(cands[c]) : cands[c].grp != cands[first].grp) continue;
       for (int w = 0; w < 2; ++w) {
         const auto k = std::make_tuple(w, cands[c].R, cands[c].cpb);
         if (!have(w, cands[c].R, cands[c].cpb) && std::find(keys.begin(), keys.end(), k) == keys.end())
           keys.push_back(k);
       }
+    }
     std::vector<HostPlan *> out;
     for (auto &k : keys) out.push_back(&prebuilt[k]);  // map nodes stay put
     const Pattern *pats[2] = {&hL, &hU};
@@ -1603,6 +1684,12 @@ int lace_gpu_ctx::autotune_trsv() {
   };
   for (size_t ci = 0; ci < cands.size(); ++ci) {
     Cand cd = cands[ci];
+    if (cd.grp > 0 && cd.grp % 2 == 0 && rep_ms[cd.fam] > 1.5f * best) {
+      if (verbose)
+        printf("trsv autotune R=%d cpb=%d warps=%d cluster=%d: skipped (its family's first shape %.3f ms per pair)\n",
+               cd.R, cd.cpb, cd.w, cd.cl, rep_ms[cd.fam] / 2);
+      continue;
+    }
     if (!have(0, cd.R, cd.cpb) || !have(1, cd.R, cd.cpb))
       if ((rc = prebuild_from(ci))) return rc;
     plan_R = cd.R;
@@ -1638,7 +1725,11 @@ int lace_gpu_ctx::autotune_trsv() {
     if (verbose)
       printf("trsv autotune R=%d cpb=%d warps=%d cluster=%d: %.3f ms per pair%s\n", cd.R, cd.cpb, cd.w, cd.cl,
              ms / 2, (st & kStatusSpinTimeout) ? " (wait timed out)" : "");
+    if (cd.grp % 2 == 1) rep_ms[cd.fam] = ms;
     if (ms < best) {
+      // the leader's plans kept on the device, so that they need no rebuild
+      // when later candidates have loaded theirs
+      if ((rc = copy_blk_plan(plans[0], kept[0], stream)) || (rc = copy_blk_plan(plans[1], kept[1], stream))) return rc;
       best = ms;
       bR = cd.R;
       bC = cd.cpb;
@@ -1647,6 +1738,10 @@ int lace_gpu_ctx::autotune_trsv() {
     }
   }
   (void)nch_min;
+  for (int w = 0; w < 2; ++w)
+    if (kept[w].valid && !(plans[w].valid && plans[w].dev.R == bR && plans[w].dev.cpb == bC))
+      swap_blk_plans(plans[w], kept[w]);
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return DEV_ERR_UNKNOWN;
   prebuilt.clear();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -2013,6 +2108,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
   }
   if (!rc && cudaStreamSynchronize(stream) != cudaSuccess) rc = DEV_ERR_UNKNOWN;
   if (rc) return rc;
+  sc.mark("solve plans");
   if (mgs && !side && cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess)
     return DEV_ERR_UNKNOWN;
   ArnoldiArgs a = arnoldi_args(m, adjoint);
@@ -2099,6 +2195,7 @@ int lace_gpu_ctx::fgmres(const double *b, double *x, int m, int restart_max, int
       LCHK(cudaMemcpyAsync(h_scal + kScalReorth, &cy->nreorth, 4, cudaMemcpyDeviceToHost, stream));
     }
     LCHK(cudaStreamSynchronize(stream));
+    if (restart == 0) sc.mark("first cycle");
     const Control &hc = *h_ctrl;
     if (restart == 0) rnorm0 = hc.rnorm0;
     // LACE's Gram-Schmidt FGMRES logs the residual at the start of every
