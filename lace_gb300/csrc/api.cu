@@ -234,16 +234,19 @@ void parilu_dropin(data_d_matrix *A, data_d_matrix *L, data_d_matrix *U, dataTyp
   // (on the GPU), so that the output containers can be prepared from the
   // start, while A's values go up and the GPU sweeps.
   bool known = false;
-  if (!bcsr && is_csr(A->storage_type) && c->bs == 0 && c->n_blk == n && c->nnzA == A->row[n] &&
-      (int)c->hArow.size() == n + 1 && (int)c->hL.ptr.size() == n + 1 && c->hL.idx.size() == (size_t)c->nnzL) {
+  const int nblk_in = bcsr ? (A->numblocks > 0 ? A->numblocks : A->row[n]) : A->row[n];
+  if (((!bcsr && is_csr(A->storage_type) && c->bs == 0 && (int)c->hArow.size() == n + 1) ||
+       (bcsr && c->bs == A->blocksize && A->row[n] == nblk_in)) &&
+      c->n_blk == n && c->nnzA == nblk_in && (int)c->hL.ptr.size() == n + 1 &&
+      c->hL.idx.size() == (size_t)c->nnzL) {
     const int *h[2] = {A->row, A->col};
     const int *d[2] = {(const int *)c->Arow.p, (const int *)c->Acol.p};
-    const size_t cnt[2] = {(size_t)n + 1, (size_t)A->row[n]};
+    const size_t cnt[2] = {(size_t)n + 1, (size_t)nblk_in};
     rc = c->same_on_device(2, h, d, cnt, &known);
     if (rc) return fail(rc);
   }
   if (known) {
-    prep.start(L, U, c, false, n, 0);
+    prep.start(L, U, c, bcsr, n, bcsr ? A->blocksize : 0);
     rc = c->upload_values_same_pattern(A->val);
   } else if (bcsr) {
     const int bs = A->blocksize;
