@@ -115,38 +115,42 @@ def test_bcsr_fgmres(lg, torch_cuda, prec):
     assert abs(res.total_iterations - r.total_iterations) <= 2
 
 
+@pytest.mark.parametrize("method", ["householder", "mgs"])
 @pytest.mark.parametrize("prec", ["fp64", "fp32"])
-def test_dropin_bcsr_fgmres(lg, torch_cuda, prec):
+def test_dropin_bcsr_fgmres(lg, torch_cuda, prec, method):
     """The block system through the LACE-named calls (a BCSR operator in
-    data_fgmres_householder_restart is this library's extension: LACE's
-    data_z_spmv takes CSR only): data_PariLU_v0_3_prescribedSweeps on the
-    Magma_BCSR operator returns BCSR / BCSC factors, which the FGMRES call
-    takes with the operator; the second round reuses the analysis.  The
-    solution equals the Context path's, the directions are within +-2 of the
-    oracle's block solve, the true residual is at the tolerance."""
+    data_fgmres_householder_restart / data_fgmres_restart is this library's
+    extension: LACE's data_z_spmv takes CSR only):
+    data_PariLU_v0_3_prescribedSweeps on the Magma_BCSR operator returns BCSR
+    / BCSC factors, which the FGMRES call takes with the operator; the second
+    round reuses the analysis.  The solution equals the Context path's, the
+    directions are within +-2 of the oracle's block solve, the true residual
+    is at the tolerance."""
     from lace_gb300 import dropin
     B = P.bcsr3d(8, seed=4)
     b = P.rhs_normal(B.n, 0)
     F = orc.bcsr_parilu(B, 3, mode="sync")
     op = {"kind": "bcsr", "bs": B.bs, "row": B.row, "col": B.col, "val": B.val}
-    r = orc.fgmres(op, orc.bcsr_precond(F, f32=prec == "fp32"), b, search_max=50, restart_max=20, rtol=1e-10)
+    solver = orc.fgmres if method == "householder" else orc.fgmres_mgs
+    r = solver(op, orc.bcsr_precond(F, f32=prec == "fp32"), b, search_max=50, restart_max=20, rtol=1e-10)
     with lg.Context(0) as ctx:
         ctx.set_options(precision=prec)
         ctx.upload(B)
         ctx.parilu0(3, residual=False)
         xd = torch_cuda.zeros(B.n, dtype=torch_cuda.float64, device="cuda")
-        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=20, rtol=1e-10)
+        res = ctx.fgmres(dev(torch_cuda, b), xd, search_max=50, restart_max=20, rtol=1e-10,
+                         orthogonalization=method)
         xc = xd.cpu().numpy()
     Am = dropin.bcsr(B)
     Bc = B.to_csr()
+    call = dropin.fgmres_householder_restart if method == "householder" else dropin.fgmres_restart
     dropin.set_options(precision=prec)
     try:
         for _ in range(2):
             L, U, info = dropin.parilu_mats(Am, max_sweeps=3)
             assert L.m.storage_type == dropin.Magma_BCSR and U.m.storage_type == dropin.Magma_BCSCU
             assert L.m.blocksize == B.bs and U.m.blocksize == B.bs
-            x, rc, glog = dropin.fgmres_householder_restart(Am, b, np.zeros(B.n), L, U, search_max=50,
-                                                           restart_max=20, rtol=1e-10, tol_type=1)
+            x, rc, glog = call(Am, b, np.zeros(B.n), L, U, search_max=50, restart_max=20, rtol=1e-10, tol_type=1)
             assert rc == 0
             assert glog["restarts"] == 0 and glog["search_directions"] == res.total_iterations
             assert abs(glog["search_directions"] - r.total_iterations) <= 2
