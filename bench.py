@@ -207,6 +207,9 @@ def run_ours(args):
     if args.only_config5:
         print(json.dumps({"config5": run_config5(args, lg, torch, torch.cuda.Stream(), local)}))
         return
+    if args.only_config3:
+        print(json.dumps({"config3": run_config3(args, lg, torch, torch.cuda.Stream(), local, hbm_peak, 0, 1)}))
+        return
     A, b = build_problem(args.grid if (args.only_mgs or args.only_householder or args.only_kernels) else GRID)
     stream = torch.cuda.Stream()
     ctx = lg.Context(local, stream=stream)
@@ -620,9 +623,11 @@ def run_config4(args, lg, torch, stream, local):
             "backward": {"value": statistics.median(bwd), "unit": "s", "iterations": its}}
 
 
-WORKLOAD5 = ("batch_aniso: 256 independent 2D 5-pt anisotropic Laplacians, side U{32..256}, eps logU[1e-3, 1] "
-             "(seed 0), 4 RHS N(0,1) each; ParILU(0) 3 sync sweeps in FP32 for every system, "
-             "FGMRES-Householder(30) per (system, rhs) to 1e-10 rel, FP64 outer")
+def workload5(count: int = 256, side_hi: int = 256) -> str:
+    return (f"batch_aniso: {count} independent 2D 5-pt anisotropic Laplacians, side U{{32..{side_hi}}}, eps "
+            "logU[1e-3, 1] (seed 0), 4 RHS N(0,1) each; ParILU(0) 3 sync sweeps in FP32 for every system, "
+            "FGMRES-Householder(30) per (system, rhs) to 1e-10 rel, FP64 outer")
+
 RESTART5 = 100
 
 
@@ -633,7 +638,9 @@ def run_config5(args, lg, torch, stream, local):
     directions per (system, rhs), true residuals on the host."""
     import ctypes as C
     from lace_gb300 import problems as P
-    systems = P.batch_aniso(count=256, side_lo=32, side_hi=256, nrhs=4, seed=0)
+    count, side_hi = args.batch_count, args.batch_side_max
+    wl5 = workload5(count, side_hi)
+    systems = P.batch_aniso(count=count, side_lo=32, side_hi=side_hi, nrhs=4, seed=0)
     nrhs = 4
     n = np.array([sy.A.n for sy in systems], dtype=np.int32)
     row_off = np.concatenate([[0], np.cumsum(n)[:-1]]).astype(np.int32)
@@ -653,7 +660,7 @@ def run_config5(args, lg, torch, stream, local):
                                  nnz_off.ctypes.data, row.ctypes.data, col.ctypes.data, val.ctypes.data, nrhs)
     if rc != 0:
         ctx.close()
-        return {"workload": WORKLOAD5, "error": int(rc)}
+        return {"workload": wl5, "error": int(rc)}
     bd = torch.tensor(B.ravel(), dtype=torch.float64, device="cuda")
     xd = torch.zeros(nrhs * N, dtype=torch.float64, device="cuda")
     iters = np.zeros(len(systems) * nrhs, dtype=np.int32)
@@ -678,7 +685,7 @@ def run_config5(args, lg, torch, stream, local):
         for r in range(nrhs):
             x = X[r, row_off[s]:row_off[s] + n[s]]
             worst = max(worst, float(np.linalg.norm(sy.B[r] - sy.A.matvec(x)) / np.linalg.norm(sy.B[r])))
-    return {"workload": WORKLOAD5, "rows": N, "nnz": int(len(col)), "rhs": nrhs,
+    return {"workload": wl5, "rows": N, "nnz": int(len(col)), "rhs": nrhs,
             "fp32": {"value": statistics.median(times), "unit": "s", "code": int(rc),
                      "directions_total": int(iters.sum()), "directions_max": int(iters.max()),
                      "directions_mean": float(iters.mean()), "worst_true_rel_resid": worst},
@@ -844,6 +851,12 @@ def main():
     ap.add_argument("--skip-jacobi", action="store_true")
     ap.add_argument("--only-config5", action="store_true",
                     help="profiling aid: the batched configuration alone (its JSON object, no contract line)")
+    ap.add_argument("--only-config3", action="store_true",
+                    help="profiling aid: the block configuration alone (its JSON object, no contract line)")
+    ap.add_argument("--batch-count", type=int, default=256,
+                    help="profiling aid: systems in the batched configuration (the benchmark's is 256)")
+    ap.add_argument("--batch-side-max", type=int, default=256,
+                    help="profiling aid: largest grid side of the batched configuration's systems (256)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel (the Arnoldi step), if captured")
     ap.add_argument("--trsv-schedule", default=None,
