@@ -686,14 +686,31 @@ __global__ void k_factor_gather_blk(int count, int bs, const int *__restrict__ m
   }
 }
 
+// one resident wave of the block sweep: as many warps as the SMs hold at
+// once, at most one per block entry (the kernel strides over the rest)
+template <typename FT, typename CT, int BSV>
+static int bcsr_sweep_grid(int nnzb) {
+  static const int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bcsr_parilu_sweep_ao<FT, CT, BSV>, kPTPB, 0) !=
+            cudaSuccess ||
+        b < 1) {
+      cudaGetLastError();
+      b = 1;
+    }
+    return b;
+  }();
+  const int grid = (nnzb + kPTPB / 32 - 1) / (kPTPB / 32);
+  return std::max(1, std::min(grid, num_sms() * per_sm));
+}
+
 template <typename FT, typename CT>
-static void bcsr_sweep_ao_bs(cudaStream_t s, int grid, int bs, int nnzb, const double *Aval, const int *Acol,
+static void bcsr_sweep_ao_bs(cudaStream_t s, int bs, int nnzb, const double *Aval, const int *Acol,
                              const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv, const void *Fold,
                              void *Fnew, double *partials, int *counter, double *step) {
 #define LACE_BSW(BSV)                                                                                   \
-  k_bcsr_parilu_sweep_ao<FT, CT, BSV><<<grid, kPTPB, 0, s>>>(nnzb, Aval, Acol, dpos, pptr, pairs,       \
-                                                             (const CT *)Dinv, (const FT *)Fold,        \
-                                                             (FT *)Fnew, partials, counter, step)
+  k_bcsr_parilu_sweep_ao<FT, CT, BSV><<<bcsr_sweep_grid<FT, CT, BSV>(nnzb), kPTPB, 0, s>>>(                \
+      nnzb, Aval, Acol, dpos, pptr, pairs, (const CT *)Dinv, (const FT *)Fold, (FT *)Fnew, partials, counter, step)
   switch (bs) {
     case 1: LACE_BSW(1); break;
     case 2: LACE_BSW(2); break;
@@ -728,16 +745,15 @@ static int warp_grid(int items) {
 void launch_bcsr_parilu_sweep_ao(cudaStream_t s, int nnzb, int bs, VType t, const double *Aval, const int *Acol,
                                  const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv,
                                  const void *Fold, void *Fnew, double *partials, int *counter, double *step) {
-  const int grid = warp_grid(nnzb);
   if (t == VType::F64)
-    bcsr_sweep_ao_bs<double, double>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials,
-                                     counter, step);
+    bcsr_sweep_ao_bs<double, double>(s, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials, counter,
+                                     step);
   else if (t == VType::F32)
-    bcsr_sweep_ao_bs<float, float>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials,
-                                   counter, step);
+    bcsr_sweep_ao_bs<float, float>(s, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials, counter,
+                                   step);
   else
-    bcsr_sweep_ao_bs<__nv_bfloat16, float>(s, grid, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew,
-                                           partials, counter, step);
+    bcsr_sweep_ao_bs<__nv_bfloat16, float>(s, bs, nnzb, Aval, Acol, dpos, pptr, pairs, Dinv, Fold, Fnew, partials,
+                                           counter, step);
 }
 
 void launch_bcsr_diag_inverse_ao(cudaStream_t s, int nb, int bs, const int *diag, VType t, const void *F,
