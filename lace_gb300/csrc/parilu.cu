@@ -686,21 +686,24 @@ __global__ void k_factor_gather_blk(int count, int bs, const int *__restrict__ m
   }
 }
 
-// one resident wave of the block sweep: as many warps as the SMs hold at
-// once, at most one per block entry (the kernel strides over the rest)
-template <typename FT, typename CT, int BSV>
-static int bcsr_sweep_grid(int nnzb) {
+// one resident wave of a warp-per-item block kernel (the sweep, or the
+// diagonal inverses): as many warps as the SMs hold at once, at most one per
+// item (the kernels stride over the rest); a grid of more blocks than stay
+// resident runs a second, partial wave
+template <typename FT, typename CT, int BSV, bool SWEEP>
+static int resident_grid(int items) {
   static const int per_sm = [] {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bcsr_parilu_sweep_ao<FT, CT, BSV>, kPTPB, 0) !=
-            cudaSuccess ||
-        b < 1) {
+    const cudaError_t e =
+        SWEEP ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bcsr_parilu_sweep_ao<FT, CT, BSV>, kPTPB, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bcsr_diag_inverse_warp<FT, CT, BSV>, kPTPB, 0);
+    if (e != cudaSuccess || b < 1) {
       cudaGetLastError();
       b = 1;
     }
     return b;
   }();
-  const int grid = (nnzb + kPTPB / 32 - 1) / (kPTPB / 32);
+  const int grid = (items + kPTPB / 32 - 1) / (kPTPB / 32);
   return std::max(1, std::min(grid, num_sms() * per_sm));
 }
 
@@ -709,7 +712,7 @@ static void bcsr_sweep_ao_bs(cudaStream_t s, int bs, int nnzb, const double *Ava
                              const int *dpos, const int *pptr, const int2 *pairs, const void *Dinv, const void *Fold,
                              void *Fnew, double *partials, int *counter, double *step) {
 #define LACE_BSW(BSV)                                                                                   \
-  k_bcsr_parilu_sweep_ao<FT, CT, BSV><<<bcsr_sweep_grid<FT, CT, BSV>(nnzb), kPTPB, 0, s>>>(                \
+  k_bcsr_parilu_sweep_ao<FT, CT, BSV><<<resident_grid<FT, CT, BSV, true>(nnzb), kPTPB, 0, s>>>(          \
       nnzb, Aval, Acol, dpos, pptr, pairs, (const CT *)Dinv, (const FT *)Fold, (FT *)Fnew, partials, counter, step)
   switch (bs) {
     case 1: LACE_BSW(1); break;
@@ -722,10 +725,11 @@ static void bcsr_sweep_ao_bs(cudaStream_t s, int bs, int nnzb, const double *Ava
 }
 
 template <typename FT, typename CT>
-static void diag_inverse_warp_bs(cudaStream_t s, int grid, int nb, int bs, const int *diag, const void *F,
-                                 void *Dinv, int *status) {
-#define LACE_DIW(BSV) \
-  k_bcsr_diag_inverse_warp<FT, CT, BSV><<<grid, kPTPB, 0, s>>>(nb, diag, (const FT *)F, (CT *)Dinv, status)
+static void diag_inverse_warp_bs(cudaStream_t s, int nb, int bs, const int *diag, const void *F, void *Dinv,
+                                 int *status) {
+#define LACE_DIW(BSV)                                                                                 \
+  k_bcsr_diag_inverse_warp<FT, CT, BSV><<<resident_grid<FT, CT, BSV, false>(nb), kPTPB, 0, s>>>(       \
+      nb, diag, (const FT *)F, (CT *)Dinv, status)
   switch (bs) {
     case 1: LACE_DIW(1); break;
     case 2: LACE_DIW(2); break;
@@ -734,12 +738,6 @@ static void diag_inverse_warp_bs(cudaStream_t s, int grid, int nb, int bs, const
     default: LACE_DIW(5); break;
   }
 #undef LACE_DIW
-}
-
-static int warp_grid(int items) {
-  int grid = (items + kPTPB / 32 - 1) / (kPTPB / 32);
-  const int cap = num_sms() * (2048 / kPTPB);
-  return grid < 1 ? 1 : (grid > cap ? cap : grid);
 }
 
 void launch_bcsr_parilu_sweep_ao(cudaStream_t s, int nnzb, int bs, VType t, const double *Aval, const int *Acol,
@@ -758,10 +756,9 @@ void launch_bcsr_parilu_sweep_ao(cudaStream_t s, int nnzb, int bs, VType t, cons
 
 void launch_bcsr_diag_inverse_ao(cudaStream_t s, int nb, int bs, const int *diag, VType t, const void *F,
                                  void *Dinv, int *status) {
-  const int grid = warp_grid(nb);
-  if (t == VType::F64) diag_inverse_warp_bs<double, double>(s, grid, nb, bs, diag, F, Dinv, status);
-  else if (t == VType::F32) diag_inverse_warp_bs<float, float>(s, grid, nb, bs, diag, F, Dinv, status);
-  else diag_inverse_warp_bs<__nv_bfloat16, float>(s, grid, nb, bs, diag, F, Dinv, status);
+  if (t == VType::F64) diag_inverse_warp_bs<double, double>(s, nb, bs, diag, F, Dinv, status);
+  else if (t == VType::F32) diag_inverse_warp_bs<float, float>(s, nb, bs, diag, F, Dinv, status);
+  else diag_inverse_warp_bs<__nv_bfloat16, float>(s, nb, bs, diag, F, Dinv, status);
 }
 
 void launch_factor_gather_blk(cudaStream_t s, int count, int bs, const int *map, VType t, const void *src,
