@@ -203,3 +203,15 @@ def test_argument_errors():
         lg.DEV_ERR_NOT_SUPPORTED
     assert L.data_sparse_reorder(C.byref(m), None, nn_map.ctypes.data_as(ip), 2) == lg.DEV_ERR_INVALID_PTR
     release(m)
+
+
+def test_empty_matrix():
+    """n = 0: nothing to number or permute, no error."""
+    L = lg.lib()
+    ip = C.POINTER(C.c_int)
+    m = container(0, np.zeros(1, dtype=np.int32), np.zeros(0, dtype=np.int32))
+    nn_map = np.zeros(1, dtype=np.int32)
+    L.data_reorder_cuthill_mckee(C.byref(m), nn_map.ctypes.data_as(ip), True)
+    assert L.lace_gpu_last_error() == 0
+    assert L.data_sparse_reorder(C.byref(m), nn_map.ctypes.data_as(ip), nn_map.ctypes.data_as(ip), 2) == 0
+    release(m)
