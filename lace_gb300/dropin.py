@@ -24,6 +24,8 @@ MagmaRowMajor, MagmaColMajor = 101, 102
 
 _libc = C.CDLL(None)
 _libc.free.argtypes = [C.c_void_p]
+_libc.malloc.restype = C.c_void_p
+_libc.malloc.argtypes = [C.c_size_t]
 
 
 def set_options(precision: str = "fp64", trsv: str = "syncfree", jacobi_sweeps: int = 8,
@@ -313,3 +315,54 @@ def zilures_bcsr(A: Mat, L: Mat, U: Mat):
     LU = DataMatrix()
     rc = lib().data_zilures_bcsr(A.m, L.m, U.m, C.byref(LU), C.byref(res), C.byref(nl))
     return res.value, nl.value, rc
+
+
+def cuthill_mckee(n: int, row, col, reverse: bool = False) -> np.ndarray:
+    """data_reorder_cuthill_mckee on a CSR pattern: nn_map[old] = new."""
+    A = csr(row, col, np.zeros(len(col)), n)
+    nn_map = np.empty(n, dtype=np.int32)
+    f = lib()
+    f.data_reorder_cuthill_mckee(A.ref, nn_map.ctypes.data_as(C.POINTER(C.c_int)), bool(reverse))
+    rc = f.lace_gpu_last_error()
+    if rc:
+        from . import LaceError
+        raise LaceError(rc, "data_reorder_cuthill_mckee")
+    return nn_map
+
+
+def sparse_reorder(n: int, row, col, val, reorder: int, blocksize: int = 0):
+    """data_sparse_reorder on a copy of A (CSR, or BCSR of n block rows when
+    blocksize > 0): (row, col, val) of A in the new numbering, P (new ->
+    old) and Pinv (old -> new).  The call replaces the container's arrays,
+    so they are handed over in memory of the C allocator."""
+    ld = blocksize * blocksize if blocksize else 1
+    M = DataMatrix()
+    M.storage_type = Magma_BCSR if blocksize else Magma_CSR
+    M.num_rows = M.num_cols = n
+    arrs = (np.ascontiguousarray(row, dtype=np.int32), np.ascontiguousarray(col, dtype=np.int32),
+            np.ascontiguousarray(val, dtype=np.float64).reshape(-1))
+    for name, a in zip(("row", "col", "val"), arrs):
+        p = _libc.malloc(max(a.nbytes, 8))
+        if not p:
+            raise MemoryError("malloc")
+        C.memmove(p, a.ctypes.data, a.nbytes)
+        setattr(M, name, p)
+    if blocksize:
+        M.blocksize, M.ldblock, M.numblocks = blocksize, ld, len(arrs[1])
+    M.nnz = len(arrs[1]) * ld
+    P = np.empty(max(n, 1), dtype=np.int32)
+    Pinv = np.empty(max(n, 1), dtype=np.int32)
+    ip = C.POINTER(C.c_int)
+    try:
+        rc = lib().data_sparse_reorder(C.byref(M), P.ctypes.data_as(ip), Pinv.ctypes.data_as(ip), int(reorder))
+        if rc:
+            from . import LaceError
+            raise LaceError(rc, "data_sparse_reorder")
+        nz = int(np.ctypeslib.as_array(C.cast(M.row, C.POINTER(C.c_int)), shape=(n + 1,))[n])
+        out = (np.ctypeslib.as_array(C.cast(M.row, C.POINTER(C.c_int)), shape=(n + 1,)).copy(),
+               np.ctypeslib.as_array(C.cast(M.col, C.POINTER(C.c_int)), shape=(max(nz, 1),)).copy()[:nz],
+               np.ctypeslib.as_array(C.cast(M.val, C.POINTER(C.c_double)), shape=(max(nz * ld, 1),)).copy()[:nz * ld])
+    finally:
+        for name in ("row", "col", "val"):
+            _libc.free(getattr(M, name))
+    return out + (P[:n], Pinv[:n])

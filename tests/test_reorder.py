@@ -215,3 +215,25 @@ def test_empty_matrix():
     assert L.lace_gpu_last_error() == 0
     assert L.data_sparse_reorder(C.byref(m), nn_map.ctypes.data_as(ip), nn_map.ctypes.data_as(ip), 2) == 0
     release(m)
+
+
+def test_python_wrappers():
+    """dropin.cuthill_mckee / dropin.sparse_reorder: the same results as the
+    entry points, LaceError for what the entry points refuse."""
+    n, row, col = cases()["components"]
+    for rev in (False, True):
+        assert np.array_equal(dropin.cuthill_mckee(n, row, col, rev), orc.cuthill_mckee(n, row, col, rev))
+    val = np.random.default_rng(3).standard_normal(len(col))
+    r2, c2, v2, Pv, Pi = dropin.sparse_reorder(n, row, col, val, 1)
+    er, ec, ev = orc.permute_csr(row, col, val, Pv, Pi)
+    assert np.array_equal(r2, er) and np.array_equal(c2, ec) and np.array_equal(v2, ev)
+    B = P.bcsr3d(3, seed=5)
+    r2, c2, v2, Pv, Pi = dropin.sparse_reorder(B.nb, B.row, B.col, np.asarray(B.val), 2, blocksize=B.bs)
+    er, ec, ev = orc.permute_csr(B.row, B.col, np.asarray(B.val).reshape(-1), Pv, Pi, ld=B.bs * B.bs)
+    assert np.array_equal(r2, er) and np.array_equal(c2, ec) and np.array_equal(v2, ev)
+    with pytest.raises(lg.LaceError):
+        dropin.sparse_reorder(n, row, col, val, 3)
+    bad = col.copy()
+    bad[0] = n
+    with pytest.raises(lg.LaceError):
+        dropin.cuthill_mckee(n, row, bad)
