@@ -55,8 +55,17 @@ class HostPool {
   }
 
  private:
-  explicit HostPool(int workers) : workers_(std::max(0, workers)), pid_(getpid()) {
-    for (int t = 1; t <= workers_; ++t) std::thread([this, t] { loop(t); }).detach();
+  // the workers that could be started (none when the process may start no
+  // more threads: every region then takes the path without the pool)
+  explicit HostPool(int workers) : pid_(getpid()) {
+    for (int t = 1; t <= workers; ++t) {
+      try {
+        std::thread([this, t] { loop(t); }).detach();
+      } catch (...) {
+        break;
+      }
+      workers_ = t;
+    }
   }
   void loop(int id) {
     unsigned long seen = 0;
@@ -72,7 +81,7 @@ class HostPool {
       if (--left_ == 0) done_.notify_one();
     }
   }
-  const int workers_;
+  int workers_ = 0;
   const pid_t pid_;
   std::mutex run_mu_, mu_;
   std::condition_variable wake_, done_;
